@@ -1,0 +1,262 @@
+"""b2r_gb300 -- the B2R stencil hot path on one GB300, host side.
+
+A thin Python face over the C ABI of ``libb2r.so`` (include/b2r.h), shaped
+like the reference's entry points (b2r.cpp, heat-3D.cu, gol-3D.cu, eqwp.cu,
+b2r_halo_sync.cu):
+
+* :class:`Domain` -- one b2r handle: the Bx*By*Bz subdomains of a global
+  domain resident on the GPU (``simu_env_init`` + ``b2r_sync_init`` +
+  ``eqwp_cuda_init``), ``step`` = the main loop of b2r.cpp:179-221
+  (halo exchange every R steps, then R model steps), ``boundary_updating``
+  and ``boundary_updating_direct`` as in b2r_halo_sync.cu.
+* :func:`heat_3D_gpu_main`, :func:`gol_3D_gpu_main` -- the per-block entries
+  of heat-3D.cu:583 and gol-3D.cu:119 on a host numpy block.
+
+All compute runs in the CUDA library; there is no CPU fallback.  Importing
+this package without a built ``libb2r.so`` raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+__all__ = ["Domain", "B2RError", "heat_3D_gpu_main", "gol_3D_gpu_main", "lib", "LIB_PATH",
+           "MODEL_HEAT", "MODEL_GOL", "MODEL_EQWP_REF", "MODEL_EQWP_STAG", "BC_SHELL",
+           "BC_PERIODIC", "FIELDS"]
+
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libb2r.so")
+
+MODEL_HEAT, MODEL_GOL, MODEL_EQWP_REF, MODEL_EQWP_STAG = 1, 2, 3, 4
+BC_SHELL, BC_PERIODIC = 0, 1
+FIELDS = {"vx": 0, "vy": 1, "vz": 2, "sxx": 3, "sxy": 4, "sxz": 5, "syy": 6, "syz": 7,
+          "szz": 8, "disp": 9, "lambda": 16, "mu": 17, "buoy": 18}
+_STATUS = {0: "B2R_OK", 1: "B2R_ERR_ARG", 2: "B2R_ERR_CUDA", 3: "B2R_ERR_OOM",
+           4: "B2R_ERR_TIMEOUT", 5: "B2R_ERR_STATE"}
+
+
+class B2RError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{_STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Config(C.Structure):
+    _fields_ = [("model", C.c_int), ("env", C.c_int * 3), ("blocks", C.c_int * 3),
+                ("R", C.c_int), ("D", C.c_int), ("boundary", C.c_int),
+                ("alpha_dt", C.c_double), ("dx", C.c_double), ("dy", C.c_double),
+                ("dz", C.c_double), ("dt", C.c_double), ("h", C.c_double),
+                ("src", C.c_int * 3)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libb2r.so (raises if it was not built: there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing; run __graft_entry__.build() first")
+    L = C.CDLL(LIB_PATH)
+    vp, i, d = C.c_void_p, C.c_int, C.c_double
+    sig = {
+        "b2r_create": ([C.POINTER(Config), C.POINTER(vp)], i),
+        "b2r_destroy": ([vp], i),
+        "b2r_last_error": ([vp], C.c_char_p),
+        "b2r_set_stream": ([vp, vp], i),
+        "b2r_synchronize": ([vp], i),
+        "b2r_geometry": ([vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                          C.POINTER(C.c_int)], i),
+        "b2r_cells": ([vp], C.c_int64),
+        "b2r_upload": ([vp, i, vp, i], i),
+        "b2r_download": ([vp, i, vp, i], i),
+        "b2r_download_blocks": ([vp, i, vp, i], i),
+        "b2r_step": ([vp, i], i),
+        "b2r_run_host": ([vp, i, vp, i, vp], i),
+        "b2r_time_step": ([vp], C.c_int64),
+        "b2r_set_source": ([vp, C.POINTER(C.c_float), i], i),
+        "b2r_boundary_updating_direct": ([vp, i, i], i),
+        "b2r_boundary_updating": ([vp, i, i], i),
+        "b2r_heat_3D_gpu_main": ([vp, i, i, C.c_char_p, i, i, i, d, d, d, d, vp,
+                                  C.POINTER(d)], i),
+        "b2r_gol_3D_gpu_main": ([vp, i, C.c_char_p, i, i, i, vp, C.POINTER(d)], i),
+        "b2r_eqwp_gpu_main": ([vp, i, i, C.POINTER(d)], i),
+        "b2r_kernel_launches": ([], C.c_int64),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def _check(st, handle=None):
+    if st != 0:
+        msg = lib().b2r_last_error(handle)
+        raise B2RError(st, msg.decode() if msg else "")
+
+
+def _ptr(a):
+    """(pointer, is_device) of a numpy array or a torch tensor."""
+    if isinstance(a, np.ndarray):
+        assert a.flags.c_contiguous
+        return C.c_void_p(a.ctypes.data), 0
+    # torch tensor
+    assert a.is_contiguous()
+    return C.c_void_p(a.data_ptr()), 1 if a.is_cuda else 0
+
+
+def _ef(edge_flag):
+    if edge_flag is None:
+        return None
+    return bytes([(v + 256) % 256 for v in edge_flag])
+
+
+class Domain:
+    """The resident subdomains of one B2R simulation (one b2r handle)."""
+
+    def __init__(self, model, env, blocks=(1, 1, 1), R=1, D=1, boundary=BC_SHELL,
+                 alpha_dt=0.01, dx=1.0, dy=1.0, dz=1.0, dt=0.0, h=1.0, src=(0, 0, 0),
+                 stream=None):
+        cfg = Config()
+        cfg.model = model
+        cfg.env[:] = list(env)
+        cfg.blocks[:] = list(blocks)
+        cfg.R, cfg.D, cfg.boundary = R, D, boundary
+        cfg.alpha_dt, cfg.dx, cfg.dy, cfg.dz = alpha_dt, dx, dy, dz
+        cfg.dt, cfg.h = dt, h
+        cfg.src[:] = list(src)
+        self.cfg = cfg
+        hnd = C.c_void_p()
+        _check(lib().b2r_create(C.byref(cfg), C.byref(hnd)))
+        self.h = hnd
+        if stream is not None:
+            self.set_stream(stream)
+        bn, dn = (C.c_int * 3)(), (C.c_int * 3)()
+        halo, cb = C.c_int(), C.c_int()
+        _check(lib().b2r_geometry(self.h, bn, C.byref(halo), dn, C.byref(cb)), self.h)
+        self.block_n = tuple(bn)
+        self.halo = halo.value
+        self.domain_n = tuple(dn)          # x, y, z
+        self.cell_bytes = cb.value
+        self.dtype = np.uint8 if cb.value == 1 else np.float32
+
+    @property
+    def domain_shape(self):
+        """numpy shape (nz, ny, nx) of a domain array."""
+        return self.domain_n[::-1]
+
+    @property
+    def cells(self):
+        return int(lib().b2r_cells(self.h))
+
+    @property
+    def time_step(self):
+        return int(lib().b2r_time_step(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().b2r_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_stream(self, stream):
+        """stream: an int handle or a torch.cuda.Stream."""
+        s = getattr(stream, "cuda_stream", stream)
+        _check(lib().b2r_set_stream(self.h, C.c_void_p(int(s))), self.h)
+
+    def synchronize(self):
+        _check(lib().b2r_synchronize(self.h), self.h)
+
+    def upload(self, arr, field=0):
+        p, dev = _ptr(arr)
+        _check(lib().b2r_upload(self.h, FIELDS.get(field, field), p, dev), self.h)
+
+    def download(self, out=None, field=0):
+        if out is None:
+            out = np.empty(self.domain_shape, self.dtype)
+        p, dev = _ptr(out)
+        _check(lib().b2r_download(self.h, FIELDS.get(field, field), p, dev), self.h)
+        return out
+
+    def download_blocks(self, field=0):
+        """dict {(bx,by,bz): padded block (nz,ny,nx)} with halos, as stored."""
+        nb = tuple(self.cfg.blocks)
+        n = self.block_n
+        out = np.empty((nb[0] * nb[1] * nb[2], n[2], n[1], n[0]), self.dtype)
+        p, dev = _ptr(out)
+        _check(lib().b2r_download_blocks(self.h, FIELDS.get(field, field), p, dev), self.h)
+        res = {}
+        for bz in range(nb[2]):
+            for by in range(nb[1]):
+                for bx in range(nb[0]):
+                    res[(bx, by, bz)] = out[bx + nb[0] * (by + nb[1] * bz)]
+        return res
+
+    def step(self, nsteps):
+        _check(lib().b2r_step(self.h, int(nsteps)), self.h)
+
+    def run_host(self, host_in, nsteps, host_out, field=0):
+        pi, _ = _ptr(host_in)
+        po, _ = _ptr(host_out)
+        _check(lib().b2r_run_host(self.h, FIELDS.get(field, field), pi, int(nsteps), po), self.h)
+        return host_out
+
+    def set_source(self, amps):
+        a = np.ascontiguousarray(amps, np.float32)
+        _check(lib().b2r_set_source(self.h, a.ctypes.data_as(C.POINTER(C.c_float)), a.size),
+               self.h)
+
+    def boundary_updating(self, time_step=0, field=0):
+        _check(lib().b2r_boundary_updating(self.h, time_step, FIELDS.get(field, field)), self.h)
+
+    def boundary_updating_direct(self, time_step=0, field=0):
+        _check(lib().b2r_boundary_updating_direct(self.h, time_step, FIELDS.get(field, field)),
+               self.h)
+
+    def eqwp_gpu_main(self, ts, R):
+        secs = C.c_double()
+        _check(lib().b2r_eqwp_gpu_main(self.h, ts, R, C.byref(secs)), self.h)
+        return secs.value
+
+
+def kernel_launches():
+    """Kernels launched by libb2r in this process so far."""
+    return int(lib().b2r_kernel_launches())
+
+
+def heat_3D_gpu_main(h_in, R, D=1, edge_flag=None, alpha_dt=0.1 * 0.1, dx=1.0, dy=1.0, dz=0.5,
+                     stream=None):
+    """heat-3D.cu:583 on a host float32 block (nz,ny,nx), in place; returns GPU seconds."""
+    assert h_in.dtype == np.float32 and h_in.flags.c_contiguous
+    nz, ny, nx = h_in.shape
+    secs = C.c_double()
+    s = getattr(stream, "cuda_stream", stream) or 0
+    _check(lib().b2r_heat_3D_gpu_main(h_in.ctypes.data_as(C.c_void_p), R, D, _ef(edge_flag), nx,
+                                      ny, nz, alpha_dt, dx, dy, dz, C.c_void_p(int(s)),
+                                      C.byref(secs)))
+    return secs.value
+
+
+def gol_3D_gpu_main(h_in, R, edge_flag=None, stream=None):
+    """gol-3D.cu:119 on a host uint8 block (nz,ny,nx), in place; returns GPU seconds."""
+    assert h_in.dtype == np.uint8 and h_in.flags.c_contiguous
+    nz, ny, nx = h_in.shape
+    secs = C.c_double()
+    s = getattr(stream, "cuda_stream", stream) or 0
+    _check(lib().b2r_gol_3D_gpu_main(h_in.ctypes.data_as(C.c_void_p), R, _ef(edge_flag), nx, ny,
+                                     nz, C.c_void_p(int(s)), C.byref(secs)))
+    return secs.value

@@ -1,0 +1,720 @@
+// b2r_api.cu -- the C ABI of libb2r (include/b2r.h): handles, geometry,
+// device memory of the resident subdomains, the period driver (halo
+// exchange + R sub-steps, b2r.cpp:179-221) and the reference-shaped per-block
+// entries (heat_3D_gpu_main, gol_3D_gpu_main, eqwp_gpu_main).
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include <cudaTypedefs.h>
+
+#include "b2r_common.cuh"
+#include "eqwp.h"
+#include "gol.h"
+#include "halo.h"
+#include "heat.h"
+
+using namespace b2r;
+
+struct b2r_handle {
+    b2r_config cfg{};
+    BlockLayout L{};
+    int cell_bytes = 4;
+    int shell = 1;              // depth of the fixed shell in domain arrays
+    cudaStream_t stream = nullptr;
+    // heat / GoL: one field, two ping-pong buffers
+    void* buf[2] = {nullptr, nullptr};
+    int cur = 0;
+    CUtensorMap tmap[2];
+    HeatCoef hc{};
+    // elastic wave: fields and material
+    float* fld[kMaxFields] = {};
+    int nfld = 0;
+    float* mat[3] = {};
+    std::vector<float> src;     // per-step source increment of sxx/syy/szz (STAG)
+    void* staging = nullptr;
+    size_t staging_bytes = 0;
+    void* bounce = nullptr;
+    size_t bounce_bytes = 0;
+    int* d_status = nullptr;
+    long long ts = 0;
+    bool halos_fresh = false;
+    std::string err;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+b2r_status fail(b2r_handle* h, b2r_status s, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (h) h->err = buf;
+    g_err = buf;
+    return s;
+}
+
+#define CK(h, call)                                                                          \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return fail(h, e_ == cudaErrorMemoryAllocation ? B2R_ERR_OOM : B2R_ERR_CUDA,     \
+                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+inline int roundup(int v, int m) { return (v + m - 1) / m * m; }
+
+// cells consumed from the halo by one time step
+int halo_per_step(const b2r_config& c)
+{
+    switch (c.model) {
+    case B2R_MODEL_HEAT: return c.D;
+    case B2R_MODEL_GOL: return 1;
+    default: return 2 * c.D;   // elastic wave: two stages of radius D
+    }
+}
+
+void fill_layout(BlockLayout& L, const int n[3], const int B[3], const int nb[3], int H,
+                 int cell_bytes, int periodic, int fixed_edge)
+{
+    const int A = 128 / cell_bytes;      // 128-byte row alignment
+    const int m = 16 / cell_bytes;       // >= 16 bytes of pad before x = 0
+    for (int a = 0; a < 3; ++a) {
+        L.n[a] = n[a];
+        L.B[a] = B[a];
+        L.nb[a] = nb[a];
+    }
+    L.nblk = nb[0] * nb[1] * nb[2];
+    L.H = H;
+    L.xoff = roundup(H + m, A) - H;
+    L.P = roundup(L.xoff + n[0] + m, A);   // >= 16 bytes of pad after the row too
+    L.periodic = periodic;
+    L.fixed_edge = fixed_edge;
+    L.plane = (long long)L.P * n[1];
+    L.bstride = L.plane * n[2];
+}
+
+size_t field_bytes(const b2r_handle* h) { return (size_t)h->L.bstride * h->L.nblk * h->cell_bytes; }
+
+size_t domain_cells(const b2r_handle* h)
+{
+    size_t c = 1;
+    for (int a = 0; a < 3; ++a) c *= (size_t)(h->cfg.env[a] + 2 * h->shell);
+    return c;
+}
+
+b2r_status ensure_staging(b2r_handle* h, size_t bytes)
+{
+    if (h->staging_bytes >= bytes) return B2R_OK;
+    if (h->staging) cudaFree(h->staging);
+    h->staging = nullptr;
+    h->staging_bytes = 0;
+    CK(h, cudaMalloc(&h->staging, bytes));
+    h->staging_bytes = bytes;
+    return B2R_OK;
+}
+
+b2r_status build_heat_maps(b2r_handle* h)
+{
+    for (int b = 0; b < 2; ++b)
+        if (!make_block_tmap(&h->tmap[b], h->buf[b], h->L, 4, heat_box_w(), heat_box_h(h->cfg.D), 1))
+            return fail(h, B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed for the heat field");
+    return B2R_OK;
+}
+
+b2r_status check_status(b2r_handle* h)
+{
+    int s = 0;
+    CK(h, cudaMemcpyAsync(&s, h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (s != DEV_OK) {
+        int zero = 0;
+        cudaMemcpy(h->d_status, &zero, sizeof(int), cudaMemcpyHostToDevice);
+        return fail(h, B2R_ERR_TIMEOUT, "a device-side bounded wait gave up (code %d)", s);
+    }
+    return B2R_OK;
+}
+
+b2r_status exchange_all(b2r_handle* h, bool staged)
+{
+    const BlockLayout& L = h->L;
+    void* bounce = nullptr;
+    int nf = 1;
+    if (h->cfg.model == B2R_MODEL_EQWP_REF || h->cfg.model == B2R_MODEL_EQWP_STAG) nf = h->nfld;
+    if (staged) {
+        size_t need = halo_bounce_elems(L) * nf * h->cell_bytes;
+        if (h->bounce_bytes < need) {
+            if (h->bounce) cudaFree(h->bounce);
+            h->bounce = nullptr;
+            h->bounce_bytes = 0;
+            CK(h, cudaMalloc(&h->bounce, need));
+            h->bounce_bytes = need;
+        }
+        bounce = h->bounce;
+    }
+    if (h->cell_bytes == 1) {
+        FieldSet<uint8_t> fs{};
+        fs.p[0] = static_cast<uint8_t*>(h->buf[h->cur]);
+        CK(h, launch_halo_exchange<uint8_t>(fs, 1, L, static_cast<uint8_t*>(bounce), h->stream));
+    } else {
+        FieldSet<float> fs{};
+        if (nf == 1) fs.p[0] = static_cast<float*>(h->buf[h->cur]);
+        else
+            for (int f = 0; f < nf; ++f) fs.p[f] = h->fld[f];
+        CK(h, launch_halo_exchange<float>(fs, nf, L, static_cast<float*>(bounce), h->stream));
+    }
+    return B2R_OK;
+}
+
+b2r_status exchange_one(b2r_handle* h, int field, bool staged)
+{
+    const BlockLayout& L = h->L;
+    void* bounce = nullptr;
+    if (staged) {
+        size_t need = halo_bounce_elems(L) * h->cell_bytes;
+        if (h->bounce_bytes < need) {
+            if (h->bounce) cudaFree(h->bounce);
+            h->bounce = nullptr;
+            h->bounce_bytes = 0;
+            CK(h, cudaMalloc(&h->bounce, need));
+            h->bounce_bytes = need;
+        }
+        bounce = h->bounce;
+    }
+    if (h->cell_bytes == 1) {
+        FieldSet<uint8_t> fs{};
+        fs.p[0] = static_cast<uint8_t*>(h->buf[h->cur]);
+        CK(h, launch_halo_exchange<uint8_t>(fs, 1, L, static_cast<uint8_t*>(bounce), h->stream));
+    } else {
+        FieldSet<float> fs{};
+        fs.p[0] = (h->nfld > 0) ? h->fld[field] : static_cast<float*>(h->buf[h->cur]);
+        CK(h, launch_halo_exchange<float>(fs, 1, L, static_cast<float*>(bounce), h->stream));
+    }
+    return B2R_OK;
+}
+
+b2r_status substep(b2r_handle* h, int i)
+{
+    switch (h->cfg.model) {
+    case B2R_MODEL_HEAT:
+        CK(h, launch_heat_substep(&h->tmap[h->cur], static_cast<float*>(h->buf[1 - h->cur]), h->L,
+                                  h->cfg.D, i, h->hc, h->d_status, h->stream, 0));
+        h->cur = 1 - h->cur;
+        return B2R_OK;
+    case B2R_MODEL_GOL:
+        CK(h, launch_gol_substep(static_cast<const uint8_t*>(h->buf[h->cur]),
+                                 static_cast<uint8_t*>(h->buf[1 - h->cur]), h->L, i, h->stream));
+        h->cur = 1 - h->cur;
+        return B2R_OK;
+    case B2R_MODEL_EQWP_REF: {
+        EqwpRefParams p = eqwp_ref_params(h->L);
+        CK(h, launch_eqwp_ref_substep(h->fld, h->L, i, (int)(h->ts - i), p, h->stream));
+        return B2R_OK;
+    }
+    case B2R_MODEL_EQWP_STAG: {
+        EqwpStagParams p{};
+        p.dt = (float)h->cfg.dt;
+        p.inv_h = (float)(1.0 / h->cfg.h);
+        for (int a = 0; a < 3; ++a) p.src[a] = h->cfg.src[a];
+        p.src_host = h->src.empty() ? nullptr : h->src.data();
+        p.src_len = (int)h->src.size();
+        CK(h, launch_eqwp_stag_substep(h->fld, h->mat, h->L, i, (int)h->ts, p, h->stream));
+        return B2R_OK;
+    }
+    default:
+        return fail(h, B2R_ERR_ARG, "unknown model %d", h->cfg.model);
+    }
+}
+
+}  // namespace
+
+namespace b2r {
+
+static std::atomic<long long> g_launches{0};
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+bool make_block_tmap(CUtensorMap* map, const void* base, const BlockLayout& L, int elem_bytes,
+                     int box_x, int box_y, int box_z)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 enc = nullptr;
+    if (!enc) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                             &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn)
+            return false;
+        enc = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    cuuint64_t dims[4] = {(cuuint64_t)L.P, (cuuint64_t)L.n[1], (cuuint64_t)L.n[2],
+                          (cuuint64_t)L.nblk};
+    cuuint64_t strides[3] = {(cuuint64_t)L.P * elem_bytes, (cuuint64_t)L.plane * elem_bytes,
+                             (cuuint64_t)L.bstride * elem_bytes};
+    cuuint32_t box[4] = {(cuuint32_t)box_x, (cuuint32_t)box_y, (cuuint32_t)box_z, 1};
+    cuuint32_t es[4] = {1, 1, 1, 1};
+    CUresult r = enc(map, elem_bytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT8,
+                     4, const_cast<void*>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+}  // namespace b2r
+
+extern "C" {
+
+b2r_status b2r_create(const b2r_config* cfg, b2r_handle** out)
+{
+    if (!cfg || !out) return fail(nullptr, B2R_ERR_ARG, "null argument");
+    *out = nullptr;
+    const b2r_config& c = *cfg;
+    if (c.model < B2R_MODEL_HEAT || c.model > B2R_MODEL_EQWP_STAG)
+        return fail(nullptr, B2R_ERR_ARG, "unknown model %d", c.model);
+    int B[3];
+    for (int a = 0; a < 3; ++a) {
+        if (c.env[a] <= 0 || c.blocks[a] <= 0)
+            return fail(nullptr, B2R_ERR_ARG, "env and blocks must be positive");
+        if (c.env[a] % c.blocks[a] != 0)   // b2r.cpp:154-159
+            return fail(nullptr, B2R_ERR_ARG,
+                        "ENV_DIM (%d) must be divisible by BLOCK_DIM (%d) on axis %d", c.env[a],
+                        c.blocks[a], a);
+        B[a] = c.env[a] / c.blocks[a];
+    }
+    if (c.model == B2R_MODEL_HEAT && (c.D < 1 || c.D > 4))
+        return fail(nullptr, B2R_ERR_ARG, "heat stencil radius D must be 1..4 (got %d)", c.D);
+    if (c.model == B2R_MODEL_GOL && c.D != 1)
+        return fail(nullptr, B2R_ERR_ARG, "Game of Life has radius D = 1");
+    if ((c.model == B2R_MODEL_EQWP_REF || c.model == B2R_MODEL_EQWP_STAG) && c.D != 2)
+        return fail(nullptr, B2R_ERR_ARG, "the elastic-wave models have radius D = 2");
+    if (c.R < 1) return fail(nullptr, B2R_ERR_ARG, "R must be >= 1");
+    const int minB = B[0] < B[1] ? (B[0] < B[2] ? B[0] : B[2]) : (B[1] < B[2] ? B[1] : B[2]);
+    if (c.R * c.D > minB / 2)   // b2r.cpp:54
+        return fail(nullptr, B2R_ERR_ARG, "should meet condition: 1 <= R*D <= min(B)/2 (R*D=%d, min B=%d)",
+                    c.R * c.D, minB);
+    const int H = c.R * halo_per_step(c);
+    if (H > minB)
+        return fail(nullptr, B2R_ERR_ARG, "halo depth %d exceeds the subdomain size %d", H, minB);
+    if (c.boundary != B2R_BC_SHELL && c.boundary != B2R_BC_PERIODIC)
+        return fail(nullptr, B2R_ERR_ARG, "unknown boundary kind %d", c.boundary);
+
+    b2r_handle* h = new (std::nothrow) b2r_handle();
+    if (!h) return fail(nullptr, B2R_ERR_OOM, "host allocation failed");
+    h->cfg = c;
+    h->cell_bytes = (c.model == B2R_MODEL_GOL) ? 1 : 4;
+    h->shell = (c.boundary == B2R_BC_PERIODIC) ? 0 : halo_per_step(c) / (c.model >= B2R_MODEL_EQWP_REF ? 2 : 1);
+    int n[3];
+    for (int a = 0; a < 3; ++a) n[a] = B[a] + 2 * H;
+    fill_layout(h->L, n, B, c.blocks, H, h->cell_bytes, c.boundary == B2R_BC_PERIODIC, -1);
+
+    b2r_status st = B2R_OK;
+    auto bail = [&](b2r_status s) {
+        b2r_destroy(h);
+        return s;
+    };
+    if (cudaMalloc(&h->d_status, sizeof(int)) != cudaSuccess)
+        return bail(fail(nullptr, B2R_ERR_CUDA, "cudaMalloc(status) failed"));
+    cudaMemset(h->d_status, 0, sizeof(int));
+    const size_t fb = field_bytes(h);
+    if (c.model == B2R_MODEL_HEAT || c.model == B2R_MODEL_GOL) {
+        for (int b = 0; b < 2; ++b) {
+            if (cudaMalloc(&h->buf[b], fb) != cudaSuccess)
+                return bail(fail(nullptr, B2R_ERR_OOM, "cudaMalloc of %zu bytes failed", fb));
+            cudaMemset(h->buf[b], 0, fb);
+        }
+        if (c.model == B2R_MODEL_HEAT) {
+            h->hc = heat_coef(c.D, c.alpha_dt, c.dx, c.dy, c.dz);
+            if ((st = build_heat_maps(h)) != B2R_OK) {
+                g_err = h->err;
+                return bail(st);
+            }
+        }
+    } else {
+        h->nfld = (c.model == B2R_MODEL_EQWP_REF) ? 10 : 9;
+        for (int f = 0; f < h->nfld; ++f) {
+            if (cudaMalloc(&h->fld[f], fb) != cudaSuccess)
+                return bail(fail(nullptr, B2R_ERR_OOM, "cudaMalloc of %zu bytes failed", fb));
+            cudaMemset(h->fld[f], 0, fb);
+        }
+        if (c.model == B2R_MODEL_EQWP_STAG) {
+            for (int m = 0; m < 3; ++m) {
+                if (cudaMalloc(&h->mat[m], fb) != cudaSuccess)
+                    return bail(fail(nullptr, B2R_ERR_OOM, "cudaMalloc of %zu bytes failed", fb));
+                cudaMemset(h->mat[m], 0, fb);
+            }
+        }
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess)
+        return bail(fail(nullptr, B2R_ERR_CUDA, "device initialisation failed"));
+    *out = h;
+    return B2R_OK;
+}
+
+b2r_status b2r_destroy(b2r_handle* h)
+{
+    if (!h) return B2R_OK;
+    for (int b = 0; b < 2; ++b)
+        if (h->buf[b]) cudaFree(h->buf[b]);
+    for (int f = 0; f < kMaxFields; ++f)
+        if (h->fld[f]) cudaFree(h->fld[f]);
+    for (int m = 0; m < 3; ++m)
+        if (h->mat[m]) cudaFree(h->mat[m]);
+    if (h->staging) cudaFree(h->staging);
+    if (h->bounce) cudaFree(h->bounce);
+    if (h->d_status) cudaFree(h->d_status);
+    delete h;
+    return B2R_OK;
+}
+
+int64_t b2r_kernel_launches(void) { return g_launches.load(); }
+
+const char* b2r_last_error(const b2r_handle* h)
+{
+    if (h) return h->err.c_str();
+    return g_err.c_str();
+}
+
+b2r_status b2r_set_stream(b2r_handle* h, void* s)
+{
+    if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
+    h->stream = static_cast<cudaStream_t>(s);
+    return B2R_OK;
+}
+
+b2r_status b2r_synchronize(b2r_handle* h)
+{
+    if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
+    CK(h, cudaStreamSynchronize(h->stream));
+    return check_status(h);
+}
+
+b2r_status b2r_geometry(const b2r_handle* h, int block_n[3], int* halo, int domain_n[3],
+                        int* cell_bytes)
+{
+    if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
+    for (int a = 0; a < 3; ++a) {
+        if (block_n) block_n[a] = h->L.n[a];
+        if (domain_n) domain_n[a] = h->cfg.env[a] + 2 * h->shell;
+    }
+    if (halo) *halo = h->L.H;
+    if (cell_bytes) *cell_bytes = h->cell_bytes;
+    return B2R_OK;
+}
+
+int64_t b2r_cells(const b2r_handle* h)
+{
+    if (!h) return 0;
+    return (int64_t)h->cfg.env[0] * h->cfg.env[1] * h->cfg.env[2];
+}
+
+int64_t b2r_time_step(const b2r_handle* h) { return h ? h->ts : -1; }
+
+b2r_status b2r_upload(b2r_handle* h, int field, const void* src, int src_is_device)
+{
+    if (!h || !src) return fail(h, B2R_ERR_ARG, "null argument");
+    const bool eq = h->nfld > 0;
+    const bool is_mat = eq && field >= B2R_F_LAMBDA && field <= B2R_F_BUOY;
+    if (!is_mat && (field < 0 || field >= (eq ? h->nfld : 1)))
+        return fail(h, B2R_ERR_ARG, "invalid field id %d", field);
+    if (is_mat && h->cfg.model != B2R_MODEL_EQWP_STAG)
+        return fail(h, B2R_ERR_ARG, "material fields exist only for the staggered model");
+    const size_t bytes = domain_cells(h) * h->cell_bytes;
+    const void* dsrc = src;
+    b2r_status st;
+    if (!src_is_device) {
+        if ((st = ensure_staging(h, bytes)) != B2R_OK) return st;
+        CK(h, cudaMemcpyAsync(h->staging, src, bytes, cudaMemcpyHostToDevice, h->stream));
+        dsrc = h->staging;
+    }
+    void* dst;
+    if (is_mat) dst = h->mat[field - B2R_F_LAMBDA];
+    else if (eq) dst = h->fld[field];
+    else dst = h->buf[h->cur];
+    if (h->cell_bytes == 1)
+        CK(h, launch_scatter<uint8_t>(static_cast<const uint8_t*>(dsrc), static_cast<uint8_t*>(dst),
+                                      h->L, h->shell, h->stream));
+    else
+        CK(h, launch_scatter<float>(static_cast<const float*>(dsrc), static_cast<float*>(dst), h->L,
+                                    h->shell, h->stream));
+    if (!eq)  // both ping-pong buffers carry the shell (heat-3D.cu:591-592)
+        CK(h, cudaMemcpyAsync(h->buf[1 - h->cur], h->buf[h->cur], field_bytes(h),
+                              cudaMemcpyDeviceToDevice, h->stream));
+    h->ts = 0;
+    h->halos_fresh = true;
+    return B2R_OK;
+}
+
+b2r_status b2r_download(b2r_handle* h, int field, void* dst, int dst_is_device)
+{
+    if (!h || !dst) return fail(h, B2R_ERR_ARG, "null argument");
+    const bool eq = h->nfld > 0;
+    if (field < 0 || field >= (eq ? h->nfld : 1))
+        return fail(h, B2R_ERR_ARG, "invalid field id %d", field);
+    const size_t bytes = domain_cells(h) * h->cell_bytes;
+    void* ddst = dst;
+    b2r_status st;
+    if (!dst_is_device) {
+        if ((st = ensure_staging(h, bytes)) != B2R_OK) return st;
+        ddst = h->staging;
+    }
+    const void* srcb = eq ? (const void*)h->fld[field] : h->buf[h->cur];
+    if (h->cell_bytes == 1)
+        CK(h, launch_gather<uint8_t>(static_cast<uint8_t*>(ddst), static_cast<const uint8_t*>(srcb),
+                                     h->L, h->shell, h->stream));
+    else
+        CK(h, launch_gather<float>(static_cast<float*>(ddst), static_cast<const float*>(srcb), h->L,
+                                   h->shell, h->stream));
+    if (!dst_is_device) {
+        CK(h, cudaMemcpyAsync(dst, h->staging, bytes, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+    }
+    return B2R_OK;
+}
+
+b2r_status b2r_download_blocks(b2r_handle* h, int field, void* dst, int dst_is_device)
+{
+    if (!h || !dst) return fail(h, B2R_ERR_ARG, "null argument");
+    const bool eq = h->nfld > 0;
+    const bool is_mat = eq && field >= B2R_F_LAMBDA && field <= B2R_F_BUOY && h->mat[0];
+    if (!is_mat && (field < 0 || field >= (eq ? h->nfld : 1)))
+        return fail(h, B2R_ERR_ARG, "invalid field id %d", field);
+    const char* srcb = static_cast<const char*>(
+        is_mat ? (const void*)h->mat[field - B2R_F_LAMBDA]
+               : (eq ? (const void*)h->fld[field] : h->buf[h->cur]));
+    const BlockLayout& L = h->L;
+    const size_t cb = h->cell_bytes;
+    CK(h, cudaMemcpy2DAsync(dst, L.n[0] * cb, srcb + L.xoff * cb, L.P * cb, L.n[0] * cb,
+                            (size_t)L.nblk * L.n[1] * L.n[2],
+                            dst_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                            h->stream));
+    if (!dst_is_device) CK(h, cudaStreamSynchronize(h->stream));
+    return B2R_OK;
+}
+
+b2r_status b2r_step(b2r_handle* h, int nsteps)
+{
+    if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
+    if (nsteps < 0) return fail(h, B2R_ERR_ARG, "nsteps must be >= 0");
+    b2r_status st;
+    for (int s = 0; s < nsteps; ++s) {
+        const int i = (int)(h->ts % h->cfg.R);
+        if (i == 0 && !h->halos_fresh)
+            if ((st = exchange_all(h, false)) != B2R_OK) return st;
+        h->halos_fresh = false;
+        if ((st = substep(h, i)) != B2R_OK) return st;
+        h->ts++;
+    }
+    return B2R_OK;
+}
+
+b2r_status b2r_run_host(b2r_handle* h, int field, const void* host_in, int nsteps, void* host_out)
+{
+    b2r_status st;
+    if ((st = b2r_upload(h, field, host_in, 0)) != B2R_OK) return st;
+    if ((st = b2r_step(h, nsteps)) != B2R_OK) return st;
+    if ((st = b2r_download(h, field, host_out, 0)) != B2R_OK) return st;
+    return check_status(h);
+}
+
+b2r_status b2r_set_source(b2r_handle* h, const float* amps, int n)
+{
+    if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
+    if (n < 0 || (n > 0 && !amps)) return fail(h, B2R_ERR_ARG, "invalid source series");
+    h->src.assign(amps, amps + n);
+    return B2R_OK;
+}
+
+b2r_status b2r_boundary_updating_direct(b2r_handle* h, int time_step, int field)
+{
+    (void)time_step;
+    if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
+    if (field < 0 || field >= (h->nfld > 0 ? h->nfld : 1))
+        return fail(h, B2R_ERR_ARG, "invalid field id %d", field);
+    return exchange_one(h, field, false);
+}
+
+b2r_status b2r_boundary_updating(b2r_handle* h, int time_step, int field)
+{
+    (void)time_step;
+    if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
+    if (field < 0 || field >= (h->nfld > 0 ? h->nfld : 1))
+        return fail(h, B2R_ERR_ARG, "invalid field id %d", field);
+    return exchange_one(h, field, true);
+}
+
+// ---------------------------------------------------------------- per-block entries
+namespace {
+
+int edge_from_flags(const char* ef)
+{
+    if (!ef) return 0;
+    int e = 0;
+    for (int a = 0; a < 3; ++a) {
+        if (ef[a] < 0) e |= 1 << (2 * a);
+        if (ef[a] > 0) e |= 1 << (2 * a + 1);
+    }
+    return e;
+}
+
+struct Scratch {
+    void* p[2] = {nullptr, nullptr};
+    ~Scratch()
+    {
+        for (int i = 0; i < 2; ++i)
+            if (p[i]) cudaFree(p[i]);
+    }
+};
+
+}  // namespace
+
+b2r_status b2r_heat_3D_gpu_main(float* h_in, int R, int D, const char* edge_flag, int Ngx, int Ngy,
+                                int Ngz, double alpha_dt, double dx, double dy, double dz,
+                                void* cuda_stream, double* gpu_seconds)
+{
+    if (!h_in) return fail(nullptr, B2R_ERR_ARG, "null h_in");
+    if (D < 1 || D > 4) return fail(nullptr, B2R_ERR_ARG, "unsupported delta %d", D);
+    if (R < 1) return fail(nullptr, B2R_ERR_ARG, "R must be >= 1");
+    const int H = R * D;
+    const int n[3] = {Ngx, Ngy, Ngz};
+    int B[3];
+    for (int a = 0; a < 3; ++a) {
+        B[a] = n[a] - 2 * H;
+        if (B[a] < 1) return fail(nullptr, B2R_ERR_ARG, "block too small for R*D = %d", H);
+    }
+    const int nb[3] = {1, 1, 1};
+    BlockLayout L{};
+    fill_layout(L, n, B, nb, H, 4, 0, edge_from_flags(edge_flag));
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    const size_t fb = (size_t)L.bstride * sizeof(float);
+    Scratch s;
+    int* d_status = nullptr;
+    CK(nullptr, cudaMalloc(&s.p[0], fb));
+    CK(nullptr, cudaMalloc(&s.p[1], fb));
+    CK(nullptr, cudaMalloc(&d_status, sizeof(int)));
+    CK(nullptr, cudaMemsetAsync(d_status, 0, sizeof(int), st));
+    // host block (dense rows of Ngx) -> pitched device rows (heat-3D.cu:590-592)
+    for (int b = 0; b < 2; ++b)
+        CK(nullptr, cudaMemcpy2DAsync((float*)s.p[b] + L.xoff, L.P * sizeof(float), h_in,
+                                      Ngx * sizeof(float), Ngx * sizeof(float), (size_t)Ngy * Ngz,
+                                      cudaMemcpyHostToDevice, st));
+    CUtensorMap tm[2];
+    for (int b = 0; b < 2; ++b)
+        if (!make_block_tmap(&tm[b], s.p[b], L, 4, heat_box_w(), heat_box_h(D), 1)) {
+            cudaFree(d_status);
+            return fail(nullptr, B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+        }
+    const HeatCoef hc = heat_coef(D, alpha_dt, dx, dy, dz);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    int cur = 0;
+    for (int i = 0; i < R; ++i) {   // heat-3D.cu:602-628
+        cudaError_t e = launch_heat_substep(&tm[cur], (float*)s.p[1 - cur], L, D, i, hc, d_status, st, 0);
+        if (e != cudaSuccess) {
+            cudaFree(d_status);
+            return fail(nullptr, B2R_ERR_CUDA, "heat launch: %s", cudaGetErrorString(e));
+        }
+        cur = 1 - cur;
+    }
+    cudaEventRecord(e1, st);
+    // planes [R*D, Ngz-R*D) back to the host (heat-3D.cu:633-635)
+    const int zc = Ngz - 2 * H;
+    CK(nullptr, cudaMemcpy2DAsync(h_in + (size_t)H * Ngx * Ngy, Ngx * sizeof(float),
+                                  (float*)s.p[cur] + L.xoff + (size_t)H * L.plane, L.P * sizeof(float),
+                                  Ngx * sizeof(float), (size_t)Ngy * zc, cudaMemcpyDeviceToHost, st));
+    int dev_st = 0;
+    CK(nullptr, cudaMemcpyAsync(&dev_st, d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(nullptr, cudaStreamSynchronize(st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d_status);
+    if (gpu_seconds) *gpu_seconds = ms / 1000.0;
+    if (dev_st != DEV_OK) return fail(nullptr, B2R_ERR_TIMEOUT, "device wait gave up (code %d)", dev_st);
+    return B2R_OK;
+}
+
+b2r_status b2r_gol_3D_gpu_main(uint8_t* h_in, int R, const char* edge_flag, int Ngx, int Ngy,
+                               int Ngz, void* cuda_stream, double* gpu_seconds)
+{
+    if (!h_in) return fail(nullptr, B2R_ERR_ARG, "null h_in");
+    if (R < 1) return fail(nullptr, B2R_ERR_ARG, "R must be >= 1");
+    const int H = R;
+    const int n[3] = {Ngx, Ngy, Ngz};
+    int B[3];
+    for (int a = 0; a < 3; ++a) {
+        B[a] = n[a] - 2 * H;
+        if (B[a] < 1) return fail(nullptr, B2R_ERR_ARG, "block too small for R = %d", R);
+    }
+    const int nb[3] = {1, 1, 1};
+    BlockLayout L{};
+    fill_layout(L, n, B, nb, H, 1, 0, edge_from_flags(edge_flag));
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    const size_t fb = (size_t)L.bstride;
+    Scratch s;
+    CK(nullptr, cudaMalloc(&s.p[0], fb));
+    CK(nullptr, cudaMalloc(&s.p[1], fb));
+    for (int b = 0; b < 2; ++b)   // gol-3D.cu:126-129
+        CK(nullptr, cudaMemcpy2DAsync((uint8_t*)s.p[b] + L.xoff, L.P, h_in, Ngx, Ngx,
+                                      (size_t)Ngy * Ngz, cudaMemcpyHostToDevice, st));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, st);
+    int cur = 0;
+    for (int i = 0; i < R; ++i) {  // gol-3D.cu:138-145
+        cudaError_t e = launch_gol_substep((const uint8_t*)s.p[cur], (uint8_t*)s.p[1 - cur], L, i, st);
+        if (e != cudaSuccess) return fail(nullptr, B2R_ERR_CUDA, "gol launch: %s", cudaGetErrorString(e));
+        cur = 1 - cur;
+    }
+    cudaEventRecord(e1, st);
+    // whole block back (gol-3D.cu:149)
+    CK(nullptr, cudaMemcpy2DAsync(h_in, Ngx, (uint8_t*)s.p[cur] + L.xoff, L.P, Ngx, (size_t)Ngy * Ngz,
+                                  cudaMemcpyDeviceToHost, st));
+    CK(nullptr, cudaStreamSynchronize(st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (gpu_seconds) *gpu_seconds = ms / 1000.0;
+    return B2R_OK;
+}
+
+b2r_status b2r_eqwp_gpu_main(b2r_handle* h, int ts, int R, double* gpu_seconds)
+{
+    if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
+    if (h->cfg.model != B2R_MODEL_EQWP_REF)
+        return fail(h, B2R_ERR_ARG, "eqwp_gpu_main needs a B2R_MODEL_EQWP_REF handle");
+    if (R < 1 || R > h->cfg.R) return fail(h, B2R_ERR_ARG, "R must be in 1..%d", h->cfg.R);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, h->stream);
+    b2r_status st = B2R_OK;
+    const long long save = h->ts;
+    for (int i = 0; i < R && st == B2R_OK; ++i) {   // eqwp.cu:677-686
+        h->ts = ts + i;
+        st = substep(h, i);
+    }
+    h->ts = save;
+    cudaEventRecord(e1, h->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (gpu_seconds) *gpu_seconds = ms / 1000.0;
+    if (st != B2R_OK) return st;
+    return check_status(h);
+}
+
+}  // extern "C"

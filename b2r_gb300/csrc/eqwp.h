@@ -1,0 +1,36 @@
+// eqwp.h -- internal interface of the elastic-wave stage kernels (eqwp.cu).
+#pragma once
+#include "b2r_common.cuh"
+
+namespace b2r {
+
+struct FieldPtrs {
+    float* p[10];   // vx, vy, vz, sxx, sxy, sxz, syy, syz, szz, disp
+};
+struct MatPtrs {
+    const float* p[3];   // lambda, mu, buoyancy
+};
+
+struct EqwpRefParams {
+    float ca, cb;                    // FD4 weights / dx
+    float l2m_dt, l_dt, mu_dt;       // dt * (lambda+2mu), dt*lambda, dt*mu
+    float dt_rho, dt2_rho;           // dt/rho, dt^2/rho
+    float fval;                      // body force (y)
+    int fsteps;                      // force active while ts < fsteps
+    int fy, fx0, fx1, fz0, fz1;      // force plane / patch (block coordinates)
+};
+
+struct EqwpStagParams {
+    float dt, inv_h;
+    int src[3];                      // source cell, global interior coordinates
+    const float* src_host;           // per-step source increment (host array)
+    int src_len;
+};
+
+EqwpRefParams eqwp_ref_params(const BlockLayout& L);
+cudaError_t launch_eqwp_ref_substep(float* const* fld, const BlockLayout& L, int step_i, int ts,
+                                    const EqwpRefParams& p, cudaStream_t st);
+cudaError_t launch_eqwp_stag_substep(float* const* fld, float* const* mat, const BlockLayout& L,
+                                     int step_i, int ts, const EqwpStagParams& p, cudaStream_t st);
+
+}  // namespace b2r

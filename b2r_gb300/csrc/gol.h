@@ -1,0 +1,12 @@
+// gol.h -- internal interface of the Game of Life kernel (gol.cu).
+#pragma once
+#include "b2r_common.cuh"
+
+namespace b2r {
+
+// One generation (shrink step_i+1) of every block, in -> out.  Cells of a
+// word outside the window are copied from `in`.
+cudaError_t launch_gol_substep(const uint8_t* in, uint8_t* out, const BlockLayout& L, int step_i,
+                               cudaStream_t st);
+
+}  // namespace b2r

@@ -1,0 +1,259 @@
+// halo.cu -- device-side B2R boundary update between subdomains resident on
+// one GPU, and the domain <-> blocks scatter/gather.
+//
+// The reference moves R*D-deep face slabs between MPI ranks dimension by
+// dimension, X then Y then Z, with growing slab extents so that edges and
+// corners arrive without diagonal messages (b2r_halo_sync.cu:195-379,
+// 389-508; transport b2r_comm.hpp).  Here every block lives in the same HBM,
+// so "send + receive" is one device copy:
+//   * direct:  one launch per axis copies each neighbour's interior slab
+//              straight into the halo (boundary_updating_direct);
+//   * staged:  pack every slab of an axis into a device bounce buffer, then
+//              unpack it (sub_matrix_pack/unpack + boundary_updating).
+// Slab extents per axis follow the reference: x slabs span interior y,z; y
+// slabs full padded x and interior z; z slabs full padded x and y.  One
+// launch covers all blocks, both sides and up to kMaxFields fields.
+#include "b2r_common.cuh"
+#include "halo.h"
+
+namespace b2r {
+
+namespace {
+
+// Slab geometry of an axis: extent e[3] (cells), with the halo axis extent H.
+struct Slab {
+    int e[3];
+    long long cells;  // e0*e1*e2
+};
+
+__host__ __device__ inline Slab slab_of(const BlockLayout& L, int axis)
+{
+    Slab s;
+    for (int a = 0; a < 3; ++a) {
+        if (a == axis) s.e[a] = L.H;
+        else if (a < axis) s.e[a] = L.n[a];     // axes already exchanged: full extent
+        else s.e[a] = L.B[a];                   // later axes: interior only
+    }
+    s.cells = (long long)s.e[0] * s.e[1] * s.e[2];
+    return s;
+}
+
+// Map slab cell (c0,c1,c2) on `side` (0 = low halo, 1 = high halo) of block
+// `blk` to destination / source element offsets.  Returns false when the
+// neighbour does not exist (domain boundary, not periodic).
+__device__ inline bool slab_map(const BlockLayout& L, int axis, int blk, int side, int c0, int c1,
+                                int c2, long long& dst, long long& src)
+{
+    int b[3] = {blk % L.nb[0], (blk / L.nb[0]) % L.nb[1], blk / (L.nb[0] * L.nb[1])};
+    int c[3] = {c0, c1, c2};
+    int d[3], s[3];
+    for (int a = 0; a < 3; ++a) {
+        if (a == axis) continue;
+        int base = (a < axis) ? 0 : L.H;
+        d[a] = s[a] = base + c[a];
+    }
+    int nbk[3] = {b[0], b[1], b[2]};
+    if (side == 0) {
+        nbk[axis] -= 1;
+        d[axis] = c[axis];                       // my low halo [0, H)
+        s[axis] = L.B[axis] + c[axis];           // neighbour's high interior slab [B, B+H)
+    } else {
+        nbk[axis] += 1;
+        d[axis] = L.B[axis] + L.H + c[axis];     // my high halo [B+H, B+2H)
+        s[axis] = L.H + c[axis];                 // neighbour's low interior slab [H, 2H)
+    }
+    if (nbk[axis] < 0 || nbk[axis] >= L.nb[axis]) {
+        if (!L.periodic) return false;
+        nbk[axis] = (nbk[axis] + L.nb[axis]) % L.nb[axis];
+    }
+    const int nblk = nbk[0] + L.nb[0] * (nbk[1] + L.nb[1] * nbk[2]);
+    dst = (long long)blk * L.bstride + (long long)d[2] * L.plane + (long long)d[1] * L.P + L.xoff + d[0];
+    src = (long long)nblk * L.bstride + (long long)s[2] * L.plane + (long long)s[1] * L.P + L.xoff + s[0];
+    return true;
+}
+
+template <typename T>
+__global__ void halo_direct_kernel(FieldSet<T> fs, const BlockLayout L, int axis, Slab sl)
+{
+    T* f = fs.p[blockIdx.y];
+    const long long per_blk = 2 * sl.cells;
+    const long long total = per_blk * L.nblk;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int blk = (int)(e / per_blk);
+        long long r = e - blk * per_blk;
+        const int side = (int)(r / sl.cells);
+        r -= side * sl.cells;
+        const int c0 = (int)(r % sl.e[0]);
+        const long long r1 = r / sl.e[0];
+        const int c1 = (int)(r1 % sl.e[1]);
+        const int c2 = (int)(r1 / sl.e[1]);
+        long long dst, src;
+        if (slab_map(L, axis, blk, side, c0, c1, c2, dst, src)) f[dst] = f[src];
+    }
+}
+
+// staged form: pack[buf] <- neighbour slab, then halo <- pack[buf]
+template <typename T>
+__global__ void halo_pack_kernel(FieldSet<T> fs, T* bounce, const BlockLayout L, int axis,
+                                 Slab sl, int unpack)
+{
+    T* f = fs.p[blockIdx.y];
+    const long long per_blk = 2 * sl.cells;
+    const long long total = per_blk * L.nblk;
+    T* buf = bounce + blockIdx.y * total;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int blk = (int)(e / per_blk);
+        long long r = e - blk * per_blk;
+        const int side = (int)(r / sl.cells);
+        r -= side * sl.cells;
+        const int c0 = (int)(r % sl.e[0]);
+        const long long r1 = r / sl.e[0];
+        const int c1 = (int)(r1 % sl.e[1]);
+        const int c2 = (int)(r1 / sl.e[1]);
+        long long dst, src;
+        if (!slab_map(L, axis, blk, side, c0, c1, c2, dst, src)) continue;
+        if (unpack) f[dst] = buf[e];
+        else buf[e] = f[src];
+    }
+}
+
+// domain array <-> blocks.  shell > 0: non-periodic domain with a `shell`
+// deep fixed shell; periodic: bare torus.
+template <typename T>
+__global__ void scatter_kernel(const T* __restrict__ dom, T* __restrict__ blocks,
+                               const BlockLayout L, int shell)
+{
+    const int dn0 = L.nb[0] * L.B[0] + 2 * shell, dn1 = L.nb[1] * L.B[1] + 2 * shell;
+    const int dn2 = L.nb[2] * L.B[2] + 2 * shell;
+    const long long rowlen = L.n[0];
+    const long long total = rowlen * L.n[1] * L.n[2] * L.nblk;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(e % rowlen);
+        long long r = e / rowlen;
+        const int y = (int)(r % L.n[1]);
+        r /= L.n[1];
+        const int z = (int)(r % L.n[2]);
+        const int blk = (int)(r / L.n[2]);
+        const int b0 = blk % L.nb[0], b1 = (blk / L.nb[0]) % L.nb[1], b2 = blk / (L.nb[0] * L.nb[1]);
+        int g0 = b0 * L.B[0] + x - L.H, g1 = b1 * L.B[1] + y - L.H, g2 = b2 * L.B[2] + z - L.H;
+        T v = T(0);
+        if (L.periodic) {
+            const int e0 = L.nb[0] * L.B[0], e1 = L.nb[1] * L.B[1], e2 = L.nb[2] * L.B[2];
+            g0 = ((g0 % e0) + e0) % e0;
+            g1 = ((g1 % e1) + e1) % e1;
+            g2 = ((g2 % e2) + e2) % e2;
+            v = dom[((long long)g2 * e1 + g1) * e0 + g0];
+        } else {
+            g0 += shell; g1 += shell; g2 += shell;
+            if (g0 >= 0 && g0 < dn0 && g1 >= 0 && g1 < dn1 && g2 >= 0 && g2 < dn2)
+                v = dom[((long long)g2 * dn1 + g1) * dn0 + g0];
+        }
+        blocks[blk * L.bstride + (long long)z * L.plane + (long long)y * L.P + L.xoff + x] = v;
+    }
+}
+
+template <typename T>
+__global__ void gather_kernel(T* __restrict__ dom, const T* __restrict__ blocks,
+                              const BlockLayout L, int shell)
+{
+    const int dn0 = L.nb[0] * L.B[0] + 2 * shell, dn1 = L.nb[1] * L.B[1] + 2 * shell;
+    const int dn2 = L.nb[2] * L.B[2] + 2 * shell;
+    const long long total = (long long)dn0 * dn1 * dn2;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int d0 = (int)(e % dn0);
+        long long r = e / dn0;
+        const int d1 = (int)(r % dn1);
+        const int d2 = (int)(r / dn1);
+        const int g[3] = {d0 - shell, d1 - shell, d2 - shell};
+        int b[3], l[3];
+        for (int a = 0; a < 3; ++a) {
+            int bb = g[a] >= 0 ? g[a] / L.B[a] : -1;
+            bb = bb < 0 ? 0 : (bb >= L.nb[a] ? L.nb[a] - 1 : bb);
+            b[a] = bb;
+            l[a] = g[a] - bb * L.B[a] + L.H;
+        }
+        const int blk = b[0] + L.nb[0] * (b[1] + L.nb[1] * b[2]);
+        dom[e] = blocks[blk * L.bstride + (long long)l[2] * L.plane + (long long)l[1] * L.P +
+                        L.xoff + l[0]];
+    }
+}
+
+inline int grid_for(long long work, int threads)
+{
+    long long g = (work + threads - 1) / threads;
+    if (g > 152LL * 32) g = 152LL * 32;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t launch_halo_exchange(const FieldSet<T>& fs, int nfields, const BlockLayout& L,
+                                 T* bounce, cudaStream_t st)
+{
+    if (L.nblk == 1 && !L.periodic) return cudaSuccess;   // all halos are shell
+    for (int axis = 0; axis < 3; ++axis) {
+        const Slab sl = slab_of(L, axis);
+        const long long work = 2 * sl.cells * L.nblk;
+        dim3 grid(grid_for(work, 256), nfields);
+        if (bounce == nullptr) {
+            halo_direct_kernel<T><<<grid, 256, 0, st>>>(fs, L, axis, sl);
+            count_launches(1);
+        } else {
+            halo_pack_kernel<T><<<grid, 256, 0, st>>>(fs, bounce, L, axis, sl, 0);
+            halo_pack_kernel<T><<<grid, 256, 0, st>>>(fs, bounce, L, axis, sl, 1);
+            count_launches(2);
+        }
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+size_t halo_bounce_elems(const BlockLayout& L)
+{
+    size_t m = 0;
+    for (int axis = 0; axis < 3; ++axis) {
+        const Slab sl = slab_of(L, axis);
+        size_t w = (size_t)(2 * sl.cells * L.nblk);
+        if (w > m) m = w;
+    }
+    return m;
+}
+
+template <typename T>
+cudaError_t launch_scatter(const T* dom, T* blocks, const BlockLayout& L, int shell, cudaStream_t st)
+{
+    const long long total = (long long)L.n[0] * L.n[1] * L.n[2] * L.nblk;
+    scatter_kernel<T><<<grid_for(total, 256), 256, 0, st>>>(dom, blocks, L, shell);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_gather(T* dom, const T* blocks, const BlockLayout& L, int shell, cudaStream_t st)
+{
+    const long long total = (long long)(L.nb[0] * L.B[0] + 2 * shell) *
+                            (L.nb[1] * L.B[1] + 2 * shell) * (L.nb[2] * L.B[2] + 2 * shell);
+    gather_kernel<T><<<grid_for(total, 256), 256, 0, st>>>(dom, blocks, L, shell);
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_halo_exchange<float>(const FieldSet<float>&, int, const BlockLayout&,
+                                                 float*, cudaStream_t);
+template cudaError_t launch_halo_exchange<uint8_t>(const FieldSet<uint8_t>&, int,
+                                                   const BlockLayout&, uint8_t*, cudaStream_t);
+template cudaError_t launch_scatter<float>(const float*, float*, const BlockLayout&, int, cudaStream_t);
+template cudaError_t launch_scatter<uint8_t>(const uint8_t*, uint8_t*, const BlockLayout&, int,
+                                             cudaStream_t);
+template cudaError_t launch_gather<float>(float*, const float*, const BlockLayout&, int, cudaStream_t);
+template cudaError_t launch_gather<uint8_t>(uint8_t*, const uint8_t*, const BlockLayout&, int,
+                                            cudaStream_t);
+
+}  // namespace b2r

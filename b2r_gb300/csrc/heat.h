@@ -1,0 +1,24 @@
+// heat.h -- internal interface of the heat sweep kernels (heat.cu).
+#pragma once
+#include "b2r_common.cuh"
+
+namespace b2r {
+
+// Folded stencil weights: u' = a0*u + sum_k ax[k-1]*(u[x-k]+u[x+k]) + ... .
+struct HeatCoef {
+    float a0;
+    float ax[4], ay[4], az[4];
+};
+
+HeatCoef heat_coef(int D, double alpha_dt, double dx, double dy, double dz);
+// TMA box of one ring slot (cells): width and height for radius D.
+int heat_box_w();
+int heat_box_h(int D);
+int heat_default_nzc(const BlockLayout& L, int D);
+// One sub-step (shrink D*(step_i+1)) of every block: reads the blocks
+// through `tin` (a tensor map over the input buffer), writes `out`.
+cudaError_t launch_heat_substep(const CUtensorMap* tin, float* out, const BlockLayout& L, int D,
+                                int step_i, const HeatCoef& c, int* status, cudaStream_t st,
+                                int nzc);
+
+}  // namespace b2r

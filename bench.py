@@ -1,0 +1,439 @@
+"""Benchmark of the B2R stencil hot path on GB300 (GLUPS + HBM roofline).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload heat1_512|heat4_512|heat_128|gol_256|eqwp_stag]
+
+One "step" = one pass of the workload: `sub_steps` time steps over the whole
+synthetic domain (e.g. 100 heat steps over 512^3).  Rank 0 prints one JSON
+line.  With N > 1 (torchrun) every rank runs an independent replica on its
+own GPU (weak scaling, no data-path collective); the timed region is bracketed
+by barriers and the slowest rank's time is used.
+
+value      GLUPS over all ranks, inputs resident in HBM (CUDA events on the
+           stream the library launches on).
+e2e        the same metric through b2r_run_host: pinned host input -> device,
+           sub_steps time steps, device -> pinned host output, every step.
+roofline   dominant kernel: algorithmic bytes per launch (bytes_per_cell x
+           cells swept by one launch) / average launch time, against the
+           measured HBM copy bandwidth.
+cpu_baseline  the reference's own heat-3D.cpp (oracle/_ref, where it was
+           built) or the oracle's restatement, on this host's cores, over a
+           bounded sample of the same workload.
+--impl reference  times that CPU implementation alone, one bounded sample
+           per step, and prints the same line with "impl": "reference".
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L2_BYTES = 129 * 2 ** 20
+
+WORKLOADS = {
+    # FP32 heat delta1 (fdm_heat_diffuse_delta1), 512^3 interior, fixed zero shell,
+    # alpha*dt/dx^2 = 0.1 on every axis, R = 1, one block
+    "heat1_512": dict(model=1, env=(512, 512, 512), blocks=(1, 1, 1), R=1, D=1, sub_steps=100,
+                      coef=(0.1, 1.0, 1.0, 1.0), bytes_per_cell=8, kernel="heat_sweep_kernel<1>"),
+    # FP32 heat delta4 (fdm_heat_diffuse_delta4), 512^3
+    "heat4_512": dict(model=1, env=(512, 512, 512), blocks=(1, 1, 1), R=1, D=4, sub_steps=100,
+                      coef=(0.02, 1.0, 1.0, 1.0), bytes_per_cell=8, kernel="heat_sweep_kernel<4>"),
+    # heat delta1 on the 128^3 case with the reference's constants (fits in L2)
+    "heat_128": dict(model=1, env=(128, 128, 128), blocks=(1, 1, 1), R=1, D=1, sub_steps=100,
+                     coef=(0.01, 1.0, 1.0, 0.5), bytes_per_cell=8, kernel="heat_sweep_kernel<1>"),
+    # 3-D Game of Life, 256^3 torus, 2x2x2 subdomains, R = 4, 400 generations
+    "gol_256": dict(model=2, env=(256, 256, 256), blocks=(2, 2, 2), R=4, D=1, sub_steps=400,
+                    bytes_per_cell=2, kernel="gol_kernel", periodic=True),
+    # staggered elastic wave 512x512x256, 2x2x1 subdomains, R = 2, 100 steps per pass
+    "eqwp_stag": dict(model=4, env=(512, 512, 256), blocks=(2, 2, 1), R=2, D=2, sub_steps=100,
+                      bytes_per_cell=84, kernel="eqwp_stag_velocity+stress"),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="heat1_512", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ helpers
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            return float(json.load(open(p))["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.rows = []
+        self.proc = None
+        self.idx = str(gpu_index)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-i", self.idx, "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        if not self.rows:
+            return None
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if "Active" in r[5 + k]
+                          and "Not" not in r[5 + k]})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def seeded_domain(wl, shape, seed=1):
+    rng = np.random.default_rng(seed)
+    if wl["model"] == 2:
+        return (rng.random(shape, dtype=np.float32) < 0.3).astype(np.uint8)
+    dom = np.zeros(shape, np.float32)
+    D = wl["D"]
+    dom[D:-D, D:-D, D:-D] = rng.random(tuple(s - 2 * D for s in shape), dtype=np.float32)
+    return dom
+
+
+# ------------------------------------------------------------------ CPU side
+def cpu_sample(wl, budget_s=10.0, nthreads=0, dom=None):
+    """Time the reference CPU path on a bounded sample of the workload.
+
+    Heat: the reference's heat_3D_cpu_main (oracle/_ref) when it was built on
+    this host, else the oracle's restatement of it (same loop nest).  GoL:
+    the oracle's restatement (the reference has no CPU Game of Life).
+    Returns (GLUPS, kind, cores, sample-description)."""
+    from oracle import orc
+    cores = nthreads or os.cpu_count()
+    env = wl["env"]
+    if wl["model"] == 1:
+        D = wl["D"]
+        if dom is None:
+            dom = seeded_domain(wl, tuple(e + 2 * D for e in env[::-1]))
+        use_ref = orc.ref_lib() is not None and D == 1
+        kind = "reference" if use_ref else "port"
+        steps, t = 0, 0.0
+        while t < budget_s or steps < 1:
+            t0 = time.perf_counter()
+            if use_ref:
+                orc.ref_heat_cpu_main(dom, 1, cores)
+            else:
+                orc.heat_cpu_main(dom, 1, D, *wl["coef"], nthreads=cores)
+            t += time.perf_counter() - t0
+            steps += 1
+        lups = steps * env[0] * env[1] * env[2]
+        what = "heat_3D_cpu_main (reference heat-3D.cpp)" if use_ref else "restated heat_3D_cpu_main"
+        return lups / t / 1e9, kind, cores, f"{steps} time step(s) of {what} on the full {env} grid"
+    if wl["model"] == 2:
+        g = seeded_domain(wl, env[::-1]) if dom is None else dom
+        steps, t = 0, 0.0
+        while t < budget_s or steps < 1:
+            t0 = time.perf_counter()
+            orc.gol_run_periodic(g, 1, cores)
+            t += time.perf_counter() - t0
+            steps += 1
+        lups = steps * env[0] * env[1] * env[2]
+        return lups / t / 1e9, "port", cores, f"{steps} generation(s) of the restated rule on the {env} torus"
+    # elastic wave: restated staggered step on a 128x128x64 sample
+    n = (128 + 8, 128 + 8, 64 + 8)
+    f = [np.zeros(n[::-1], np.float32) for _ in range(9)]
+    m = [np.full(n[::-1], v, np.float32) for v in (8e9, 8e9, 1 / 2300.0)]
+    steps, t = 0, 0.0
+    while t < budget_s or steps < 1:
+        t0 = time.perf_counter()
+        orc.eqwp_stag_step(f, m, 1e-4, 10.0, 0, 4, 63, (64, 64, 32), 1.0)
+        t += time.perf_counter() - t0
+        steps += 1
+    return steps * 128 * 128 * 64 / t / 1e9, "port", cores, f"{steps} step(s) of the restated staggered scheme on 128x128x64"
+
+
+def run_reference(args, wl):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle.build as ob
+    ob.build_oracle()
+    ob.build_ref()
+    env = wl["env"]
+    D = wl["D"]
+    shape = env[::-1] if wl["model"] == 2 else tuple(e + 2 * D for e in env[::-1])
+    dom = seeded_domain(wl, shape) if wl["model"] in (1, 2) else None
+    for _ in range(args.warmup):
+        cpu_sample(wl, budget_s=0.0, dom=dom)
+    vals, kind, cores, sample = [], None, None, None
+    t_all = 0.0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        v, kind, cores, sample = cpu_sample(wl, budget_s=0.0, dom=dom)
+        t_all += time.perf_counter() - t0
+        vals.append(v)
+    value = float(np.mean(vals))
+    line = {"metric": "GLUPS", "value": round(value, 4), "unit": "GLUPS", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1000 * t_all / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if wl["model"] != 2 else "u8",
+            "data": "synthetic (seeded)", "config": config_of(args, wl),
+            "cpu_baseline": {"value": round(value, 4), "unit": "GLUPS", "cores": cores, "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": "GLUPS", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_of(args, wl):
+    cells = wl["env"][0] * wl["env"][1] * wl["env"][2]
+    foot = cells * (1 if wl["model"] == 2 else 4) * (2 if wl["model"] in (1, 2) else 12)
+    return {"workload": args.workload, "env": list(wl["env"]), "blocks": list(wl["blocks"]),
+            "R": wl["R"], "D": wl["D"], "time_steps_per_step": wl["sub_steps"],
+            "coef": list(wl.get("coef", [])), "periodic": bool(wl.get("periodic", False)),
+            "l2": ("inputs larger than L2" if foot > L2_BYTES else "L2 flushed between timed steps"),
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+# ------------------------------------------------------------------ GPU side
+def make_domain(b2r, wl, stream):
+    kw = dict(blocks=wl["blocks"], R=wl["R"], D=wl["D"], stream=stream,
+              boundary=b2r.BC_PERIODIC if wl.get("periodic") else b2r.BC_SHELL)
+    if wl["model"] == 1:
+        a, dx, dy, dz = wl["coef"]
+        kw.update(alpha_dt=a, dx=dx, dy=dy, dz=dz)
+    if wl["model"] == 4:
+        h = 10.0
+        kw.update(h=h, dt=0.5 * h / (4000 * 3 ** 0.5 * (9 / 8 + 1 / 24)),
+                  src=tuple(e // 2 for e in wl["env"]))
+    return b2r.Domain(wl["model"], wl["env"], **kw)
+
+
+def load_inputs(d, wl, torch, dev):
+    """Seeded inputs, created on the host and uploaded once (resident in HBM)."""
+    if wl["model"] in (1, 2):
+        host = seeded_domain(wl, d.domain_shape)
+        d.upload(host)
+        return host
+    rng = np.random.default_rng(3)
+    layers = 8
+    vp_l = rng.uniform(2000, 4000, layers)
+    rho_l = rng.uniform(2000, 2600, layers)
+    shape = d.domain_shape
+    idx = np.minimum(np.arange(shape[1]) * layers // shape[1], layers - 1)
+    vp = np.broadcast_to(vp_l[idx][None, :, None], shape)
+    rho = np.broadcast_to(rho_l[idx][None, :, None], shape)
+    mu = rho * (vp / 3 ** 0.5) ** 2
+    lam = rho * vp ** 2 - 2 * mu
+    for name, arr in (("lambda", lam), ("mu", mu), ("buoy", 1.0 / rho)):
+        d.upload(np.ascontiguousarray(arr, np.float32), field=name)
+    zero = np.zeros(shape, np.float32)
+    for k in range(9):
+        d.upload(zero, field=k)
+    dt = d.cfg.dt
+    t = np.arange(wl["sub_steps"] * 64) * dt - 1.2 / 10.0
+    a = (np.pi * 10.0 * t) ** 2
+    d.set_source((1e6 * dt * (1 - 2 * a) * np.exp(-a)).astype(np.float32))
+    return zero
+
+
+def run_ours(args, wl):
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    import __graft_entry__
+    if rank == 0 or world == 1:
+        __graft_entry__.build()
+    if world > 1:
+        dist.barrier()
+    import b2r_gb300 as b2r
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    stream = torch.cuda.Stream(device=dev)
+    d = make_domain(b2r, wl, stream)
+    host = load_inputs(d, wl, torch, dev)
+    d.synchronize()
+    n = wl["sub_steps"]
+    cells = wl["env"][0] * wl["env"][1] * wl["env"][2]
+    small = config_of(args, wl)["l2"] != "inputs larger than L2"
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev) if small else None
+
+    for _ in range(args.warmup):
+        d.step(n)
+    d.synchronize()
+
+    # ---- device-resident timed region
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize(dev)
+    l0 = b2r.kernel_launches()
+    total_ms = 0.0
+    if small:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            d.step(n)
+            e1.record(stream)
+            e1.synchronize()
+            total_ms += e0.elapsed_time(e1)
+    else:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            d.step(n)
+        e1.record(stream)
+        e1.synchronize()
+        total_ms = e0.elapsed_time(e1)
+    launches = b2r.kernel_launches() - l0
+    d.synchronize()
+    torch.cuda.synchronize(dev)
+    barrier()
+    clk = clocks.stop()
+    t = torch.tensor([total_ms], device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item()) / args.steps
+    value = world * cells * n / (ms / 1000.0) / 1e9
+
+    # ---- e2e through the C ABI with pinned host buffers
+    e2e_val, h2d, d2h = None, 0, 0
+    if wl["model"] in (1, 2):
+        pin_in = torch.from_numpy(host).pin_memory()
+        pin_out = torch.empty_like(pin_in).pin_memory()
+        d.run_host(pin_in, n, pin_out)              # warm
+        barrier()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            d.run_host(pin_in, n, pin_out)
+        torch.cuda.synchronize(dev)
+        barrier()
+        te = torch.tensor([(time.perf_counter() - t0) * 1000.0], device=dev)
+        if world > 1:
+            dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        ems = float(te.item()) / args.steps
+        e2e_val = world * cells * n / (ems / 1000.0) / 1e9
+        h2d = d2h = host.nbytes
+
+    # ---- roofline of the dominant kernel
+    peak, peak_src = measured_peak()
+    per_launch_ms = ms / max(1, launches / args.steps) if wl["model"] == 1 else None
+    roof = None
+    if wl["model"] == 1:
+        algo = wl["bytes_per_cell"] * cells
+        achieved = algo / (per_launch_ms / 1000.0) / 1e9
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": profiled_traffic(args.workload),
+                "peak_source": peak_src, "kernel": wl["kernel"],
+                "algorithmic_bytes_per_launch": algo}
+    elif wl["model"] == 2:
+        algo = wl["bytes_per_cell"] * cells * n
+        achieved = algo / (ms / 1000.0) / 1e9
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": profiled_traffic(args.workload),
+                "peak_source": peak_src, "kernel": wl["kernel"],
+                "note": "whole-step average incl. halo exchanges; the 33.5 MB working set is L2-resident"}
+    else:
+        algo = wl["bytes_per_cell"] * cells * n
+        achieved = algo / (ms / 1000.0) / 1e9
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": profiled_traffic(args.workload),
+                "peak_source": peak_src, "kernel": wl["kernel"], "note": "whole-step average"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, kind, cores, sample = cpu_sample(wl, budget_s=10.0)
+        cpu = {"value": round(v, 4), "unit": "GLUPS", "cores": cores, "kind": kind, "sample": sample}
+
+    if rank == 0:
+        line = {"metric": "GLUPS", "value": round(value, 3), "unit": "GLUPS", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "u8" if wl["model"] == 2 else "f32",
+                "data": "synthetic (seeded U[0,1) / Bernoulli(0.3) / layered model)",
+                "config": config_of(args, wl),
+                "e2e": ({"value": round(e2e_val, 3), "unit": "GLUPS", "h2d_bytes_per_step": h2d,
+                         "d2h_bytes_per_step": d2h} if e2e_val is not None else None),
+                "gpu_launches": int(launches),
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clk}
+        print(json.dumps(line), flush=True)
+    d.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def profiled_traffic(workload):
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p)).get(workload)
+        except Exception:
+            return None
+    return None
+
+
+def main():
+    args = parse()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, wl)
+    else:
+        run_ours(args, wl)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,163 @@
+/*
+ * b2r.h -- C ABI of libb2r: the B2R stencil hot path on one GB300 (sm_103a).
+ *
+ * Plain C: pointers, sizes and ints only.  A cudaStream_t is passed as
+ * void*.  Every entry point returns a b2r_status; nothing calls exit().
+ *
+ * Model: the global domain of env[0] x env[1] x env[2] interior cells is
+ * tiled by blocks[0] x blocks[1] x blocks[2] subdomains (the reference's
+ * BLOCK_DIM_X/Y/Z, b2r.cpp:139-146), each stored on the device as a padded
+ * block of (B + 2H) cells per axis with B = env/blocks and halo depth
+ * H = R * (cells consumed by one time step) -- the reference's
+ * B2R_BLOCK_SIZE_* = B + 2*B2R_D*B2R_R (b2r.cpp:61-64).  One period = one
+ * halo exchange between the resident subdomains (device-side
+ * boundary_updating, b2r_halo_sync.cu:442) followed by R time steps during
+ * which the valid region of every block shrinks (heat-3D.cu:191).
+ *
+ * Host data layout (identical to the reference, heat-3D.cpp:42-45): x
+ * fastest, index z*nx*ny + y*nx + x.  A "domain array" is the global field:
+ * for B2R_BC_SHELL it carries a fixed shell of `shell` = D cells around the
+ * interior ((env+2D) cells per axis, e.g. 130^3 for a 128^3 heat interior);
+ * for B2R_BC_PERIODIC it is the bare torus (env cells per axis).
+ */
+#ifndef B2R_H
+#define B2R_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    B2R_OK = 0,
+    B2R_ERR_ARG = 1,      /* invalid argument or configuration */
+    B2R_ERR_CUDA = 2,     /* a CUDA runtime call failed */
+    B2R_ERR_OOM = 3,      /* device allocation failed */
+    B2R_ERR_TIMEOUT = 4,  /* a bounded device-side wait gave up */
+    B2R_ERR_STATE = 5     /* call not valid in the handle's current state */
+} b2r_status;
+
+typedef enum {
+    B2R_MODEL_HEAT = 1,       /* fdm_heat_diffuse_delta1..4 (heat-3D.cu:173-521) */
+    B2R_MODEL_GOL = 2,        /* gol_3d_kernel (gol-3D.cu:30-102) */
+    B2R_MODEL_EQWP_REF = 3,   /* eqwp_fd4_stress + eqwp_fd4_v{x,y,z} (eqwp.cu:60-477) */
+    B2R_MODEL_EQWP_STAG = 4   /* staggered-grid FD4 elastic wave, layered material */
+} b2r_model;
+
+typedef enum { B2R_BC_SHELL = 0, B2R_BC_PERIODIC = 1 } b2r_boundary;
+
+/* Field ids.  Heat and GoL have one field (0).  Elastic wave: */
+enum {
+    B2R_F_VX = 0, B2R_F_VY, B2R_F_VZ, B2R_F_SXX, B2R_F_SXY, B2R_F_SXZ,
+    B2R_F_SYY, B2R_F_SYZ, B2R_F_SZZ, B2R_F_DISP,      /* 9: displacement (REF) */
+    B2R_F_LAMBDA = 16, B2R_F_MU = 17, B2R_F_BUOY = 18 /* material (STAG) */
+};
+
+typedef struct {
+    int model;          /* b2r_model */
+    int env[3];         /* ENV_DIM_X/Y/Z (b2r_config.h:6-8) */
+    int blocks[3];      /* BLOCK_DIM_X/Y/Z; env[a] % blocks[a] == 0 (b2r.cpp:154) */
+    int R;              /* B2R_R >= 1; R*D <= min(B)/2 (b2r.cpp:54) */
+    int D;              /* stencil radius: heat 1..4 (B2R_D), GoL 1, eqwp 2 */
+    int boundary;       /* b2r_boundary */
+    /* heat: u += alpha_dt*(Lx/dx^2 + Ly/dy^2 + Lz/dz^2) (heat-3D.cu:228-231) */
+    double alpha_dt, dx, dy, dz;
+    /* eqwp STAG: time step and grid spacing; source cell (global interior
+       coordinates) for the explosive source */
+    double dt, h;
+    int src[3];
+} b2r_config;
+
+typedef struct b2r_handle b2r_handle;
+
+/* ---- life cycle ------------------------------------------------------- */
+/* Validates cfg as simu_env_init does (b2r.cpp:47-67, 154-159) and allocates
+ * every device field.  Replaces b2r_sync_init (b2r_halo_sync.cu:74) and
+ * eqwp_cuda_init (eqwp.cu:515). */
+b2r_status b2r_create(const b2r_config* cfg, b2r_handle** out);
+/* Replaces b2r_sync_finalize (b2r_halo_sync.cu:121) / eqwp_cuda_finalize
+ * (eqwp.cu:592). */
+b2r_status b2r_destroy(b2r_handle* h);
+const char* b2r_last_error(const b2r_handle* h);
+/* All work of the handle is enqueued on this stream (default: legacy 0). */
+b2r_status b2r_set_stream(b2r_handle* h, void* cuda_stream);
+b2r_status b2r_synchronize(b2r_handle* h);
+
+/* Geometry: padded block size per axis, halo depth H, host domain size per
+ * axis, bytes per cell. */
+b2r_status b2r_geometry(const b2r_handle* h, int block_n[3], int* halo,
+                        int domain_n[3], int* cell_bytes);
+/* Cells advanced per time step over the whole domain (env product). */
+int64_t b2r_cells(const b2r_handle* h);
+
+/* ---- data movement ------------------------------------------------------ */
+/* Load a domain array into every block (interiors, halos and shell).
+ * src_is_device: 0 = host memory (pinned recommended), 1 = device memory.
+ * Resets the time-step counter to 0. */
+b2r_status b2r_upload(b2r_handle* h, int field, const void* src, int src_is_device);
+/* Gather the block interiors (and the shell) into a domain array. */
+b2r_status b2r_download(b2r_handle* h, int field, void* dst, int dst_is_device);
+
+/* Copy every padded block of a field, halos included, into a dense array of
+ * blocks*Ngz*Ngy*Ngx cells (block index slowest, x fastest) -- the per-rank
+ * blocks of the reference (B2R_BLOCK_SIZE_*, b2r.h:81-85) side by side. */
+b2r_status b2r_download_blocks(b2r_handle* h, int field, void* dst, int dst_is_device);
+
+/* ---- time stepping ------------------------------------------------------ */
+/* Advance nsteps time steps: periods of one halo exchange of every field
+ * (b2r.cpp:197-206) and R steps (b2r.cpp:215); a trailing partial period
+ * runs fewer steps.  Asynchronous on the handle's stream. */
+b2r_status b2r_step(b2r_handle* h, int nsteps);
+/* Upload, b2r_step, download: the whole job through host buffers. */
+b2r_status b2r_run_host(b2r_handle* h, int field, const void* host_in, int nsteps,
+                        void* host_out);
+/* Time steps done since the last upload. */
+int64_t b2r_time_step(const b2r_handle* h);
+
+/* Explosive source of the staggered model: amps[t] is added to sxx, syy and
+ * szz of the source cell (cfg.src) after the stress update of time step t
+ * (t < n).  Copied; n = 0 clears it. */
+b2r_status b2r_set_source(b2r_handle* h, const float* amps, int n);
+
+/* ---- B2R boundary update (b2r_halo_sync.cu) ------------------------------ */
+/* Device-side X->Y->Z halo exchange of one field between the resident
+ * subdomains.  _direct copies neighbour slabs straight into the halos
+ * (boundary_updating_direct, b2r_halo_sync.cu:389-431); the staged form packs
+ * every face slab into a device bounce buffer and unpacks it
+ * (sub_matrix_pack/unpack_{x,y,z} + boundary_updating,
+ * b2r_halo_sync.cu:195-379, 442-508).  Both give identical halos.
+ * time_step is the reference's message-tag argument; it is recorded only. */
+b2r_status b2r_boundary_updating_direct(b2r_handle* h, int time_step, int field);
+b2r_status b2r_boundary_updating(b2r_handle* h, int time_step, int field);
+
+/* Number of CUDA kernels this library has launched in this process. */
+int64_t b2r_kernel_launches(void);
+
+/* ---- reference-shaped per-block entries ---------------------------------- */
+/* heat_3D_gpu_main (heat-3D.cu:583): R sub-steps of the order-D heat
+ * stencil on one padded host block of Ngx*Ngy*Ngz cells with shrinking
+ * region [D(i+1), N-1-D(i+1)], then the planes [R*D, Ngz-R*D) are copied
+ * back into h_in.  edge_flag[3] in {-1,0,1} per axis as the reference
+ * documents (-1 low face on the domain boundary, 1 high face, 0 inside);
+ * NULL means 0,0,0.  On a boundary face the H = R*D deep halo is not updated
+ * (fdm_heat_diffuse_delta1_verify, heat-3D.cu:81-114).  *gpu_seconds (may be
+ * NULL) receives the device time of the sub-steps (cudaEvent, as
+ * heat-3D.cu:595-641).  Coefficients as in b2r_config. */
+b2r_status b2r_heat_3D_gpu_main(float* h_in, int R, int D, const char* edge_flag,
+                                int Ngx, int Ngy, int Ngz, double alpha_dt,
+                                double dx, double dy, double dz, void* cuda_stream,
+                                double* gpu_seconds);
+/* gol_3D_gpu_main (gol-3D.cu:119): R generations on one padded host block,
+ * region [i+1, N-2-i]; the whole block is copied back (gol-3D.cu:149). */
+b2r_status b2r_gol_3D_gpu_main(uint8_t* h_in, int R, const char* edge_flag, int Ngx,
+                               int Ngy, int Ngz, void* cuda_stream, double* gpu_seconds);
+/* eqwp_gpu_main (eqwp.cu:661): R steps of the reference elastic-wave model on
+ * the handle's fields (model B2R_MODEL_EQWP_REF), ts = the outer time step
+ * (selects the body force, eqwp.cu:135).  Does not exchange halos. */
+b2r_status b2r_eqwp_gpu_main(b2r_handle* h, int ts, int R, double* gpu_seconds);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

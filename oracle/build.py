@@ -1,0 +1,60 @@
+"""Build recipe for the oracle (test infrastructure only).
+
+* ``liborc.so``  -- the CPU restatement in b2r_oracle.c (always built).
+* ``_ref/libheat_ref.so`` -- the reference's own heat-3D.cpp compiled from
+  its source tree, with a two-line config shim for its
+  ``#include "../b2r_config.h"`` (heat-3D.cpp:16) and
+  ``CPU_N_THRD`` (used at heat-3D.cpp:51,66,87,111, defined nowhere in the
+  reference) set to the OpenMP runtime thread count.  Built only where the
+  reference source tree is present; the output stays in ``oracle/_ref/``.
+
+Both are compiled with ``-ffp-contract=off`` so float/double expressions are
+evaluated exactly as written on x86-64 and aarch64.
+"""
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_SRC = os.environ.get("B2R_REFERENCE_SRC", "/root/reference")
+CFLAGS = ["-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"]
+
+
+def _newer(out, srcs):
+    if not os.path.exists(out):
+        return False
+    t = os.path.getmtime(out)
+    return all(os.path.getmtime(s) <= t for s in srcs)
+
+
+def build_oracle(force=False):
+    src = os.path.join(HERE, "b2r_oracle.c")
+    out = os.path.join(HERE, "liborc.so")
+    hdr = os.path.join(HERE, "b2r_oracle.h")
+    if force or not _newer(out, [src, hdr]):
+        subprocess.check_call(["gcc", "-std=gnu11", *CFLAGS, "-o", out, src, "-lm"])
+    return out
+
+
+def build_ref(force=False):
+    """Compile the reference's heat-3D.cpp; returns the .so path or None."""
+    ref = os.path.join(REF_SRC, "heat-3D.cpp")
+    if not os.path.exists(ref):
+        return None
+    refdir = os.path.join(HERE, "_ref")
+    inc = os.path.join(refdir, "inc")
+    sub = os.path.join(inc, "sub")
+    os.makedirs(sub, exist_ok=True)
+    with open(os.path.join(inc, "b2r_config.h"), "w") as f:
+        f.write("#pragma once\n#define B2R_D 1\n")
+    wrap = os.path.join(HERE, "ref_shim", "heat_ref_wrap.cpp")
+    out = os.path.join(refdir, "libheat_ref.so")
+    if force or not _newer(out, [ref, wrap]):
+        subprocess.check_call(["g++", *CFLAGS, "-I", sub, "-include", "omp.h",
+                               "-DCPU_N_THRD=omp_get_max_threads()",
+                               "-o", out, ref, wrap])
+    return out
+
+
+if __name__ == "__main__":
+    print(build_oracle(force=True))
+    print(build_ref(force=True))

@@ -1,0 +1,101 @@
+"""GPU elastic-wave models against the oracle (relative L2 <= 1e-5)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+NAMES = ["vx", "vy", "vz", "sxx", "sxy", "sxz", "syy", "syz", "szz", "disp"]
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def ref_force(env, shell=2):
+    """Force patch of eqwp.cu:135,561-566 (reference block Ng = B+4, R = 1),
+    in domain-array coordinates with a `shell`-deep shell."""
+    ngx, ngz = env[0] + 4, env[2] + 4
+    return dict(fy=shell + env[1] - 7, fx0=shell + ngx // 2 - 2, fx1=shell + ngx // 2 + ngx // 10 - 2,
+                fz0=shell + ngz // 2 - 2, fz1=shell + ngz // 2 + ngz // 10 - 2, fval=-1e4, fsteps=50)
+
+
+@pytest.mark.parametrize("env", [(40, 32, 24), (70, 20, 33)])
+def test_eqwp_ref_matches_oracle(b2r, orc, env):
+    nsteps = 30
+    shape = tuple(e + 4 for e in env[::-1])
+    rng = np.random.default_rng(3)
+    init = [np.zeros(shape, np.float32) for _ in range(10)]
+    for k in range(9):   # small random start so every term is exercised
+        init[k][2:-2, 2:-2, 2:-2] = ((rng.random(env[::-1]) - 0.5) * 1e-2).astype(np.float32)
+    with b2r.Domain(b2r.MODEL_EQWP_REF, env, D=2, R=1) as d:
+        for k in range(10):
+            d.upload(init[k], field=k)
+        d.step(nsteps)
+        got = [d.download(field=k) for k in range(10)]
+        d.synchronize()
+    ref = [a.copy() for a in init]
+    ref64 = [a.astype(np.float64) for a in init]
+    force = ref_force(env)
+    for ts in range(nsteps):
+        orc.eqwp_ref_substep(ref, 0, 2, 63, ts, force)
+        orc.eqwp_ref_substep(ref64, 0, 2, 63, ts, force)
+    for k in range(10):
+        r32, r64 = rel_l2(got[k], ref[k]), rel_l2(got[k], ref64[k])
+        print(f"{NAMES[k]}: rel-L2 vs oracle FP32 {r32:.2e}, vs FP64 {r64:.2e}")
+        assert r32 <= TOL, NAMES[k]
+
+
+def layered(env, seed=3, layers=8):
+    """8 horizontal layers (along y): vp U[2000,4000], vs = vp/sqrt(3), rho U[2000,2600]."""
+    rng = np.random.default_rng(seed)
+    vp_l = rng.uniform(2000, 4000, layers)
+    rho_l = rng.uniform(2000, 2600, layers)
+    ny = env[1] + 4
+    idx = np.minimum(np.arange(ny) * layers // ny, layers - 1)
+    shape = tuple(e + 4 for e in env[::-1])
+    vp = np.broadcast_to(vp_l[idx][None, :, None], shape)
+    rho = np.broadcast_to(rho_l[idx][None, :, None], shape)
+    vs = vp / np.sqrt(3.0)
+    mu = rho * vs ** 2
+    lam = rho * vp ** 2 - 2 * mu
+    return [np.ascontiguousarray(m, np.float64) for m in (lam, mu, 1.0 / rho)]
+
+
+def ricker(n, dt, f0, amp):
+    t = np.arange(n) * dt - 1.2 / f0
+    a = (np.pi * f0 * t) ** 2
+    return amp * (1 - 2 * a) * np.exp(-a)
+
+
+@pytest.mark.parametrize("blocks,R", [((1, 1, 1), 1), ((2, 2, 1), 2), ((2, 1, 2), 1)])
+def test_eqwp_stag_matches_oracle(b2r, orc, blocks, R):
+    env = (48, 40, 32)
+    nsteps = 40
+    h = 10.0
+    mat = layered(env)
+    dt = 0.5 * h / (4000 * np.sqrt(3) * (9 / 8 + 1 / 24))
+    src = (env[0] // 2, env[1] // 2, env[2] // 2)
+    amps = ricker(nsteps, dt, 10.0, 1e6 * dt).astype(np.float32)
+    with b2r.Domain(b2r.MODEL_EQWP_STAG, env, blocks=blocks, R=R, D=2, dt=dt, h=h, src=src) as d:
+        for m, name in enumerate(["lambda", "mu", "buoy"]):
+            d.upload(mat[m].astype(np.float32), field=name)
+        zero = np.zeros(d.domain_shape, np.float32)
+        for k in range(9):
+            d.upload(zero, field=k)
+        d.set_source(amps)
+        d.step(nsteps)
+        got = [d.download(field=k) for k in range(9)]
+        d.synchronize()
+    f = [np.zeros(zero.shape, np.float32) for _ in range(9)]
+    f64 = [np.zeros(zero.shape, np.float64) for _ in range(9)]
+    m32 = [np.ascontiguousarray(m.astype(np.float32)) for m in mat]
+    sc = tuple(s + 2 for s in src)
+    for t in range(nsteps):
+        orc.eqwp_stag_step(f, m32, dt, h, 0, 2, 63, sc, float(amps[t]))
+        orc.eqwp_stag_step(f64, mat, dt, h, 0, 2, 63, sc, float(amps[t]))
+    for k in range(9):
+        r32, r64 = rel_l2(got[k], f[k]), rel_l2(got[k], f64[k])
+        print(f"{NAMES[k]} blocks={blocks} R={R}: vs FP32 {r32:.2e}, vs FP64 {r64:.2e}")
+        assert r32 <= TOL, NAMES[k]

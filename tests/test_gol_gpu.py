@@ -1,0 +1,69 @@
+"""GPU Game of Life: bit-exact against the oracle (integer work)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def bernoulli(env, p, seed):
+    rng = np.random.default_rng(seed)
+    return (rng.random(env[::-1]) < p).astype(np.uint8)
+
+
+@pytest.mark.parametrize("env,blocks,R", [((64, 64, 64), (2, 2, 2), 4), ((64, 48, 40), (1, 1, 1), 1),
+                                          ((70, 36, 50), (2, 3, 1), 2), ((33, 17, 9), (1, 1, 1), 3)])
+def test_gol_periodic_bit_exact_every_period(b2r, orc, env, blocks, R):
+    dom = bernoulli(env, 0.3, 2)
+    ref = dom.copy()
+    with b2r.Domain(b2r.MODEL_GOL, env, blocks=blocks, R=R, D=1, boundary=b2r.BC_PERIODIC) as d:
+        d.upload(dom)
+        for period in range(3):
+            d.step(R)
+            orc.gol_run_periodic(ref, R)
+            got = d.download()
+            assert np.array_equal(got, ref), f"period {period}"
+        d.synchronize()
+
+
+def test_gol_invariant_in_R_and_blocks(b2r):
+    env = (48, 48, 48)
+    dom = bernoulli(env, 0.3, 4)
+    outs = []
+    for blocks, R in [((1, 1, 1), 1), ((2, 2, 2), 1), ((2, 2, 2), 2), ((2, 2, 2), 4), ((1, 2, 3), 4)]:
+        with b2r.Domain(b2r.MODEL_GOL, env, blocks=blocks, R=R, D=1, boundary=b2r.BC_PERIODIC) as d:
+            d.upload(dom)
+            d.step(12)
+            outs.append(d.download())
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+
+
+def test_gol_fixed_shell(b2r, orc):
+    env = (40, 30, 20)
+    dom = np.zeros(tuple(e + 2 for e in env[::-1]), np.uint8)
+    dom[1:-1, 1:-1, 1:-1] = bernoulli(env, 0.35, 6)
+    dom[0] = 1                                   # a live shell face stays live
+    with b2r.Domain(b2r.MODEL_GOL, env, blocks=(2, 1, 2), R=2, D=1) as d:
+        d.upload(dom)
+        d.step(6)
+        got = d.download()
+    a, b = dom.copy(), dom.copy()
+    for _ in range(6):
+        orc.gol_substep(a, b, 0, 1, 63)
+        a, b = b, a
+    assert np.array_equal(got, a)
+
+
+@pytest.mark.parametrize("R", [1, 2, 4])
+def test_gol_3D_gpu_main_block_entry(b2r, orc, R):
+    rng = np.random.default_rng(R)
+    blk = (rng.random((21, 37, 45)) < 0.3).astype(np.uint8)
+    got = blk.copy()
+    b2r.gol_3D_gpu_main(got, R)
+    a, b = blk.copy(), blk.copy()
+    for i in range(R):
+        orc.gol_substep(a, b, i, R, 0)
+        a, b = b, a
+    # the valid interior after R generations is bit-exact
+    s = (slice(R, -R),) * 3
+    assert np.array_equal(got[s], a[s])

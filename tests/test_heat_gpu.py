@@ -1,0 +1,134 @@
+"""GPU parity of the heat kernels (delta1-4) against the oracle.
+
+Tolerance: FP32 on the GPU vs the oracle's FP32-storage restatement of the
+reference arithmetic: relative L2 <= 1e-5 (the benchmark spec's bound).  The
+oracle itself is bit-exact to the reference's heat_3D_cpu_main (see
+test_oracle.py), so the chain GPU ~ oracle == reference holds.  Each case also
+reports the error against the FP64 run of the same scheme.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+TOL = 1e-5
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def shell_domain(env, D, seed):
+    dom = np.zeros(tuple(e + 2 * D for e in env[::-1]), np.float32)
+    rng = np.random.default_rng(seed)
+    dom[D:-D, D:-D, D:-D] = rng.random(env[::-1], dtype=np.float32)
+    return dom
+
+
+def run_gpu(b2r, dom, env, D, nsteps, coef, blocks=(1, 1, 1), R=1):
+    with b2r.Domain(b2r.MODEL_HEAT, env, blocks=blocks, R=R, D=D, alpha_dt=coef[0], dx=coef[1],
+                    dy=coef[2], dz=coef[3]) as d:
+        assert d.domain_shape == dom.shape
+        d.upload(dom)
+        d.step(nsteps)
+        out = d.download()
+        d.synchronize()
+    return out
+
+
+@pytest.mark.parametrize("D", [1, 2, 3, 4])
+@pytest.mark.parametrize("env", [(64, 48, 40), (131, 37, 29), (257, 20, 12)])
+def test_heat_domain_matches_oracle(b2r, orc, D, env):
+    coef = (0.1, 1.0, 1.0, 1.0) if D == 1 else (0.02, 1.0, 1.3, 0.9)
+    dom = shell_domain(env, D, 100 + D)
+    got = run_gpu(b2r, dom, env, D, 12, coef)
+    ref = dom.copy()
+    orc.heat_run(ref, D, D, 12, *coef)
+    ref64 = dom.astype(np.float64)
+    orc.heat_run(ref64, D, D, 12, *coef)
+    r32, r64 = rel_l2(got, ref), rel_l2(got, ref64)
+    print(f"D={D} env={env}: rel-L2 vs oracle FP32 {r32:.2e}, vs FP64 {r64:.2e}")
+    assert r32 <= TOL and r64 <= TOL
+    # the fixed shell is never written
+    s = np.ones(dom.shape, bool)
+    s[D:-D, D:-D, D:-D] = False
+    assert np.array_equal(got[s], dom[s])
+
+
+def test_heat_matches_reference_fixture(b2r):
+    g = np.load(os.path.join(GOLD, "heat_d1_small.npz"))
+    dom = g["in_shell"]
+    env = tuple(n - 2 for n in dom.shape[::-1])
+    got = run_gpu(b2r, dom, env, 1, 10, (0.1 * 0.1, 1.0, 1.0, 0.5))
+    assert rel_l2(got, g["out_r1x10"]) <= TOL
+
+
+@pytest.mark.parametrize("coef", [(0.1 * 0.1, 1.0, 1.0, 0.5), (0.1, 1.0, 1.0, 1.0)])
+def test_heat_128_config(b2r, orc, coef):
+    """128^3 interior, 100 steps, R=1: the reference's constants and the
+    isotropic alpha*dt/dx^2 = 0.1 of the benchmark configuration."""
+    meta = json.load(open(os.path.join(GOLD, "heat_d1_cfg128.json")))
+    dom = np.zeros((130, 130, 130), np.float32)
+    rng = np.random.default_rng(meta["seed"])
+    dom[1:-1, 1:-1, 1:-1] = rng.random((128, 128, 128), dtype=np.float32)
+    got = run_gpu(b2r, dom, (128, 128, 128), 1, 100, coef)
+    ref = dom.copy()
+    orc.heat_run(ref, 1, 1, 100, *coef)
+    r = rel_l2(got, ref)
+    print(f"128^3 x100 coef={coef}: rel-L2 {r:.2e}")
+    assert r <= TOL
+    if coef[3] == 0.5:
+        assert abs(got.astype(np.float64).sum() - meta["sum_out"]) / meta["sum_out"] < 1e-5
+
+
+@pytest.mark.parametrize("D,R,blocks", [(1, 2, (2, 2, 2)), (1, 4, (4, 1, 2)), (2, 3, (2, 2, 1)),
+                                        (3, 1, (1, 2, 2)), (4, 2, (2, 1, 1))])
+def test_heat_invariant_in_R_and_blocks(b2r, D, R, blocks):
+    env = (96, 48, 64)
+    coef = (0.02, 1.0, 1.0, 0.8)
+    dom = shell_domain(env, D, 5)
+    one = run_gpu(b2r, dom, env, D, 11, coef)
+    many = run_gpu(b2r, dom, env, D, 11, coef, blocks=blocks, R=R)
+    # every cell is computed by the same instructions from the same inputs
+    assert np.array_equal(one, many)
+
+
+@pytest.mark.parametrize("R,ef", [(1, None), (3, None), (2, (-1, 0, 1)), (3, (1, -1, 0))])
+def test_heat_3D_gpu_main_block_entry(b2r, orc, R, ef):
+    """heat-3D.cu:583 semantics: R shrinking sub-steps on one padded block,
+    planes [R*D, Ngz-R*D) copied back."""
+    rng = np.random.default_rng(R)
+    blk = rng.random((30, 26, 41), dtype=np.float32)
+    got = blk.copy()
+    b2r.heat_3D_gpu_main(got, R, D=1, edge_flag=ef)
+    # oracle: same ping-pong, region and copy-back
+    edge = 0
+    if ef:
+        for a in range(3):
+            edge |= (1 << (2 * a)) if ef[a] < 0 else 0
+            edge |= (1 << (2 * a + 1)) if ef[a] > 0 else 0
+    a, b = blk.copy(), blk.copy()
+    for i in range(R):
+        orc.heat_substep(a, b, 1, i, R, edge, **orc.REF_HEAT)
+        a, b = b, a
+    ref = blk.copy()
+    ref[R:-R] = a[R:-R]
+    assert rel_l2(got, ref) <= TOL
+    # untouched planes stay bit-identical
+    assert np.array_equal(got[:R], blk[:R]) and np.array_equal(got[-R:], blk[-R:])
+
+
+def test_run_host_roundtrip(b2r, orc):
+    env = (40, 40, 40)
+    dom = shell_domain(env, 1, 9)
+    out = np.empty_like(dom)
+    with b2r.Domain(b2r.MODEL_HEAT, env, D=1, alpha_dt=0.1) as d:
+        d.run_host(dom, 5, out)
+    ref = dom.copy()
+    orc.heat_run(ref, 1, 1, 5, 0.1, 1.0, 1.0, 1.0)
+    assert rel_l2(out, ref) <= TOL
