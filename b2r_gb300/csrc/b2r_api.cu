@@ -557,8 +557,10 @@ int edge_from_flags(const char* ef)
     if (!ef) return 0;
     int e = 0;
     for (int a = 0; a < 3; ++a) {
-        if (ef[a] < 0) e |= 1 << (2 * a);
-        if (ef[a] > 0) e |= 1 << (2 * a + 1);
+        // plain char is unsigned on aarch64: read the flags as signed bytes
+        const signed char v = static_cast<signed char>(ef[a]);
+        if (v < 0) e |= 1 << (2 * a);
+        if (v > 0) e |= 1 << (2 * a + 1);
     }
     return e;
 }
