@@ -152,6 +152,24 @@ b2r_status b2r_heat_3D_gpu_main(float* h_in, int R, int D, const char* edge_flag
  * region [i+1, N-2-i]; the whole block is copied back (gol-3D.cu:149). */
 b2r_status b2r_gol_3D_gpu_main(uint8_t* h_in, int R, const char* edge_flag, int Ngx,
                                int Ngy, int Ngz, void* cuda_stream, double* gpu_seconds);
+/* No counterpart in the reference.  The computation of b2r_heat_3D_gpu_main
+ * for callers that cannot allocate device memory -- e.g. code running inside
+ * a framework that owns all device memory through its own pool and forbids
+ * raw cudaMalloc/cudaFree (whose implicit device-wide synchronisation would
+ * stall its other streams).  d_in and d_out are device blocks of
+ * Ngx*Ngy*Ngz floats (may be the same block); on return d_out holds d_in
+ * with planes [R*D, Ngz-R*D) replaced by the result of R sub-steps.  The
+ * ping-pong blocks live in a fixed 32 MiB device array inside the library
+ * (held by every GPU that loads it until exit): blocks whose padded size
+ * exceeds 4,194,304 cells per buffer (about 160^3) are rejected with
+ * B2R_ERR_ARG and a message on stderr.  All calls share that array, so calls
+ * that overlap on the GPU race; the first call on each device looks up the
+ * array's address and should come before any stream capture.  Synchronous
+ * on cuda_stream; allocates nothing. */
+b2r_status b2r_heat_3D_gpu_main_noalloc(const float* d_in, float* d_out, int R, int D,
+                                        const char* edge_flag, int Ngx, int Ngy, int Ngz,
+                                        double alpha_dt, double dx, double dy, double dz,
+                                        void* cuda_stream);
 /* eqwp_gpu_main (eqwp.cu:661): R steps of the reference elastic-wave model on
  * the handle's fields (model B2R_MODEL_EQWP_REF), ts = the outer time step
  * (selects the body force, eqwp.cu:135).  Does not exchange halos. */
