@@ -43,6 +43,9 @@ WORKLOADS = {
     # alpha*dt/dx^2 = 0.1 on every axis, R = 1, one block
     "heat1_512": dict(model=1, env=(512, 512, 512), blocks=(1, 1, 1), R=1, D=1, sub_steps=100,
                       coef=(0.1, 1.0, 1.0, 1.0), bytes_per_cell=8, kernel="heat_sweep_kernel<1>"),
+    # the same kernel on 384^3 (226 MB per field, > L2): the profiling case
+    "heat1_384": dict(model=1, env=(384, 384, 384), blocks=(1, 1, 1), R=1, D=1, sub_steps=20,
+                      coef=(0.1, 1.0, 1.0, 1.0), bytes_per_cell=8, kernel="heat_sweep_kernel<1>"),
     # FP32 heat delta4 (fdm_heat_diffuse_delta4), 512^3
     "heat4_512": dict(model=1, env=(512, 512, 512), blocks=(1, 1, 1), R=1, D=4, sub_steps=100,
                       coef=(0.02, 1.0, 1.0, 1.0), bytes_per_cell=8, kernel="heat_sweep_kernel<4>"),
