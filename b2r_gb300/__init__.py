@@ -73,6 +73,7 @@ def lib():
         "b2r_download": ([vp, i, vp, i], i),
         "b2r_download_blocks": ([vp, i, vp, i], i),
         "b2r_step": ([vp, i], i),
+        "b2r_set_graphs": ([vp, i], i),
         "b2r_run_host": ([vp, i, vp, i, vp], i),
         "b2r_time_step": ([vp], C.c_int64),
         "b2r_set_source": ([vp, C.POINTER(C.c_float), i], i),
@@ -177,6 +178,10 @@ class Domain:
         """stream: an int handle or a torch.cuda.Stream."""
         s = getattr(stream, "cuda_stream", stream)
         _check(lib().b2r_set_stream(self.h, C.c_void_p(int(s))), self.h)
+
+    def set_graphs(self, enable):
+        """Replay whole periods from CUDA graphs (needs a non-default stream)."""
+        _check(lib().b2r_set_graphs(self.h, 1 if enable else 0), self.h)
 
     def synchronize(self):
         _check(lib().b2r_synchronize(self.h), self.h)

@@ -43,6 +43,11 @@ struct b2r_handle {
     int* d_status = nullptr;
     long long ts = 0;
     bool halos_fresh = false;
+    // CUDA graphs of whole periods (heat, GoL on a non-default stream)
+    bool graphs = true;
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};   // by ping-pong buffer at start
+    int gsteps = 0;                                   // time steps per graph launch
+    long long gkernels = 0;                           // kernels per graph launch
     std::string err;
 };
 
@@ -206,7 +211,7 @@ b2r_status substep(b2r_handle* h, int i)
     switch (h->cfg.model) {
     case B2R_MODEL_HEAT:
         CK(h, launch_heat_substep(&h->tmap[h->cur], static_cast<float*>(h->buf[1 - h->cur]), h->L,
-                                  h->cfg.D, i, h->hc, h->d_status, h->stream, 0));
+                                  h->cfg.D, i, h->hc, h->d_status, h->stream));
         h->cur = 1 - h->cur;
         return B2R_OK;
     case B2R_MODEL_GOL:
@@ -232,6 +237,53 @@ b2r_status substep(b2r_handle* h, int i)
     default:
         return fail(h, B2R_ERR_ARG, "unknown model %d", h->cfg.model);
     }
+}
+
+void drop_graphs(b2r_handle* h)
+{
+    for (int c = 0; c < 2; ++c)
+        if (h->gexec[c]) {
+            cudaGraphExecDestroy(h->gexec[c]);
+            h->gexec[c] = nullptr;
+        }
+    h->gsteps = 0;
+}
+
+b2r_status run_period(b2r_handle* h)
+{
+    b2r_status st;
+    if ((st = exchange_all(h, false)) != B2R_OK) return st;
+    for (int i = 0; i < h->cfg.R; ++i)
+        if ((st = substep(h, i)) != B2R_OK) return st;
+    return B2R_OK;
+}
+
+// Capture `periods` whole periods starting from ping-pong buffer `c`.
+b2r_status capture_graph(b2r_handle* h, int c, int periods)
+{
+    const int save_cur = h->cur;
+    const long long save_ts = h->ts;
+    h->cur = c;
+    const long long k0 = b2r_kernel_launches();
+    CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    b2r_status st = B2R_OK;
+    for (int p = 0; p < periods && st == B2R_OK; ++p) st = run_period(h);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    const long long nk = b2r_kernel_launches() - k0;
+    b2r::count_launches(-nk);               // captured, not launched
+    h->cur = save_cur;
+    h->ts = save_ts;
+    if (st != B2R_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) return fail(h, B2R_ERR_CUDA, "stream capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&h->gexec[c], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(h, B2R_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    h->gkernels = nk;
+    return B2R_OK;
 }
 
 }  // namespace
@@ -360,6 +412,7 @@ b2r_status b2r_create(const b2r_config* cfg, b2r_handle** out)
 b2r_status b2r_destroy(b2r_handle* h)
 {
     if (!h) return B2R_OK;
+    drop_graphs(h);
     for (int b = 0; b < 2; ++b)
         if (h->buf[b]) cudaFree(h->buf[b]);
     for (int f = 0; f < kMaxFields; ++f)
@@ -503,14 +556,46 @@ b2r_status b2r_step(b2r_handle* h, int nsteps)
     if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
     if (nsteps < 0) return fail(h, B2R_ERR_ARG, "nsteps must be >= 0");
     b2r_status st;
-    for (int s = 0; s < nsteps; ++s) {
+    const bool use_graphs = h->graphs && h->stream != nullptr &&
+                            (h->cfg.model == B2R_MODEL_HEAT || h->cfg.model == B2R_MODEL_GOL);
+    int s = 0;
+    while (s < nsteps) {
         const int i = (int)(h->ts % h->cfg.R);
+        if (use_graphs && i == 0) {
+            // whole periods replayed from a graph: >= 32 time steps per launch
+            const int periods = (32 + h->cfg.R - 1) / h->cfg.R;
+            const int unit = periods * h->cfg.R;
+            if (nsteps - s >= unit) {
+                if (h->gsteps != unit) {
+                    drop_graphs(h);
+                    h->gsteps = unit;
+                }
+                if (!h->gexec[h->cur])
+                    if ((st = capture_graph(h, h->cur, periods)) != B2R_OK) return st;
+                CK(h, cudaGraphLaunch(h->gexec[h->cur], h->stream));
+                b2r::count_launches(h->gkernels);
+                if (unit & 1) h->cur = 1 - h->cur;
+                h->ts += unit;
+                h->halos_fresh = false;
+                s += unit;
+                continue;
+            }
+        }
         if (i == 0 && !h->halos_fresh)
             if ((st = exchange_all(h, false)) != B2R_OK) return st;
         h->halos_fresh = false;
         if ((st = substep(h, i)) != B2R_OK) return st;
         h->ts++;
+        ++s;
     }
+    return B2R_OK;
+}
+
+b2r_status b2r_set_graphs(b2r_handle* h, int enable)
+{
+    if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
+    h->graphs = enable != 0;
+    if (!h->graphs) drop_graphs(h);
     return B2R_OK;
 }
 
@@ -619,7 +704,7 @@ b2r_status b2r_heat_3D_gpu_main(float* h_in, int R, int D, const char* edge_flag
     cudaEventRecord(e0, st);
     int cur = 0;
     for (int i = 0; i < R; ++i) {   // heat-3D.cu:602-628
-        cudaError_t e = launch_heat_substep(&tm[cur], (float*)s.p[1 - cur], L, D, i, hc, d_status, st, 0);
+        cudaError_t e = launch_heat_substep(&tm[cur], (float*)s.p[1 - cur], L, D, i, hc, d_status, st);
         if (e != cudaSuccess) {
             cudaFree(d_status);
             return fail(nullptr, B2R_ERR_CUDA, "heat launch: %s", cudaGetErrorString(e));

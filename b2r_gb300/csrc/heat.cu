@@ -38,10 +38,23 @@ struct HeatCfg {
     static constexpr size_t SMEM = size_t(S) * SLOT * sizeof(float) + S * sizeof(uint64_t) + 16 + 128;
 };
 
+// Work schedule of one launch: the plane-tiles (block, tile row, tile
+// column, output plane) in that order are split into G equal contiguous
+// ranges, one per CTA, and G CTAs are all resident at once.  A range spans
+// at most a few tile columns, so every CTA streams about the same number of
+// planes and the launch has no partial last wave.
+struct HeatSched {
+    int ntx, nty, NZ;        // tile columns / rows per block, output planes per column
+    long long W;             // total plane-tiles
+};
+
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;"); }
+
 template <int D, int RY, int S>
 __global__ void __launch_bounds__(kThreads)
 heat_sweep_kernel(const __grid_constant__ CUtensorMap tin, float* __restrict__ out,
-                  const BlockLayout L, const int step_i, const int nzc, const HeatCoef C,
+                  const BlockLayout L, const int step_i, const HeatCoef C, const HeatSched sch,
                   int* __restrict__ status)
 {
     using Cfg = HeatCfg<D, RY, S>;
@@ -52,27 +65,6 @@ heat_sweep_kernel(const __grid_constant__ CUtensorMap tin, float* __restrict__ o
     int& abort_flag = *reinterpret_cast<int*>(bar + S);
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
-    const int edge = edge_bits(L, blk);
-    int lo[3], hi[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) stage_region(L, edge, a, D * (step_i + 1), lo[a], hi[a]);
-
-    const int xs_begin = (L.xoff + D) & ~3;
-    const int xs0 = xs_begin + blockIdx.x * kTX;        // storage x of tile column 0
-    const int y0 = D + blockIdx.y * Cfg::TY;            // block y of tile row 0
-    // uniform early exits (before any barrier is initialised)
-    if (xs0 - L.xoff > hi[0] || xs0 + kTX - 1 - L.xoff < lo[0]) return;
-    if (y0 > hi[1] || y0 + Cfg::TY - 1 < lo[1]) return;
-    const int nz_out = hi[2] - lo[2] + 1;
-    const int per = (nz_out + nzc - 1) / nzc;
-    const int zs = lo[2] + zc * per;
-    const int ze = min(hi[2], zs + per - 1);
-    if (nz_out <= 0 || zs > ze) return;
-
-    const int first = zs - D;                 // first input plane
-    const int np = (ze + D) - first + 1;      // input planes streamed
-
     if (tid == 0) {
         abort_flag = 0;
 #pragma unroll
@@ -80,125 +72,190 @@ heat_sweep_kernel(const __grid_constant__ CUtensorMap tin, float* __restrict__ o
         fence_mbar_init();
     }
     __syncthreads();
-    if (tid == 0) {
-        for (int s = 0; s < S && s < np; ++s) {
-            mbar_expect_tx(&bar[s], Cfg::PLANE * sizeof(float));
-            tma_load_4d(smem + s * Cfg::SLOT, &tin, xs0 - 4, y0 - D, first + s, blk, &bar[s]);
-        }
-    }
+    // the input was written by the previous launch on this stream
+    pdl_wait();
+    pdl_trigger();
 
-    // coefficients in registers
     const float a0 = C.a0;
     float ax[D], ay[D], az[D];
 #pragma unroll
     for (int k = 0; k < D; ++k) { ax[k] = C.ax[k]; ay[k] = C.ay[k]; az[k] = C.az[k]; }
 
-    const int xb = xs0 + 4 * lane - L.xoff;             // block x of this lane's first cell
-    bool vx[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) vx[j] = (xb + j >= lo[0]) && (xb + j <= hi[0]);
-    const bool vx_all = vx[0] && vx[1] && vx[2] && vx[3];
-    const bool vx_any = vx[0] || vx[1] || vx[2] || vx[3];
+    const long long G = gridDim.x;
+    long long w = sch.W * blockIdx.x / G;
+    const long long w_end = sch.W * (blockIdx.x + 1) / G;
+    unsigned gp = 0;             // ring position: planes streamed by this CTA so far
+    bool aborted = false;
+    int pr = 0, np = 0;
+    unsigned issued_hi = 0;
+    while (w < w_end && !aborted) {
+        const long long col = w / sch.NZ;
+        const int zi0 = (int)(w - col * sch.NZ);
+        const long long zrem = (long long)zi0 + (w_end - w);
+        const int zi1 = zrem < sch.NZ ? (int)zrem : sch.NZ;
+        w += zi1 - zi0;
+        const int tx = (int)(col % sch.ntx);
+        const long long r = col / sch.ntx;
+        const int ty = (int)(r % sch.nty);
+        const int blk = (int)(r / sch.nty);
 
-    float4 q[RY][2 * D + 1];
-    float* const outb = out + (long long)blk * L.bstride + xs0 + 4 * lane;
+        const int edge = edge_bits(L, blk);
+        int lo[3], hi[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) stage_region(L, edge, a, D * (step_i + 1), lo[a], hi[a]);
+        const int xs0 = ((L.xoff + D) & ~3) + tx * kTX;      // storage x of tile column 0
+        const int y0 = D + ty * Cfg::TY;                     // block y of tile row 0
+        if (xs0 - L.xoff > hi[0] || xs0 + kTX - 1 - L.xoff < lo[0]) continue;
+        if (y0 > hi[1] || y0 + Cfg::TY - 1 < lo[1]) continue;
+        const int zs = max(D + zi0, lo[2]);
+        const int ze = min(D + zi1 - 1, hi[2]);
+        if (zs > ze) continue;
 
-    int pr = 0;
-    for (; pr < np; ++pr) {
-        const int slot = pr % S;
-        if (!mbar_wait_bounded(&bar[slot], (pr / S) & 1)) {
-            abort_flag = 1;
+        const int first = zs - D;               // first input plane
+        np = (ze + D) - first + 1;              // input planes streamed
+        if (tid == 0) {
+            for (int s = 0; s < S && s < np; ++s) {
+                const unsigned g = gp + s;
+                mbar_expect_tx(&bar[g % S], Cfg::PLANE * sizeof(float));
+                tma_load_4d(smem + (g % S) * Cfg::SLOT, &tin, xs0 - 4, y0 - D, first + s, blk,
+                            &bar[g % S]);
+            }
         }
-        const float* pl = smem + slot * Cfg::SLOT;
+        issued_hi = gp + min(S, np);
+
+        const int xb = xs0 + 4 * lane - L.xoff;             // block x of this lane's first cell
+        bool vx[4];
 #pragma unroll
-        for (int r = 0; r < RY; ++r) {
+        for (int j = 0; j < 4; ++j) vx[j] = (xb + j >= lo[0]) && (xb + j <= hi[0]);
+        const bool vx_all = vx[0] && vx[1] && vx[2] && vx[3];
+        const bool vx_any = vx[0] || vx[1] || vx[2] || vx[3];
+
+        float4 q[RY][2 * D + 1];
+        float* const outb = out + (long long)blk * L.bstride + xs0 + 4 * lane;
+
+        for (pr = 0; pr < np; ++pr) {
+            const unsigned g = gp + pr;
+            if (!mbar_wait_bounded(&bar[g % S], (g / S) & 1)) abort_flag = 1;
+            const float* pl = smem + (g % S) * Cfg::SLOT;
 #pragma unroll
-            for (int k = 0; k < 2 * D; ++k) q[r][k] = q[r][k + 1];
-            const int row = D + warp * RY + r;
-            q[r][2 * D] = *reinterpret_cast<const float4*>(pl + row * Cfg::BW + 4 + 4 * lane);
-        }
-        if (pr >= 2 * D && vx_any) {
-            const int z = first + pr - D;
-            const float* pc = smem + ((pr - D) % S) * Cfg::SLOT;
+            for (int r2 = 0; r2 < RY; ++r2) {
 #pragma unroll
-            for (int r = 0; r < RY; ++r) {
-                const int y = y0 + warp * RY + r;
-                if (y < lo[1] || y > hi[1]) continue;
-                const int row = D + warp * RY + r;
-                const float* prow = pc + row * Cfg::BW + 4 * lane;
-                const float4 xl = *reinterpret_cast<const float4*>(prow);
-                const float4 c4 = q[r][D];
-                const float4 xr = *reinterpret_cast<const float4*>(prow + 8);
-                const float v[12] = {xl.x, xl.y, xl.z, xl.w, c4.x, c4.y, c4.z, c4.w,
-                                     xr.x, xr.y, xr.z, xr.w};
-                float res[4];
+                for (int k = 0; k < 2 * D; ++k) q[r2][k] = q[r2][k + 1];
+                const int row = D + warp * RY + r2;
+                q[r2][2 * D] = *reinterpret_cast<const float4*>(pl + row * Cfg::BW + 4 + 4 * lane);
+            }
+            if (pr >= 2 * D && vx_any) {
+                const int z = first + pr - D;
+                const float* pc = smem + ((g - D) % S) * Cfg::SLOT;
 #pragma unroll
-                for (int j = 0; j < 4; ++j) res[j] = a0 * v[4 + j];
+                for (int r2 = 0; r2 < RY; ++r2) {
+                    const int y = y0 + warp * RY + r2;
+                    if (y < lo[1] || y > hi[1]) continue;
+                    const int row = D + warp * RY + r2;
+                    const float* prow = pc + row * Cfg::BW + 4 * lane;
+                    const float4 xl = *reinterpret_cast<const float4*>(prow);
+                    const float4 c4 = q[r2][D];
+                    const float4 xr = *reinterpret_cast<const float4*>(prow + 8);
+                    const float v[12] = {xl.x, xl.y, xl.z, xl.w, c4.x, c4.y, c4.z, c4.w,
+                                         xr.x, xr.y, xr.z, xr.w};
+                    float res[4];
 #pragma unroll
-                for (int k = 1; k <= D; ++k) {
-                    const float4 ym = *reinterpret_cast<const float4*>(prow + 4 - k * Cfg::BW);
-                    const float4 yp = *reinterpret_cast<const float4*>(prow + 4 + k * Cfg::BW);
-                    const float4 zm = q[r][D - k];
-                    const float4 zp = q[r][D + k];
-                    const float ys[4] = {ym.x + yp.x, ym.y + yp.y, ym.z + yp.z, ym.w + yp.w};
-                    const float zsum[4] = {zm.x + zp.x, zm.y + zp.y, zm.z + zp.z, zm.w + zp.w};
+                    for (int j = 0; j < 4; ++j) res[j] = a0 * v[4 + j];
 #pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        res[j] = fmaf(ax[k - 1], v[4 + j - k] + v[4 + j + k], res[j]);
-                        res[j] = fmaf(ay[k - 1], ys[j], res[j]);
-                        res[j] = fmaf(az[k - 1], zsum[j], res[j]);
+                    for (int k = 1; k <= D; ++k) {
+                        const float4 ym = *reinterpret_cast<const float4*>(prow + 4 - k * Cfg::BW);
+                        const float4 yp = *reinterpret_cast<const float4*>(prow + 4 + k * Cfg::BW);
+                        const float4 zm = q[r2][D - k];
+                        const float4 zp = q[r2][D + k];
+                        const float ys[4] = {ym.x + yp.x, ym.y + yp.y, ym.z + yp.z, ym.w + yp.w};
+                        const float zsum[4] = {zm.x + zp.x, zm.y + zp.y, zm.z + zp.z, zm.w + zp.w};
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            res[j] = fmaf(ax[k - 1], v[4 + j - k] + v[4 + j + k], res[j]);
+                            res[j] = fmaf(ay[k - 1], ys[j], res[j]);
+                            res[j] = fmaf(az[k - 1], zsum[j], res[j]);
+                        }
+                    }
+                    float* dst = outb + (long long)z * L.plane + (long long)y * L.P;
+                    if (vx_all) {
+                        *reinterpret_cast<float4*>(dst) = make_float4(res[0], res[1], res[2], res[3]);
+                    } else {
+#pragma unroll
+                        for (int j = 0; j < 4; ++j)
+                            if (vx[j]) dst[j] = res[j];
                     }
                 }
-                float* dst = outb + (long long)z * L.plane + (long long)y * L.P;
-                if (vx_all) {
-                    *reinterpret_cast<float4*>(dst) = make_float4(res[0], res[1], res[2], res[3]);
-                } else {
-#pragma unroll
-                    for (int j = 0; j < 4; ++j)
-                        if (vx[j]) dst[j] = res[j];
+            }
+            __syncthreads();
+            if (abort_flag) {
+                aborted = true;
+                break;
+            }
+            if (pr >= D) {
+                const int nxt = pr - D + S;
+                if (nxt < np) {
+                    const unsigned g2 = gp + nxt;
+                    if (tid == 0) {
+                        mbar_expect_tx(&bar[g2 % S], Cfg::PLANE * sizeof(float));
+                        tma_load_4d(smem + (g2 % S) * Cfg::SLOT, &tin, xs0 - 4, y0 - D, first + nxt,
+                                    blk, &bar[g2 % S]);
+                    }
+                    issued_hi = g2 + 1;
                 }
             }
         }
-        __syncthreads();
-        if (abort_flag) break;
-        if (tid == 0 && pr >= D) {
-            const int nxt = pr - D + S;
-            if (nxt < np) {
-                const int s2 = (pr - D) % S;
-                mbar_expect_tx(&bar[s2], Cfg::PLANE * sizeof(float));
-                tma_load_4d(smem + s2 * Cfg::SLOT, &tin, xs0 - 4, y0 - D, first + nxt, blk,
-                            &bar[s2]);
-            }
-        }
+        if (!aborted) gp += np;
     }
-    if (abort_flag && tid == 0) {
+    if (aborted && tid == 0) {
         report(status, DEV_TIMEOUT);
         // drain the loads still in flight (bounded) before the CTA retires
-        const int issued = min(np, (pr >= D ? pr - D + S : S));
-        for (int p = pr; p < issued; ++p) mbar_wait_bounded(&bar[p % S], (p / S) & 1, 100000000ull);
+        for (unsigned g = gp + pr; g < issued_hi; ++g)
+            mbar_wait_bounded(&bar[g % S], (g / S) & 1, 100000000ull);
     }
 }
 
 template <int D, int RY, int S>
 cudaError_t launch_t(const CUtensorMap* tin, float* out, const BlockLayout& L, int step_i,
-                     const HeatCoef& c, int* status, cudaStream_t st, int nzc)
+                     const HeatCoef& c, int* status, cudaStream_t st)
 {
     using Cfg = HeatCfg<D, RY, S>;
     auto kern = heat_sweep_kernel<D, RY, S>;
-    static bool attr_done = false;
-    if (!attr_done) {
+    static int resident = 0;    // CTAs resident on the whole GPU
+    if (resident == 0) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)Cfg::SMEM);
         if (e != cudaSuccess) return e;
-        attr_done = true;
+        int dev = 0, sms = 0, occ = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreads, Cfg::SMEM);
+        if (e != cudaSuccess) return e;
+        resident = (occ > 0 ? occ : 1) * (sms > 0 ? sms : 1);
     }
+    HeatSched sch;
     const int xs_begin = (L.xoff + D) & ~3;
     const int xs_end = L.xoff + L.n[0] - D;              // exclusive
-    const int ntx = (xs_end - xs_begin + kTX - 1) / kTX;
-    const int nty = (L.n[1] - 2 * D + Cfg::TY - 1) / Cfg::TY;
-    dim3 grid(ntx, nty, L.nblk * nzc);
-    kern<<<grid, kThreads, Cfg::SMEM, st>>>(*tin, out, L, step_i, nzc, c, status);
+    sch.ntx = (xs_end - xs_begin + kTX - 1) / kTX;
+    sch.nty = (L.n[1] - 2 * D + Cfg::TY - 1) / Cfg::TY;
+    sch.NZ = L.n[2] - 2 * D;
+    sch.W = (long long)sch.ntx * sch.nty * sch.NZ * L.nblk;
+    // every CTA streams >= 16 output planes, at most one CTA per resident slot
+    long long G = sch.W / 16;
+    if (G > resident) G = resident;
+    if (G < 1) G = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)G);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = Cfg::SMEM;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kern, *tin, out, L, step_i, c, sch, status);
     count_launches(1);
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 
@@ -227,34 +284,14 @@ HeatCoef heat_coef(int D, double alpha_dt, double dx, double dy, double dz)
     return c;
 }
 
-int heat_default_nzc(const BlockLayout& L, int D)
-{
-    // enough CTAs for ~4 waves of 5 resident CTAs on 152 SMs, chunks >= 32 planes
-    const int TY = kWarps * 2;
-    const int xs_begin = (L.xoff + D) & ~3;
-    const int ntx = (L.xoff + L.n[0] - D - xs_begin + kTX - 1) / kTX;
-    const int nty = (L.n[1] - 2 * D + TY - 1) / TY;
-    const long long tiles = (long long)ntx * nty * L.nblk;
-    const long long want = 152LL * 5 * 4;
-    int nzc = (int)((want + tiles - 1) / tiles);
-    const int nz_out = L.n[2] - 2 * D;
-    int maxc = nz_out / 32;
-    if (maxc < 1) maxc = 1;
-    if (nzc > maxc) nzc = maxc;
-    if (nzc < 1) nzc = 1;
-    return nzc;
-}
-
 cudaError_t launch_heat_substep(const CUtensorMap* tin, float* out, const BlockLayout& L, int D,
-                                int step_i, const HeatCoef& c, int* status, cudaStream_t st,
-                                int nzc)
+                                int step_i, const HeatCoef& c, int* status, cudaStream_t st)
 {
-    if (nzc <= 0) nzc = heat_default_nzc(L, D);
     switch (D) {
-    case 1: return launch_t<1, 2, 4>(tin, out, L, step_i, c, status, st, nzc);
-    case 2: return launch_t<2, 2, 5>(tin, out, L, step_i, c, status, st, nzc);
-    case 3: return launch_t<3, 2, 6>(tin, out, L, step_i, c, status, st, nzc);
-    case 4: return launch_t<4, 2, 7>(tin, out, L, step_i, c, status, st, nzc);
+    case 1: return launch_t<1, 2, 4>(tin, out, L, step_i, c, status, st);
+    case 2: return launch_t<2, 2, 5>(tin, out, L, step_i, c, status, st);
+    case 3: return launch_t<3, 2, 6>(tin, out, L, step_i, c, status, st);
+    case 4: return launch_t<4, 2, 7>(tin, out, L, step_i, c, status, st);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -14,11 +14,11 @@ HeatCoef heat_coef(int D, double alpha_dt, double dx, double dy, double dz);
 // TMA box of one ring slot (cells): width and height for radius D.
 int heat_box_w();
 int heat_box_h(int D);
-int heat_default_nzc(const BlockLayout& L, int D);
 // One sub-step (shrink D*(step_i+1)) of every block: reads the blocks
 // through `tin` (a tensor map over the input buffer), writes `out`.
+// Persistent launch (one CTA per resident slot, balanced contiguous work
+// ranges) with programmatic dependent launch on `st`.
 cudaError_t launch_heat_substep(const CUtensorMap* tin, float* out, const BlockLayout& L, int D,
-                                int step_i, const HeatCoef& c, int* status, cudaStream_t st,
-                                int nzc);
+                                int step_i, const HeatCoef& c, int* status, cudaStream_t st);
 
 }  // namespace b2r

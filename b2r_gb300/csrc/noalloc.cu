@@ -141,7 +141,7 @@ extern "C" b2r_status b2r_heat_3D_gpu_main_noalloc(const float* d_in, float* d_o
     const HeatCoef hc = heat_coef(D, alpha_dt, dx, dy, dz);
     int cur = 0;
     for (int i = 0; i < R; ++i) {   // heat-3D.cu:602-628
-        if ((e = launch_heat_substep(&tm[cur], buf[1 - cur], L, D, i, hc, status, st, 0)) != cudaSuccess)
+        if ((e = launch_heat_substep(&tm[cur], buf[1 - cur], L, D, i, hc, status, st)) != cudaSuccess)
             return nfail(B2R_ERR_CUDA, "heat launch", e);
         cur = 1 - cur;
     }

@@ -109,6 +109,10 @@ b2r_status b2r_download_blocks(b2r_handle* h, int field, void* dst, int dst_is_d
  * (b2r.cpp:197-206) and R steps (b2r.cpp:215); a trailing partial period
  * runs fewer steps.  Asynchronous on the handle's stream. */
 b2r_status b2r_step(b2r_handle* h, int nsteps);
+/* Replay whole periods (halo exchange + R sub-steps, >= 32 time steps) from
+ * CUDA graphs captured on first use (heat and Game of Life, when the handle
+ * has a non-default stream).  Default on; results are identical either way. */
+b2r_status b2r_set_graphs(b2r_handle* h, int enable);
 /* Upload, b2r_step, download: the whole job through host buffers. */
 b2r_status b2r_run_host(b2r_handle* h, int field, const void* host_in, int nsteps,
                         void* host_out);
