@@ -74,6 +74,8 @@ def lib():
         "b2r_download_blocks": ([vp, i, vp, i], i),
         "b2r_step": ([vp, i], i),
         "b2r_set_graphs": ([vp, i], i),
+        "b2r_set_tuning": ([vp, i, i], i),
+        "b2r_autotune": ([vp, i, C.POINTER(C.c_int), C.POINTER(d)], i),
         "b2r_run_host": ([vp, i, vp, i, vp], i),
         "b2r_time_step": ([vp], C.c_int64),
         "b2r_set_source": ([vp, C.POINTER(C.c_float), i], i),
@@ -182,6 +184,18 @@ class Domain:
     def set_graphs(self, enable):
         """Replay whole periods from CUDA graphs (needs a non-default stream)."""
         _check(lib().b2r_set_graphs(self.h, 1 if enable else 0), self.h)
+
+    def set_tuning(self, zchunk=None, ctas_per_sm=None, pdl=None):
+        for key, v in ((1, zchunk), (2, ctas_per_sm), (3, pdl)):
+            if v is not None:
+                _check(lib().b2r_set_tuning(self.h, key, int(v)), self.h)
+
+    def autotune(self, trial_steps=4):
+        """Pick the fastest heat launch schedule; returns ({...}, ms per step)."""
+        best = (C.c_int * 3)()
+        ms = C.c_double()
+        _check(lib().b2r_autotune(self.h, trial_steps, best, C.byref(ms)), self.h)
+        return {"zchunk": best[0], "ctas_per_sm": best[1], "pdl": best[2]}, ms.value
 
     def synchronize(self):
         _check(lib().b2r_synchronize(self.h), self.h)

@@ -7,7 +7,10 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include <cudaTypedefs.h>
@@ -31,6 +34,7 @@ struct b2r_handle {
     int cur = 0;
     CUtensorMap tmap[2];
     HeatCoef hc{};
+    HeatTune tune{};
     // elastic wave: fields and material
     float* fld[kMaxFields] = {};
     int nfld = 0;
@@ -52,6 +56,24 @@ struct b2r_handle {
 };
 
 namespace {
+
+// autotuning results per (model, D, block size, blocks), shared by handles
+
+struct TuneKey {
+    int model, D, n0, n1, n2, nblk;
+    bool operator<(const TuneKey& o) const
+    {
+        return std::tie(model, D, n0, n1, n2, nblk) < std::tie(o.model, o.D, o.n0, o.n1, o.n2, o.nblk);
+    }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, HeatTune> g_tune_cache;
+
+TuneKey key_of(const b2r_handle* h)
+{
+    return TuneKey{h->cfg.model, h->cfg.D, h->L.n[0], h->L.n[1], h->L.n[2], h->L.nblk};
+}
+
 
 thread_local std::string g_err;
 
@@ -211,7 +233,7 @@ b2r_status substep(b2r_handle* h, int i)
     switch (h->cfg.model) {
     case B2R_MODEL_HEAT:
         CK(h, launch_heat_substep(&h->tmap[h->cur], static_cast<float*>(h->buf[1 - h->cur]), h->L,
-                                  h->cfg.D, i, h->hc, h->d_status, h->stream));
+                                  h->cfg.D, i, h->hc, h->d_status, h->stream, h->tune));
         h->cur = 1 - h->cur;
         return B2R_OK;
     case B2R_MODEL_GOL:
@@ -383,6 +405,11 @@ b2r_status b2r_create(const b2r_config* cfg, b2r_handle** out)
         }
         if (c.model == B2R_MODEL_HEAT) {
             h->hc = heat_coef(c.D, c.alpha_dt, c.dx, c.dy, c.dz);
+            {
+                std::lock_guard<std::mutex> lock(g_tune_mu);
+                auto it = g_tune_cache.find(key_of(h));
+                if (it != g_tune_cache.end()) h->tune = it->second;
+            }
             if ((st = build_heat_maps(h)) != B2R_OK) {
                 g_err = h->err;
                 return bail(st);
@@ -632,6 +659,96 @@ b2r_status b2r_boundary_updating(b2r_handle* h, int time_step, int field)
     if (field < 0 || field >= (h->nfld > 0 ? h->nfld : 1))
         return fail(h, B2R_ERR_ARG, "invalid field id %d", field);
     return exchange_one(h, field, true);
+}
+
+// ---------------------------------------------------------------- autotuning
+
+b2r_status b2r_set_tuning(b2r_handle* h, int key, int value)
+{
+    if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
+    switch (key) {
+    case B2R_TUNE_ZCHUNK: h->tune.zchunk = value; break;
+    case B2R_TUNE_CTAS_PER_SM: h->tune.ctas_per_sm = value; break;
+    case B2R_TUNE_PDL: h->tune.pdl = value != 0; break;
+    default: return fail(h, B2R_ERR_ARG, "unknown tuning key %d", key);
+    }
+    drop_graphs(h);
+    return B2R_OK;
+}
+
+b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* best_ms)
+{
+    if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
+    if (h->cfg.model != B2R_MODEL_HEAT) return fail(h, B2R_ERR_ARG, "autotuning covers the heat sweep");
+    if (trial_steps < 1) trial_steps = 4;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_tune_cache.find(key_of(h));
+        if (it != g_tune_cache.end()) {
+            h->tune = it->second;
+            if (best) { best[0] = h->tune.zchunk; best[1] = h->tune.ctas_per_sm; best[2] = h->tune.pdl; }
+            if (best_ms) *best_ms = -1.0;
+            drop_graphs(h);
+            return B2R_OK;
+        }
+    }
+    // keep the simulation state: trials run on the live buffers, which are
+    // restored afterwards
+    const size_t fb = field_bytes(h);
+    void* save = nullptr;
+    CK(h, cudaMalloc(&save, fb));
+    CK(h, cudaMemcpyAsync(save, h->buf[h->cur], fb, cudaMemcpyDeviceToDevice, h->stream));
+    const int save_cur = h->cur;
+    const long long save_ts = h->ts;
+    const bool save_fresh = h->halos_fresh;
+    const bool save_graphs = h->graphs;
+    h->graphs = false;
+    static const int zchunks[] = {0, 16, 32, 64, 128, 256};
+    static const int persist[] = {0, 1, 2, 3, 4, 5, 6};
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    HeatTune bestT = h->tune;
+    float bestMs = 1e30f;
+    b2r_status st = B2R_OK;
+    for (int pdl = 0; pdl < 2 && st == B2R_OK; ++pdl)
+        for (int zc : zchunks)
+            for (int cp : persist) {
+                if (zc > h->L.n[2]) continue;
+                h->tune.zchunk = zc;
+                h->tune.ctas_per_sm = cp;
+                h->tune.pdl = pdl;
+                if ((st = b2r_step(h, 1)) != B2R_OK) break;       // warm
+                cudaEventRecord(e0, h->stream);
+                if ((st = b2r_step(h, trial_steps)) != B2R_OK) break;
+                cudaEventRecord(e1, h->stream);
+                cudaEventSynchronize(e1);
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms < bestMs) {
+                    bestMs = ms;
+                    bestT = h->tune;
+                }
+            }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    h->tune = bestT;
+    h->cur = save_cur;
+    h->ts = save_ts;
+    h->halos_fresh = save_fresh;
+    h->graphs = save_graphs;
+    cudaMemcpyAsync(h->buf[h->cur], save, fb, cudaMemcpyDeviceToDevice, h->stream);
+    cudaStreamSynchronize(h->stream);
+    cudaFree(save);
+    if (st != B2R_OK) return st;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tune_cache[key_of(h)] = bestT;
+    }
+    drop_graphs(h);
+    if (best) { best[0] = bestT.zchunk; best[1] = bestT.ctas_per_sm; best[2] = bestT.pdl; }
+    if (best_ms) *best_ms = bestMs / trial_steps;
+    return check_status(h);
 }
 
 // ---------------------------------------------------------------- per-block entries

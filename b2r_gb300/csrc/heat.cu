@@ -38,14 +38,16 @@ struct HeatCfg {
     static constexpr size_t SMEM = size_t(S) * SLOT * sizeof(float) + S * sizeof(uint64_t) + 16 + 128;
 };
 
-// Work schedule of one launch: the plane-tiles (block, tile row, tile
-// column, output plane) in that order are split into G equal contiguous
-// ranges, one per CTA, and G CTAs are all resident at once.  A range spans
-// at most a few tile columns, so every CTA streams about the same number of
-// planes and the launch has no partial last wave.
+// Work schedule of one launch: units = (block, z-chunk of Lz output planes,
+// tile row, tile column) numbered with the tile column fastest, dealt
+// round-robin to gridDim.x CTAs.  Units that run at the same time are
+// neighbouring tiles of the same planes, so whole DRAM rows are fetched
+// together and the tile skirts hit L2.  gridDim.x = number of units gives one
+// unit per CTA; a smaller grid makes the CTAs persistent.
 struct HeatSched {
-    int ntx, nty, NZ;        // tile columns / rows per block, output planes per column
-    long long W;             // total plane-tiles
+    int ntx, nty;            // tile columns / rows per block
+    int NZ, Lz, nzc;         // output planes per column, planes per chunk, chunks
+    long long U;             // units
 };
 
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
@@ -81,23 +83,19 @@ heat_sweep_kernel(const __grid_constant__ CUtensorMap tin, float* __restrict__ o
 #pragma unroll
     for (int k = 0; k < D; ++k) { ax[k] = C.ax[k]; ay[k] = C.ay[k]; az[k] = C.az[k]; }
 
-    const long long G = gridDim.x;
-    long long w = sch.W * blockIdx.x / G;
-    const long long w_end = sch.W * (blockIdx.x + 1) / G;
     unsigned gp = 0;             // ring position: planes streamed by this CTA so far
     bool aborted = false;
     int pr = 0, np = 0;
     unsigned issued_hi = 0;
-    while (w < w_end && !aborted) {
-        const long long col = w / sch.NZ;
-        const int zi0 = (int)(w - col * sch.NZ);
-        const long long zrem = (long long)zi0 + (w_end - w);
-        const int zi1 = zrem < sch.NZ ? (int)zrem : sch.NZ;
-        w += zi1 - zi0;
-        const int tx = (int)(col % sch.ntx);
-        const long long r = col / sch.ntx;
+    for (long long u = blockIdx.x; u < sch.U && !aborted; u += gridDim.x) {
+        const int tx = (int)(u % sch.ntx);
+        long long r = u / sch.ntx;
         const int ty = (int)(r % sch.nty);
-        const int blk = (int)(r / sch.nty);
+        r /= sch.nty;
+        const int zc = (int)(r % sch.nzc);
+        const int blk = (int)(r / sch.nzc);
+        const int zi0 = zc * sch.Lz;
+        const int zi1 = min(sch.NZ, zi0 + sch.Lz);
 
         const int edge = edge_bits(L, blk);
         int lo[3], hi[3];
@@ -216,11 +214,12 @@ heat_sweep_kernel(const __grid_constant__ CUtensorMap tin, float* __restrict__ o
 
 template <int D, int RY, int S>
 cudaError_t launch_t(const CUtensorMap* tin, float* out, const BlockLayout& L, int step_i,
-                     const HeatCoef& c, int* status, cudaStream_t st)
+                     const HeatCoef& c, int* status, cudaStream_t st, const HeatTune& tune)
 {
     using Cfg = HeatCfg<D, RY, S>;
     auto kern = heat_sweep_kernel<D, RY, S>;
     static int resident = 0;    // CTAs resident on the whole GPU
+    static int resident_per_sm = 0;
     if (resident == 0) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)Cfg::SMEM);
@@ -230,7 +229,8 @@ cudaError_t launch_t(const CUtensorMap* tin, float* out, const BlockLayout& L, i
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreads, Cfg::SMEM);
         if (e != cudaSuccess) return e;
-        resident = (occ > 0 ? occ : 1) * (sms > 0 ? sms : 1);
+        resident_per_sm = occ > 0 ? occ : 1;
+        resident = resident_per_sm * (sms > 0 ? sms : 1);
     }
     HeatSched sch;
     const int xs_begin = (L.xoff + D) & ~3;
@@ -238,10 +238,27 @@ cudaError_t launch_t(const CUtensorMap* tin, float* out, const BlockLayout& L, i
     sch.ntx = (xs_end - xs_begin + kTX - 1) / kTX;
     sch.nty = (L.n[1] - 2 * D + Cfg::TY - 1) / Cfg::TY;
     sch.NZ = L.n[2] - 2 * D;
-    sch.W = (long long)sch.ntx * sch.nty * sch.NZ * L.nblk;
-    // every CTA streams >= 16 output planes, at most one CTA per resident slot
-    long long G = sch.W / 16;
-    if (G > resident) G = resident;
+    const long long tiles = (long long)sch.ntx * sch.nty * L.nblk;
+    int Lz = tune.zchunk;
+    if (Lz <= 0) {
+        // default: about 4 waves of resident CTAs, chunks of at least 32 planes
+        long long nzc = (4LL * resident + tiles - 1) / tiles;
+        const long long maxc = sch.NZ / 32 > 0 ? sch.NZ / 32 : 1;
+        if (nzc > maxc) nzc = maxc;
+        if (nzc < 1) nzc = 1;
+        Lz = (int)((sch.NZ + nzc - 1) / nzc);
+    }
+    if (Lz > sch.NZ) Lz = sch.NZ;
+    if (Lz < 1) Lz = 1;
+    sch.Lz = Lz;
+    sch.nzc = (sch.NZ + Lz - 1) / Lz;
+    sch.U = tiles * sch.nzc;
+    long long G = sch.U;                                 // one unit per CTA
+    if (tune.ctas_per_sm > 0) {                          // persistent
+        const long long cap = (long long)resident / (resident_per_sm > 0 ? resident_per_sm : 1) *
+                              (tune.ctas_per_sm < resident_per_sm ? tune.ctas_per_sm : resident_per_sm);
+        if (G > cap) G = cap;
+    }
     if (G < 1) G = 1;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)G);
@@ -252,7 +269,7 @@ cudaError_t launch_t(const CUtensorMap* tin, float* out, const BlockLayout& L, i
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = tune.pdl ? 1 : 0;
     cudaError_t e = cudaLaunchKernelEx(&cfg, kern, *tin, out, L, step_i, c, sch, status);
     count_launches(1);
     if (e != cudaSuccess) return e;
@@ -285,13 +302,14 @@ HeatCoef heat_coef(int D, double alpha_dt, double dx, double dy, double dz)
 }
 
 cudaError_t launch_heat_substep(const CUtensorMap* tin, float* out, const BlockLayout& L, int D,
-                                int step_i, const HeatCoef& c, int* status, cudaStream_t st)
+                                int step_i, const HeatCoef& c, int* status, cudaStream_t st,
+                                const HeatTune& tune)
 {
     switch (D) {
-    case 1: return launch_t<1, 2, 4>(tin, out, L, step_i, c, status, st);
-    case 2: return launch_t<2, 2, 5>(tin, out, L, step_i, c, status, st);
-    case 3: return launch_t<3, 2, 6>(tin, out, L, step_i, c, status, st);
-    case 4: return launch_t<4, 2, 7>(tin, out, L, step_i, c, status, st);
+    case 1: return launch_t<1, 2, 4>(tin, out, L, step_i, c, status, st, tune);
+    case 2: return launch_t<2, 2, 5>(tin, out, L, step_i, c, status, st, tune);
+    case 3: return launch_t<3, 2, 6>(tin, out, L, step_i, c, status, st, tune);
+    case 4: return launch_t<4, 2, 7>(tin, out, L, step_i, c, status, st, tune);
     default: return cudaErrorInvalidValue;
     }
 }

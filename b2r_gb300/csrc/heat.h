@@ -16,9 +16,17 @@ int heat_box_w();
 int heat_box_h(int D);
 // One sub-step (shrink D*(step_i+1)) of every block: reads the blocks
 // through `tin` (a tensor map over the input buffer), writes `out`.
-// Persistent launch (one CTA per resident slot, balanced contiguous work
-// ranges) with programmatic dependent launch on `st`.
+// Launch schedule knobs (the autotuner's search space).
+struct HeatTune {
+    int zchunk = 0;        // output planes per work unit; 0 = about 4 waves, >= 32 planes
+    int ctas_per_sm = 0;   // 0 = one CTA per unit; k > 0 = persistent, k CTAs per SM
+    int pdl = 1;           // programmatic dependent launch on the stream
+};
+
+// One sub-step of every block: units (block, z-chunk, tile row, tile column)
+// dealt round-robin to the CTAs.
 cudaError_t launch_heat_substep(const CUtensorMap* tin, float* out, const BlockLayout& L, int D,
-                                int step_i, const HeatCoef& c, int* status, cudaStream_t st);
+                                int step_i, const HeatCoef& c, int* status, cudaStream_t st,
+                                const HeatTune& tune = HeatTune());
 
 }  // namespace b2r

@@ -113,6 +113,16 @@ b2r_status b2r_step(b2r_handle* h, int nsteps);
  * CUDA graphs captured on first use (heat and Game of Life, when the handle
  * has a non-default stream).  Default on; results are identical either way. */
 b2r_status b2r_set_graphs(b2r_handle* h, int enable);
+/* Launch-schedule knobs of the heat sweep (the autotuner's search space). */
+enum { B2R_TUNE_ZCHUNK = 1, B2R_TUNE_CTAS_PER_SM = 2, B2R_TUNE_PDL = 3 };
+b2r_status b2r_set_tuning(b2r_handle* h, int key, int value);
+/* Time every schedule candidate (z-chunk length x persistent CTAs per SM x
+ * programmatic dependent launch) for trial_steps time steps on the live
+ * fields, keep the fastest, restore the fields and the time step.  Results
+ * are cached per (model, D, block size, block count) for the process and
+ * applied to later handles of the same shape.  best[3] (may be NULL) gets
+ * {zchunk, ctas_per_sm, pdl}; *best_ms the time per step (-1 if cached). */
+b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* best_ms);
 /* Upload, b2r_step, download: the whole job through host buffers. */
 b2r_status b2r_run_host(b2r_handle* h, int field, const void* host_in, int nsteps,
                         void* host_out);
