@@ -241,12 +241,14 @@ cudaError_t launch_t(const CUtensorMap* tin, float* out, const BlockLayout& L, i
     const long long tiles = (long long)sch.ntx * sch.nty * L.nblk;
     int Lz = tune.zchunk;
     if (Lz <= 0) {
-        // default: about 4 waves of resident CTAs, chunks of at least 32 planes
-        long long nzc = (4LL * resident + tiles - 1) / tiles;
-        const long long maxc = sch.NZ / 32 > 0 ? sch.NZ / 32 : 1;
-        if (nzc > maxc) nzc = maxc;
-        if (nzc < 1) nzc = 1;
-        Lz = (int)((sch.NZ + nzc - 1) / nzc);
+        // default: chunks of 16 planes (the fastest on 512^3 D=1 of every
+        // schedule the autotuner tries), fewer when the grid would be small
+        Lz = 16;
+        if (tiles * ((sch.NZ + 15) / 16) < 2LL * resident) {
+            long long nzc = (2LL * resident + tiles - 1) / tiles;
+            if (nzc > sch.NZ / 4) nzc = sch.NZ / 4 > 0 ? sch.NZ / 4 : 1;
+            Lz = (int)((sch.NZ + nzc - 1) / nzc);
+        }
     }
     if (Lz > sch.NZ) Lz = sch.NZ;
     if (Lz < 1) Lz = 1;
