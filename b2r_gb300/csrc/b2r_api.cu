@@ -122,7 +122,7 @@ void fill_layout(BlockLayout& L, const int n[3], const int B[3], const int nb[3]
     L.nblk = nb[0] * nb[1] * nb[2];
     L.H = H;
     L.xoff = roundup(H + m, A) - H;
-    L.P = roundup(L.xoff + n[0] + m, A);   // >= 16 bytes of pad after the row too
+    L.P = roundup(L.xoff + n[0] + 2 * m, A);   // >= 32 bytes of pad after the row
     L.periodic = periodic;
     L.fixed_edge = fixed_edge;
     L.plane = (long long)L.P * n[1];

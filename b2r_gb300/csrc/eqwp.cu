@@ -25,13 +25,35 @@ namespace b2r {
 
 namespace {
 
-constexpr int kBX = 32, kBY = 8;
+// Thread = 4 consecutive x cells (one float4) of one row; CTA = 32 x 8
+// threads = a 128 x 8 tile; z marched over a chunk.
+constexpr int kBX = 32, kBY = 8, kTXc = 4 * kBX;
 
 enum { VX, VY, VZ, SXX, SXY, SXZ, SYY, SYZ, SZZ, DISP };
 
-struct Q5 {
-    float m2, m1, c, p1, p2;
-    __device__ __forceinline__ void shift(float nv)
+__device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+__device__ __forceinline__ float4 ldw4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ float cmp(const float4& v, int j)
+{
+    return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
+}
+
+// 12 cells x-4 .. x+7 of a row around the thread's 4 cells
+struct Row12 {
+    float v[12];
+    __device__ __forceinline__ void load(const float* p)
+    {
+        const float4 a = ld4(p - 4), b = ld4(p), c = ld4(p + 4);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+        v[8] = c.x; v[9] = c.y; v[10] = c.z; v[11] = c.w;
+    }
+};
+
+// five planes z-2 .. z+2 of the thread's 4 cells
+struct Q5v {
+    float4 m2, m1, c, p1, p2;
+    __device__ __forceinline__ void shift(float4 nv)
     {
         m2 = m1; m1 = c; c = p1; p1 = p2; p2 = nv;
     }
@@ -57,128 +79,198 @@ __device__ __forceinline__ Win window(const BlockLayout& L, int blk, int zc, int
     return w;
 }
 
-// collocated FD4 derivative (times 1/dx folded into the coefficients)
-__device__ __forceinline__ float dc(float m2, float m1, float p1, float p2, float a, float b)
+// Common prologue: this thread's cells, their x mask, the row base pointer offset.
+struct Cell {
+    int blk, y, xb;             // block, row, block x of the first of the 4 cells
+    bool vx[4], any, all;
+    long long base;             // element offset of (xb, y, 0) in the field buffers
+};
+
+__device__ __forceinline__ bool cell_setup(const BlockLayout& L, const Win& w, int blk, Cell& c)
 {
-    return a * (p2 - m2) + b * (p1 - m1);
+    const int xs0 = ((L.xoff + 2) & ~3) + blockIdx.x * kTXc + 4 * threadIdx.x;
+    c.blk = blk;
+    c.xb = xs0 - L.xoff;
+    c.y = 2 + blockIdx.y * kBY + threadIdx.y;
+    if (!w.ok || c.y < w.lo[1] || c.y > w.hi[1]) return false;
+    c.any = false;
+    c.all = true;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        c.vx[j] = c.xb + j >= w.lo[0] && c.xb + j <= w.hi[0];
+        c.any |= c.vx[j];
+        c.all &= c.vx[j];
+    }
+    c.base = (long long)blk * L.bstride + (long long)c.y * L.P + xs0;
+    return c.any;
 }
 
-// ------------------------------------------------------------ REF stress stage
+// read-modify-write of the thread's 4 cells: f[id+j] += d[j] where valid
+__device__ __forceinline__ void add4(float* f, const Cell& c, const float (&d)[4])
+{
+    if (c.all) {
+        float4 o = ldw4(f);
+        o.x += d[0]; o.y += d[1]; o.z += d[2]; o.w += d[3];
+        *reinterpret_cast<float4*>(f) = o;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (c.vx[j]) f[j] += d[j];
+    }
+}
+
+// ------------------------------------------------------------ REF (collocated FD4)
+// d/dx of the 4 cells from a 12-cell row, d/dy from rows +-1, +-2, d/dz from a queue
+__device__ __forceinline__ float dcx(const Row12& r, int j, float a, float b)
+{
+    return a * (r.v[6 + j] - r.v[2 + j]) + b * (r.v[5 + j] - r.v[3 + j]);
+}
+__device__ __forceinline__ float dc4(const float4& m2, const float4& m1, const float4& p1,
+                                     const float4& p2, int j, float a, float b)
+{
+    return a * (cmp(p2, j) - cmp(m2, j)) + b * (cmp(p1, j) - cmp(m1, j));
+}
+
 __global__ void __launch_bounds__(kBX * kBY)
 eqwp_ref_stress(FieldPtrs F, const BlockLayout L, int step_i, int nzc, EqwpRefParams p)
 {
     const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
     const Win w = window(L, blk, zc, nzc, 4 * step_i + 2);
-    const int x = 2 + blockIdx.x * kBX + threadIdx.x;
-    const int y = 2 + blockIdx.y * kBY + threadIdx.y;
-    if (!w.ok || x < w.lo[0] || x > w.hi[0] || y < w.lo[1] || y > w.hi[1]) return;
-    const long long base = (long long)blk * L.bstride + (long long)y * L.P + L.xoff + x;
+    Cell c;
+    if (!cell_setup(L, w, blk, c)) return;
     const long long P = L.P, S = L.plane;
-    const float* vx = F.p[VX] + base;
-    const float* vy = F.p[VY] + base;
-    const float* vz = F.p[VZ] + base;
-    Q5 qx, qy, qz;
+    const float* vx = F.p[VX] + c.base;
+    const float* vy = F.p[VY] + c.base;
+    const float* vz = F.p[VZ] + c.base;
+    Q5v qx, qy, qz;
     {
         const long long o = (long long)(w.zs - 2) * S;
-        qx.m1 = __ldg(vx + o); qy.m1 = __ldg(vy + o); qz.m1 = __ldg(vz + o);
-        qx.c = __ldg(vx + o + S); qy.c = __ldg(vy + o + S); qz.c = __ldg(vz + o + S);
-        qx.p1 = __ldg(vx + o + 2 * S); qy.p1 = __ldg(vy + o + 2 * S); qz.p1 = __ldg(vz + o + 2 * S);
-        qx.p2 = __ldg(vx + o + 3 * S); qy.p2 = __ldg(vy + o + 3 * S); qz.p2 = __ldg(vz + o + 3 * S);
+        qx.m1 = ld4(vx + o); qy.m1 = ld4(vy + o); qz.m1 = ld4(vz + o);
+        qx.c = ld4(vx + o + S); qy.c = ld4(vy + o + S); qz.c = ld4(vz + o + S);
+        qx.p1 = ld4(vx + o + 2 * S); qy.p1 = ld4(vy + o + 2 * S); qz.p1 = ld4(vz + o + 2 * S);
+        qx.p2 = ld4(vx + o + 3 * S); qy.p2 = ld4(vy + o + 3 * S); qz.p2 = ld4(vz + o + 3 * S);
     }
     const float a = p.ca, b = p.cb;
     for (int z = w.zs; z <= w.ze; ++z) {
         const long long o = (long long)z * S;
-        qx.shift(__ldg(vx + o + 2 * S));
-        qy.shift(__ldg(vy + o + 2 * S));
-        qz.shift(__ldg(vz + o + 2 * S));
-        const float* X = vx + o;
-        const float* Y = vy + o;
-        const float* Z = vz + o;
-        const float dvxx = dc(__ldg(X - 2), __ldg(X - 1), __ldg(X + 1), __ldg(X + 2), a, b);
-        const float dvxy = dc(__ldg(X - 2 * P), __ldg(X - P), __ldg(X + P), __ldg(X + 2 * P), a, b);
-        const float dvxz = dc(qx.m2, qx.m1, qx.p1, qx.p2, a, b);
-        const float dvyx = dc(__ldg(Y - 2), __ldg(Y - 1), __ldg(Y + 1), __ldg(Y + 2), a, b);
-        const float dvyy = dc(__ldg(Y - 2 * P), __ldg(Y - P), __ldg(Y + P), __ldg(Y + 2 * P), a, b);
-        const float dvyz = dc(qy.m2, qy.m1, qy.p1, qy.p2, a, b);
-        const float dvzx = dc(__ldg(Z - 2), __ldg(Z - 1), __ldg(Z + 1), __ldg(Z + 2), a, b);
-        const float dvzy = dc(__ldg(Z - 2 * P), __ldg(Z - P), __ldg(Z + P), __ldg(Z + 2 * P), a, b);
-        const float dvzz = dc(qz.m2, qz.m1, qz.p1, qz.p2, a, b);
-        const long long id = base + o;
-        // eqwp.cu:460-473, with dt folded into the Lame constants
-        F.p[SXX][id] += p.l2m_dt * dvxx + p.l_dt * (dvyy + dvzz);
-        F.p[SYY][id] += p.l2m_dt * dvyy + p.l_dt * (dvxx + dvzz);
-        F.p[SZZ][id] += p.l2m_dt * dvzz + p.l_dt * (dvxx + dvyy);
-        F.p[SXY][id] += p.mu_dt * (dvxy + dvyx);
-        F.p[SXZ][id] += p.mu_dt * (dvxz + dvzx);
-        F.p[SYZ][id] += p.mu_dt * (dvyz + dvzy);
+        qx.shift(ld4(vx + o + 2 * S));
+        qy.shift(ld4(vy + o + 2 * S));
+        qz.shift(ld4(vz + o + 2 * S));
+        Row12 rx, ry, rz;
+        rx.load(vx + o);
+        ry.load(vy + o);
+        rz.load(vz + o);
+        const float4 xm2 = ld4(vx + o - 2 * P), xm1 = ld4(vx + o - P), xp1 = ld4(vx + o + P), xp2 = ld4(vx + o + 2 * P);
+        const float4 ym2 = ld4(vy + o - 2 * P), ym1 = ld4(vy + o - P), yp1 = ld4(vy + o + P), yp2 = ld4(vy + o + 2 * P);
+        const float4 zm2 = ld4(vz + o - 2 * P), zm1 = ld4(vz + o - P), zp1 = ld4(vz + o + P), zp2 = ld4(vz + o + 2 * P);
+        float dxx[4], dyy[4], dzz[4], dxy[4], dxz[4], dyz[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float dvxx = dcx(rx, j, a, b);
+            const float dvxy = dc4(xm2, xm1, xp1, xp2, j, a, b);
+            const float dvxz = dc4(qx.m2, qx.m1, qx.p1, qx.p2, j, a, b);
+            const float dvyx = dcx(ry, j, a, b);
+            const float dvyy = dc4(ym2, ym1, yp1, yp2, j, a, b);
+            const float dvyz = dc4(qy.m2, qy.m1, qy.p1, qy.p2, j, a, b);
+            const float dvzx = dcx(rz, j, a, b);
+            const float dvzy = dc4(zm2, zm1, zp1, zp2, j, a, b);
+            const float dvzz = dc4(qz.m2, qz.m1, qz.p1, qz.p2, j, a, b);
+            // eqwp.cu:460-473, dt folded into the Lame constants
+            dxx[j] = p.l2m_dt * dvxx + p.l_dt * (dvyy + dvzz);
+            dyy[j] = p.l2m_dt * dvyy + p.l_dt * (dvxx + dvzz);
+            dzz[j] = p.l2m_dt * dvzz + p.l_dt * (dvxx + dvyy);
+            dxy[j] = p.mu_dt * (dvxy + dvyx);
+            dxz[j] = p.mu_dt * (dvxz + dvzx);
+            dyz[j] = p.mu_dt * (dvyz + dvzy);
+        }
+        add4(F.p[SXX] + c.base + o, c, dxx);
+        add4(F.p[SYY] + c.base + o, c, dyy);
+        add4(F.p[SZZ] + c.base + o, c, dzz);
+        add4(F.p[SXY] + c.base + o, c, dxy);
+        add4(F.p[SXZ] + c.base + o, c, dxz);
+        add4(F.p[SYZ] + c.base + o, c, dyz);
     }
 }
 
-// ------------------------------------------------------------ REF velocity stage
 __global__ void __launch_bounds__(kBX * kBY)
 eqwp_ref_velocity(FieldPtrs F, const BlockLayout L, int step_i, int nzc, EqwpRefParams p, int ts)
 {
     const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
     const Win w = window(L, blk, zc, nzc, 4 * step_i + 4);
-    const int x = 2 + blockIdx.x * kBX + threadIdx.x;
-    const int y = 2 + blockIdx.y * kBY + threadIdx.y;
-    if (!w.ok || x < w.lo[0] || x > w.hi[0] || y < w.lo[1] || y > w.hi[1]) return;
-    const long long base = (long long)blk * L.bstride + (long long)y * L.P + L.xoff + x;
+    Cell c;
+    if (!cell_setup(L, w, blk, c)) return;
     const long long P = L.P, S = L.plane;
-    const float* sxx = F.p[SXX] + base;
-    const float* sxy = F.p[SXY] + base;
-    const float* sxz = F.p[SXZ] + base;
-    const float* syy = F.p[SYY] + base;
-    const float* syz = F.p[SYZ] + base;
-    const float* szz = F.p[SZZ] + base;
-    Q5 qxz, qyz, qzz;
+    const float* sxx = F.p[SXX] + c.base;
+    const float* sxy = F.p[SXY] + c.base;
+    const float* sxz = F.p[SXZ] + c.base;
+    const float* syy = F.p[SYY] + c.base;
+    const float* syz = F.p[SYZ] + c.base;
+    const float* szz = F.p[SZZ] + c.base;
+    Q5v qxz, qyz, qzz;
     {
         const long long o = (long long)(w.zs - 2) * S;
-        qxz.m1 = __ldg(sxz + o); qyz.m1 = __ldg(syz + o); qzz.m1 = __ldg(szz + o);
-        qxz.c = __ldg(sxz + o + S); qyz.c = __ldg(syz + o + S); qzz.c = __ldg(szz + o + S);
-        qxz.p1 = __ldg(sxz + o + 2 * S); qyz.p1 = __ldg(syz + o + 2 * S); qzz.p1 = __ldg(szz + o + 2 * S);
-        qxz.p2 = __ldg(sxz + o + 3 * S); qyz.p2 = __ldg(syz + o + 3 * S); qzz.p2 = __ldg(szz + o + 3 * S);
+        qxz.m1 = ld4(sxz + o); qyz.m1 = ld4(syz + o); qzz.m1 = ld4(szz + o);
+        qxz.c = ld4(sxz + o + S); qyz.c = ld4(syz + o + S); qzz.c = ld4(szz + o + S);
+        qxz.p1 = ld4(sxz + o + 2 * S); qyz.p1 = ld4(syz + o + 2 * S); qzz.p1 = ld4(szz + o + 2 * S);
+        qxz.p2 = ld4(sxz + o + 3 * S); qyz.p2 = ld4(syz + o + 3 * S); qzz.p2 = ld4(szz + o + 3 * S);
     }
     const float a = p.ca, b = p.cb;
-    const bool frow = (y == p.fy) && (ts < p.fsteps) && x >= p.fx0 && x < p.fx1;
+    const bool frow = (c.y == p.fy) && (ts < p.fsteps);
     for (int z = w.zs; z <= w.ze; ++z) {
         const long long o = (long long)z * S;
-        qxz.shift(__ldg(sxz + o + 2 * S));
-        qyz.shift(__ldg(syz + o + 2 * S));
-        qzz.shift(__ldg(szz + o + 2 * S));
-        const float* XX = sxx + o;
-        const float* XY = sxy + o;
-        const float* XZ = sxz + o;
-        const float* YY = syy + o;
-        const float* YZ = syz + o;
-        const float dsxx_x = dc(__ldg(XX - 2), __ldg(XX - 1), __ldg(XX + 1), __ldg(XX + 2), a, b);
-        const float dsxy_y = dc(__ldg(XY - 2 * P), __ldg(XY - P), __ldg(XY + P), __ldg(XY + 2 * P), a, b);
-        const float dsxz_z = dc(qxz.m2, qxz.m1, qxz.p1, qxz.p2, a, b);
-        const float dsxy_x = dc(__ldg(XY - 2), __ldg(XY - 1), __ldg(XY + 1), __ldg(XY + 2), a, b);
-        const float dsyy_y = dc(__ldg(YY - 2 * P), __ldg(YY - P), __ldg(YY + P), __ldg(YY + 2 * P), a, b);
-        const float dsyz_z = dc(qyz.m2, qyz.m1, qyz.p1, qyz.p2, a, b);
-        const float dsxz_x = dc(__ldg(XZ - 2), __ldg(XZ - 1), __ldg(XZ + 1), __ldg(XZ + 2), a, b);
-        const float dsyz_y = dc(__ldg(YZ - 2 * P), __ldg(YZ - P), __ldg(YZ + P), __ldg(YZ + 2 * P), a, b);
-        const float dszz_z = dc(qzz.m2, qzz.m1, qzz.p1, qzz.p2, a, b);
-        const long long id = base + o;
-        float sy = dsxy_x + dsyy_y + dsyz_z;
-        if (frow && z >= p.fz0 && z < p.fz1) sy += p.fval;
-        F.p[VX][id] += p.dt_rho * (dsxx_x + dsxy_y + dsxz_z);
-        F.p[VY][id] += p.dt_rho * sy;
-        F.p[DISP][id] += p.dt2_rho * sy;
-        F.p[VZ][id] += p.dt_rho * (dsxz_x + dsyz_y + dszz_z);
+        qxz.shift(ld4(sxz + o + 2 * S));
+        qyz.shift(ld4(syz + o + 2 * S));
+        qzz.shift(ld4(szz + o + 2 * S));
+        Row12 rxx, rxy, rxz;
+        rxx.load(sxx + o);
+        rxy.load(sxy + o);
+        rxz.load(sxz + o);
+        const float4 xym2 = ld4(sxy + o - 2 * P), xym1 = ld4(sxy + o - P), xyp1 = ld4(sxy + o + P), xyp2 = ld4(sxy + o + 2 * P);
+        const float4 yym2 = ld4(syy + o - 2 * P), yym1 = ld4(syy + o - P), yyp1 = ld4(syy + o + P), yyp2 = ld4(syy + o + 2 * P);
+        const float4 yzm2 = ld4(syz + o - 2 * P), yzm1 = ld4(syz + o - P), yzp1 = ld4(syz + o + P), yzp2 = ld4(syz + o + 2 * P);
+        const bool fz = frow && z >= p.fz0 && z < p.fz1;
+        float dvx[4], dvy[4], dvz[4], dd[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float sx = dcx(rxx, j, a, b) + dc4(xym2, xym1, xyp1, xyp2, j, a, b) +
+                             dc4(qxz.m2, qxz.m1, qxz.p1, qxz.p2, j, a, b);
+            float sy = dcx(rxy, j, a, b) + dc4(yym2, yym1, yyp1, yyp2, j, a, b) +
+                       dc4(qyz.m2, qyz.m1, qyz.p1, qyz.p2, j, a, b);
+            const float sz = dcx(rxz, j, a, b) + dc4(yzm2, yzm1, yzp1, yzp2, j, a, b) +
+                             dc4(qzz.m2, qzz.m1, qzz.p1, qzz.p2, j, a, b);
+            if (fz && c.xb + j >= p.fx0 && c.xb + j < p.fx1) sy += p.fval;
+            dvx[j] = p.dt_rho * sx;
+            dvy[j] = p.dt_rho * sy;
+            dvz[j] = p.dt_rho * sz;
+            dd[j] = p.dt2_rho * sy;
+        }
+        add4(F.p[VX] + c.base + o, c, dvx);
+        add4(F.p[VY] + c.base + o, c, dvy);
+        add4(F.p[VZ] + c.base + o, c, dvz);
+        add4(F.p[DISP] + c.base + o, c, dd);
     }
 }
 
-// ------------------------------------------------------------ STAG stages
-// forward (at i+1/2) and backward (at i-1/2) staggered 4th-order differences
-__device__ __forceinline__ float dp(float m1, float c, float p1, float p2)
+// ------------------------------------------------------------ STAG (staggered FD4)
+// forward difference at i+1/2 and backward at i-1/2, 4th order (9/8, -1/24)
+__device__ __forceinline__ float dpx(const Row12& r, int j)
 {
-    return 1.125f * (p1 - c) - (1.f / 24.f) * (p2 - m1);
+    return 1.125f * (r.v[5 + j] - r.v[4 + j]) - (1.f / 24.f) * (r.v[6 + j] - r.v[3 + j]);
 }
-__device__ __forceinline__ float dm(float m2, float m1, float c, float p1)
+__device__ __forceinline__ float dmx(const Row12& r, int j)
 {
-    return 1.125f * (c - m1) - (1.f / 24.f) * (p1 - m2);
+    return 1.125f * (r.v[4 + j] - r.v[3 + j]) - (1.f / 24.f) * (r.v[5 + j] - r.v[2 + j]);
+}
+// rows/planes -2..+2 around the cell: Dp uses -1..+2, Dm uses -2..+1
+__device__ __forceinline__ float dp4(const float4& m1, const float4& c, const float4& p1,
+                                     const float4& p2, int j)
+{
+    return 1.125f * (cmp(p1, j) - cmp(c, j)) - (1.f / 24.f) * (cmp(p2, j) - cmp(m1, j));
+}
+__device__ __forceinline__ float dm4(const float4& m2, const float4& m1, const float4& c,
+                                     const float4& p1, int j)
+{
+    return 1.125f * (cmp(c, j) - cmp(m1, j)) - (1.f / 24.f) * (cmp(p1, j) - cmp(m2, j));
 }
 
 __global__ void __launch_bounds__(kBX * kBY)
@@ -187,51 +279,53 @@ eqwp_stag_velocity(FieldPtrs F, MatPtrs M, const BlockLayout L, int step_i, int 
 {
     const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
     const Win w = window(L, blk, zc, nzc, 4 * step_i + 2);
-    const int x = 2 + blockIdx.x * kBX + threadIdx.x;
-    const int y = 2 + blockIdx.y * kBY + threadIdx.y;
-    if (!w.ok || x < w.lo[0] || x > w.hi[0] || y < w.lo[1] || y > w.hi[1]) return;
-    const long long base = (long long)blk * L.bstride + (long long)y * L.P + L.xoff + x;
+    Cell c;
+    if (!cell_setup(L, w, blk, c)) return;
     const long long P = L.P, S = L.plane;
-    const float* sxx = F.p[SXX] + base;
-    const float* sxy = F.p[SXY] + base;
-    const float* sxz = F.p[SXZ] + base;
-    const float* syy = F.p[SYY] + base;
-    const float* syz = F.p[SYZ] + base;
-    const float* szz = F.p[SZZ] + base;
-    const float* buoy = M.p[2] + base;
-    Q5 qxz, qyz, qzz;
+    const float* sxx = F.p[SXX] + c.base;
+    const float* sxy = F.p[SXY] + c.base;
+    const float* sxz = F.p[SXZ] + c.base;
+    const float* syy = F.p[SYY] + c.base;
+    const float* syz = F.p[SYZ] + c.base;
+    const float* szz = F.p[SZZ] + c.base;
+    const float* buoy = M.p[2] + c.base;
+    Q5v qxz, qyz, qzz;
     {
         const long long o = (long long)(w.zs - 2) * S;
-        qxz.m1 = __ldg(sxz + o); qyz.m1 = __ldg(syz + o); qzz.m1 = __ldg(szz + o);
-        qxz.c = __ldg(sxz + o + S); qyz.c = __ldg(syz + o + S); qzz.c = __ldg(szz + o + S);
-        qxz.p1 = __ldg(sxz + o + 2 * S); qyz.p1 = __ldg(syz + o + 2 * S); qzz.p1 = __ldg(szz + o + 2 * S);
-        qxz.p2 = __ldg(sxz + o + 3 * S); qyz.p2 = __ldg(syz + o + 3 * S); qzz.p2 = __ldg(szz + o + 3 * S);
+        qxz.m1 = ld4(sxz + o); qyz.m1 = ld4(syz + o); qzz.m1 = ld4(szz + o);
+        qxz.c = ld4(sxz + o + S); qyz.c = ld4(syz + o + S); qzz.c = ld4(szz + o + S);
+        qxz.p1 = ld4(sxz + o + 2 * S); qyz.p1 = ld4(syz + o + 2 * S); qzz.p1 = ld4(szz + o + 2 * S);
+        qxz.p2 = ld4(sxz + o + 3 * S); qyz.p2 = ld4(syz + o + 3 * S); qzz.p2 = ld4(szz + o + 3 * S);
     }
     const float k = p.dt * p.inv_h;
     for (int z = w.zs; z <= w.ze; ++z) {
         const long long o = (long long)z * S;
-        qxz.shift(__ldg(sxz + o + 2 * S));
-        qyz.shift(__ldg(syz + o + 2 * S));
-        qzz.shift(__ldg(szz + o + 2 * S));
-        const float* XX = sxx + o;
-        const float* XY = sxy + o;
-        const float* XZ = sxz + o;
-        const float* YY = syy + o;
-        const float* YZ = syz + o;
-        const float ax = dp(__ldg(XX - 1), __ldg(XX), __ldg(XX + 1), __ldg(XX + 2)) +
-                         dm(__ldg(XY - 2 * P), __ldg(XY - P), __ldg(XY), __ldg(XY + P)) +
-                         dm(qxz.m2, qxz.m1, qxz.c, qxz.p1);
-        const float ay = dm(__ldg(XY - 2), __ldg(XY - 1), __ldg(XY), __ldg(XY + 1)) +
-                         dp(__ldg(YY - P), __ldg(YY), __ldg(YY + P), __ldg(YY + 2 * P)) +
-                         dm(qyz.m2, qyz.m1, qyz.c, qyz.p1);
-        const float az = dm(__ldg(XZ - 2), __ldg(XZ - 1), __ldg(XZ), __ldg(XZ + 1)) +
-                         dm(__ldg(YZ - 2 * P), __ldg(YZ - P), __ldg(YZ), __ldg(YZ + P)) +
-                         dp(qzz.m1, qzz.c, qzz.p1, qzz.p2);
-        const long long id = base + o;
-        const float kb = k * __ldg(buoy + o);
-        F.p[VX][id] += kb * ax;
-        F.p[VY][id] += kb * ay;
-        F.p[VZ][id] += kb * az;
+        qxz.shift(ld4(sxz + o + 2 * S));
+        qyz.shift(ld4(syz + o + 2 * S));
+        qzz.shift(ld4(szz + o + 2 * S));
+        Row12 rxx, rxy, rxz;
+        rxx.load(sxx + o);
+        rxy.load(sxy + o);
+        rxz.load(sxz + o);
+        const float4 xym2 = ld4(sxy + o - 2 * P), xym1 = ld4(sxy + o - P), xyp1 = ld4(sxy + o + P);
+        const float4 yym1 = ld4(syy + o - P), yyc = ld4(syy + o), yyp1 = ld4(syy + o + P), yyp2 = ld4(syy + o + 2 * P);
+        const float4 yzm2 = ld4(syz + o - 2 * P), yzm1 = ld4(syz + o - P), yzp1 = ld4(syz + o + P);
+        const float4 xyc = make_float4(rxy.v[4], rxy.v[5], rxy.v[6], rxy.v[7]);
+        const float4 bb = ld4(buoy + o);
+        float dvx[4], dvy[4], dvz[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float ax = dpx(rxx, j) + dm4(xym2, xym1, xyc, xyp1, j) + dm4(qxz.m2, qxz.m1, qxz.c, qxz.p1, j);
+            const float ay = dmx(rxy, j) + dp4(yym1, yyc, yyp1, yyp2, j) + dm4(qyz.m2, qyz.m1, qyz.c, qyz.p1, j);
+            const float az = dmx(rxz, j) + dm4(yzm2, yzm1, qyz.c, yzp1, j) + dp4(qzz.m1, qzz.c, qzz.p1, qzz.p2, j);
+            const float kb = k * cmp(bb, j);
+            dvx[j] = kb * ax;
+            dvy[j] = kb * ay;
+            dvz[j] = kb * az;
+        }
+        add4(F.p[VX] + c.base + o, c, dvx);
+        add4(F.p[VY] + c.base + o, c, dvy);
+        add4(F.p[VZ] + c.base + o, c, dvz);
     }
 }
 
@@ -241,64 +335,80 @@ eqwp_stag_stress(FieldPtrs F, MatPtrs M, const BlockLayout L, int step_i, int nz
 {
     const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
     const Win w = window(L, blk, zc, nzc, 4 * step_i + 4);
-    const int x = 2 + blockIdx.x * kBX + threadIdx.x;
-    const int y = 2 + blockIdx.y * kBY + threadIdx.y;
-    if (!w.ok || x < w.lo[0] || x > w.hi[0] || y < w.lo[1] || y > w.hi[1]) return;
-    const long long base = (long long)blk * L.bstride + (long long)y * L.P + L.xoff + x;
+    Cell c;
+    if (!cell_setup(L, w, blk, c)) return;
     const long long P = L.P, S = L.plane;
-    const float* vx = F.p[VX] + base;
-    const float* vy = F.p[VY] + base;
-    const float* vz = F.p[VZ] + base;
-    const float* lam = M.p[0] + base;
-    const float* mu = M.p[1] + base;
-    Q5 qx, qy, qz;
+    const float* vx = F.p[VX] + c.base;
+    const float* vy = F.p[VY] + c.base;
+    const float* vz = F.p[VZ] + c.base;
+    const float* lam = M.p[0] + c.base;
+    const float* mu = M.p[1] + c.base;
+    Q5v qx, qy, qz;
     {
         const long long o = (long long)(w.zs - 2) * S;
-        qx.m1 = __ldg(vx + o); qy.m1 = __ldg(vy + o); qz.m1 = __ldg(vz + o);
-        qx.c = __ldg(vx + o + S); qy.c = __ldg(vy + o + S); qz.c = __ldg(vz + o + S);
-        qx.p1 = __ldg(vx + o + 2 * S); qy.p1 = __ldg(vy + o + 2 * S); qz.p1 = __ldg(vz + o + 2 * S);
-        qx.p2 = __ldg(vx + o + 3 * S); qy.p2 = __ldg(vy + o + 3 * S); qz.p2 = __ldg(vz + o + 3 * S);
+        qx.m1 = ld4(vx + o); qy.m1 = ld4(vy + o); qz.m1 = ld4(vz + o);
+        qx.c = ld4(vx + o + S); qy.c = ld4(vy + o + S); qz.c = ld4(vz + o + S);
+        qx.p1 = ld4(vx + o + 2 * S); qy.p1 = ld4(vy + o + 2 * S); qz.p1 = ld4(vz + o + 2 * S);
+        qx.p2 = ld4(vx + o + 3 * S); qy.p2 = ld4(vy + o + 3 * S); qz.p2 = ld4(vz + o + 3 * S);
     }
     const float k = p.dt * p.inv_h;
     // source cell of this block, in block coordinates
     const int b0 = blk % L.nb[0], b1 = (blk / L.nb[0]) % L.nb[1], b2 = blk / (L.nb[0] * L.nb[1]);
     const int sx = p.src[0] - b0 * L.B[0] + L.H, sy = p.src[1] - b1 * L.B[1] + L.H,
               sz = p.src[2] - b2 * L.B[2] + L.H;
-    const bool srow = (x == sx) && (y == sy);
+    const bool srow = (c.y == sy) && sx >= c.xb && sx < c.xb + 4;
     for (int z = w.zs; z <= w.ze; ++z) {
         const long long o = (long long)z * S;
-        qx.shift(__ldg(vx + o + 2 * S));
-        qy.shift(__ldg(vy + o + 2 * S));
-        qz.shift(__ldg(vz + o + 2 * S));
-        const float* X = vx + o;
-        const float* Y = vy + o;
-        const float* Z = vz + o;
-        const float exx = dm(__ldg(X - 2), __ldg(X - 1), __ldg(X), __ldg(X + 1));
-        const float eyy = dm(__ldg(Y - 2 * P), __ldg(Y - P), __ldg(Y), __ldg(Y + P));
-        const float ezz = dm(qz.m2, qz.m1, qz.c, qz.p1);
-        const float vx_y = dp(__ldg(X - P), __ldg(X), __ldg(X + P), __ldg(X + 2 * P));
-        const float vy_x = dp(__ldg(Y - 1), __ldg(Y), __ldg(Y + 1), __ldg(Y + 2));
-        const float vx_z = dp(qx.m1, qx.c, qx.p1, qx.p2);
-        const float vz_x = dp(__ldg(Z - 1), __ldg(Z), __ldg(Z + 1), __ldg(Z + 2));
-        const float vy_z = dp(qy.m1, qy.c, qy.p1, qy.p2);
-        const float vz_y = dp(__ldg(Z - P), __ldg(Z), __ldg(Z + P), __ldg(Z + 2 * P));
-        const long long id = base + o;
-        const float l = __ldg(lam + o), m = __ldg(mu + o);
-        const float l2m = l + 2.f * m;
-        float dxx = k * (l2m * exx + l * (eyy + ezz));
-        float dyy = k * (l2m * eyy + l * (exx + ezz));
-        float dzz = k * (l2m * ezz + l * (exx + eyy));
-        if (srow && z == sz) {
-            dxx += src_amp;
-            dyy += src_amp;
-            dzz += src_amp;
+        qx.shift(ld4(vx + o + 2 * S));
+        qy.shift(ld4(vy + o + 2 * S));
+        qz.shift(ld4(vz + o + 2 * S));
+        Row12 rx, ry, rz;
+        rx.load(vx + o);
+        ry.load(vy + o);
+        rz.load(vz + o);
+        const float4 xc = make_float4(rx.v[4], rx.v[5], rx.v[6], rx.v[7]);
+        const float4 yc = make_float4(ry.v[4], ry.v[5], ry.v[6], ry.v[7]);
+        const float4 zc4 = make_float4(rz.v[4], rz.v[5], rz.v[6], rz.v[7]);
+        const float4 xm1 = ld4(vx + o - P), xp1 = ld4(vx + o + P), xp2 = ld4(vx + o + 2 * P);
+        const float4 ym2 = ld4(vy + o - 2 * P), ym1 = ld4(vy + o - P), yp1 = ld4(vy + o + P);
+        const float4 zm1 = ld4(vz + o - P), zp1 = ld4(vz + o + P), zp2 = ld4(vz + o + 2 * P);
+        const float4 l4 = ld4(lam + o), m4 = ld4(mu + o);
+        const bool src_here = srow && z == sz;
+        float dxx[4], dyy[4], dzz[4], dxy[4], dxz[4], dyz[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float exx = dmx(rx, j);
+            const float eyy = dm4(ym2, ym1, yc, yp1, j);
+            const float ezz = dm4(qz.m2, qz.m1, qz.c, qz.p1, j);
+            const float vx_y = dp4(xm1, xc, xp1, xp2, j);
+            const float vy_x = dpx(ry, j);
+            const float vx_z = dp4(qx.m1, qx.c, qx.p1, qx.p2, j);
+            const float vz_x = dpx(rz, j);
+            const float vy_z = dp4(qy.m1, qy.c, qy.p1, qy.p2, j);
+            const float vz_y = dp4(zm1, zc4, zp1, zp2, j);
+            const float l = cmp(l4, j), m = cmp(m4, j);
+            const float l2m = l + 2.f * m;
+            float axx = k * (l2m * exx + l * (eyy + ezz));
+            float ayy = k * (l2m * eyy + l * (exx + ezz));
+            float azz = k * (l2m * ezz + l * (exx + eyy));
+            if (src_here && c.xb + j == sx) {
+                axx += src_amp;
+                ayy += src_amp;
+                azz += src_amp;
+            }
+            dxx[j] = axx;
+            dyy[j] = ayy;
+            dzz[j] = azz;
+            dxy[j] = k * m * (vx_y + vy_x);
+            dxz[j] = k * m * (vx_z + vz_x);
+            dyz[j] = k * m * (vy_z + vz_y);
         }
-        F.p[SXX][id] += dxx;
-        F.p[SYY][id] += dyy;
-        F.p[SZZ][id] += dzz;
-        F.p[SXY][id] += k * m * (vx_y + vy_x);
-        F.p[SXZ][id] += k * m * (vx_z + vz_x);
-        F.p[SYZ][id] += k * m * (vy_z + vz_y);
+        add4(F.p[SXX] + c.base + o, c, dxx);
+        add4(F.p[SYY] + c.base + o, c, dyy);
+        add4(F.p[SZZ] + c.base + o, c, dzz);
+        add4(F.p[SXY] + c.base + o, c, dxy);
+        add4(F.p[SXZ] + c.base + o, c, dxz);
+        add4(F.p[SYZ] + c.base + o, c, dyz);
     }
 }
 
@@ -310,8 +420,10 @@ struct Grid {
 Grid stage_grid(const BlockLayout& L)
 {
     Grid r;
-    const int nx = L.n[0] - 4, ny = L.n[1] - 4;
-    const int tx = (nx + kBX - 1) / kBX, ty = (ny + kBY - 1) / kBY;
+    const int xs_begin = (L.xoff + 2) & ~3;
+    const int xs_end = L.xoff + L.n[0] - 2;               // exclusive
+    const int tx = (xs_end - xs_begin + kTXc - 1) / kTXc;
+    const int ty = (L.n[1] - 4 + kBY - 1) / kBY;
     const long long tiles = (long long)tx * ty * L.nblk;
     const long long want = 152LL * 8 * 3;
     int nzc = (int)((want + tiles - 1) / tiles);

@@ -55,6 +55,9 @@ WORKLOADS = {
     # 3-D Game of Life, 256^3 torus, 2x2x2 subdomains, R = 4, 400 generations
     "gol_256": dict(model=2, env=(256, 256, 256), blocks=(2, 2, 2), R=4, D=1, sub_steps=400,
                     bytes_per_cell=2, kernel="gol_kernel", periodic=True),
+    # the reference's collocated elastic-wave model, 512x512x256, one block, R = 1
+    "eqwp_ref": dict(model=3, env=(512, 512, 256), blocks=(1, 1, 1), R=1, D=2, sub_steps=100,
+                     bytes_per_cell=80, kernel="eqwp_ref_stress+velocity"),
     # staggered elastic wave 512x512x256, 2x2x1 subdomains, R = 2, 100 steps per pass
     "eqwp_stag": dict(model=4, env=(512, 512, 256), blocks=(2, 2, 1), R=2, D=2, sub_steps=100,
                       bytes_per_cell=84, kernel="eqwp_stag_velocity+stress"),
@@ -257,6 +260,11 @@ def load_inputs(d, wl, torch, dev):
         host = seeded_domain(wl, d.domain_shape)
         d.upload(host)
         return host
+    if wl["model"] == 3:
+        zero = np.zeros(d.domain_shape, np.float32)
+        for k in range(10):
+            d.upload(zero, field=k)
+        return zero
     rng = np.random.default_rng(3)
     layers = 8
     vp_l = rng.uniform(2000, 4000, layers)
