@@ -16,7 +16,7 @@ LIB = os.path.join(HERE, "libb2r.so")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-         "-I", os.path.join(HERE, "..", "include")]
+         "-I", os.path.join(HERE, "..", "include")] + os.environ.get("B2R_NVCC_FLAGS", "").split()
 
 
 def _deps_newer(obj, src):

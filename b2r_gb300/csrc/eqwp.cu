@@ -28,6 +28,9 @@ namespace {
 // Thread = 4 consecutive x cells (one float4) of one row; CTA = 32 x 8
 // threads = a 128 x 8 tile; z marched over a chunk.
 constexpr int kBX = 32, kBY = 8, kTXc = 4 * kBX;
+#ifndef B2R_EQWP_MINB
+#define B2R_EQWP_MINB 2   // resident CTAs per SM the register budget is fitted to
+#endif
 
 enum { VX, VY, VZ, SXX, SXY, SXZ, SYY, SYZ, SZZ, DISP };
 
@@ -105,17 +108,30 @@ __device__ __forceinline__ bool cell_setup(const BlockLayout& L, const Win& w, i
     return c.any;
 }
 
-// read-modify-write of the thread's 4 cells: f[id+j] += d[j] where valid
-__device__ __forceinline__ void add4(float* f, const Cell& c, const float (&d)[4])
+// Read-modify-write of the thread's 4 cells, split so that every load of an
+// iteration is issued before any store (the field pointers may alias as far
+// as the compiler knows, so a fused load-add-store per field would serialise
+// one DRAM round trip per field).
+__device__ __forceinline__ float4 rd4(const float* f, const Cell& c)
 {
+    if (c.all) return ldw4(f);
+    float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (c.vx[0]) o.x = f[0];
+    if (c.vx[1]) o.y = f[1];
+    if (c.vx[2]) o.z = f[2];
+    if (c.vx[3]) o.w = f[3];
+    return o;
+}
+__device__ __forceinline__ void wr4(float* f, const Cell& c, float4 o, const float (&d)[4])
+{
+    o.x += d[0]; o.y += d[1]; o.z += d[2]; o.w += d[3];
     if (c.all) {
-        float4 o = ldw4(f);
-        o.x += d[0]; o.y += d[1]; o.z += d[2]; o.w += d[3];
         *reinterpret_cast<float4*>(f) = o;
     } else {
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-            if (c.vx[j]) f[j] += d[j];
+        if (c.vx[0]) f[0] = o.x;
+        if (c.vx[1]) f[1] = o.y;
+        if (c.vx[2]) f[2] = o.z;
+        if (c.vx[3]) f[3] = o.w;
     }
 }
 
@@ -131,7 +147,7 @@ __device__ __forceinline__ float dc4(const float4& m2, const float4& m1, const f
     return a * (cmp(p2, j) - cmp(m2, j)) + b * (cmp(p1, j) - cmp(m1, j));
 }
 
-__global__ void __launch_bounds__(kBX * kBY)
+__global__ void __launch_bounds__(kBX * kBY, B2R_EQWP_MINB)
 eqwp_ref_stress(FieldPtrs F, const BlockLayout L, int step_i, int nzc, EqwpRefParams p)
 {
     const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
@@ -163,6 +179,11 @@ eqwp_ref_stress(FieldPtrs F, const BlockLayout L, int step_i, int nzc, EqwpRefPa
         const float4 xm2 = ld4(vx + o - 2 * P), xm1 = ld4(vx + o - P), xp1 = ld4(vx + o + P), xp2 = ld4(vx + o + 2 * P);
         const float4 ym2 = ld4(vy + o - 2 * P), ym1 = ld4(vy + o - P), yp1 = ld4(vy + o + P), yp2 = ld4(vy + o + 2 * P);
         const float4 zm2 = ld4(vz + o - 2 * P), zm1 = ld4(vz + o - P), zp1 = ld4(vz + o + P), zp2 = ld4(vz + o + 2 * P);
+        float* const dst[6] = {F.p[SXX] + c.base + o, F.p[SYY] + c.base + o, F.p[SZZ] + c.base + o,
+                               F.p[SXY] + c.base + o, F.p[SXZ] + c.base + o, F.p[SYZ] + c.base + o};
+        float4 old[6];
+#pragma unroll
+        for (int f = 0; f < 6; ++f) old[f] = rd4(dst[f], c);
         float dxx[4], dyy[4], dzz[4], dxy[4], dxz[4], dyz[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -183,16 +204,16 @@ eqwp_ref_stress(FieldPtrs F, const BlockLayout L, int step_i, int nzc, EqwpRefPa
             dxz[j] = p.mu_dt * (dvxz + dvzx);
             dyz[j] = p.mu_dt * (dvyz + dvzy);
         }
-        add4(F.p[SXX] + c.base + o, c, dxx);
-        add4(F.p[SYY] + c.base + o, c, dyy);
-        add4(F.p[SZZ] + c.base + o, c, dzz);
-        add4(F.p[SXY] + c.base + o, c, dxy);
-        add4(F.p[SXZ] + c.base + o, c, dxz);
-        add4(F.p[SYZ] + c.base + o, c, dyz);
+        wr4(dst[0], c, old[0], dxx);
+        wr4(dst[1], c, old[1], dyy);
+        wr4(dst[2], c, old[2], dzz);
+        wr4(dst[3], c, old[3], dxy);
+        wr4(dst[4], c, old[4], dxz);
+        wr4(dst[5], c, old[5], dyz);
     }
 }
 
-__global__ void __launch_bounds__(kBX * kBY)
+__global__ void __launch_bounds__(kBX * kBY, B2R_EQWP_MINB)
 eqwp_ref_velocity(FieldPtrs F, const BlockLayout L, int step_i, int nzc, EqwpRefParams p, int ts)
 {
     const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
@@ -229,6 +250,11 @@ eqwp_ref_velocity(FieldPtrs F, const BlockLayout L, int step_i, int nzc, EqwpRef
         const float4 yym2 = ld4(syy + o - 2 * P), yym1 = ld4(syy + o - P), yyp1 = ld4(syy + o + P), yyp2 = ld4(syy + o + 2 * P);
         const float4 yzm2 = ld4(syz + o - 2 * P), yzm1 = ld4(syz + o - P), yzp1 = ld4(syz + o + P), yzp2 = ld4(syz + o + 2 * P);
         const bool fz = frow && z >= p.fz0 && z < p.fz1;
+        float* const dst[4] = {F.p[VX] + c.base + o, F.p[VY] + c.base + o, F.p[VZ] + c.base + o,
+                               F.p[DISP] + c.base + o};
+        float4 old[4];
+#pragma unroll
+        for (int f = 0; f < 4; ++f) old[f] = rd4(dst[f], c);
         float dvx[4], dvy[4], dvz[4], dd[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -244,10 +270,10 @@ eqwp_ref_velocity(FieldPtrs F, const BlockLayout L, int step_i, int nzc, EqwpRef
             dvz[j] = p.dt_rho * sz;
             dd[j] = p.dt2_rho * sy;
         }
-        add4(F.p[VX] + c.base + o, c, dvx);
-        add4(F.p[VY] + c.base + o, c, dvy);
-        add4(F.p[VZ] + c.base + o, c, dvz);
-        add4(F.p[DISP] + c.base + o, c, dd);
+        wr4(dst[0], c, old[0], dvx);
+        wr4(dst[1], c, old[1], dvy);
+        wr4(dst[2], c, old[2], dvz);
+        wr4(dst[3], c, old[3], dd);
     }
 }
 
@@ -273,7 +299,7 @@ __device__ __forceinline__ float dm4(const float4& m2, const float4& m1, const f
     return 1.125f * (cmp(c, j) - cmp(m1, j)) - (1.f / 24.f) * (cmp(p1, j) - cmp(m2, j));
 }
 
-__global__ void __launch_bounds__(kBX * kBY)
+__global__ void __launch_bounds__(kBX * kBY, B2R_EQWP_MINB)
 eqwp_stag_velocity(FieldPtrs F, MatPtrs M, const BlockLayout L, int step_i, int nzc,
                    EqwpStagParams p)
 {
@@ -312,6 +338,10 @@ eqwp_stag_velocity(FieldPtrs F, MatPtrs M, const BlockLayout L, int step_i, int 
         const float4 yzm2 = ld4(syz + o - 2 * P), yzm1 = ld4(syz + o - P), yzp1 = ld4(syz + o + P);
         const float4 xyc = make_float4(rxy.v[4], rxy.v[5], rxy.v[6], rxy.v[7]);
         const float4 bb = ld4(buoy + o);
+        float* const dst[3] = {F.p[VX] + c.base + o, F.p[VY] + c.base + o, F.p[VZ] + c.base + o};
+        float4 old[3];
+#pragma unroll
+        for (int f = 0; f < 3; ++f) old[f] = rd4(dst[f], c);
         float dvx[4], dvy[4], dvz[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -323,13 +353,13 @@ eqwp_stag_velocity(FieldPtrs F, MatPtrs M, const BlockLayout L, int step_i, int 
             dvy[j] = kb * ay;
             dvz[j] = kb * az;
         }
-        add4(F.p[VX] + c.base + o, c, dvx);
-        add4(F.p[VY] + c.base + o, c, dvy);
-        add4(F.p[VZ] + c.base + o, c, dvz);
+        wr4(dst[0], c, old[0], dvx);
+        wr4(dst[1], c, old[1], dvy);
+        wr4(dst[2], c, old[2], dvz);
     }
 }
 
-__global__ void __launch_bounds__(kBX * kBY)
+__global__ void __launch_bounds__(kBX * kBY, B2R_EQWP_MINB)
 eqwp_stag_stress(FieldPtrs F, MatPtrs M, const BlockLayout L, int step_i, int nzc,
                  EqwpStagParams p, float src_amp)
 {
@@ -374,6 +404,11 @@ eqwp_stag_stress(FieldPtrs F, MatPtrs M, const BlockLayout L, int step_i, int nz
         const float4 zm1 = ld4(vz + o - P), zp1 = ld4(vz + o + P), zp2 = ld4(vz + o + 2 * P);
         const float4 l4 = ld4(lam + o), m4 = ld4(mu + o);
         const bool src_here = srow && z == sz;
+        float* const dst[6] = {F.p[SXX] + c.base + o, F.p[SYY] + c.base + o, F.p[SZZ] + c.base + o,
+                               F.p[SXY] + c.base + o, F.p[SXZ] + c.base + o, F.p[SYZ] + c.base + o};
+        float4 old[6];
+#pragma unroll
+        for (int f = 0; f < 6; ++f) old[f] = rd4(dst[f], c);
         float dxx[4], dyy[4], dzz[4], dxy[4], dxz[4], dyz[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -403,12 +438,12 @@ eqwp_stag_stress(FieldPtrs F, MatPtrs M, const BlockLayout L, int step_i, int nz
             dxz[j] = k * m * (vx_z + vz_x);
             dyz[j] = k * m * (vy_z + vz_y);
         }
-        add4(F.p[SXX] + c.base + o, c, dxx);
-        add4(F.p[SYY] + c.base + o, c, dyy);
-        add4(F.p[SZZ] + c.base + o, c, dzz);
-        add4(F.p[SXY] + c.base + o, c, dxy);
-        add4(F.p[SXZ] + c.base + o, c, dxz);
-        add4(F.p[SYZ] + c.base + o, c, dyz);
+        wr4(dst[0], c, old[0], dxx);
+        wr4(dst[1], c, old[1], dyy);
+        wr4(dst[2], c, old[2], dzz);
+        wr4(dst[3], c, old[3], dxy);
+        wr4(dst[4], c, old[4], dxz);
+        wr4(dst[5], c, old[5], dyz);
     }
 }
 

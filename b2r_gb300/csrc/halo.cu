@@ -72,46 +72,42 @@ __device__ inline bool slab_map(const BlockLayout& L, int axis, int blk, int sid
     return true;
 }
 
+// One (field, block, side) per blockIdx.y; slab cells (x fastest) over
+// blockIdx.x/threadIdx.x with 32-bit index arithmetic.
 template <typename T>
 __global__ void halo_direct_kernel(FieldSet<T> fs, const BlockLayout L, int axis, Slab sl)
 {
-    T* f = fs.p[blockIdx.y];
-    const long long per_blk = 2 * sl.cells;
-    const long long total = per_blk * L.nblk;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-         e += (long long)gridDim.x * blockDim.x) {
-        const int blk = (int)(e / per_blk);
-        long long r = e - blk * per_blk;
-        const int side = (int)(r / sl.cells);
-        r -= side * sl.cells;
-        const int c0 = (int)(r % sl.e[0]);
-        const long long r1 = r / sl.e[0];
-        const int c1 = (int)(r1 % sl.e[1]);
-        const int c2 = (int)(r1 / sl.e[1]);
+    const int side = blockIdx.y & 1;
+    const int blk = (blockIdx.y >> 1) % L.nblk;
+    const int fld = (blockIdx.y >> 1) / L.nblk;
+    T* f = fs.p[fld];
+    const int cells = (int)sl.cells;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < cells; e += gridDim.x * blockDim.x) {
+        const int c0 = e % sl.e[0];
+        const int r1 = e / sl.e[0];
+        const int c1 = r1 % sl.e[1];
+        const int c2 = r1 / sl.e[1];
         long long dst, src;
         if (slab_map(L, axis, blk, side, c0, c1, c2, dst, src)) f[dst] = f[src];
     }
 }
 
-// staged form: pack[buf] <- neighbour slab, then halo <- pack[buf]
+// staged form: bounce[slab] <- neighbour slab, then halo <- bounce[slab]
 template <typename T>
 __global__ void halo_pack_kernel(FieldSet<T> fs, T* bounce, const BlockLayout L, int axis,
                                  Slab sl, int unpack)
 {
-    T* f = fs.p[blockIdx.y];
-    const long long per_blk = 2 * sl.cells;
-    const long long total = per_blk * L.nblk;
-    T* buf = bounce + blockIdx.y * total;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-         e += (long long)gridDim.x * blockDim.x) {
-        const int blk = (int)(e / per_blk);
-        long long r = e - blk * per_blk;
-        const int side = (int)(r / sl.cells);
-        r -= side * sl.cells;
-        const int c0 = (int)(r % sl.e[0]);
-        const long long r1 = r / sl.e[0];
-        const int c1 = (int)(r1 % sl.e[1]);
-        const int c2 = (int)(r1 / sl.e[1]);
+    const int side = blockIdx.y & 1;
+    const int blk = (blockIdx.y >> 1) % L.nblk;
+    const int fld = (blockIdx.y >> 1) / L.nblk;
+    T* f = fs.p[fld];
+    const int cells = (int)sl.cells;
+    T* buf = bounce + ((long long)fld * L.nblk * 2 + blk * 2 + side) * sl.cells;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < cells; e += gridDim.x * blockDim.x) {
+        const int c0 = e % sl.e[0];
+        const int r1 = e / sl.e[0];
+        const int c1 = r1 % sl.e[1];
+        const int c2 = r1 / sl.e[1];
         long long dst, src;
         if (!slab_map(L, axis, blk, side, c0, c1, c2, dst, src)) continue;
         if (unpack) f[dst] = buf[e];
@@ -199,8 +195,12 @@ cudaError_t launch_halo_exchange(const FieldSet<T>& fs, int nfields, const Block
     if (L.nblk == 1 && !L.periodic) return cudaSuccess;   // all halos are shell
     for (int axis = 0; axis < 3; ++axis) {
         const Slab sl = slab_of(L, axis);
-        const long long work = 2 * sl.cells * L.nblk;
-        dim3 grid(grid_for(work, 256), nfields);
+        long long gx = (sl.cells + 255) / 256;
+        const long long per_y = 2LL * L.nblk * nfields;
+        const long long cap = (152LL * 32 + per_y - 1) / per_y;   // ~32 CTAs per SM overall
+        if (gx > cap) gx = cap;
+        if (gx < 1) gx = 1;
+        dim3 grid((unsigned)gx, (unsigned)per_y);
         if (bounce == nullptr) {
             halo_direct_kernel<T><<<grid, 256, 0, st>>>(fs, L, axis, sl);
             count_launches(1);
