@@ -20,7 +20,7 @@ import os
 
 import numpy as np
 
-__all__ = ["Domain", "B2RError", "heat_3D_gpu_main", "gol_3D_gpu_main", "lib", "LIB_PATH",
+__all__ = ["Domain", "Batch", "B2RError", "heat_3D_gpu_main", "gol_3D_gpu_main", "lib", "LIB_PATH",
            "MODEL_HEAT", "MODEL_GOL", "MODEL_EQWP_REF", "MODEL_EQWP_STAG", "BC_SHELL",
            "BC_PERIODIC", "FIELDS"]
 
@@ -46,6 +46,12 @@ class Config(C.Structure):
                 ("alpha_dt", C.c_double), ("dx", C.c_double), ("dy", C.c_double),
                 ("dz", C.c_double), ("dt", C.c_double), ("h", C.c_double),
                 ("src", C.c_int * 3)]
+
+
+class BatchItem(C.Structure):
+    _fields_ = [("env", C.c_int * 3), ("D", C.c_int), ("nsteps", C.c_int),
+                ("alpha_dt", C.c_double), ("dx", C.c_double), ("dy", C.c_double),
+                ("dz", C.c_double)]
 
 
 _lib = None
@@ -86,6 +92,16 @@ def lib():
         "b2r_gol_3D_gpu_main": ([vp, i, C.c_char_p, i, i, i, vp, C.POINTER(d)], i),
         "b2r_eqwp_gpu_main": ([vp, i, i, C.POINTER(d)], i),
         "b2r_kernel_launches": ([], C.c_int64),
+        "b2r_batch_create": ([C.POINTER(BatchItem), i, C.POINTER(vp)], i),
+        "b2r_batch_destroy": ([vp], i),
+        "b2r_batch_last_error": ([], C.c_char_p),
+        "b2r_batch_upload": ([vp, i, vp, i, vp], i),
+        "b2r_batch_download": ([vp, i, vp, i, vp], i),
+        "b2r_batch_run": ([vp, vp, i], i),
+        "b2r_batch_synchronize": ([vp, vp], i),
+        "b2r_batch_lups": ([vp], C.c_int64),
+        "b2r_batch_set_zchunk": ([vp, i], i),
+        "b2r_batch_autotune": ([vp, vp, C.POINTER(C.c_int), C.POINTER(d)], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -250,6 +266,85 @@ class Domain:
         secs = C.c_double()
         _check(lib().b2r_eqwp_gpu_main(self.h, ts, R, C.byref(secs)), self.h)
         return secs.value
+
+
+def _bcheck(st):
+    if st != 0:
+        msg = lib().b2r_batch_last_error()
+        raise B2RError(st, msg.decode() if msg else "")
+
+
+class Batch:
+    """Independent heat instances advanced in one persistent launch (b2r_batch_*).
+
+    items: iterable of dicts with env (x, y, z), D, nsteps and optionally
+    alpha_dt, dx, dy, dz.  Instance arrays have a fixed shell of D cells."""
+
+    def __init__(self, items, stream=None):
+        items = list(items)
+        arr = (BatchItem * len(items))()
+        for k, it in enumerate(items):
+            arr[k].env[:] = list(it["env"])
+            arr[k].D = it["D"]
+            arr[k].nsteps = it["nsteps"]
+            arr[k].alpha_dt = it.get("alpha_dt", 0.01)
+            arr[k].dx, arr[k].dy, arr[k].dz = it.get("dx", 1.0), it.get("dy", 1.0), it.get("dz", 1.0)
+        self.items = items
+        hnd = C.c_void_p()
+        _bcheck(lib().b2r_batch_create(arr, len(items), C.byref(hnd)))
+        self.h = hnd
+        self.stream = C.c_void_p(int(getattr(stream, "cuda_stream", stream) or 0))
+
+    def shape(self, i):
+        it = self.items[i]
+        return tuple(e + 2 * it["D"] for e in it["env"][::-1])
+
+    @property
+    def lups(self):
+        return int(lib().b2r_batch_lups(self.h))
+
+    def upload(self, i, arr):
+        p, dev = _ptr(arr)
+        _bcheck(lib().b2r_batch_upload(self.h, i, p, dev, self.stream))
+
+    def download(self, i, out=None):
+        if out is None:
+            out = np.empty(self.shape(i), np.float32)
+        p, dev = _ptr(out)
+        _bcheck(lib().b2r_batch_download(self.h, i, p, dev, self.stream))
+        return out
+
+    def run(self, graph=True):
+        _bcheck(lib().b2r_batch_run(self.h, self.stream, 1 if graph else 0))
+
+    def synchronize(self):
+        _bcheck(lib().b2r_batch_synchronize(self.h, self.stream))
+
+    def set_zchunk(self, z):
+        _bcheck(lib().b2r_batch_set_zchunk(self.h, int(z)))
+
+    def autotune(self):
+        z = C.c_int()
+        ms = C.c_double()
+        _bcheck(lib().b2r_batch_autotune(self.h, self.stream, C.byref(z), C.byref(ms)))
+        return z.value, ms.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().b2r_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def kernel_launches():

@@ -16,27 +16,15 @@
 // One HBM read and one write per cell and sub-step; the skirt re-reads hit L2.
 #include <cstdio>
 
-#include "b2r_common.cuh"
-#include "heat.h"
+#include "heat_unit.cuh"
 
 namespace b2r {
 
 namespace {
 
-constexpr int kTX = 128;     // tile width (cells): 32 lanes x float4
-constexpr int kWarps = 8;
-constexpr int kThreads = 32 * kWarps;
-
-template <int D, int RY, int S>
-struct HeatCfg {
-    static constexpr int TY = kWarps * RY;
-    static constexpr int BW = kTX + 8;       // 4-cell skirt on both sides (D <= 4)
-    static constexpr int BH = TY + 2 * D;
-    static constexpr int PLANE = BW * BH;    // floats of one tile plane
-    static constexpr int SLOT = (PLANE + 31) / 32 * 32;   // ring slot stride: 128-byte aligned
-    // ring, then S mbarriers, then the abort flag, plus 128 B to align the base
-    static constexpr size_t SMEM = size_t(S) * SLOT * sizeof(float) + S * sizeof(uint64_t) + 16 + 128;
-};
+using heatk::kThreads;
+using heatk::kTX;
+using heatk::kWarps;
 
 // Work schedule of one launch: units = (block, z-chunk of Lz output planes,
 // tile row, tile column) numbered with the tile column fastest, dealt
@@ -53,41 +41,26 @@ struct HeatSched {
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;"); }
 
+// resident CTAs per SM the register budget is fitted to, by stencil radius
+template <int D>
+struct MinBlocks {
+    static constexpr int value = D == 1 ? 5 : (D == 2 ? 3 : 2);
+};
+
 template <int D, int RY, int S>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, MinBlocks<D>::value)
 heat_sweep_kernel(const __grid_constant__ CUtensorMap tin, float* __restrict__ out,
                   const BlockLayout L, const int step_i, const HeatCoef C, const HeatSched sch,
                   int* __restrict__ status)
 {
-    using Cfg = HeatCfg<D, RY, S>;
+    using Cfg = heatk::Cfg<D, RY, S>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    // TMA destinations must be 128-byte aligned: align the base by hand
-    float* smem = reinterpret_cast<float*>(smem_raw + ((128 - (smem_u32(smem_raw) & 127)) & 127));
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + S * Cfg::SLOT);
-    int& abort_flag = *reinterpret_cast<int*>(bar + S);
-
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) {
-        abort_flag = 0;
-#pragma unroll
-        for (int s = 0; s < S; ++s) mbar_init(&bar[s], 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
+    heatk::Ring rg;
+    heatk::ring_init<S, Cfg::SLOT>(rg, smem_raw);
     // the input was written by the previous launch on this stream
     pdl_wait();
     pdl_trigger();
-
-    const float a0 = C.a0;
-    float ax[D], ay[D], az[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) { ax[k] = C.ax[k]; ay[k] = C.ay[k]; az[k] = C.az[k]; }
-
-    unsigned gp = 0;             // ring position: planes streamed by this CTA so far
-    bool aborted = false;
-    int pr = 0, np = 0;
-    unsigned issued_hi = 0;
-    for (long long u = blockIdx.x; u < sch.U && !aborted; u += gridDim.x) {
+    for (long long u = blockIdx.x; u < sch.U; u += gridDim.x) {
         const int tx = (int)(u % sch.ntx);
         long long r = u / sch.ntx;
         const int ty = (int)(r % sch.nty);
@@ -96,119 +69,11 @@ heat_sweep_kernel(const __grid_constant__ CUtensorMap tin, float* __restrict__ o
         const int blk = (int)(r / sch.nzc);
         const int zi0 = zc * sch.Lz;
         const int zi1 = min(sch.NZ, zi0 + sch.Lz);
-
-        const int edge = edge_bits(L, blk);
-        int lo[3], hi[3];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) stage_region(L, edge, a, D * (step_i + 1), lo[a], hi[a]);
-        const int xs0 = ((L.xoff + D) & ~3) + tx * kTX;      // storage x of tile column 0
-        const int y0 = D + ty * Cfg::TY;                     // block y of tile row 0
-        if (xs0 - L.xoff > hi[0] || xs0 + kTX - 1 - L.xoff < lo[0]) continue;
-        if (y0 > hi[1] || y0 + Cfg::TY - 1 < lo[1]) continue;
-        const int zs = max(D + zi0, lo[2]);
-        const int ze = min(D + zi1 - 1, hi[2]);
-        if (zs > ze) continue;
-
-        const int first = zs - D;               // first input plane
-        np = (ze + D) - first + 1;              // input planes streamed
-        if (tid == 0) {
-            for (int s = 0; s < S && s < np; ++s) {
-                const unsigned g = gp + s;
-                mbar_expect_tx(&bar[g % S], Cfg::PLANE * sizeof(float));
-                tma_load_4d(smem + (g % S) * Cfg::SLOT, &tin, xs0 - 4, y0 - D, first + s, blk,
-                            &bar[g % S]);
-            }
+        if (!heatk::sweep_unit<D, RY, S, Cfg::SLOT>(&tin, out, L, step_i, C, blk, tx, ty, zi0, zi1, rg)) {
+            if (threadIdx.x == 0) report(status, DEV_TIMEOUT);
+            heatk::ring_drain<S>(rg);
+            return;
         }
-        issued_hi = gp + min(S, np);
-
-        const int xb = xs0 + 4 * lane - L.xoff;             // block x of this lane's first cell
-        bool vx[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) vx[j] = (xb + j >= lo[0]) && (xb + j <= hi[0]);
-        const bool vx_all = vx[0] && vx[1] && vx[2] && vx[3];
-        const bool vx_any = vx[0] || vx[1] || vx[2] || vx[3];
-
-        float4 q[RY][2 * D + 1];
-        float* const outb = out + (long long)blk * L.bstride + xs0 + 4 * lane;
-
-        for (pr = 0; pr < np; ++pr) {
-            const unsigned g = gp + pr;
-            if (!mbar_wait_bounded(&bar[g % S], (g / S) & 1)) abort_flag = 1;
-            const float* pl = smem + (g % S) * Cfg::SLOT;
-#pragma unroll
-            for (int r2 = 0; r2 < RY; ++r2) {
-#pragma unroll
-                for (int k = 0; k < 2 * D; ++k) q[r2][k] = q[r2][k + 1];
-                const int row = D + warp * RY + r2;
-                q[r2][2 * D] = *reinterpret_cast<const float4*>(pl + row * Cfg::BW + 4 + 4 * lane);
-            }
-            if (pr >= 2 * D && vx_any) {
-                const int z = first + pr - D;
-                const float* pc = smem + ((g - D) % S) * Cfg::SLOT;
-#pragma unroll
-                for (int r2 = 0; r2 < RY; ++r2) {
-                    const int y = y0 + warp * RY + r2;
-                    if (y < lo[1] || y > hi[1]) continue;
-                    const int row = D + warp * RY + r2;
-                    const float* prow = pc + row * Cfg::BW + 4 * lane;
-                    const float4 xl = *reinterpret_cast<const float4*>(prow);
-                    const float4 c4 = q[r2][D];
-                    const float4 xr = *reinterpret_cast<const float4*>(prow + 8);
-                    const float v[12] = {xl.x, xl.y, xl.z, xl.w, c4.x, c4.y, c4.z, c4.w,
-                                         xr.x, xr.y, xr.z, xr.w};
-                    float res[4];
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) res[j] = a0 * v[4 + j];
-#pragma unroll
-                    for (int k = 1; k <= D; ++k) {
-                        const float4 ym = *reinterpret_cast<const float4*>(prow + 4 - k * Cfg::BW);
-                        const float4 yp = *reinterpret_cast<const float4*>(prow + 4 + k * Cfg::BW);
-                        const float4 zm = q[r2][D - k];
-                        const float4 zp = q[r2][D + k];
-                        const float ys[4] = {ym.x + yp.x, ym.y + yp.y, ym.z + yp.z, ym.w + yp.w};
-                        const float zsum[4] = {zm.x + zp.x, zm.y + zp.y, zm.z + zp.z, zm.w + zp.w};
-#pragma unroll
-                        for (int j = 0; j < 4; ++j) {
-                            res[j] = fmaf(ax[k - 1], v[4 + j - k] + v[4 + j + k], res[j]);
-                            res[j] = fmaf(ay[k - 1], ys[j], res[j]);
-                            res[j] = fmaf(az[k - 1], zsum[j], res[j]);
-                        }
-                    }
-                    float* dst = outb + (long long)z * L.plane + (long long)y * L.P;
-                    if (vx_all) {
-                        *reinterpret_cast<float4*>(dst) = make_float4(res[0], res[1], res[2], res[3]);
-                    } else {
-#pragma unroll
-                        for (int j = 0; j < 4; ++j)
-                            if (vx[j]) dst[j] = res[j];
-                    }
-                }
-            }
-            __syncthreads();
-            if (abort_flag) {
-                aborted = true;
-                break;
-            }
-            if (pr >= D) {
-                const int nxt = pr - D + S;
-                if (nxt < np) {
-                    const unsigned g2 = gp + nxt;
-                    if (tid == 0) {
-                        mbar_expect_tx(&bar[g2 % S], Cfg::PLANE * sizeof(float));
-                        tma_load_4d(smem + (g2 % S) * Cfg::SLOT, &tin, xs0 - 4, y0 - D, first + nxt,
-                                    blk, &bar[g2 % S]);
-                    }
-                    issued_hi = g2 + 1;
-                }
-            }
-        }
-        if (!aborted) gp += np;
-    }
-    if (aborted && tid == 0) {
-        report(status, DEV_TIMEOUT);
-        // drain the loads still in flight (bounded) before the CTA retires
-        for (unsigned g = gp + pr; g < issued_hi; ++g)
-            mbar_wait_bounded(&bar[g % S], (g / S) & 1, 100000000ull);
     }
 }
 
@@ -216,7 +81,7 @@ template <int D, int RY, int S>
 cudaError_t launch_t(const CUtensorMap* tin, float* out, const BlockLayout& L, int step_i,
                      const HeatCoef& c, int* status, cudaStream_t st, const HeatTune& tune)
 {
-    using Cfg = HeatCfg<D, RY, S>;
+    using Cfg = heatk::Cfg<D, RY, S>;
     auto kern = heat_sweep_kernel<D, RY, S>;
     static int resident = 0;    // CTAs resident on the whole GPU
     static int resident_per_sm = 0;

@@ -1,0 +1,198 @@
+// heat_unit.cuh -- one work unit of the heat sweep: one 128 x TY tile of one
+// block over a chunk of output planes, one sub-step.  Shared by the plain
+// sweep (heat.cu) and the batched persistent kernel (batch.cu).
+//
+// Every input plane of the tile plus a D-row / 4-column skirt arrives in
+// shared memory by one TMA 4-D box (x, y, z, block) into an S-deep ring with
+// one mbarrier per slot; each thread holds 4 consecutive x cells of RY rows
+// and keeps 2D+1 planes of them in a float4 register queue along z; the xy
+// neighbours of the current plane come from shared memory.  The ring position
+// (planes streamed so far) carries over from unit to unit, so a persistent
+// CTA keeps its barriers' phases consistent across units.
+//
+// Scheme (heat-3D.cu:228-231, 315-318, 410-413, 514-517), folded:
+//     u' = a0*u + sum_k [ax_k (u[x-k]+u[x+k]) + ay_k (..y..) + az_k (..z..)].
+#pragma once
+#include "b2r_common.cuh"
+#include "heat.h"
+
+namespace b2r {
+namespace heatk {
+
+constexpr int kTX = 128;     // tile width (cells): 32 lanes x float4
+constexpr int kWarps = 8;
+constexpr int kThreads = 32 * kWarps;
+
+// ring geometry for radius D, RY rows per warp, S slots of SLOT floats
+template <int D, int RY, int S, int SLOT_ = 0>
+struct Cfg {
+    static constexpr int TY = kWarps * RY;
+    static constexpr int BW = kTX + 8;       // 4-cell skirt on both sides (D <= 4)
+    static constexpr int BH = TY + 2 * D;
+    static constexpr int PLANE = BW * BH;    // floats of one tile plane
+    static constexpr int SLOT = SLOT_ > 0 ? SLOT_ : (PLANE + 31) / 32 * 32;   // 128-byte aligned
+    // ring, then S mbarriers, then the abort flag, plus 128 B to align the base
+    static constexpr size_t SMEM = size_t(S) * SLOT * sizeof(float) + S * sizeof(uint64_t) + 16 + 128;
+};
+
+// Per-CTA ring state in shared memory / registers.
+struct Ring {
+    float* smem;
+    uint64_t* bar;
+    int* abort_flag;
+    unsigned gp;          // planes streamed by this CTA so far (ring position)
+    unsigned issued_hi;   // ring position one past the last plane issued
+    unsigned stop;        // ring position where an abort happened
+};
+
+template <int S, int SLOT>
+__device__ __forceinline__ void ring_init(Ring& rg, unsigned char* smem_raw)
+{
+    // TMA destinations must be 128-byte aligned: align the base by hand
+    rg.smem = reinterpret_cast<float*>(smem_raw + ((128 - (smem_u32(smem_raw) & 127)) & 127));
+    rg.bar = reinterpret_cast<uint64_t*>(rg.smem + S * SLOT);
+    rg.abort_flag = reinterpret_cast<int*>(rg.bar + S);
+    rg.gp = rg.issued_hi = rg.stop = 0;
+    if (threadIdx.x == 0) {
+        *rg.abort_flag = 0;
+#pragma unroll
+        for (int s = 0; s < S; ++s) mbar_init(&rg.bar[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+}
+
+// After an abort: thread 0 waits (bounded) for the loads still in flight.
+template <int S>
+__device__ __forceinline__ void ring_drain(const Ring& rg)
+{
+    if (threadIdx.x == 0)
+        for (unsigned g = rg.stop; g < rg.issued_hi; ++g)
+            mbar_wait_bounded(&rg.bar[g % S], (g / S) & 1, 100000000ull);
+}
+
+// Sweep one unit.  Returns false if a bounded wait gave up (all threads
+// agree: the decision is taken after a __syncthreads on a shared flag).
+template <int D, int RY, int S, int SLOT>
+__device__ __forceinline__ bool sweep_unit(const CUtensorMap* tmap, float* __restrict__ out,
+                                           const BlockLayout& L, int step_i, const HeatCoef& C,
+                                           int blk, int tx, int ty, int zi0, int zi1, Ring& rg)
+{
+    using G = Cfg<D, RY, S, SLOT>;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int edge = edge_bits(L, blk);
+    int lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) stage_region(L, edge, a, D * (step_i + 1), lo[a], hi[a]);
+    const int xs0 = ((L.xoff + D) & ~3) + tx * kTX;      // storage x of tile column 0
+    const int y0 = D + ty * G::TY;                       // block y of tile row 0
+    if (xs0 - L.xoff > hi[0] || xs0 + kTX - 1 - L.xoff < lo[0]) return true;
+    if (y0 > hi[1] || y0 + G::TY - 1 < lo[1]) return true;
+    const int zs = max(D + zi0, lo[2]);
+    const int ze = min(D + zi1 - 1, hi[2]);
+    if (zs > ze) return true;
+
+    const float a0 = C.a0;
+    float ax[D], ay[D], az[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) { ax[k] = C.ax[k]; ay[k] = C.ay[k]; az[k] = C.az[k]; }
+
+    const unsigned gp = rg.gp;
+    const int first = zs - D;                // first input plane
+    const int np = (ze + D) - first + 1;     // input planes streamed
+    if (tid == 0) {
+        for (int s = 0; s < S && s < np; ++s) {
+            const unsigned g = gp + s;
+            mbar_expect_tx(&rg.bar[g % S], G::PLANE * sizeof(float));
+            tma_load_4d(rg.smem + (g % S) * SLOT, tmap, xs0 - 4, y0 - D, first + s, blk, &rg.bar[g % S]);
+        }
+    }
+    rg.issued_hi = gp + min(S, np);
+
+    const int xb = xs0 + 4 * lane - L.xoff;             // block x of this lane's first cell
+    bool vx[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) vx[j] = (xb + j >= lo[0]) && (xb + j <= hi[0]);
+    const bool vx_all = vx[0] && vx[1] && vx[2] && vx[3];
+    const bool vx_any = vx[0] || vx[1] || vx[2] || vx[3];
+
+    float4 q[RY][2 * D + 1];
+    float* const outb = out + (long long)blk * L.bstride + xs0 + 4 * lane;
+
+    for (int pr = 0; pr < np; ++pr) {
+        const unsigned g = gp + pr;
+        if (!mbar_wait_bounded(&rg.bar[g % S], (g / S) & 1)) *rg.abort_flag = 1;
+        const float* pl = rg.smem + (g % S) * SLOT;
+#pragma unroll
+        for (int r2 = 0; r2 < RY; ++r2) {
+#pragma unroll
+            for (int k = 0; k < 2 * D; ++k) q[r2][k] = q[r2][k + 1];
+            const int row = D + warp * RY + r2;
+            q[r2][2 * D] = *reinterpret_cast<const float4*>(pl + row * G::BW + 4 + 4 * lane);
+        }
+        if (pr >= 2 * D && vx_any) {
+            const int z = first + pr - D;
+            const float* pc = rg.smem + ((g - D) % S) * SLOT;
+#pragma unroll
+            for (int r2 = 0; r2 < RY; ++r2) {
+                const int y = y0 + warp * RY + r2;
+                if (y < lo[1] || y > hi[1]) continue;
+                const int row = D + warp * RY + r2;
+                const float* prow = pc + row * G::BW + 4 * lane;
+                const float4 xl = *reinterpret_cast<const float4*>(prow);
+                const float4 c4 = q[r2][D];
+                const float4 xr = *reinterpret_cast<const float4*>(prow + 8);
+                const float v[12] = {xl.x, xl.y, xl.z, xl.w, c4.x, c4.y, c4.z, c4.w,
+                                     xr.x, xr.y, xr.z, xr.w};
+                float res[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) res[j] = a0 * v[4 + j];
+#pragma unroll
+                for (int k = 1; k <= D; ++k) {
+                    const float4 ym = *reinterpret_cast<const float4*>(prow + 4 - k * G::BW);
+                    const float4 yp = *reinterpret_cast<const float4*>(prow + 4 + k * G::BW);
+                    const float4 zm = q[r2][D - k];
+                    const float4 zp = q[r2][D + k];
+                    const float ys[4] = {ym.x + yp.x, ym.y + yp.y, ym.z + yp.z, ym.w + yp.w};
+                    const float zsum[4] = {zm.x + zp.x, zm.y + zp.y, zm.z + zp.z, zm.w + zp.w};
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        res[j] = fmaf(ax[k - 1], v[4 + j - k] + v[4 + j + k], res[j]);
+                        res[j] = fmaf(ay[k - 1], ys[j], res[j]);
+                        res[j] = fmaf(az[k - 1], zsum[j], res[j]);
+                    }
+                }
+                float* dst = outb + (long long)z * L.plane + (long long)y * L.P;
+                if (vx_all) {
+                    *reinterpret_cast<float4*>(dst) = make_float4(res[0], res[1], res[2], res[3]);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (vx[j]) dst[j] = res[j];
+                }
+            }
+        }
+        __syncthreads();
+        if (*rg.abort_flag) {
+            rg.stop = g;
+            return false;
+        }
+        if (pr >= D) {
+            const int nxt = pr - D + S;
+            if (nxt < np) {
+                const unsigned g2 = gp + nxt;
+                if (tid == 0) {
+                    mbar_expect_tx(&rg.bar[g2 % S], G::PLANE * sizeof(float));
+                    tma_load_4d(rg.smem + (g2 % S) * SLOT, tmap, xs0 - 4, y0 - D, first + nxt, blk,
+                                &rg.bar[g2 % S]);
+                }
+                rg.issued_hi = g2 + 1;
+            }
+        }
+    }
+    rg.gp = gp + np;
+    return true;
+}
+
+}  // namespace heatk
+}  // namespace b2r

@@ -55,6 +55,10 @@ WORKLOADS = {
     # 3-D Game of Life, 256^3 torus, 2x2x2 subdomains, R = 4, 400 generations
     "gol_256": dict(model=2, env=(256, 256, 256), blocks=(2, 2, 2), R=4, D=1, sub_steps=400,
                     bytes_per_cell=2, kernel="gol_kernel", periodic=True),
+    # 64 independent heat instances, edges U{32,48,..,192} per axis, D U{1..4},
+    # steps U[50,500], seed 4, in one persistent launch replayed from a CUDA graph
+    "batch64": dict(model=5, n=64, seed=4, env=(0, 0, 0), blocks=(1, 1, 1), R=1, D=0, sub_steps=0,
+                    bytes_per_cell=8, kernel="batch_kernel"),
     # the reference's collocated elastic-wave model, 512x512x256, one block, R = 1
     "eqwp_ref": dict(model=3, env=(512, 512, 256), blocks=(1, 1, 1), R=1, D=2, sub_steps=100,
                      bytes_per_cell=80, kernel="eqwp_ref_stress+velocity"),
@@ -287,6 +291,97 @@ def load_inputs(d, wl, torch, dev):
     return zero
 
 
+def batch_items(wl):
+    rng = np.random.default_rng(wl["seed"])
+    edges = np.arange(32, 193, 16)
+    items = []
+    for _ in range(wl["n"]):
+        items.append(dict(env=tuple(int(v) for v in rng.choice(edges, 3)), D=int(rng.integers(1, 5)),
+                          nsteps=int(rng.integers(50, 501)), alpha_dt=0.02, dx=1.0, dy=1.0, dz=1.0))
+    return items
+
+
+def run_batch(args, wl):
+    """Config 4: batched instances vs the same instances as sequential plain runs."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    import b2r_gb300 as b2r
+    dev = torch.device("cuda", 0)
+    items = batch_items(wl)
+    rng = np.random.default_rng(wl["seed"] + 1)
+    ins = []
+    for it in items:
+        D = it["D"]
+        a = np.zeros(tuple(e + 2 * D for e in it["env"][::-1]), np.float32)
+        a[D:-D, D:-D, D:-D] = rng.random(it["env"][::-1], dtype=np.float32)
+        ins.append(a)
+    stream = torch.cuda.Stream(device=dev)
+    bt = b2r.Batch(items, stream=stream)
+    for i, a in enumerate(ins):
+        bt.upload(i, a)
+    tuned = bt.autotune()
+    lups = bt.lups
+    for _ in range(args.warmup):
+        bt.run()
+    bt.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    l0 = b2r.kernel_launches()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        bt.run()
+    e1.record(stream)
+    e1.synchronize()
+    launches = b2r.kernel_launches() - l0
+    bt.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    value = lups / (ms / 1e3) / 1e9
+    got = [bt.download(i) for i in range(len(items))]
+    # the same instances as sequential plain runs (one handle each, graphs on)
+    seq_ms = 0.0
+    max_rel = 0.0
+    for i, it in enumerate(items):
+        with b2r.Domain(b2r.MODEL_HEAT, it["env"], D=it["D"], alpha_dt=0.02, stream=stream) as d:
+            d.upload(ins[i])
+            d.step(it["nsteps"])              # warm the graphs
+            d.upload(ins[i])
+            d.synchronize()
+            a0 = torch.cuda.Event(enable_timing=True)
+            a1 = torch.cuda.Event(enable_timing=True)
+            a0.record(stream)
+            d.step(it["nsteps"])
+            a1.record(stream)
+            a1.synchronize()
+            seq_ms += a0.elapsed_time(a1)
+            plain = d.download()
+        max_rel = max(max_rel, float(np.linalg.norm(got[i].astype(np.float64) - plain) /
+                                     np.linalg.norm(plain.astype(np.float64))))
+    seq = lups / (seq_ms / 1e3) / 1e9
+    peak, peak_src = measured_peak()
+    achieved = wl["bytes_per_cell"] * lups / (ms / 1e3) / 1e9
+    bt.close()
+    line = {"metric": "GLUPS", "value": round(value, 3), "unit": "GLUPS", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded U[0,1))",
+            "config": {"workload": args.workload, "instances": len(items), "lups_per_step": lups,
+                       "autotuned_zchunk": tuned[0],
+                       "sequential_plain_glups": round(seq, 3),
+                       "batched_over_sequential": round(value / seq, 3),
+                       "max_rel_l2_vs_sequential": max_rel,
+                       "l2": "inputs larger than L2"},
+            "e2e": None, "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_src,
+                         "kernel": "batch_kernel", "note": "8 B per lattice-site update, whole run"},
+            "cpu_baseline": None, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def run_ours(args, wl):
     import torch
     import torch.distributed as dist
@@ -442,6 +537,8 @@ def main():
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, wl)
+    elif wl["model"] == 5:
+        run_batch(args, wl)
     else:
         run_ours(args, wl)
 

@@ -189,6 +189,45 @@ b2r_status b2r_heat_3D_gpu_main_noalloc(const float* d_in, float* d_out, int R, 
  * (selects the body force, eqwp.cu:135).  Does not exchange halos. */
 b2r_status b2r_eqwp_gpu_main(b2r_handle* h, int ts, int R, double* gpu_seconds);
 
+/* ---- batched instances (no reference counterpart) ------------------------ */
+/* Many independent single-block heat domains of uneven sizes and stencil
+ * orders advanced in one persistent launch driven by a device work queue of
+ * (time step, instance, tile chunk) items, replayable from a CUDA graph.
+ * Each instance is a domain array with a fixed shell of D cells
+ * ((env+2D) cells per axis, reference layout) stepped nsteps times with the
+ * heat scheme; results are identical to a plain b2r_step run of the same
+ * instance. */
+typedef struct {
+    int env[3];                      /* interior cells per axis */
+    int D;                           /* stencil radius 1..4 */
+    int nsteps;                      /* time steps of this instance */
+    double alpha_dt, dx, dy, dz;     /* heat coefficients as in b2r_config */
+} b2r_batch_item;
+typedef struct b2r_batch b2r_batch;
+
+b2r_status b2r_batch_create(const b2r_batch_item* items, int n, b2r_batch** out);
+b2r_status b2r_batch_destroy(b2r_batch* b);
+const char* b2r_batch_last_error(void);
+/* Domain array of instance i (caller order) into both of its buffers. */
+b2r_status b2r_batch_upload(b2r_batch* b, int i, const float* src, int src_is_device,
+                            void* cuda_stream);
+/* Result of instance i after its nsteps (synchronous for host dst). */
+b2r_status b2r_batch_download(b2r_batch* b, int i, float* dst, int dst_is_device,
+                              void* cuda_stream);
+/* Run every instance to its nsteps: one persistent launch (plus two counter
+ * resets), captured once into a CUDA graph and replayed when use_graph != 0
+ * and the stream is not the legacy default stream.  Asynchronous. */
+b2r_status b2r_batch_run(b2r_batch* b, void* cuda_stream, int use_graph);
+/* Wait for the stream and report a device-side timeout of the work queue. */
+b2r_status b2r_batch_synchronize(b2r_batch* b, void* cuda_stream);
+/* Total lattice-site updates of one run (sum of cells x steps). */
+int64_t b2r_batch_lups(const b2r_batch* b);
+/* Planes per work unit along z (0 = whole column). */
+b2r_status b2r_batch_set_zchunk(b2r_batch* b, int zchunk);
+/* Time whole runs with each z-chunk candidate (8, 16, 32, 64, whole column)
+ * on the uploaded inputs, keep the fastest and restore the inputs. */
+b2r_status b2r_batch_autotune(b2r_batch* b, void* cuda_stream, int* best_zchunk, double* best_ms);
+
 #ifdef __cplusplus
 }
 #endif

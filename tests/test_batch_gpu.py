@@ -1,0 +1,81 @@
+"""Batched persistent launch: every instance matches its own plain run."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def mix(n, seed, max_edge=96, max_steps=40):
+    rng = np.random.default_rng(seed)
+    edges = np.arange(32, max_edge + 1, 16)
+    items = []
+    for _ in range(n):
+        items.append(dict(env=tuple(int(v) for v in rng.choice(edges, 3)), D=int(rng.integers(1, 5)),
+                          nsteps=int(rng.integers(5, max_steps + 1)), alpha_dt=0.02, dx=1.0, dy=1.0,
+                          dz=1.0))
+    return items
+
+
+def inputs(items, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for it in items:
+        D = it["D"]
+        a = np.zeros(tuple(e + 2 * D for e in it["env"][::-1]), np.float32)
+        a[D:-D, D:-D, D:-D] = rng.random(it["env"][::-1], dtype=np.float32)
+        out.append(a)
+    return out
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_batch_matches_plain_runs(b2r, orc, graph):
+    import torch
+    items = mix(12, 1)
+    ins = inputs(items, 2)
+    s = torch.cuda.Stream()
+    with b2r.Batch(items, stream=s) as bt:
+        for i, a in enumerate(ins):
+            bt.upload(i, a)
+        bt.run(graph=graph)
+        bt.synchronize()
+        got = [bt.download(i) for i in range(len(items))]
+        # a second run from the same inputs gives the same bits
+        for i, a in enumerate(ins):
+            bt.upload(i, a)
+        bt.run(graph=graph)
+        bt.synchronize()
+        again = [bt.download(i) for i in range(len(items))]
+    for i, it in enumerate(items):
+        with b2r.Domain(b2r.MODEL_HEAT, it["env"], D=it["D"], alpha_dt=0.02) as d:
+            d.upload(ins[i])
+            d.step(it["nsteps"])
+            plain = d.download()
+        assert np.array_equal(got[i], plain), i
+        assert np.array_equal(again[i], plain), i
+    # and the oracle agrees within the FP32 tolerance on a couple of them
+    for i in (0, 5):
+        ref = ins[i].copy()
+        it = items[i]
+        orc.heat_run(ref, it["D"], it["D"], it["nsteps"], 0.02, 1.0, 1.0, 1.0)
+        rel = np.linalg.norm(got[i].astype(np.float64) - ref) / np.linalg.norm(ref)
+        assert rel <= 1e-5
+
+
+def test_batch_autotune_keeps_inputs(b2r):
+    import torch
+    items = mix(6, 3, max_edge=64, max_steps=12)
+    ins = inputs(items, 4)
+    s = torch.cuda.Stream()
+    with b2r.Batch(items, stream=s) as bt:
+        for i, a in enumerate(ins):
+            bt.upload(i, a)
+        z, ms = bt.autotune()
+        assert z in (8, 16, 32, 64, 0) and ms > 0
+        bt.run()
+        bt.synchronize()
+        got = [bt.download(i) for i in range(len(items))]
+    for i, it in enumerate(items):
+        with b2r.Domain(b2r.MODEL_HEAT, it["env"], D=it["D"], alpha_dt=0.02) as d:
+            d.upload(ins[i])
+            d.step(it["nsteps"])
+            assert np.array_equal(got[i], d.download()), i
