@@ -27,9 +27,22 @@ namespace b2r {
 namespace {
 
 using heatk::kThreads;
-constexpr int kS = 7;                                          // ring slots (D = 4 needs 7)
-constexpr int kSlot = heatk::Cfg<4, 2, kS>::SLOT;             // largest plane (D = 4)
-constexpr size_t kSmem = heatk::Cfg<4, 2, kS>::SMEM;
+// One ring for every stencil order: 5 slots (D = 4 needs D+1), each as large
+// as the biggest plane.  D <= 2 tiles have 2 rows per warp, D >= 3 tiles one
+// (their register queues are 2D+1 planes deep), so the kernel fits 3 CTAs/SM.
+constexpr int kS = 5;
+template <int D>
+struct RowsPerWarp {
+    static constexpr int value = D <= 2 ? 2 : 1;
+};
+constexpr int cmax(int a, int b) { return a > b ? a : b; }
+constexpr int kSlot = cmax(cmax(heatk::Cfg<1, 2, kS>::SLOT, heatk::Cfg<2, 2, kS>::SLOT),
+                           cmax(heatk::Cfg<3, 1, kS>::SLOT, heatk::Cfg<4, 1, kS>::SLOT));
+constexpr size_t kSmem = size_t(kS) * kSlot * sizeof(float) + kS * sizeof(uint64_t) + 16 + 128;
+constexpr int kBoxH[5] = {0, heatk::Cfg<1, 2, kS>::BH, heatk::Cfg<2, 2, kS>::BH,
+                          heatk::Cfg<3, 1, kS>::BH, heatk::Cfg<4, 1, kS>::BH};
+constexpr int kTileY[5] = {0, heatk::Cfg<1, 2, kS>::TY, heatk::Cfg<2, 2, kS>::TY,
+                           heatk::Cfg<3, 1, kS>::TY, heatk::Cfg<4, 1, kS>::TY};
 
 struct InstDev {
     BlockLayout L;
@@ -59,7 +72,7 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
 }
 
 template <int D>
-__device__ __forceinline__ bool run_unit(const BatchArgs& a, const InstDev& in, int k, int t, int u,
+__device__ __noinline__ bool run_unit(const BatchArgs& a, const InstDev& in, int k, int t, int u,
                                          heatk::Ring& rg)
 {
     const int tx = u % in.ntx;
@@ -68,11 +81,11 @@ __device__ __forceinline__ bool run_unit(const BatchArgs& a, const InstDev& in, 
     const int zc = r / in.nty;
     const int zi0 = zc * in.Lz;
     const int zi1 = min(in.NZ, zi0 + in.Lz);
-    return heatk::sweep_unit<D, 2, kS, kSlot>(&a.maps[2 * k + (t & 1)], in.buf[(t + 1) & 1], in.L, 0,
-                                               in.C, 0, tx, ty, zi0, zi1, rg);
+    return heatk::sweep_unit<D, RowsPerWarp<D>::value, kS, kSlot>(
+        &a.maps[2 * k + (t & 1)], in.buf[(t + 1) & 1], in.L, 0, in.C, 0, tx, ty, zi0, zi1, rg);
 }
 
-__global__ void __launch_bounds__(kThreads, 2) batch_kernel(const BatchArgs a)
+__global__ void __launch_bounds__(kThreads, 3) batch_kernel(const BatchArgs a)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     heatk::Ring rg;
@@ -301,14 +314,14 @@ b2r_status b2r_batch_create(const b2r_batch_item* items, int n, b2r_batch** out)
         in.C = heat_coef(D, it.alpha_dt, it.dx, it.dy, it.dz);
         const int xs_begin = (L.xoff + D) & ~3;
         in.ntx = (L.xoff + L.n[0] - D - xs_begin + heatk::kTX - 1) / heatk::kTX;
-        in.nty = (L.n[1] - 2 * D + 15) / 16;
+        in.nty = (L.n[1] - 2 * D + kTileY[D] - 1) / kTileY[D];
         in.NZ = L.n[2] - 2 * D;
         const size_t fb = (size_t)L.bstride * sizeof(float);
         for (int s = 0; s < 2; ++s) {
             if (cudaMalloc(&in.buf[s], fb) != cudaSuccess)
                 return bail(bfail(B2R_ERR_OOM, "instance allocation failed"));
             cudaMemset(in.buf[s], 0, fb);
-            if (!make_block_tmap(&b->maps[2 * k + s], in.buf[s], L, 4, heatk::kTX + 8, 16 + 2 * D, 1))
+            if (!make_block_tmap(&b->maps[2 * k + s], in.buf[s], L, 4, heatk::kTX + 8, kBoxH[D], 1))
                 return bail(bfail(B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed"));
         }
         b->maxsteps = std::max(b->maxsteps, it.nsteps);
