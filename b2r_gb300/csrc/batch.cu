@@ -60,7 +60,7 @@ struct BatchArgs {
     unsigned long long* head;            // next item (zeroed per run)
     unsigned* done;                      // finished units per instance (zeroed per run)
     int* status;
-    int maxsteps;
+    int maxsteps, ninst;
     long long total;
 };
 
@@ -85,39 +85,55 @@ __device__ __noinline__ bool run_unit(const BatchArgs& a, const InstDev& in, int
         &a.maps[2 * k + (t & 1)], in.buf[(t + 1) & 1], in.L, 0, in.C, 0, tx, ty, zi0, zi1, rg);
 }
 
+// Item -> (step, instance, unit) by binary searches in the shared-memory
+// copies of the schedule tables.
+__device__ __forceinline__ void decode(long long item, const long long* step_off, const int* active,
+                                       const long long* prefix, int maxsteps, int& t, int& k, int& u)
+{
+    int lo = 0, hi = maxsteps;                      // last t with step_off[t] <= item
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (step_off[mid] <= item) lo = mid; else hi = mid;
+    }
+    t = lo;
+    const long long r = item - step_off[t];
+    int kl = 0, kh = active[t];                     // last k with prefix[k] <= r
+    while (kh - kl > 1) {
+        const int mid = (kl + kh) >> 1;
+        if (prefix[mid] <= r) kl = mid; else kh = mid;
+    }
+    k = kl;
+    u = (int)(r - prefix[k]);
+}
+
 __global__ void __launch_bounds__(kThreads, 3) batch_kernel(const BatchArgs a)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     heatk::Ring rg;
     heatk::ring_init<kS, kSlot>(rg, smem_raw);
-    __shared__ long long s_item;
-    __shared__ int s_ok;
+    // schedule tables after the ring (the ring ends 16 bytes after its barriers)
+    long long* s_step_off = reinterpret_cast<long long*>(
+        reinterpret_cast<unsigned char*>(rg.abort_flag) + 16);
+    long long* s_prefix = s_step_off + (a.maxsteps + 1);
+    int* s_active = reinterpret_cast<int*>(s_prefix + (a.ninst + 1));
+    for (int i = threadIdx.x; i <= a.maxsteps; i += blockDim.x) {
+        s_step_off[i] = a.step_off[i];
+        s_active[i] = a.active[i];
+    }
+    for (int i = threadIdx.x; i <= a.ninst; i += blockDim.x) s_prefix[i] = a.unit_prefix[i];
+    __shared__ long long s_next;
+    __shared__ int s_t, s_k, s_u, s_ok;
+    if (threadIdx.x == 0) s_next = (long long)atomicAdd(a.head, 1ull);
+    __syncthreads();
     for (;;) {
-        if (threadIdx.x == 0) s_item = (long long)atomicAdd(a.head, 1ull);
-        __syncthreads();
-        const long long item = s_item;
+        const long long item = s_next;
         if (item >= a.total) break;
-        // decode (step, instance, unit)
-        int lo = 0, hi = a.maxsteps;                    // step: last t with step_off[t] <= item
-        while (hi - lo > 1) {
-            const int mid = (lo + hi) >> 1;
-            if (a.step_off[mid] <= item) lo = mid; else hi = mid;
-        }
-        const int t = lo;
-        const long long r = item - a.step_off[t];
-        int kl = 0, kh = a.active[t];                   // instance: last k with prefix[k] <= r
-        while (kh - kl > 1) {
-            const int mid = (kl + kh) >> 1;
-            if (a.unit_prefix[mid] <= r) kl = mid; else kh = mid;
-        }
-        const int k = kl;
-        const int u = (int)(r - a.unit_prefix[k]);
-        const InstDev& in = a.inst[k];
-        // wait for step t-1 of this instance (bounded)
         if (threadIdx.x == 0) {
+            int t, k, u;
+            decode(item, s_step_off, s_active, s_prefix, a.maxsteps, t, k, u);
             int ok = 1;
-            if (t > 0) {
-                const unsigned need = (unsigned)t * (unsigned)in.units;
+            if (t > 0) {        // wait for step t-1 of this instance (bounded)
+                const unsigned need = (unsigned)t * (unsigned)a.inst[k].units;
                 if (ld_acquire(&a.done[k]) < need) {
                     const uint64_t t0 = global_ns();
                     while (ld_acquire(&a.done[k]) < need) {
@@ -125,19 +141,26 @@ __global__ void __launch_bounds__(kThreads, 3) batch_kernel(const BatchArgs a)
                             ok = 0;
                             break;
                         }
-                        __nanosleep(200);
+                        __nanosleep(100);
                     }
                 }
                 // data written by other CTAs' generic stores is read by TMA
                 asm volatile("fence.proxy.async.global;" ::: "memory");
             }
+            s_t = t;
+            s_k = k;
+            s_u = u;
             s_ok = ok;
+            // claim the next item now, so it is ready when this one is done
+            s_next = (long long)atomicAdd(a.head, 1ull);
         }
         __syncthreads();
         if (!s_ok) {
             if (threadIdx.x == 0) report(a.status, DEV_TIMEOUT);
             return;                          // no load of this CTA is in flight here
         }
+        const int t = s_t, k = s_k, u = s_u;
+        const InstDev& in = a.inst[k];
         bool ok;
         switch (in.D) {
         case 1: ok = run_unit<1>(a, in, k, t, u, rg); break;
@@ -182,6 +205,7 @@ struct b2r_batch {
     long long total = 0;
     int lz_policy = 16;              // z chunk cap per unit (autotuned)
     int grid = 0;
+    size_t smem = 0;                 // ring + schedule tables
     cudaGraphExec_t gexec = nullptr;
     cudaStream_t gstream = nullptr;
     long long launches = 0;
@@ -251,8 +275,9 @@ b2r_status enqueue_run(b2r_batch* b, cudaStream_t st)
     a.done = b->d_done;
     a.status = b->d_status;
     a.maxsteps = b->maxsteps;
+    a.ninst = b->n;
     a.total = b->total;
-    batch_kernel<<<b->grid, kThreads, kSmem, st>>>(a);
+    batch_kernel<<<b->grid, kThreads, b->smem, st>>>(a);
     BCK(cudaGetLastError(), "batch launch");
     return B2R_OK;
 }
@@ -339,12 +364,14 @@ b2r_status b2r_batch_create(const b2r_batch_item* items, int n, b2r_batch** out)
     if (cudaMemcpy(b->d_maps, b->maps.data(), sizeof(CUtensorMap) * 2 * n, cudaMemcpyHostToDevice) != cudaSuccess)
         return bail(bfail(B2R_ERR_CUDA, "copy tensor maps"));
     // persistent grid: every resident slot
-    if (cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem) != cudaSuccess)
+    b->smem = kSmem + sizeof(long long) * (b->maxsteps + 1 + n + 1) + sizeof(int) * (b->maxsteps + 1) + 16;
+    if (b->smem > 200 * 1024) return bail(bfail(B2R_ERR_ARG, "too many time steps for the batch schedule"));
+    if (cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem) != cudaSuccess)
         return bail(bfail(B2R_ERR_CUDA, "smem attribute"));
     int dev = 0, sms = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel, kThreads, kSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel, kThreads, b->smem);
     b->grid = std::max(1, occ) * std::max(1, sms);
     b2r_status st = build_schedule(b);
     if (st != B2R_OK) return bail(st);
