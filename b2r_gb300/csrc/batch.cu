@@ -121,14 +121,15 @@ __global__ void __launch_bounds__(kThreads, 3) batch_kernel(const BatchArgs a)
         s_active[i] = a.active[i];
     }
     for (int i = threadIdx.x; i <= a.ninst; i += blockDim.x) s_prefix[i] = a.unit_prefix[i];
-    __shared__ long long s_next;
+    __shared__ long long s_next, s_cur;
     __shared__ int s_t, s_k, s_u, s_ok;
     if (threadIdx.x == 0) s_next = (long long)atomicAdd(a.head, 1ull);
-    __syncthreads();
     for (;;) {
-        const long long item = s_next;
-        if (item >= a.total) break;
+        __syncthreads();                     // every thread is done with the last item's values
         if (threadIdx.x == 0) {
+            const long long item = s_next;
+            s_cur = item;
+            if (item < a.total) {
             int t, k, u;
             decode(item, s_step_off, s_active, s_prefix, a.maxsteps, t, k, u);
             int ok = 1;
@@ -153,8 +154,10 @@ __global__ void __launch_bounds__(kThreads, 3) batch_kernel(const BatchArgs a)
             s_ok = ok;
             // claim the next item now, so it is ready when this one is done
             s_next = (long long)atomicAdd(a.head, 1ull);
+            }
         }
         __syncthreads();
+        if (s_cur >= a.total) break;
         if (!s_ok) {
             if (threadIdx.x == 0) report(a.status, DEV_TIMEOUT);
             return;                          // no load of this CTA is in flight here
