@@ -106,7 +106,10 @@ __device__ __forceinline__ void decode(long long item, const long long* step_off
     u = (int)(r - prefix[k]);
 }
 
-__global__ void __launch_bounds__(kThreads, 3) batch_kernel(const BatchArgs a)
+#ifndef B2R_BATCH_MINB
+#define B2R_BATCH_MINB 3   // resident CTAs per SM the register budget is fitted to
+#endif
+__global__ void __launch_bounds__(kThreads, B2R_BATCH_MINB) batch_kernel(const BatchArgs a)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     heatk::Ring rg;
@@ -176,9 +179,13 @@ __global__ void __launch_bounds__(kThreads, 3) batch_kernel(const BatchArgs a)
             heatk::ring_drain<kS>(rg);
             return;
         }
-        __threadfence();                     // this unit's stores, before the count
-        __syncthreads();
-        if (threadIdx.x == 0) atomicAdd(&a.done[k], 1u);
+        __syncthreads();                     // every store of this unit is issued
+        if (threadIdx.x == 0) {
+            // release at gpu scope; PTX fences are cumulative, so this orders
+            // the whole CTA's stores (ordered before it by the barrier) before
+            // the count that the next step's readers acquire
+            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&a.done[k]) : "memory");
+        }
     }
 }
 
