@@ -28,21 +28,21 @@ namespace {
 
 using heatk::kThreads;
 // One ring for every stencil order: 5 slots (D = 4 needs D+1), each as large
-// as the biggest plane; 2 rows per warp for every order; 2 CTAs/SM with the
-// whole register queue of D = 4 in registers (no spills).
+// as the biggest plane.  D <= 2 tiles have 2 rows per warp, D >= 3 tiles one
+// (their register queues are 2D+1 planes deep); 2 CTAs/SM without spills.
 constexpr int kS = 5;
 template <int D>
 struct RowsPerWarp {
-    static constexpr int value = 2;
+    static constexpr int value = D <= 2 ? 2 : 1;
 };
 constexpr int cmax(int a, int b) { return a > b ? a : b; }
 constexpr int kSlot = cmax(cmax(heatk::Cfg<1, 2, kS>::SLOT, heatk::Cfg<2, 2, kS>::SLOT),
-                           cmax(heatk::Cfg<3, 2, kS>::SLOT, heatk::Cfg<4, 2, kS>::SLOT));
+                           cmax(heatk::Cfg<3, 1, kS>::SLOT, heatk::Cfg<4, 1, kS>::SLOT));
 constexpr size_t kSmem = size_t(kS) * kSlot * sizeof(float) + kS * sizeof(uint64_t) + 16 + 128;
 constexpr int kBoxH[5] = {0, heatk::Cfg<1, 2, kS>::BH, heatk::Cfg<2, 2, kS>::BH,
-                          heatk::Cfg<3, 2, kS>::BH, heatk::Cfg<4, 2, kS>::BH};
+                          heatk::Cfg<3, 1, kS>::BH, heatk::Cfg<4, 1, kS>::BH};
 constexpr int kTileY[5] = {0, heatk::Cfg<1, 2, kS>::TY, heatk::Cfg<2, 2, kS>::TY,
-                           heatk::Cfg<3, 2, kS>::TY, heatk::Cfg<4, 2, kS>::TY};
+                           heatk::Cfg<3, 1, kS>::TY, heatk::Cfg<4, 1, kS>::TY};
 
 struct InstDev {
     BlockLayout L;
@@ -71,8 +71,13 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
     return v;
 }
 
+#ifdef B2R_BATCH_INLINE
+#define B2R_UNIT_INLINE __forceinline__
+#else
+#define B2R_UNIT_INLINE __noinline__
+#endif
 template <int D>
-__device__ __noinline__ bool run_unit(const BatchArgs& a, const InstDev& in, int k, int t, int u,
+__device__ B2R_UNIT_INLINE bool run_unit(const BatchArgs& a, const InstDev& in, int k, int t, int u,
                                          heatk::Ring& rg)
 {
     const int tx = u % in.ntx;
