@@ -71,10 +71,12 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
     return v;
 }
 
-#ifdef B2R_BATCH_INLINE
-#define B2R_UNIT_INLINE __forceinline__
-#else
+// the four unit bodies are inlined into the kernel (measured faster than
+// separate calls, whose calling convention spills the register queues)
+#ifdef B2R_BATCH_NOINLINE
 #define B2R_UNIT_INLINE __noinline__
+#else
+#define B2R_UNIT_INLINE __forceinline__
 #endif
 template <int D>
 __device__ B2R_UNIT_INLINE bool run_unit(const BatchArgs& a, const InstDev& in, int k, int t, int u,
