@@ -92,6 +92,10 @@ def lib():
         "b2r_gol_3D_gpu_main": ([vp, i, C.c_char_p, i, i, i, vp, C.POINTER(d)], i),
         "b2r_eqwp_gpu_main": ([vp, i, i, C.POINTER(d)], i),
         "b2r_kernel_launches": ([], C.c_int64),
+        "b2r_eqwp_record": ([vp, i, i, C.POINTER(C.c_int), C.POINTER(C.c_float)], i),
+        "b2r_eqwp_misfit_gradient": ([vp, i, i, C.POINTER(C.c_int), C.POINTER(C.c_float), i,
+                                      C.POINTER(d), C.POINTER(d), C.POINTER(d), C.POINTER(d),
+                                      C.POINTER(C.c_float)], i),
         "b2r_batch_create": ([C.POINTER(BatchItem), i, C.POINTER(vp)], i),
         "b2r_batch_destroy": ([vp], i),
         "b2r_batch_last_error": ([], C.c_char_p),
@@ -261,6 +265,30 @@ class Domain:
     def boundary_updating_direct(self, time_step=0, field=0):
         _check(lib().b2r_boundary_updating_direct(self.h, time_step, FIELDS.get(field, field)),
                self.h)
+
+    def eqwp_record(self, nsteps, rec_xyz):
+        """vy at receivers (global interior x, y, z) after every step: (nsteps, nrec)."""
+        rec = np.ascontiguousarray(rec_xyz, np.int32).reshape(-1, 3)
+        out = np.empty((nsteps, len(rec)), np.float32)
+        _check(lib().b2r_eqwp_record(self.h, nsteps, len(rec), rec.ctypes.data_as(C.POINTER(C.c_int)),
+                                     out.ctypes.data_as(C.POINTER(C.c_float))), self.h)
+        return out
+
+    def eqwp_misfit_gradient(self, nsteps, rec_xyz, d_obs, ckpt_every=50):
+        """(J, (g_lambda, g_mu, g_rho), d_syn): gradients are env-shaped FP64 arrays (z, y, x)."""
+        rec = np.ascontiguousarray(rec_xyz, np.int32).reshape(-1, 3)
+        obs = np.ascontiguousarray(d_obs, np.float32)
+        env = tuple(self.cfg.env)[::-1]
+        g = [np.empty(env, np.float64) for _ in range(3)]
+        J = C.c_double()
+        syn = np.empty((nsteps, len(rec)), np.float32)
+        dp = C.POINTER(C.c_double)
+        _check(lib().b2r_eqwp_misfit_gradient(
+            self.h, nsteps, len(rec), rec.ctypes.data_as(C.POINTER(C.c_int)),
+            obs.ctypes.data_as(C.POINTER(C.c_float)), ckpt_every, C.byref(J),
+            g[0].ctypes.data_as(dp), g[1].ctypes.data_as(dp), g[2].ctypes.data_as(dp),
+            syn.ctypes.data_as(C.POINTER(C.c_float))), self.h)
+        return J.value, tuple(g), syn
 
     def eqwp_gpu_main(self, ts, R):
         secs = C.c_double()

@@ -9,6 +9,7 @@
 #include <new>
 #include <map>
 #include <mutex>
+#include <algorithm>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -748,6 +749,182 @@ b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* bes
     drop_graphs(h);
     if (best) { best[0] = bestT.zchunk; best[1] = bestT.ctas_per_sm; best[2] = bestT.pdl; }
     if (best_ms) *best_ms = bestMs / trial_steps;
+    return check_status(h);
+}
+
+// ---------------------------------------------------------------- adjoint (staggered model)
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf()
+    {
+        if (p) cudaFree(p);
+    }
+};
+
+b2r_status adj_check(b2r_handle* h)
+{
+    if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
+    if (h->cfg.model != B2R_MODEL_EQWP_STAG)
+        return fail(h, B2R_ERR_ARG, "the adjoint covers the staggered elastic-wave model");
+    if (h->L.nblk != 1 || h->cfg.R != 1)
+        return fail(h, B2R_ERR_ARG, "the adjoint runs on one block with R = 1");
+    return B2R_OK;
+}
+
+// receiver element offsets (global interior coordinates -> block storage)
+b2r_status rec_offsets(b2r_handle* h, int nrec, const int* rec_xyz, std::vector<long long>& idx)
+{
+    idx.resize(nrec);
+    for (int r = 0; r < nrec; ++r) {
+        int c[3];
+        for (int a = 0; a < 3; ++a) {
+            c[a] = rec_xyz[3 * r + a];
+            if (c[a] < 0 || c[a] >= h->cfg.env[a]) return fail(h, B2R_ERR_ARG, "receiver %d outside the domain", r);
+            c[a] += h->L.H;
+        }
+        idx[r] = (long long)c[2] * h->L.plane + (long long)c[1] * h->L.P + h->L.xoff + c[0];
+    }
+    return B2R_OK;
+}
+
+}  // namespace
+
+b2r_status b2r_eqwp_record(b2r_handle* h, int nsteps, int nrec, const int* rec_xyz, float* d_out)
+{
+    b2r_status st;
+    if ((st = adj_check(h)) != B2R_OK) return st;
+    if (nsteps < 0 || nrec <= 0 || !rec_xyz || !d_out) return fail(h, B2R_ERR_ARG, "invalid receivers");
+    std::vector<long long> idx;
+    if ((st = rec_offsets(h, nrec, rec_xyz, idx)) != B2R_OK) return st;
+    DevBuf d_idx, d_rec;
+    CK(h, cudaMalloc(&d_idx.p, sizeof(long long) * nrec));
+    CK(h, cudaMalloc(&d_rec.p, sizeof(float) * (size_t)nrec * (nsteps > 0 ? nsteps : 1)));
+    CK(h, cudaMemcpyAsync(d_idx.p, idx.data(), sizeof(long long) * nrec, cudaMemcpyHostToDevice, h->stream));
+    h->ts = 0;
+    for (int n = 0; n < nsteps; ++n) {
+        if ((st = substep(h, 0)) != B2R_OK) return st;
+        h->ts++;
+        CK(h, adjoint_sample(h->fld[B2R_F_VY], (const long long*)d_idx.p, nrec, (float*)d_rec.p + (size_t)n * nrec,
+                             h->stream));
+    }
+    CK(h, cudaMemcpyAsync(d_out, d_rec.p, sizeof(float) * (size_t)nrec * nsteps, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return check_status(h);
+}
+
+b2r_status b2r_eqwp_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const int* rec_xyz,
+                                    const float* d_obs, int ckpt_every, double* misfit,
+                                    double* grad_lambda, double* grad_mu, double* grad_rho,
+                                    float* d_syn)
+{
+    b2r_status st;
+    if ((st = adj_check(h)) != B2R_OK) return st;
+    if (nsteps <= 0 || nrec <= 0 || !rec_xyz || !d_obs) return fail(h, B2R_ERR_ARG, "invalid receivers / steps");
+    const int K = ckpt_every > 0 ? ckpt_every : nsteps;
+    std::vector<long long> idx;
+    if ((st = rec_offsets(h, nrec, rec_xyz, idx)) != B2R_OK) return st;
+    const size_t fb = field_bytes(h);
+    const size_t nseg = (size_t)(nsteps + K - 1) / K;
+    // device buffers (freed on every return path)
+    std::vector<DevBuf> ckpt(nseg * 9), replay((size_t)(K + 1) * 9), tmp(18), gb(3);
+    DevBuf d_idx, d_rec, d_res;
+    for (auto& b : ckpt) CK(h, cudaMalloc(&b.p, fb));
+    for (auto& b : replay) CK(h, cudaMalloc(&b.p, fb));
+    for (auto& b : tmp) {
+        CK(h, cudaMalloc(&b.p, fb));
+        CK(h, cudaMemsetAsync(b.p, 0, fb, h->stream));
+    }
+    const size_t gbytes = (size_t)h->L.bstride * sizeof(double);
+    for (auto& b : gb) {
+        CK(h, cudaMalloc(&b.p, gbytes));
+        CK(h, cudaMemsetAsync(b.p, 0, gbytes, h->stream));
+    }
+    CK(h, cudaMalloc(&d_idx.p, sizeof(long long) * nrec));
+    CK(h, cudaMalloc(&d_rec.p, sizeof(float) * (size_t)nrec * nsteps));
+    CK(h, cudaMalloc(&d_res.p, sizeof(float) * (size_t)nrec * nsteps));
+    CK(h, cudaMemcpyAsync(d_idx.p, idx.data(), sizeof(long long) * nrec, cudaMemcpyHostToDevice, h->stream));
+    const long long* didx = (const long long*)d_idx.p;
+
+    // forward with checkpoints every K steps and receiver samples
+    h->ts = 0;
+    for (int n = 0; n < nsteps; ++n) {
+        if (n % K == 0)
+            for (int f = 0; f < 9; ++f)
+                CK(h, cudaMemcpyAsync(ckpt[(n / K) * 9 + f].p, h->fld[f], fb, cudaMemcpyDeviceToDevice, h->stream));
+        if ((st = substep(h, 0)) != B2R_OK) return st;
+        h->ts++;
+        CK(h, adjoint_sample(h->fld[B2R_F_VY], didx, nrec, (float*)d_rec.p + (size_t)n * nrec, h->stream));
+    }
+    // misfit and residual (host, FP64)
+    std::vector<float> syn((size_t)nrec * nsteps), res((size_t)nrec * nsteps);
+    CK(h, cudaMemcpyAsync(syn.data(), d_rec.p, sizeof(float) * syn.size(), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    double J = 0.0;
+    for (size_t i = 0; i < syn.size(); ++i) {
+        const double r = (double)syn[i] - (double)d_obs[i];
+        res[i] = (float)r;
+        J += 0.5 * r * r;
+    }
+    if (misfit) *misfit = J;
+    if (d_syn) std::copy(syn.begin(), syn.end(), d_syn);
+    CK(h, cudaMemcpyAsync(d_res.p, res.data(), sizeof(float) * res.size(), cudaMemcpyHostToDevice, h->stream));
+
+    // reverse sweep, segment by segment, recomputing each segment forward
+    float* tp[18];
+    for (int k = 0; k < 18; ++k) tp[k] = (float*)tmp[k].p;
+    double* gp[3] = {(double*)gb[0].p, (double*)gb[1].p, (double*)gb[2].p};
+    const float* mat[3] = {h->mat[0], h->mat[1], h->mat[2]};
+    int lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = h->L.H;
+        hi[a] = h->L.n[a] - 1 - h->L.H;
+    }
+    const float dt_h = (float)(h->cfg.dt / h->cfg.h);
+    // stress fields of a state in the order xx, xy, xz, yy, yz, zz
+    static const int sidx[6] = {B2R_F_SXX, B2R_F_SXY, B2R_F_SXZ, B2R_F_SYY, B2R_F_SYZ, B2R_F_SZZ};
+    for (long long sgi = (long long)nseg - 1; sgi >= 0; --sgi) {
+        const int n0 = (int)sgi * K;
+        const int n1 = std::min(nsteps, n0 + K);
+        for (int f = 0; f < 9; ++f) {
+            CK(h, cudaMemcpyAsync(h->fld[f], ckpt[sgi * 9 + f].p, fb, cudaMemcpyDeviceToDevice, h->stream));
+            CK(h, cudaMemcpyAsync(replay[f].p, h->fld[f], fb, cudaMemcpyDeviceToDevice, h->stream));
+        }
+        h->ts = n0;
+        for (int n = n0; n < n1; ++n) {
+            if ((st = substep(h, 0)) != B2R_OK) return st;
+            h->ts++;
+            const size_t k = (size_t)(n + 1 - n0);
+            for (int f = 0; f < 9; ++f)
+                CK(h, cudaMemcpyAsync(replay[k * 9 + f].p, h->fld[f], fb, cudaMemcpyDeviceToDevice, h->stream));
+        }
+        for (int n = n1 - 1; n >= n0; --n) {
+            CK(h, adjoint_inject(tp[1], didx, nrec, (const float*)d_res.p + (size_t)n * nrec, h->stream));
+            const size_t kv = (size_t)(n + 1 - n0), ks = (size_t)(n - n0);
+            const float* fv[3] = {(const float*)replay[kv * 9 + 0].p, (const float*)replay[kv * 9 + 1].p,
+                                  (const float*)replay[kv * 9 + 2].p};
+            const float* fs[6];
+            for (int j = 0; j < 6; ++j) fs[j] = (const float*)replay[ks * 9 + sidx[j]].p;
+            CK(h, adjoint_step(tp, fv, fs, mat, gp, h->L, dt_h, lo, hi, h->stream));
+        }
+    }
+    // gradients out (interior cells, x fastest), g_rho = -g_b / rho^2
+    double* outs[3] = {grad_lambda, grad_mu, grad_rho};
+    const size_t ncell = (size_t)h->cfg.env[0] * h->cfg.env[1] * h->cfg.env[2];
+    DevBuf d_out;
+    CK(h, cudaMalloc(&d_out.p, ncell * sizeof(double)));
+    for (int m = 0; m < 3; ++m) {
+        if (!outs[m]) continue;
+        CK(h, adjoint_grad_out(gp[m], h->mat[2], m == 2, h->L, (double*)d_out.p, h->stream));
+        CK(h, cudaMemcpyAsync(outs[m], d_out.p, ncell * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    }
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->ts = nsteps;
+    h->halos_fresh = false;
     return check_status(h);
 }
 

@@ -33,4 +33,15 @@ cudaError_t launch_eqwp_ref_substep(float* const* fld, const BlockLayout& L, int
 cudaError_t launch_eqwp_stag_substep(float* const* fld, float* const* mat, const BlockLayout& L,
                                      int step_i, int ts, const EqwpStagParams& p, cudaStream_t st);
 
+// adjoint.cu: receiver sampling / injection and one reverse step of the
+// staggered scheme (tmp = vb[3], sb[6], q[6], w[3]; stress order xx, xy, xz,
+// yy, yz, zz), gradients in FP64.
+cudaError_t adjoint_sample(const float* vy, const long long* d_idx, int nrec, float* out, cudaStream_t st);
+cudaError_t adjoint_inject(float* vby, const long long* d_idx, int nrec, const float* res, cudaStream_t st);
+cudaError_t adjoint_step(float* const* tmp, const float* const* fwd_v, const float* const* fwd_s,
+                         const float* const* mat, double* const* g, const BlockLayout& L, float dt_h,
+                         const int lo[3], const int hi[3], cudaStream_t st);
+cudaError_t adjoint_grad_out(const double* g, const float* buoy, int rho, const BlockLayout& L,
+                             double* out, cudaStream_t st);
+
 }  // namespace b2r

@@ -189,6 +189,23 @@ b2r_status b2r_heat_3D_gpu_main_noalloc(const float* d_in, float* d_out, int R, 
  * (selects the body force, eqwp.cu:135).  Does not exchange halos. */
 b2r_status b2r_eqwp_gpu_main(b2r_handle* h, int ts, int R, double* gpu_seconds);
 
+/* ---- adjoint of the staggered elastic wave (no reference counterpart) ---- */
+/* Forward nsteps from the current fields and record vy at nrec receivers
+ * (rec_xyz: 3*nrec global interior coordinates) after every step into
+ * d_out[nsteps*nrec] (host).  One block, R = 1, model B2R_MODEL_EQWP_STAG. */
+b2r_status b2r_eqwp_record(b2r_handle* h, int nsteps, int nrec, const int* rec_xyz, float* d_out);
+/* Misfit J = 1/2 sum (d_syn - d_obs)^2 of the same recording and its
+ * gradient with respect to lambda, mu and rho per interior cell (host
+ * arrays of env cells, x fastest, FP64; any may be NULL), by the discrete
+ * adjoint run backward in time.  The forward state is checkpointed every
+ * ckpt_every steps (<= 0: once) and each segment is recomputed before its
+ * reverse sweep.  Gradients accumulate in FP64.  d_syn (may be NULL) gets
+ * the synthetic recording.  The fields end in an unspecified state. */
+b2r_status b2r_eqwp_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const int* rec_xyz,
+                                    const float* d_obs, int ckpt_every, double* misfit,
+                                    double* grad_lambda, double* grad_mu, double* grad_rho,
+                                    float* d_syn);
+
 /* ---- batched instances (no reference counterpart) ------------------------ */
 /* Many independent single-block heat domains of uneven sizes and stencil
  * orders advanced in one persistent launch driven by a device work queue of

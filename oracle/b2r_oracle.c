@@ -452,3 +452,95 @@ void orc_eqwp_stag_step_f64(double* const* f, const double* const* m,
     const double C1 = 9.0 / 8.0, C2 = -1.0 / 24.0;
     STAG_BODY(double, C1, C2)
 }
+
+/* ------------------------------------------------------------------------ */
+/* discrete adjoint of the staggered step (no reference counterpart)         */
+/* ------------------------------------------------------------------------ */
+/* Dp^T = -Dm and Dm^T = -Dp; fields outside the window are zero in q and w. */
+static inline double dpd(const double* f, ptrdiff_t s)
+{
+    return 1.125 * (f[s] - f[0]) + (-1.0 / 24.0) * (f[2 * s] - f[-s]);
+}
+static inline double dmd(const double* f, ptrdiff_t s)
+{
+    return 1.125 * (f[0] - f[-s]) + (-1.0 / 24.0) * (f[s] - f[-2 * s]);
+}
+
+void orc_eqwp_stag_adjoint_step_f64(double* const* tmp, const double* const* fv,
+                                    const double* const* fs, const double* const* m,
+                                    double* const* g, int nx, int ny, int nz, double k,
+                                    const int* lo, const int* hi)
+{
+    const size_t n = (size_t)nx * ny * nz;
+    const ptrdiff_t sy = nx, sz = (ptrdiff_t)nx * ny;
+    double* q[6];
+    double* w[3];
+    for (int i = 0; i < 6; ++i) q[i] = (double*)calloc(n, sizeof(double));
+    for (int i = 0; i < 3; ++i) w[i] = (double*)calloc(n, sizeof(double));
+    double** vb = (double**)tmp;
+    double** sb = (double**)tmp + 3;
+#define INW(x, y, z) ((x) >= lo[0] && (x) <= hi[0] && (y) >= lo[1] && (y) <= hi[1] && (z) >= lo[2] && (z) <= hi[2])
+    /* stress stage: q = C sb on W, gradients of lambda and mu */
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < nz; z++)
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++) {
+                if (!INW(x, y, z)) continue;
+                size_t id = IDX(x, y, z);
+                double l = m[0][id], mu = m[1][id];
+                double tr = sb[0][id] + sb[3][id] + sb[5][id];
+                q[0][id] = 2 * mu * sb[0][id] + l * tr;
+                q[3][id] = 2 * mu * sb[3][id] + l * tr;
+                q[5][id] = 2 * mu * sb[5][id] + l * tr;
+                q[1][id] = mu * sb[1][id];
+                q[2][id] = mu * sb[2][id];
+                q[4][id] = mu * sb[4][id];
+                double exx = dmd(fv[0] + id, 1), eyy = dmd(fv[1] + id, sy), ezz = dmd(fv[2] + id, sz);
+                double gxy = dpd(fv[0] + id, sy) + dpd(fv[1] + id, 1);
+                double gxz = dpd(fv[0] + id, sz) + dpd(fv[2] + id, 1);
+                double gyz = dpd(fv[1] + id, sz) + dpd(fv[2] + id, sy);
+                g[0][id] += k * (exx + eyy + ezz) * tr;
+                g[1][id] += k * (2 * (exx * sb[0][id] + eyy * sb[3][id] + ezz * sb[5][id]) +
+                                 gxy * sb[1][id] + gxz * sb[2][id] + gyz * sb[4][id]);
+            }
+#pragma omp parallel for schedule(static)
+    for (int z = 2; z < nz - 2; z++)
+        for (int y = 2; y < ny - 2; y++)
+            for (int x = 2; x < nx - 2; x++) {
+                size_t id = IDX(x, y, z);
+                vb[0][id] -= k * (dpd(q[0] + id, 1) + dmd(q[1] + id, sy) + dmd(q[2] + id, sz));
+                vb[1][id] -= k * (dpd(q[3] + id, sy) + dmd(q[1] + id, 1) + dmd(q[4] + id, sz));
+                vb[2][id] -= k * (dpd(q[5] + id, sz) + dmd(q[2] + id, 1) + dmd(q[4] + id, sy));
+            }
+    /* velocity stage: w = b vb on W, gradient of buoyancy */
+#pragma omp parallel for schedule(static)
+    for (int z = 0; z < nz; z++)
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++) {
+                if (!INW(x, y, z)) continue;
+                size_t id = IDX(x, y, z);
+                double b = m[2][id];
+                w[0][id] = b * vb[0][id];
+                w[1][id] = b * vb[1][id];
+                w[2][id] = b * vb[2][id];
+                double ax = dpd(fs[0] + id, 1) + dmd(fs[1] + id, sy) + dmd(fs[2] + id, sz);
+                double ay = dmd(fs[1] + id, 1) + dpd(fs[3] + id, sy) + dmd(fs[4] + id, sz);
+                double az = dmd(fs[2] + id, 1) + dmd(fs[4] + id, sy) + dpd(fs[5] + id, sz);
+                g[2][id] += k * (ax * vb[0][id] + ay * vb[1][id] + az * vb[2][id]);
+            }
+#pragma omp parallel for schedule(static)
+    for (int z = 2; z < nz - 2; z++)
+        for (int y = 2; y < ny - 2; y++)
+            for (int x = 2; x < nx - 2; x++) {
+                size_t id = IDX(x, y, z);
+                sb[0][id] -= k * dmd(w[0] + id, 1);
+                sb[3][id] -= k * dmd(w[1] + id, sy);
+                sb[5][id] -= k * dmd(w[2] + id, sz);
+                sb[1][id] -= k * (dpd(w[0] + id, sy) + dpd(w[1] + id, 1));
+                sb[2][id] -= k * (dpd(w[0] + id, sz) + dpd(w[2] + id, 1));
+                sb[4][id] -= k * (dpd(w[1] + id, sz) + dpd(w[2] + id, sy));
+            }
+#undef INW
+    for (int i = 0; i < 6; ++i) free(q[i]);
+    for (int i = 0; i < 3; ++i) free(w[i]);
+}

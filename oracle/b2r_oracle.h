@@ -96,6 +96,16 @@ void orc_eqwp_stag_step_f64(double* const* f, const double* const* m,
                             int i, int H, int edge, int src_x, int src_y, int src_z,
                             double src);
 
+/* One reverse step of the discrete adjoint of orc_eqwp_stag_step_f64 on the
+ * window [lo, hi] (inclusive, per axis): tmp = vb[3] (vx, vy, vz), sb[6]
+ * (xx, xy, xz, yy, yz, zz); fv = forward v after the step (3); fs = forward
+ * stress before the step (6, same order); m = lambda, mu, buoyancy; g =
+ * gradients wrt lambda, mu, buoyancy (accumulated).  k = dt/dx. */
+void orc_eqwp_stag_adjoint_step_f64(double* const* tmp, const double* const* fv,
+                                    const double* const* fs, const double* const* m,
+                                    double* const* g, int nx, int ny, int nz, double k,
+                                    const int* lo, const int* hi);
+
 #ifdef __cplusplus
 }
 #endif

@@ -56,6 +56,9 @@ def lib():
         L.orc_eqwp_stag_step_f64.argtypes = [C.POINTER(_dp), C.POINTER(_dp), i, i, i, d, d,
                                              i, i, i, i, i, i, d]
         L.orc_region.argtypes = [i, i, i, i, i, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.orc_eqwp_stag_adjoint_step_f64.argtypes = [C.POINTER(_dp), C.POINTER(_dp), C.POINTER(_dp),
+                                                     C.POINTER(_dp), C.POINTER(_dp), i, i, i, d,
+                                                     C.POINTER(C.c_int), C.POINTER(C.c_int)]
         _lib = L
     return _lib
 
@@ -252,3 +255,48 @@ def halo_exchange(blocks, nb, H, periodic=False):
                     s[a] = src_s if a == axis else ext[a]
                 blk[d[2], d[1], d[0]] = src[s[2], s[1], s[0]]
     return blocks
+
+
+# ---------------------------------------------------------------- adjoint (FP64)
+def eqwp_stag_adjoint_step(tmp, fv, fs, mat, g, k, lo, hi):
+    """One reverse step of the discrete adjoint (orc_eqwp_stag_adjoint_step_f64)."""
+    nz, ny, nx = tmp[0].shape
+    P = lambda arrs: (_dp * len(arrs))(*[_ptr(a, _dp) for a in arrs])
+    lib().orc_eqwp_stag_adjoint_step_f64(P(tmp), P(fv), P(fs), P(mat), P(g), nx, ny, nz, k,
+                                         (C.c_int * 3)(*lo), (C.c_int * 3)(*hi))
+
+
+def eqwp_stag_record(fields, mat, dt, dx, H, src_xyz, amps, rec, nsteps):
+    """Forward nsteps (one block, fixed shell H); returns all states and vy at
+    the receivers (rec: list of (x, y, z) block coordinates) after each step."""
+    states = [[f.copy() for f in fields]]
+    cur = [f.copy() for f in fields]
+    d = np.zeros((nsteps, len(rec)), np.float64)
+    for n in range(nsteps):
+        eqwp_stag_step(cur, mat, dt, dx, 0, H, 63, src_xyz, float(amps[n]) if n < len(amps) else 0.0)
+        for r, (x, y, z) in enumerate(rec):
+            d[n, r] = cur[1][z, y, x]
+        states.append([f.copy() for f in cur])
+    return states, d
+
+
+def eqwp_stag_gradient(fields, mat, dt, dx, H, src_xyz, amps, rec, nsteps, d_obs):
+    """FP64 misfit J = 1/2 |d - d_obs|^2 and its gradient wrt lambda, mu, rho
+    (full block arrays) by the discrete adjoint."""
+    states, d = eqwp_stag_record(fields, mat, dt, dx, H, src_xyz, amps, rec, nsteps)
+    res = d - d_obs
+    J = 0.5 * float(np.sum(res * res))
+    shape = fields[0].shape
+    tmp = [np.zeros(shape) for _ in range(9)]      # vb(3), sb(6: xx xy xz yy yz zz)
+    g = [np.zeros(shape) for _ in range(3)]
+    lo = (H, H, H)
+    hi = tuple(shape[2 - a] - 1 - H for a in range(3))
+    sidx = [3, 4, 5, 6, 7, 8]                       # sxx sxy sxz syy syz szz in field order
+    for n in range(nsteps - 1, -1, -1):
+        for r, (x, y, z) in enumerate(rec):
+            tmp[1][z, y, x] += res[n, r]
+        fv = states[n + 1][:3]
+        fs = [states[n][k] for k in sidx]
+        eqwp_stag_adjoint_step(tmp, fv, fs, mat, g, dt / dx, lo, hi)
+    g_rho = -g[2] * mat[2] ** 2
+    return J, (g[0], g[1], g_rho), d, tmp
