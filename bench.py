@@ -59,6 +59,11 @@ WORKLOADS = {
     # steps U[50,500], seed 4, in one persistent launch replayed from a CUDA graph
     "batch64": dict(model=5, n=64, seed=4, env=(0, 0, 0), blocks=(1, 1, 1), R=1, D=0, sub_steps=0,
                     bytes_per_cell=8, kernel="batch_kernel"),
+    # adjoint gradient of a receiver misfit wrt lambda, mu, rho: 256^3, layered model
+    # + 5% Gaussian anomaly (sigma 8 cells) for the observed data, 64 receivers on the
+    # top plane, Ricker 12 Hz, 2000 steps, checkpoints every 50 steps
+    "adjoint256": dict(model=6, env=(256, 256, 256), blocks=(1, 1, 1), R=1, D=2, sub_steps=2000,
+                       nrec=64, ckpt=50, f0=12.0, bytes_per_cell=84, kernel="adjoint"),
     # the reference's collocated elastic-wave model, 512x512x256, one block, R = 1
     "eqwp_ref": dict(model=3, env=(512, 512, 256), blocks=(1, 1, 1), R=1, D=2, sub_steps=100,
                      bytes_per_cell=80, kernel="eqwp_ref_stress+velocity"),
@@ -388,6 +393,107 @@ def run_batch(args, wl):
     print(json.dumps(line), flush=True)
 
 
+def run_adjoint(args, wl):
+    """Config 5: misfit gradient by the adjoint vs one forward of the same run."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    import b2r_gb300 as b2r
+    env, n = wl["env"], wl["sub_steps"]
+    h = 10.0
+    dt = 0.5 * h / (4400 * 3 ** 0.5 * (9 / 8 + 1 / 24))
+    src = tuple(e // 2 for e in env)
+    rng = np.random.default_rng(3)
+    layers = 8
+    vp_l = rng.uniform(2000, 4000, layers)
+    rho_l = rng.uniform(2000, 2600, layers)
+    shape = tuple(e + 4 for e in env[::-1])
+    idx = np.minimum(np.arange(shape[1]) * layers // shape[1], layers - 1)
+
+    def model(anomaly):
+        vp = np.broadcast_to(vp_l[idx][None, :, None], shape).astype(np.float64)
+        rho = np.broadcast_to(rho_l[idx][None, :, None], shape).astype(np.float64)
+        if anomaly:
+            z = np.arange(shape[0])[:, None, None] - shape[0] / 2
+            y = np.arange(shape[1])[None, :, None] - shape[1] / 2
+            x = np.arange(shape[2])[None, None, :] - shape[2] / 2
+            vp = vp * (1 + anomaly * np.exp(-(x * x + y * y + z * z) / (2 * 8.0 ** 2)))
+        mu = rho * (vp / 3 ** 0.5) ** 2
+        return [rho * vp ** 2 - 2 * mu, mu, 1.0 / rho]
+
+    t = np.arange(n) * dt - 1.2 / wl["f0"]
+    a = (np.pi * wl["f0"] * t) ** 2
+    amps = (1e7 * dt * (1 - 2 * a) * np.exp(-a)).astype(np.float32)
+    k = int(np.sqrt(wl["nrec"]))
+    gx = np.linspace(8, env[0] - 9, k).astype(np.int32)
+    gz = np.linspace(8, env[2] - 9, k).astype(np.int32)
+    rec = np.array([(x, 2, z) for x in gx for z in gz], np.int32)
+
+    def domain(mat):
+        d = b2r.Domain(b2r.MODEL_EQWP_STAG, env, D=2, R=1, dt=dt, h=h, src=src)
+        for name, m in zip(("lambda", "mu", "buoy"), mat):
+            d.upload(np.ascontiguousarray(m, np.float32), field=name)
+        zero = np.zeros(d.domain_shape, np.float32)
+        for f in range(9):
+            d.upload(zero, field=f)
+        d.set_source(amps)
+        return d, zero
+
+    d, zero = domain(model(0.05))
+    d_obs = d.eqwp_record(n, rec)
+    d.close()
+    d, zero = domain(model(0.0))
+    torch.cuda.synchronize()
+    fwd_ms = []
+    for _ in range(max(1, args.warmup // 2)):
+        for f in range(9):
+            d.upload(zero, field=f)
+        t0 = time.perf_counter()
+        d.eqwp_record(n, rec)
+        fwd_ms.append((time.perf_counter() - t0) * 1e3)
+    clocks = ClockSampler(0)
+    clocks.start()
+    l0 = b2r.kernel_launches()
+    grad_ms = []
+    for _ in range(max(1, args.steps)):
+        for f in range(9):
+            d.upload(zero, field=f)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        J, g, _ = d.eqwp_misfit_gradient(n, rec, d_obs, ckpt_every=wl["ckpt"])
+        grad_ms.append((time.perf_counter() - t0) * 1e3)
+    launches = b2r.kernel_launches() - l0
+    clk = clocks.stop()
+    for f in range(9):
+        d.upload(zero, field=f)
+    t0 = time.perf_counter()
+    d.eqwp_record(n, rec)
+    fwd_ms.append((time.perf_counter() - t0) * 1e3)
+    d.close()
+    cells = env[0] * env[1] * env[2]
+    gms = float(np.median(grad_ms))
+    fms = float(np.median(fwd_ms))
+    value = cells * n / (gms / 1e3) / 1e9
+    peak, peak_src = measured_peak()
+    line = {"metric": "GLUPS", "value": round(value, 3), "unit": "GLUPS", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(gms, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded layered model, Gaussian anomaly, Ricker source)",
+            "config": {"workload": args.workload, "env": list(env), "time_steps": n,
+                       "receivers": len(rec), "checkpoint_every": wl["ckpt"],
+                       "forward_ms": round(fms, 1), "gradient_ms": round(gms, 1),
+                       "gradient_over_forward": round(gms / fms, 3), "misfit": J,
+                       "l2": "inputs larger than L2"},
+            "e2e": None, "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "achieved": round(wl["bytes_per_cell"] * value, 1),
+                         "peak": peak, "unit": "GB/s",
+                         "frac": round(wl["bytes_per_cell"] * value / peak, 4), "traffic": None,
+                         "peak_source": peak_src, "kernel": "adjoint (whole gradient)",
+                         "note": "84 B per cell-step of the forward, over the whole gradient time"},
+            "cpu_baseline": None, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def run_ours(args, wl):
     import torch
     import torch.distributed as dist
@@ -545,6 +651,8 @@ def main():
         run_reference(args, wl)
     elif wl["model"] == 5:
         run_batch(args, wl)
+    elif wl["model"] == 6:
+        run_adjoint(args, wl)
     else:
         run_ours(args, wl)
 
