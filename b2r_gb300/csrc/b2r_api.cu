@@ -34,6 +34,7 @@ struct b2r_handle {
     void* buf[2] = {nullptr, nullptr};
     int cur = 0;
     CUtensorMap tmap[2];
+    CUtensorMap tmap2[2];       // boxes of the two-step kernel (D = 1)
     HeatCoef hc{};
     HeatTune tune{};
     // elastic wave: fields and material
@@ -51,6 +52,7 @@ struct b2r_handle {
     // CUDA graphs of whole periods (heat, GoL on a non-default stream)
     bool graphs = true;
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};   // by ping-pong buffer at start
+    bool gflip[2] = {false, false};                   // the graph ends on the other buffer
     int gsteps = 0;                                   // time steps per graph launch
     long long gkernels = 0;                           // kernels per graph launch
     std::string err;
@@ -152,10 +154,24 @@ b2r_status ensure_staging(b2r_handle* h, size_t bytes)
 
 b2r_status build_heat_maps(b2r_handle* h)
 {
-    for (int b = 0; b < 2; ++b)
+    for (int b = 0; b < 2; ++b) {
         if (!make_block_tmap(&h->tmap[b], h->buf[b], h->L, 4, heat_box_w(), heat_box_h(h->cfg.D), 1))
             return fail(h, B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed for the heat field");
+        if (h->cfg.D == 1 &&
+            !make_block_tmap(&h->tmap2[b], h->buf[b], h->L, 4, heat2_box_w(), heat2_box_h(), 1))
+            return fail(h, B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed for the heat field");
+    }
     return B2R_OK;
+}
+
+// Can sub-steps i and i+1 run in one two-step launch?  Radius 1 only, and no
+// halo exchange may fall between them: within one period, or always when the
+// exchange is empty (one block, not periodic).
+bool heat_fuse_ok(const b2r_handle* h, int i)
+{
+    if (h->cfg.model != B2R_MODEL_HEAT || h->cfg.D != 1 || h->tune.tblock < 2) return false;
+    if (h->L.nblk == 1 && !h->L.periodic) return true;
+    return i + 1 < h->cfg.R;
 }
 
 b2r_status check_status(b2r_handle* h)
@@ -272,12 +288,21 @@ void drop_graphs(b2r_handle* h)
     h->gsteps = 0;
 }
 
+b2r_status substep2(b2r_handle* h, int i);
+
 b2r_status run_period(b2r_handle* h)
 {
     b2r_status st;
     if ((st = exchange_all(h, false)) != B2R_OK) return st;
-    for (int i = 0; i < h->cfg.R; ++i)
-        if ((st = substep(h, i)) != B2R_OK) return st;
+    for (int i = 0; i < h->cfg.R;) {
+        if (i + 1 < h->cfg.R && heat_fuse_ok(h, i)) {
+            if ((st = substep2(h, i)) != B2R_OK) return st;
+            i += 2;
+        } else {
+            if ((st = substep(h, i)) != B2R_OK) return st;
+            ++i;
+        }
+    }
     return B2R_OK;
 }
 
@@ -295,6 +320,7 @@ b2r_status capture_graph(b2r_handle* h, int c, int periods)
     cudaError_t e = cudaStreamEndCapture(h->stream, &g);
     const long long nk = b2r_kernel_launches() - k0;
     b2r::count_launches(-nk);               // captured, not launched
+    h->gflip[c] = (h->cur != c);
     h->cur = save_cur;
     h->ts = save_ts;
     if (st != B2R_OK) {
@@ -306,6 +332,14 @@ b2r_status capture_graph(b2r_handle* h, int c, int periods)
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(h, B2R_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
     h->gkernels = nk;
+    return B2R_OK;
+}
+
+b2r_status substep2(b2r_handle* h, int i)
+{
+    CK(h, launch_heat_substep2(&h->tmap2[h->cur], static_cast<float*>(h->buf[1 - h->cur]), h->L, i, h->hc,
+                               h->d_status, h->stream, h->tune.zchunk2));
+    h->cur = 1 - h->cur;
     return B2R_OK;
 }
 
@@ -602,7 +636,7 @@ b2r_status b2r_step(b2r_handle* h, int nsteps)
                     if ((st = capture_graph(h, h->cur, periods)) != B2R_OK) return st;
                 CK(h, cudaGraphLaunch(h->gexec[h->cur], h->stream));
                 b2r::count_launches(h->gkernels);
-                if (unit & 1) h->cur = 1 - h->cur;
+                if (h->gflip[h->cur]) h->cur = 1 - h->cur;
                 h->ts += unit;
                 h->halos_fresh = false;
                 s += unit;
@@ -612,6 +646,12 @@ b2r_status b2r_step(b2r_handle* h, int nsteps)
         if (i == 0 && !h->halos_fresh)
             if ((st = exchange_all(h, false)) != B2R_OK) return st;
         h->halos_fresh = false;
+        if (nsteps - s >= 2 && heat_fuse_ok(h, i)) {
+            if ((st = substep2(h, i)) != B2R_OK) return st;
+            h->ts += 2;
+            s += 2;
+            continue;
+        }
         if ((st = substep(h, i)) != B2R_OK) return st;
         h->ts++;
         ++s;
@@ -671,6 +711,8 @@ b2r_status b2r_set_tuning(b2r_handle* h, int key, int value)
     case B2R_TUNE_ZCHUNK: h->tune.zchunk = value; break;
     case B2R_TUNE_CTAS_PER_SM: h->tune.ctas_per_sm = value; break;
     case B2R_TUNE_PDL: h->tune.pdl = value != 0; break;
+    case B2R_TUNE_TBLOCK: h->tune.tblock = value; break;
+    case B2R_TUNE_ZCHUNK2: h->tune.zchunk2 = value; break;
     default: return fail(h, B2R_ERR_ARG, "unknown tuning key %d", key);
     }
     drop_graphs(h);
@@ -712,13 +754,24 @@ b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* bes
     HeatTune bestT = h->tune;
     float bestMs = 1e30f;
     b2r_status st = B2R_OK;
-    for (int pdl = 0; pdl < 2 && st == B2R_OK; ++pdl)
+    // candidates: the two-step sweep (radius 1) by z-chunk, then the one-step
+    // sweep by z-chunk x persistent CTAs per SM x PDL
+    struct Cand { int tb, zc2, zc, cp, pdl; };
+    std::vector<Cand> cands;
+    if (h->cfg.D == 1)
+        for (int z2 : {0, 16, 32, 64}) cands.push_back({2, z2, 0, 0, 1});
+    for (int pdl = 0; pdl < 2; ++pdl)
         for (int zc : zchunks)
-            for (int cp : persist) {
-                if (zc > h->L.n[2]) continue;
-                h->tune.zchunk = zc;
-                h->tune.ctas_per_sm = cp;
-                h->tune.pdl = pdl;
+            for (int cp : persist)
+                if (zc <= h->L.n[2]) cands.push_back({1, 0, zc, cp, pdl});
+    for (const Cand& cd : cands)
+            {
+                if (st != B2R_OK) break;
+                h->tune.tblock = cd.tb;
+                h->tune.zchunk2 = cd.zc2;
+                h->tune.zchunk = cd.zc;
+                h->tune.ctas_per_sm = cd.cp;
+                h->tune.pdl = cd.pdl;
                 if ((st = b2r_step(h, 1)) != B2R_OK) break;       // warm
                 cudaEventRecord(e0, h->stream);
                 if ((st = b2r_step(h, trial_steps)) != B2R_OK) break;
@@ -747,7 +800,7 @@ b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* bes
         g_tune_cache[key_of(h)] = bestT;
     }
     drop_graphs(h);
-    if (best) { best[0] = bestT.zchunk; best[1] = bestT.ctas_per_sm; best[2] = bestT.pdl; }
+    if (best) { best[0] = bestT.tblock == 2 ? bestT.zchunk2 : bestT.zchunk; best[1] = bestT.ctas_per_sm; best[2] = bestT.pdl; }
     if (best_ms) *best_ms = bestMs / trial_steps;
     return check_status(h);
 }

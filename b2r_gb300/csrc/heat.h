@@ -18,9 +18,11 @@ int heat_box_h(int D);
 // through `tin` (a tensor map over the input buffer), writes `out`.
 // Launch schedule knobs (the autotuner's search space).
 struct HeatTune {
-    int zchunk = 0;        // output planes per work unit; 0 = about 4 waves, >= 32 planes
+    int zchunk = 0;        // output planes per work unit; 0 = 16 (fewer for small grids)
     int ctas_per_sm = 0;   // 0 = one CTA per unit; k > 0 = persistent, k CTAs per SM
     int pdl = 1;           // programmatic dependent launch on the stream
+    int tblock = 2;        // time steps per HBM pass (2 = heat2.cu, radius 1 only)
+    int zchunk2 = 0;       // output planes per unit of the two-step kernel (0 = 16)
 };
 
 // One sub-step of every block: units (block, z-chunk, tile row, tile column)
@@ -28,5 +30,12 @@ struct HeatTune {
 cudaError_t launch_heat_substep(const CUtensorMap* tin, float* out, const BlockLayout& L, int D,
                                 int step_i, const HeatCoef& c, int* status, cudaStream_t st,
                                 const HeatTune& tune = HeatTune());
+
+// Two sub-steps (step_i, step_i+1) of radius 1 per launch (heat2.cu).  The
+// tensor map must have the box heat2_box_w() x heat2_box_h().
+int heat2_box_w();
+int heat2_box_h();
+cudaError_t launch_heat_substep2(const CUtensorMap* tin, float* out, const BlockLayout& L, int step_i,
+                                 const HeatCoef& c, int* status, cudaStream_t st, int zchunk);
 
 }  // namespace b2r

@@ -114,7 +114,13 @@ b2r_status b2r_step(b2r_handle* h, int nsteps);
  * has a non-default stream).  Default on; results are identical either way. */
 b2r_status b2r_set_graphs(b2r_handle* h, int enable);
 /* Launch-schedule knobs of the heat sweep (the autotuner's search space). */
-enum { B2R_TUNE_ZCHUNK = 1, B2R_TUNE_CTAS_PER_SM = 2, B2R_TUNE_PDL = 3 };
+enum {
+    B2R_TUNE_ZCHUNK = 1,       /* planes per work unit of the one-step sweep (0 = 16) */
+    B2R_TUNE_CTAS_PER_SM = 2,  /* 0 = one CTA per unit, k = persistent k CTAs per SM */
+    B2R_TUNE_PDL = 3,          /* programmatic dependent launch on / off */
+    B2R_TUNE_TBLOCK = 4,       /* time steps per HBM pass: 2 (radius 1, default) or 1 */
+    B2R_TUNE_ZCHUNK2 = 5       /* planes per work unit of the two-step sweep (0 = 16) */
+};
 b2r_status b2r_set_tuning(b2r_handle* h, int key, int value);
 /* Time every schedule candidate (z-chunk length x persistent CTAs per SM x
  * programmatic dependent launch) for trial_steps time steps on the live

@@ -132,3 +132,30 @@ def test_run_host_roundtrip(b2r, orc):
     ref = dom.copy()
     orc.heat_run(ref, 1, 1, 5, 0.1, 1.0, 1.0, 1.0)
     assert rel_l2(out, ref) <= TOL
+
+
+@pytest.mark.parametrize("env,blocks,R,periodic", [((131, 37, 29), (1, 1, 1), 1, False),
+                                                   ((250, 61, 47), (1, 1, 1), 3, False),
+                                                   ((96, 48, 64), (2, 2, 2), 3, False),
+                                                   ((64, 64, 48), (2, 1, 2), 4, True),
+                                                   ((33, 17, 9), (1, 1, 1), 1, False)])
+def test_two_step_sweep_bit_identical(b2r, orc, env, blocks, R, periodic):
+    """Two sub-steps per HBM pass (radius 1) against one step per launch."""
+    bc = b2r.BC_PERIODIC if periodic else b2r.BC_SHELL
+    rng = np.random.default_rng(8)
+    if periodic:
+        dom = rng.random(env[::-1], dtype=np.float32)
+    else:
+        dom = shell_domain(env, 1, 8)
+    outs = []
+    for tb in (1, 2):
+        with b2r.Domain(b2r.MODEL_HEAT, env, blocks=blocks, R=R, D=1, boundary=bc, alpha_dt=0.1) as d:
+            d.set_tuning(tblock=tb)
+            d.upload(dom)
+            d.step(11)
+            outs.append(d.download())
+    assert np.array_equal(outs[0], outs[1])
+    if not periodic:
+        ref = dom.copy()
+        orc.heat_run(ref, 1, 1, 11, 0.1, 1.0, 1.0, 1.0)
+        assert rel_l2(outs[1], ref) <= TOL
