@@ -290,32 +290,43 @@ void drop_graphs(b2r_handle* h)
 
 b2r_status substep2(b2r_handle* h, int i);
 
-b2r_status run_period(b2r_handle* h)
+// Advance n time steps from h->ts: a halo exchange at every period start
+// (skipped right after an upload, whose scatter filled the halos), two steps
+// per launch where heat_fuse_ok allows, one otherwise.
+b2r_status advance(b2r_handle* h, int n)
 {
     b2r_status st;
-    if ((st = exchange_all(h, false)) != B2R_OK) return st;
-    for (int i = 0; i < h->cfg.R;) {
-        if (i + 1 < h->cfg.R && heat_fuse_ok(h, i)) {
+    for (int s = 0; s < n;) {
+        const int i = (int)(h->ts % h->cfg.R);
+        if (i == 0 && !h->halos_fresh)
+            if ((st = exchange_all(h, false)) != B2R_OK) return st;
+        h->halos_fresh = false;
+        if (n - s >= 2 && heat_fuse_ok(h, i)) {
             if ((st = substep2(h, i)) != B2R_OK) return st;
-            i += 2;
+            h->ts += 2;
+            s += 2;
         } else {
             if ((st = substep(h, i)) != B2R_OK) return st;
-            ++i;
+            h->ts++;
+            ++s;
         }
     }
     return B2R_OK;
 }
 
-// Capture `periods` whole periods starting from ping-pong buffer `c`.
+// Capture `periods` whole periods starting from ping-pong buffer `c` at a
+// period start.
 b2r_status capture_graph(b2r_handle* h, int c, int periods)
 {
     const int save_cur = h->cur;
     const long long save_ts = h->ts;
+    const bool save_fresh = h->halos_fresh;
     h->cur = c;
+    h->ts = 0;
+    h->halos_fresh = false;
     const long long k0 = b2r_kernel_launches();
     CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    b2r_status st = B2R_OK;
-    for (int p = 0; p < periods && st == B2R_OK; ++p) st = run_period(h);
+    b2r_status st = advance(h, periods * h->cfg.R);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(h->stream, &g);
     const long long nk = b2r_kernel_launches() - k0;
@@ -323,6 +334,7 @@ b2r_status capture_graph(b2r_handle* h, int c, int periods)
     h->gflip[c] = (h->cur != c);
     h->cur = save_cur;
     h->ts = save_ts;
+    h->halos_fresh = save_fresh;
     if (st != B2R_OK) {
         if (g) cudaGraphDestroy(g);
         return st;
@@ -643,18 +655,15 @@ b2r_status b2r_step(b2r_handle* h, int nsteps)
                 continue;
             }
         }
-        if (i == 0 && !h->halos_fresh)
-            if ((st = exchange_all(h, false)) != B2R_OK) return st;
-        h->halos_fresh = false;
-        if (nsteps - s >= 2 && heat_fuse_ok(h, i)) {
-            if ((st = substep2(h, i)) != B2R_OK) return st;
-            h->ts += 2;
-            s += 2;
-            continue;
+        // up to the next period start (or all of it when nothing is graphed)
+        int chunk = nsteps - s;
+        if (use_graphs && i != 0) chunk = std::min(chunk, h->cfg.R - i);
+        if (use_graphs && i == 0) {
+            const int periods = (32 + h->cfg.R - 1) / h->cfg.R;
+            chunk = std::min(chunk, periods * h->cfg.R);
         }
-        if ((st = substep(h, i)) != B2R_OK) return st;
-        h->ts++;
-        ++s;
+        if ((st = advance(h, chunk)) != B2R_OK) return st;
+        s += chunk;
     }
     return B2R_OK;
 }
