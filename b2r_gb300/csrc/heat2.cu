@@ -74,176 +74,224 @@ __device__ __forceinline__ float4 sel(const bool (&m)[4], float4 a, float4 b)
     return make_float4(m[0] ? a.x : b.x, m[1] ? a.y : b.y, m[2] ? a.z : b.z, m[3] ? a.w : b.w);
 }
 
+// Per-unit state of the plane loop.  The 3-plane queues rotate by index:
+// at loop phase PH (= pr mod 3) the newest plane goes to slot PH, so the
+// planes p-2, p-1, p sit in slots (PH+1)%3, (PH+2)%3, PH and no register is
+// moved.
+struct H2Ctx {
+    float4 q0[2][3], q1[2][3];
+    const float* ring;
+    float* s1;
+    uint64_t* bar;
+    int* abort_flag;
+    float* outb;                 // out + block + lane's storage x
+    const CUtensorMap* tmap;
+    HeatCoef C;
+    long long plane, P;
+    unsigned gp;
+    int np, first, zs, ze, xs0, y0, blk, ya, warp, lane, tid;
+    int lo1z, hi1z, lo2z, hi2z;
+    bool m1[2][4];               // stage-1 window, x and y part
+    bool in2y[2], st_all, st_any;
+    bool in2x[4];
+    unsigned issued_hi;
+    bool aborted;
+    unsigned stop;
+};
+
+template <int PH>
+__device__ __forceinline__ void h2_iter(H2Ctx& c, int pr)
+{
+    constexpr int CZ = (PH + 2) % 3, MZ = (PH + 1) % 3, NZ = PH;
+    const unsigned g = c.gp + pr;
+    if (!mbar_wait_bounded(&c.bar[g % kS2], (g / kS2) & 1)) *c.abort_flag = 1;
+    const float* pl = c.ring + (g % kS2) * kPlane;
+#pragma unroll
+    for (int rr = 0; rr < 2; ++rr)
+        c.q0[rr][NZ] = *reinterpret_cast<const float4*>(pl + (2 * c.warp + 1 + rr) * kBoxW + 4 * c.lane);
+    const int p = c.first + pr;
+    // ---- stage 1 at plane z1 = p-1
+    if (pr >= 2) {
+        const int z1 = p - 1;
+        const float* pc = c.ring + ((g - 1) % kS2) * kPlane;
+        const float4 up = *reinterpret_cast<const float4*>(pc + (2 * c.warp) * kBoxW + 4 * c.lane);
+        const float4 dn = *reinterpret_cast<const float4*>(pc + (2 * c.warp + 3) * kBoxW + 4 * c.lane);
+        const bool zin = z1 >= c.lo1z && z1 <= c.hi1z;
+        float* s1p = c.s1 + (z1 & 1) * kP1;
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr) {
+            const float4 ce = c.q0[rr][CZ];
+            const float l = __shfl_up_sync(0xffffffffu, ce.w, 1);
+            const float rt = __shfl_down_sync(0xffffffffu, ce.x, 1);
+            const float4 ym = rr == 0 ? up : c.q0[0][CZ];
+            const float4 yp = rr == 0 ? c.q0[1][CZ] : dn;
+            const float4 v = upd(c.C, ce, l, rt, ym, yp, c.q0[rr][MZ], c.q0[rr][NZ]);
+            float4 res;
+            if (zin) {
+                res.x = c.m1[rr][0] ? v.x : ce.x;
+                res.y = c.m1[rr][1] ? v.y : ce.y;
+                res.z = c.m1[rr][2] ? v.z : ce.z;
+                res.w = c.m1[rr][3] ? v.w : ce.w;
+            } else {
+                res = ce;
+            }
+            *reinterpret_cast<float4*>(s1p + (2 * c.warp + rr) * kBoxW + 4 * c.lane) = res;
+            c.q1[rr][NZ] = res;
+        }
+    }
+    // ---- stage 2 at plane z2 = p-2 (stage-1 planes p-3, p-2, p-1 in q1)
+    if (pr >= 4) {
+        const int z2 = p - 2;
+        const float* sp = c.s1 + (z2 & 1) * kP1;
+        const int wu = 2 * c.warp - 1, wd = 2 * c.warp + 2;
+        const float4 up = *reinterpret_cast<const float4*>(sp + (wu < 0 ? 0 : wu) * kBoxW + 4 * c.lane);
+        const float4 dn = *reinterpret_cast<const float4*>(sp + (wd >= kRows1 ? kRows1 - 1 : wd) * kBoxW + 4 * c.lane);
+        const bool zin = z2 >= c.lo2z && z2 <= c.hi2z && z2 >= c.zs && z2 <= c.ze;
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr) {
+            const float4 ce = c.q1[rr][CZ];
+            const float l = __shfl_up_sync(0xffffffffu, ce.w, 1);
+            const float rt = __shfl_down_sync(0xffffffffu, ce.x, 1);
+            const float4 ym = rr == 0 ? up : c.q1[0][CZ];
+            const float4 yp = rr == 0 ? c.q1[1][CZ] : dn;
+            const float4 v = upd(c.C, ce, l, rt, ym, yp, c.q1[rr][MZ], c.q1[rr][NZ]);
+            if (zin && c.in2y[rr] && c.st_any) {
+                float* dst = c.outb + (long long)z2 * c.plane + (long long)(c.ya + rr) * c.P;
+                if (c.st_all) {
+                    *reinterpret_cast<float4*>(dst) = v;
+                } else {
+                    if (c.in2x[0]) dst[0] = v.x;
+                    if (c.in2x[1]) dst[1] = v.y;
+                    if (c.in2x[2]) dst[2] = v.z;
+                    if (c.in2x[3]) dst[3] = v.w;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (*c.abort_flag) {
+        c.aborted = true;
+        c.stop = g;
+        return;
+    }
+    // plane p-1 is no longer needed: refill its slot with plane p-1+S
+    if (pr >= 1) {
+        const int nxt = pr - 1 + kS2;
+        if (nxt < c.np) {
+            const unsigned g2 = c.gp + nxt;
+            if (c.tid == 0) {
+                mbar_expect_tx(&c.bar[g2 % kS2], kPlane * 4);
+                tma_load_4d(const_cast<float*>(c.ring) + (g2 % kS2) * kPlane, c.tmap, c.xs0, c.y0 - 2,
+                            c.first + nxt, c.blk, &c.bar[g2 % kS2]);
+            }
+            c.issued_hi = g2 + 1;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(kT2, 2)
 heat2_kernel(const __grid_constant__ CUtensorMap tin, float* __restrict__ out, const BlockLayout L,
              const int step_i, const HeatCoef C, const H2Sched sch, int* __restrict__ status)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
+    H2Ctx c;
     float* ring = reinterpret_cast<float*>(smem_raw + ((128 - (smem_u32(smem_raw) & 127)) & 127));
-    float* s1 = ring + kS2 * kPlane;                      // 2 stage-1 planes
-    uint64_t* bar = reinterpret_cast<uint64_t*>(s1 + 2 * kP1);
-    int* abort_flag = reinterpret_cast<int*>(bar + kS2);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) {
-        *abort_flag = 0;
-        for (int s = 0; s < kS2; ++s) mbar_init(&bar[s], 1);
+    c.ring = ring;
+    c.s1 = ring + kS2 * kPlane;                          // 2 stage-1 planes
+    c.bar = reinterpret_cast<uint64_t*>(c.s1 + 2 * kP1);
+    c.abort_flag = reinterpret_cast<int*>(c.bar + kS2);
+    c.tid = threadIdx.x;
+    c.lane = c.tid & 31;
+    c.warp = c.tid >> 5;
+    c.tmap = &tin;
+    c.C = C;
+    c.plane = L.plane;
+    c.P = L.P;
+    if (c.tid == 0) {
+        *c.abort_flag = 0;
+        for (int s = 0; s < kS2; ++s) mbar_init(&c.bar[s], 1);
         fence_mbar_init();
     }
     __syncthreads();
     pdl_wait2();
     pdl_trigger2();
 
-    unsigned gp = 0, issued_hi = 0, stop = 0;
-    bool aborted = false;
-    for (long long u = blockIdx.x; u < sch.U && !aborted; u += gridDim.x) {
+    c.gp = 0;
+    c.issued_hi = 0;
+    c.stop = 0;
+    c.aborted = false;
+    for (long long u = blockIdx.x; u < sch.U && !c.aborted; u += gridDim.x) {
         const int tx = (int)(u % sch.ntx);
         long long r = u / sch.ntx;
         const int ty = (int)(r % sch.nty);
         r /= sch.nty;
         const int zc = (int)(r % sch.nzc);
-        const int blk = (int)(r / sch.nzc);
-        const int edge = edge_bits(L, blk);
+        c.blk = (int)(r / sch.nzc);
+        const int edge = edge_bits(L, c.blk);
         int lo1[3], hi1[3], lo2[3], hi2[3];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             stage_region(L, edge, a, step_i + 1, lo1[a], hi1[a]);
             stage_region(L, edge, a, step_i + 2, lo2[a], hi2[a]);
         }
-        const int xs0 = sch.out0 - 4 + tx * kOutW;       // storage x of lane 0's first cell
-        const int y0 = 1 + ty * kOutH;                   // block y of output row 0
+        c.xs0 = sch.out0 - 4 + tx * kOutW;               // storage x of lane 0's first cell
+        c.y0 = 1 + ty * kOutH;                           // block y of output row 0
         const int zi0 = zc * sch.Lz;
-        const int zs = max(1 + zi0, lo2[2]);
-        const int ze = min(zi0 + sch.Lz, hi2[2]);        // output planes [zs, ze]
-        if (zs > ze) continue;
-        if (xs0 + 4 - L.xoff > hi2[0] || xs0 + 123 - L.xoff < lo2[0]) continue;
-        if (y0 > hi2[1] || y0 + kOutH - 1 < lo2[1]) continue;
-        const int first = zs - 2;                        // first input plane
-        const int np = ze + 2 - first + 1;
-        if (tid == 0)
-            for (int s = 0; s < kS2 && s < np; ++s) {
-                const unsigned g = gp + s;
-                mbar_expect_tx(&bar[g % kS2], kPlane * 4);
-                tma_load_4d(ring + (g % kS2) * kPlane, &tin, xs0, y0 - 2, first + s, blk, &bar[g % kS2]);
+        c.zs = max(1 + zi0, lo2[2]);
+        c.ze = min(zi0 + sch.Lz, hi2[2]);                // output planes [zs, ze]
+        if (c.zs > c.ze) continue;
+        if (c.xs0 + 4 - L.xoff > hi2[0] || c.xs0 + 123 - L.xoff < lo2[0]) continue;
+        if (c.y0 > hi2[1] || c.y0 + kOutH - 1 < lo2[1]) continue;
+        c.first = c.zs - 2;                              // first input plane
+        c.np = c.ze + 2 - c.first + 1;
+        c.lo1z = lo1[2];
+        c.hi1z = hi1[2];
+        c.lo2z = lo2[2];
+        c.hi2z = hi2[2];
+        if (c.tid == 0)
+            for (int s = 0; s < kS2 && s < c.np; ++s) {
+                const unsigned g = c.gp + s;
+                mbar_expect_tx(&c.bar[g % kS2], kPlane * 4);
+                tma_load_4d(ring + (g % kS2) * kPlane, &tin, c.xs0, c.y0 - 2, c.first + s, c.blk,
+                            &c.bar[g % kS2]);
             }
-        issued_hi = gp + min(kS2, np);
+        c.issued_hi = c.gp + min(kS2, c.np);
 
         // this thread's cells: storage x xs0+4*lane.., stage-1 rows 2w, 2w+1
-        const int xb = xs0 + 4 * lane - L.xoff;          // block x of the first cell
-        const int ya = y0 - 1 + 2 * warp;                // block y of stage-1 row 2w
-        bool in1x[4], in2x[4];
+        const int xb = c.xs0 + 4 * c.lane - L.xoff;      // block x of the first cell
+        c.ya = c.y0 - 1 + 2 * c.warp;                    // block y of stage-1 row 2w
+        bool in1x[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             in1x[j] = xb + j >= lo1[0] && xb + j <= hi1[0];
-            in2x[j] = xb + j >= lo2[0] && xb + j <= hi2[0] && lane >= 1 && lane <= 30;
+            c.in2x[j] = xb + j >= lo2[0] && xb + j <= hi2[0] && c.lane >= 1 && c.lane <= 30;
         }
-        const bool in1y[2] = {ya >= lo1[1] && ya <= hi1[1], ya + 1 >= lo1[1] && ya + 1 <= hi1[1]};
-        const bool in2y[2] = {ya >= lo2[1] && ya <= hi2[1] && 2 * warp >= 1,
-                              ya + 1 >= lo2[1] && ya + 1 <= hi2[1] && 2 * warp + 1 <= kOutH};
-        const bool st_all = in2x[0] && in2x[1] && in2x[2] && in2x[3];
-        const bool st_any = in2x[0] || in2x[1] || in2x[2] || in2x[3];
-
-        float4 q0[2][3], q1[2][3];       // [row][plane]: input / stage-1 queues (z-1, z, z+1)
-        float* const outb = out + (long long)blk * L.bstride + xs0 + 4 * lane;
-
-        for (int pr = 0; pr < np; ++pr) {
-            const unsigned g = gp + pr;
-            if (!mbar_wait_bounded(&bar[g % kS2], (g / kS2) & 1)) *abort_flag = 1;
-            const float* pl = ring + (g % kS2) * kPlane;
-            // push input plane p (box rows 2w+1, 2w+2 = stage-1 rows 2w, 2w+1)
 #pragma unroll
-            for (int rr = 0; rr < 2; ++rr) {
-                q0[rr][0] = q0[rr][1];
-                q0[rr][1] = q0[rr][2];
-                q0[rr][2] = *reinterpret_cast<const float4*>(pl + (2 * warp + 1 + rr) * kBoxW + 4 * lane);
-            }
-            const int p = first + pr;
-            // ---- stage 1 at plane z1 = p-1
-            if (pr >= 2) {
-                const int z1 = p - 1;
-                const float* pc = ring + ((g - 1) % kS2) * kPlane;   // input plane z1
-                const float4 up = *reinterpret_cast<const float4*>(pc + (2 * warp) * kBoxW + 4 * lane);
-                const float4 dn = *reinterpret_cast<const float4*>(pc + (2 * warp + 3) * kBoxW + 4 * lane);
-                const bool zin = z1 >= lo1[2] && z1 <= hi1[2];
-                float4 res[2];
+        for (int rr = 0; rr < 2; ++rr) {
+            const bool y1 = c.ya + rr >= lo1[1] && c.ya + rr <= hi1[1];
 #pragma unroll
-                for (int rr = 0; rr < 2; ++rr) {
-                    const float4 c = q0[rr][1];
-                    const float l = __shfl_up_sync(0xffffffffu, c.w, 1);
-                    const float rt = __shfl_down_sync(0xffffffffu, c.x, 1);
-                    const float4 ym = rr == 0 ? up : q0[0][1];
-                    const float4 yp = rr == 0 ? q0[1][1] : dn;
-                    const float4 v = upd(C, c, l, rt, ym, yp, q0[rr][0], q0[rr][2]);
-                    bool m[4];
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) m[j] = zin && in1y[rr] && in1x[j];
-                    res[rr] = sel(m, v, c);
-                }
-                float* s1p = s1 + (z1 & 1) * kP1;
-                *reinterpret_cast<float4*>(s1p + (2 * warp) * kBoxW + 4 * lane) = res[0];
-                *reinterpret_cast<float4*>(s1p + (2 * warp + 1) * kBoxW + 4 * lane) = res[1];
-#pragma unroll
-                for (int rr = 0; rr < 2; ++rr) {
-                    q1[rr][0] = q1[rr][1];
-                    q1[rr][1] = q1[rr][2];
-                    q1[rr][2] = res[rr];
-                }
-            }
-            // ---- stage 2 at plane z2 = p-2 (stage-1 planes z2-1 .. z2+1 in q1)
-            if (pr >= 4) {
-                const int z2 = p - 2;
-                const float* sp = s1 + (z2 & 1) * kP1;              // stage-1 plane z2
-                const int wu = 2 * warp - 1, wd = 2 * warp + 2;     // rows of other warps
-                const float4 up = wu >= 0 ? *reinterpret_cast<const float4*>(sp + wu * kBoxW + 4 * lane)
-                                          : make_float4(0.f, 0.f, 0.f, 0.f);
-                const float4 dn = wd < kRows1 ? *reinterpret_cast<const float4*>(sp + wd * kBoxW + 4 * lane)
-                                              : make_float4(0.f, 0.f, 0.f, 0.f);
-                const bool zin = z2 >= lo2[2] && z2 <= hi2[2] && z2 >= zs && z2 <= ze;
-#pragma unroll
-                for (int rr = 0; rr < 2; ++rr) {
-                    const float4 c = q1[rr][1];
-                    const float l = __shfl_up_sync(0xffffffffu, c.w, 1);
-                    const float rt = __shfl_down_sync(0xffffffffu, c.x, 1);
-                    const float4 ym = rr == 0 ? up : q1[0][1];
-                    const float4 yp = rr == 0 ? q1[1][1] : dn;
-                    const float4 v = upd(C, c, l, rt, ym, yp, q1[rr][0], q1[rr][2]);
-                    if (zin && in2y[rr] && st_any) {
-                        float* dst = outb + (long long)z2 * L.plane + (long long)(ya + rr) * L.P;
-                        if (st_all) {
-                            *reinterpret_cast<float4*>(dst) = v;
-                        } else {
-                            if (in2x[0]) dst[0] = v.x;
-                            if (in2x[1]) dst[1] = v.y;
-                            if (in2x[2]) dst[2] = v.z;
-                            if (in2x[3]) dst[3] = v.w;
-                        }
-                    }
-                }
-            }
-            __syncthreads();
-            if (*abort_flag) {
-                aborted = true;
-                stop = g;
-                break;
-            }
-            // plane p-1 is no longer needed: refill its slot with plane p-1+S
-            if (pr >= 1) {
-                const int nxt = pr - 1 + kS2;
-                if (nxt < np) {
-                    const unsigned g2 = gp + nxt;
-                    if (tid == 0) {
-                        mbar_expect_tx(&bar[g2 % kS2], kPlane * 4);
-                        tma_load_4d(ring + (g2 % kS2) * kPlane, &tin, xs0, y0 - 2, first + nxt, blk,
-                                    &bar[g2 % kS2]);
-                    }
-                    issued_hi = g2 + 1;
-                }
-            }
+            for (int j = 0; j < 4; ++j) c.m1[rr][j] = y1 && in1x[j];
         }
-        if (!aborted) gp += np;
+        c.in2y[0] = c.ya >= lo2[1] && c.ya <= hi2[1] && 2 * c.warp >= 1;
+        c.in2y[1] = c.ya + 1 >= lo2[1] && c.ya + 1 <= hi2[1] && 2 * c.warp + 1 <= kOutH;
+        c.st_all = c.in2x[0] && c.in2x[1] && c.in2x[2] && c.in2x[3];
+        c.st_any = c.in2x[0] || c.in2x[1] || c.in2x[2] || c.in2x[3];
+        c.outb = out + (long long)c.blk * L.bstride + c.xs0 + 4 * c.lane;
+
+        for (int pr = 0; pr < c.np;) {
+            h2_iter<0>(c, pr++);
+            if (c.aborted || pr >= c.np) break;
+            h2_iter<1>(c, pr++);
+            if (c.aborted || pr >= c.np) break;
+            h2_iter<2>(c, pr++);
+            if (c.aborted) break;
+        }
+        if (!c.aborted) c.gp += c.np;
     }
-    if (aborted && tid == 0) {
+    if (c.aborted && c.tid == 0) {
         report(status, DEV_TIMEOUT);
-        for (unsigned g = stop; g < issued_hi; ++g) mbar_wait_bounded(&bar[g % kS2], (g / kS2) & 1, 100000000ull);
+        for (unsigned g = c.stop; g < c.issued_hi; ++g)
+            mbar_wait_bounded(&c.bar[g % kS2], (g / kS2) & 1, 100000000ull);
     }
 }
 
