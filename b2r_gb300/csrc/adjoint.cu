@@ -14,175 +14,217 @@
 //   3. velocity stage: w = b*vb on W (0 elsewhere);  sb += dt*D^T w;
 //      g_b += dt*(D s)*vb on W
 // with Dp^T = -Dm and Dm^T = -Dp for the 4th-order staggered differences.
-// Gradients accumulate in FP64.  g_rho = -g_b / rho^2 at the end.
+// The per-step gradient increments are formed in FP32 and accumulated in
+// FP64 (this GPU's FP64 rate is a small fraction of its FP32 rate, so the
+// products stay in FP32).  g_rho = -g_b / rho^2 at the end.
 #include <cstdio>
 #include <vector>
 
 #include "b2r_common.cuh"
 #include "eqwp.h"
+#include "eqwp_tile.cuh"
 
 namespace b2r {
 namespace {
 
-constexpr float C1 = 1.125f, C2 = -1.f / 24.f;
+using namespace eqk;
 
-__device__ __forceinline__ float dpf(const float* f, long long s)
-{
-    return C1 * (f[s] - f[0]) + C2 * (f[2 * s] - f[-s]);
-}
-__device__ __forceinline__ float dmf(const float* f, long long s)
-{
-    return C1 * (f[0] - f[-s]) + C2 * (f[s] - f[-2 * s]);
-}
-
-struct Adj {
-    float* vb[3];          // adjoint velocity
-    float* sb[6];          // adjoint stress: xx, xy, xz, yy, yz, zz
-    float* q[6];           // C*sb on W
-    float* w[3];           // b*vb on W
-    const float* v[3];     // forward velocity v^{n+1}
-    const float* s[6];     // forward stress s^n (for the velocity-stage gradient)
-    const float* lam;
-    const float* mu;
-    const float* buoy;
-    double* g_lam;
-    double* g_mu;
-    double* g_b;
-    float dt_h;            // dt / h
-    int lo[3], hi[3];      // window W (inclusive)
+// FP64 gradient cells of a thread, loaded before and stored after the
+// field stores of an iteration (32-byte aligned: the first cell of a thread
+// is a multiple of 4 elements from the buffer base)
+struct G4 {
+    double v[4];
+    __device__ __forceinline__ void load(const double* g, const Cell& c)
+    {
+        if (c.all) {
+            const double2 a = reinterpret_cast<const double2*>(g)[0];
+            const double2 b = reinterpret_cast<const double2*>(g)[1];
+            v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) v[j] = c.vx[j] ? g[j] : 0.0;
+        }
+    }
+    __device__ __forceinline__ void store(double* g, const Cell& c) const
+    {
+        if (c.all) {
+            reinterpret_cast<double2*>(g)[0] = make_double2(v[0], v[1]);
+            reinterpret_cast<double2*>(g)[1] = make_double2(v[2], v[3]);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (c.vx[j]) g[j] = v[j];
+        }
+    }
 };
 
-__device__ __forceinline__ bool cell_of(const BlockLayout& L, long long e, int& x, int& y, int& z)
-{
-    x = (int)(e % L.n[0]);
-    const long long r = e / L.n[0];
-    y = (int)(r % L.n[1]);
-    z = (int)(r / L.n[1]);
-    return true;
-}
+// sb component (xx, xy, xz, yy, yz, zz numbering) of each strain row of StrOp
+__device__ constexpr int kStrainS[6] = {0, 3, 5, 1, 2, 4};
 
-__device__ __forceinline__ bool in_w(const Adj& A, int x, int y, int z)
-{
-    return x >= A.lo[0] && x <= A.hi[0] && y >= A.lo[1] && y <= A.hi[1] && z >= A.lo[2] && z <= A.hi[2];
-}
+struct AdjV {
+    const float* q[6];     // C*sb of the later step (xx, xy, xz, yy, yz, zz)
+    float* vb[3];          // adjoint velocity, updated
+    float* w[3];           // b*vb on the window (out)
+    const float* acc[3];   // forward stencil sums (D s^n) of this step
+    const float* buoy;
+    double* g_b;
+    float k;               // dt / h
+};
 
-// 2a: q = C*sb on W, 0 elsewhere; lambda / mu gradients on W (uses v^{n+1})
-__global__ void adj_q_kernel(Adj A, const BlockLayout L)
+struct AdjS {
+    const float* w[3];     // b*vb of this step
+    float* sb[6];          // adjoint stress, updated (xx, xy, xz, yy, yz, zz)
+    float* q[6];           // C*sb for the earlier step (out)
+    const float* v[3];     // forward velocity v^n
+    const float* lam;
+    const float* mu;
+    double* g_lam;
+    double* g_mu;
+    float k;
+};
+
+// Adjoint of the stress stage of step n followed by the velocity-stage
+// weighting:  vb -= k * D q  (D^T E = -D: the transpose of the strain
+// operator is minus the velocity-stage operator), then w = b * vb and
+// g_b += k * (D s^n) . vb on the window.
+__global__ void __launch_bounds__(kBX * kBY, B2R_EQWP_MINB)
+adj_velocity_kernel(AdjV A, const BlockLayout L, int nzc)
 {
-    const long long total = (long long)L.n[0] * L.n[1] * L.n[2];
+    const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
+    const Win w = window(L, blk, zc, nzc, 2);
+    Cell c;
+    if (!cell_setup(L, w, blk, c)) return;
     const long long P = L.P, S = L.plane;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-         e += (long long)gridDim.x * blockDim.x) {
-        int x, y, z;
-        cell_of(L, e, x, y, z);
-        const long long id = (long long)z * S + (long long)y * P + L.xoff + x;
-        if (!in_w(A, x, y, z)) {
-            for (int k = 0; k < 6; ++k) A.q[k][id] = 0.f;
-            continue;
+    VelOp op;
+    op.xx = A.q[0] + c.base;
+    op.xy = A.q[1] + c.base;
+    op.xz = A.q[2] + c.base;
+    op.yy = A.q[3] + c.base;
+    op.yz = A.q[4] + c.base;
+    op.zz = A.q[5] + c.base;
+    op.begin(w.zs, S);
+    for (int z = w.zs; z <= w.ze; ++z) {
+        const long long o = (long long)z * S + c.base;
+        float a[3][4];
+        op.eval(o - c.base, P, S, a[0], a[1], a[2]);
+        const float4 bb = ld4(A.buoy + o);
+        float4 vb[3], ac[3];
+#pragma unroll
+        for (int f = 0; f < 3; ++f) {
+            vb[f] = rd4(A.vb[f] + o, c);
+            ac[f] = ld4(A.acc[f] + o);
         }
-        const float l = A.lam[id], m = A.mu[id];
-        const float sxx = A.sb[0][id], sxy = A.sb[1][id], sxz = A.sb[2][id];
-        const float syy = A.sb[3][id], syz = A.sb[4][id], szz = A.sb[5][id];
-        const float tr = sxx + syy + szz;
-        A.q[0][id] = 2.f * m * sxx + l * tr;
-        A.q[3][id] = 2.f * m * syy + l * tr;
-        A.q[5][id] = 2.f * m * szz + l * tr;
-        A.q[1][id] = m * sxy;
-        A.q[2][id] = m * sxz;
-        A.q[4][id] = m * syz;
-        // strain of v^{n+1} (the forward stress stage, eqwp.cu STAG)
-        const float* vx = A.v[0] + id;
-        const float* vy = A.v[1] + id;
-        const float* vz = A.v[2] + id;
-        const float exx = dmf(vx, 1), eyy = dmf(vy, P), ezz = dmf(vz, S);
-        const float gxy = dpf(vx, P) + dpf(vy, 1);
-        const float gxz = dpf(vx, S) + dpf(vz, 1);
-        const float gyz = dpf(vy, S) + dpf(vz, P);
-        const double k = (double)A.dt_h;
-        A.g_lam[id] += k * ((double)exx + eyy + ezz) * (double)tr;
-        A.g_mu[id] += k * (2.0 * ((double)exx * sxx + (double)eyy * syy + (double)ezz * szz) +
-                           (double)gxy * sxy + (double)gxz * sxz + (double)gyz * syz);
-    }
-}
-
-// 2b: vb += dt*E^T q  (E: exx = Dm_x vx, eyy = Dm_y vy, ezz = Dm_z vz,
-// gxy = Dp_y vx + Dp_x vy, gxz = Dp_z vx + Dp_x vz, gyz = Dp_z vy + Dp_y vz)
-__global__ void adj_vb_kernel(Adj A, const BlockLayout L)
-{
-    const long long total = (long long)L.n[0] * L.n[1] * L.n[2];
-    const long long P = L.P, S = L.plane;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-         e += (long long)gridDim.x * blockDim.x) {
-        int x, y, z;
-        cell_of(L, e, x, y, z);
-        if (x < 2 || y < 2 || z < 2 || x > L.n[0] - 3 || y > L.n[1] - 3 || z > L.n[2] - 3) continue;
-        const long long id = (long long)z * S + (long long)y * P + L.xoff + x;
-        const float* qxx = A.q[0] + id;
-        const float* qxy = A.q[1] + id;
-        const float* qxz = A.q[2] + id;
-        const float* qyy = A.q[3] + id;
-        const float* qyz = A.q[4] + id;
-        const float* qzz = A.q[5] + id;
-        const float k = A.dt_h;
-        A.vb[0][id] -= k * (dpf(qxx, 1) + dmf(qxy, P) + dmf(qxz, S));
-        A.vb[1][id] -= k * (dpf(qyy, P) + dmf(qxy, 1) + dmf(qyz, S));
-        A.vb[2][id] -= k * (dpf(qzz, S) + dmf(qxz, 1) + dmf(qyz, P));
-    }
-}
-
-// 3a: w = b*vb on W (0 elsewhere); g_b += dt*(D s^n).vb on W
-__global__ void adj_w_kernel(Adj A, const BlockLayout L)
-{
-    const long long total = (long long)L.n[0] * L.n[1] * L.n[2];
-    const long long P = L.P, S = L.plane;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-         e += (long long)gridDim.x * blockDim.x) {
-        int x, y, z;
-        cell_of(L, e, x, y, z);
-        const long long id = (long long)z * S + (long long)y * P + L.xoff + x;
-        if (!in_w(A, x, y, z)) {
-            for (int k = 0; k < 3; ++k) A.w[k][id] = 0.f;
-            continue;
+        G4 gb;
+        gb.load(A.g_b + o, c);
+        float d[3][4];
+#pragma unroll
+        for (int f = 0; f < 3; ++f)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) d[f][j] = -(A.k * a[f][j]);
+#pragma unroll
+        for (int f = 0; f < 3; ++f) vb[f] = wr4(A.vb[f] + o, c, vb[f], d[f]);
+        float wv[3][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float b = cmp(bb, j);
+            const float x = cmp(vb[0], j), y = cmp(vb[1], j), zz = cmp(vb[2], j);
+            wv[0][j] = b * x;
+            wv[1][j] = b * y;
+            wv[2][j] = b * zz;
+            gb.v[j] += (double)(A.k * (cmp(ac[0], j) * x + cmp(ac[1], j) * y + cmp(ac[2], j) * zz));
         }
-        const float b = A.buoy[id];
-        const float vbx = A.vb[0][id], vby = A.vb[1][id], vbz = A.vb[2][id];
-        A.w[0][id] = b * vbx;
-        A.w[1][id] = b * vby;
-        A.w[2][id] = b * vbz;
-        const float* sxx = A.s[0] + id;
-        const float* sxy = A.s[1] + id;
-        const float* sxz = A.s[2] + id;
-        const float* syy = A.s[3] + id;
-        const float* syz = A.s[4] + id;
-        const float* szz = A.s[5] + id;
-        const float ax = dpf(sxx, 1) + dmf(sxy, P) + dmf(sxz, S);
-        const float ay = dmf(sxy, 1) + dpf(syy, P) + dmf(syz, S);
-        const float az = dmf(sxz, 1) + dmf(syz, P) + dpf(szz, S);
-        A.g_b[id] += (double)A.dt_h * ((double)ax * vbx + (double)ay * vby + (double)az * vbz);
+#pragma unroll
+        for (int f = 0; f < 3; ++f) st4(A.w[f] + o, c, wv[f]);
+        gb.store(A.g_b + o, c);
     }
 }
 
-// 3b: sb += dt*D^T w  (velocity stage: ax = Dp_x sxx + Dm_y sxy + Dm_z sxz, ...)
-__global__ void adj_sb_kernel(Adj A, const BlockLayout L)
+// Adjoint of the velocity stage of step n followed by the stress weighting
+// of step n-1:  sb -= k * E w  (D^T = -E), then q = C(lambda, mu) * sb on
+// the window.
+__global__ void __launch_bounds__(kBX * kBY, B2R_EQWP_MINB)
+adj_stress_kernel(AdjS A, const BlockLayout L, int nzc)
 {
-    const long long total = (long long)L.n[0] * L.n[1] * L.n[2];
+    const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
+    const Win w = window(L, blk, zc, nzc, 4);
+    Cell c;
+    if (!cell_setup(L, w, blk, c)) return;
     const long long P = L.P, S = L.plane;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-         e += (long long)gridDim.x * blockDim.x) {
-        int x, y, z;
-        cell_of(L, e, x, y, z);
-        if (x < 2 || y < 2 || z < 2 || x > L.n[0] - 3 || y > L.n[1] - 3 || z > L.n[2] - 3) continue;
-        const long long id = (long long)z * S + (long long)y * P + L.xoff + x;
-        const float* wx = A.w[0] + id;
-        const float* wy = A.w[1] + id;
-        const float* wz = A.w[2] + id;
-        const float k = A.dt_h;
-        A.sb[0][id] -= k * dmf(wx, 1);
-        A.sb[3][id] -= k * dmf(wy, P);
-        A.sb[5][id] -= k * dmf(wz, S);
-        A.sb[1][id] -= k * (dpf(wx, P) + dpf(wy, 1));
-        A.sb[2][id] -= k * (dpf(wx, S) + dpf(wz, 1));
-        A.sb[4][id] -= k * (dpf(wy, S) + dpf(wz, P));
+    StrOp ow;
+    ow.x = A.w[0] + c.base;
+    ow.y = A.w[1] + c.base;
+    ow.z = A.w[2] + c.base;
+    ow.begin(w.zs, S);
+    for (int z = w.zs; z <= w.ze; ++z) {
+        const long long o = (long long)z * S + c.base;
+        float ew[6][4];
+        ow.eval(o - c.base, P, S, ew);
+        const float4 l4 = ld4(A.lam + o), m4 = ld4(A.mu + o);
+        float4 sb[6];
+#pragma unroll
+        for (int f = 0; f < 6; ++f) sb[f] = rd4(A.sb[kStrainS[f]] + o, c);
+        float d[6][4];
+#pragma unroll
+        for (int f = 0; f < 6; ++f)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) d[f][j] = -(A.k * ew[f][j]);
+#pragma unroll
+        for (int f = 0; f < 6; ++f) sb[f] = wr4(A.sb[kStrainS[f]] + o, c, sb[f], d[f]);
+        float qv[6][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float l = cmp(l4, j), m = cmp(m4, j);
+            const float sxx = cmp(sb[0], j), syy = cmp(sb[1], j), szz = cmp(sb[2], j);
+            const float tr = sxx + syy + szz;
+            qv[0][j] = 2.f * m * sxx + l * tr;
+            qv[1][j] = 2.f * m * syy + l * tr;
+            qv[2][j] = 2.f * m * szz + l * tr;
+            qv[3][j] = m * cmp(sb[3], j);
+            qv[4][j] = m * cmp(sb[4], j);
+            qv[5][j] = m * cmp(sb[5], j);
+        }
+#pragma unroll
+        for (int f = 0; f < 6; ++f) st4(A.q[kStrainS[f]] + o, c, qv[f]);
+    }
+}
+
+// lambda / mu gradients of the stress stage of step n-1 on the window:
+// g_lambda += k * tr(E v^n) tr(sb),  g_mu += k * (2 e_ii sb_ii + gamma_ij sb_ij)
+__global__ void __launch_bounds__(kBX * kBY, B2R_EQWP_MINB)
+adj_grad_lm_kernel(AdjS A, const BlockLayout L, int nzc)
+{
+    const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
+    const Win w = window(L, blk, zc, nzc, 4);
+    Cell c;
+    if (!cell_setup(L, w, blk, c)) return;
+    const long long P = L.P, S = L.plane;
+    StrOp ov;
+    ov.x = A.v[0] + c.base;
+    ov.y = A.v[1] + c.base;
+    ov.z = A.v[2] + c.base;
+    ov.begin(w.zs, S);
+    for (int z = w.zs; z <= w.ze; ++z) {
+        const long long o = (long long)z * S + c.base;
+        float ev[6][4];
+        ov.eval(o - c.base, P, S, ev);
+        float4 sb[6];
+#pragma unroll
+        for (int f = 0; f < 6; ++f) sb[f] = ld4(A.sb[kStrainS[f]] + o);
+        G4 gl, gm;
+        gl.load(A.g_lam + o, c);
+        gm.load(A.g_mu + o, c);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float sxx = cmp(sb[0], j), syy = cmp(sb[1], j), szz = cmp(sb[2], j);
+            const float sxy = cmp(sb[3], j), sxz = cmp(sb[4], j), syz = cmp(sb[5], j);
+            const float tr = sxx + syy + szz;
+            const float exx = ev[0][j], eyy = ev[1][j], ezz = ev[2][j];
+            gl.v[j] += (double)(A.k * ((exx + eyy + ezz) * tr));
+            gm.v[j] += (double)(A.k * (2.f * (exx * sxx + eyy * syy + ezz * szz) +
+                                       (ev[3][j] * sxy + ev[4][j] * sxz + ev[5][j] * syz)));
+        }
+        gl.store(A.g_lam + o, c);
+        gm.store(A.g_mu + o, c);
     }
 }
 
@@ -266,40 +308,43 @@ cudaError_t adjoint_inject(float* vby, const long long* d_idx, int nrec, const f
     return cudaGetLastError();
 }
 
-// One reverse step.  fwd_v: v^{n+1} (3 fields), fwd_s: s^n (6 fields in the
-// order xx, xy, xz, yy, yz, zz).
-cudaError_t adjoint_step(float* const* tmp, const float* const* fwd_v, const float* const* fwd_s,
+// Reverse step n: q (from the later step) -> vb, w, g_b; then, unless n is
+// the first step, w -> sb, q for step n-1, g_lambda, g_mu.  tmp = vb[3],
+// sb[6], q[6], w[3]; v_n = forward v^n, acc_n = forward D s^n.
+cudaError_t adjoint_step(float* const* tmp, const float* const* v_n, const float* const* acc_n,
                          const float* const* mat, double* const* g, const BlockLayout& L, float dt_h,
-                         const int lo[3], const int hi[3], cudaStream_t st)
+                         bool last, cudaStream_t st)
 {
-    Adj A;
+    AdjV V;
+    AdjS T;
     for (int k = 0; k < 3; ++k) {
-        A.vb[k] = tmp[k];
-        A.w[k] = tmp[15 + k];
-        A.v[k] = fwd_v[k];
+        V.vb[k] = tmp[k];
+        V.w[k] = tmp[15 + k];
+        V.acc[k] = acc_n[k];
+        T.w[k] = tmp[15 + k];
+        T.v[k] = v_n[k];
     }
     for (int k = 0; k < 6; ++k) {
-        A.sb[k] = tmp[3 + k];
-        A.q[k] = tmp[9 + k];
-        A.s[k] = fwd_s[k];
+        V.q[k] = tmp[9 + k];
+        T.sb[k] = tmp[3 + k];
+        T.q[k] = tmp[9 + k];
     }
-    A.lam = mat[0];
-    A.mu = mat[1];
-    A.buoy = mat[2];
-    A.g_lam = g[0];
-    A.g_mu = g[1];
-    A.g_b = g[2];
-    A.dt_h = dt_h;
-    for (int a = 0; a < 3; ++a) {
-        A.lo[a] = lo[a];
-        A.hi[a] = hi[a];
+    V.buoy = mat[2];
+    V.g_b = g[2];
+    V.k = dt_h;
+    T.lam = mat[0];
+    T.mu = mat[1];
+    T.g_lam = g[0];
+    T.g_mu = g[1];
+    T.k = dt_h;
+    const Grid gr = stage_grid(L);
+    adj_velocity_kernel<<<gr.g, dim3(kBX, kBY), 0, st>>>(V, L, gr.nzc);
+    count_launches(1);
+    if (!last) {
+        adj_stress_kernel<<<gr.g, dim3(kBX, kBY), 0, st>>>(T, L, gr.nzc);
+        adj_grad_lm_kernel<<<gr.g, dim3(kBX, kBY), 0, st>>>(T, L, gr.nzc);
+        count_launches(2);
     }
-    const int grid = grid_for((long long)L.n[0] * L.n[1] * L.n[2]);
-    adj_q_kernel<<<grid, 256, 0, st>>>(A, L);
-    adj_vb_kernel<<<grid, 256, 0, st>>>(A, L);
-    adj_w_kernel<<<grid, 256, 0, st>>>(A, L);
-    adj_sb_kernel<<<grid, 256, 0, st>>>(A, L);
-    count_launches(4);
     return cudaGetLastError();
 }
 

@@ -55,6 +55,10 @@ struct b2r_handle {
     bool gflip[2] = {false, false};                   // the graph ends on the other buffer
     int gsteps = 0;                                   // time steps per graph launch
     long long gkernels = 0;                           // kernels per graph launch
+    // misfit-gradient workspace (checkpoints, replay, adjoint fields, FP64
+    // gradients), kept for the next call on this handle
+    void* adj_ws = nullptr;
+    size_t adj_ws_bytes = 0;
     std::string err;
 };
 
@@ -245,6 +249,17 @@ b2r_status exchange_one(b2r_handle* h, int field, bool staged)
     return B2R_OK;
 }
 
+EqwpStagParams stag_params(const b2r_handle* h)
+{
+    EqwpStagParams p{};
+    p.dt = (float)h->cfg.dt;
+    p.inv_h = (float)(1.0 / h->cfg.h);
+    for (int a = 0; a < 3; ++a) p.src[a] = h->cfg.src[a];
+    p.src_host = h->src.empty() ? nullptr : h->src.data();
+    p.src_len = (int)h->src.size();
+    return p;
+}
+
 b2r_status substep(b2r_handle* h, int i)
 {
     switch (h->cfg.model) {
@@ -264,12 +279,7 @@ b2r_status substep(b2r_handle* h, int i)
         return B2R_OK;
     }
     case B2R_MODEL_EQWP_STAG: {
-        EqwpStagParams p{};
-        p.dt = (float)h->cfg.dt;
-        p.inv_h = (float)(1.0 / h->cfg.h);
-        for (int a = 0; a < 3; ++a) p.src[a] = h->cfg.src[a];
-        p.src_host = h->src.empty() ? nullptr : h->src.data();
-        p.src_len = (int)h->src.size();
+        const EqwpStagParams p = stag_params(h);
         CK(h, launch_eqwp_stag_substep(h->fld, h->mat, h->L, i, (int)h->ts, p, h->stream));
         return B2R_OK;
     }
@@ -487,6 +497,7 @@ b2r_status b2r_destroy(b2r_handle* h)
 {
     if (!h) return B2R_OK;
     drop_graphs(h);
+    if (h->adj_ws) cudaFree(h->adj_ws);
     for (int b = 0; b < 2; ++b)
         if (h->buf[b]) cudaFree(h->buf[b]);
     for (int f = 0; f < kMaxFields; ++f)
@@ -892,20 +903,49 @@ b2r_status b2r_eqwp_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const i
     if ((st = rec_offsets(h, nrec, rec_xyz, idx)) != B2R_OK) return st;
     const size_t fb = field_bytes(h);
     const size_t nseg = (size_t)(nsteps + K - 1) / K;
-    // device buffers (freed on every return path)
-    std::vector<DevBuf> ckpt(nseg * 9), replay((size_t)(K + 1) * 9), tmp(18), gb(3);
-    DevBuf d_idx, d_rec, d_res;
-    for (auto& b : ckpt) CK(h, cudaMalloc(&b.p, fb));
-    for (auto& b : replay) CK(h, cudaMalloc(&b.p, fb));
-    for (auto& b : tmp) {
-        CK(h, cudaMalloc(&b.p, fb));
-        CK(h, cudaMemsetAsync(b.p, 0, fb, h->stream));
-    }
+    // workspace, carved from one allocation kept on the handle: checkpoints
+    // (9 fields each), the replayed velocities v^{n0+k} (k = 1..K; k = 0 is
+    // the checkpoint) and stencil sums of a segment, the replay's stresses,
+    // the adjoint fields and the FP64 gradients
     const size_t gbytes = (size_t)h->L.bstride * sizeof(double);
-    for (auto& b : gb) {
-        CK(h, cudaMalloc(&b.p, gbytes));
-        CK(h, cudaMemsetAsync(b.p, 0, gbytes, h->stream));
+    const size_t nf_ckpt = nseg * 9, nf_v = (size_t)(K + 1) * 3, nf_a = (size_t)K * 3;
+    const size_t nfields = nf_ckpt + nf_v + nf_a + 6 + 18;
+    const size_t fba = (fb + 255) & ~(size_t)255, gba = (gbytes + 255) & ~(size_t)255;
+    const size_t need = nfields * fba + 3 * gba;
+    if (h->adj_ws_bytes < need) {
+        if (h->adj_ws) cudaFree(h->adj_ws);
+        h->adj_ws = nullptr;
+        h->adj_ws_bytes = 0;
+        if (cudaMalloc(&h->adj_ws, need) != cudaSuccess) {
+            cudaGetLastError();
+            h->adj_ws = nullptr;
+            return fail(h, B2R_ERR_OOM, "misfit gradient needs %zu bytes of workspace", need);
+        }
+        h->adj_ws_bytes = need;
     }
+    char* ws = static_cast<char*>(h->adj_ws);
+    auto carve = [&](size_t n, std::vector<float*>& out) {
+        out.resize(n);
+        for (size_t i = 0; i < n; ++i, ws += fba) out[i] = reinterpret_cast<float*>(ws);
+    };
+    std::vector<float*> ckpt, vrep, arep, srep, tmp;
+    carve(nf_ckpt, ckpt);
+    carve(nf_v, vrep);
+    carve(nf_a, arep);
+    carve(6, srep);
+    carve(18, tmp);
+    double* gp[3];
+    for (int m = 0; m < 3; ++m, ws += gba) {
+        gp[m] = reinterpret_cast<double*>(ws);
+        CK(h, cudaMemsetAsync(gp[m], 0, gbytes, h->stream));
+    }
+    DevBuf d_idx, d_rec, d_res;
+    // cells outside the update window never change: every replay slot starts
+    // as a copy of the initial state there
+    for (size_t k = 0; k < vrep.size(); ++k)
+        CK(h, cudaMemcpyAsync(vrep[k], h->fld[B2R_F_VX + k % 3], fb, cudaMemcpyDeviceToDevice, h->stream));
+    for (float* b : arep) CK(h, cudaMemsetAsync(b, 0, fb, h->stream));
+    for (float* b : tmp) CK(h, cudaMemsetAsync(b, 0, fb, h->stream));
     CK(h, cudaMalloc(&d_idx.p, sizeof(long long) * nrec));
     CK(h, cudaMalloc(&d_rec.p, sizeof(float) * (size_t)nrec * nsteps));
     CK(h, cudaMalloc(&d_res.p, sizeof(float) * (size_t)nrec * nsteps));
@@ -917,7 +957,7 @@ b2r_status b2r_eqwp_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const i
     for (int n = 0; n < nsteps; ++n) {
         if (n % K == 0)
             for (int f = 0; f < 9; ++f)
-                CK(h, cudaMemcpyAsync(ckpt[(n / K) * 9 + f].p, h->fld[f], fb, cudaMemcpyDeviceToDevice, h->stream));
+                CK(h, cudaMemcpyAsync(ckpt[(n / K) * 9 + f], h->fld[f], fb, cudaMemcpyDeviceToDevice, h->stream));
         if ((st = substep(h, 0)) != B2R_OK) return st;
         h->ts++;
         CK(h, adjoint_sample(h->fld[B2R_F_VY], didx, nrec, (float*)d_rec.p + (size_t)n * nrec, h->stream));
@@ -936,42 +976,37 @@ b2r_status b2r_eqwp_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const i
     if (d_syn) std::copy(syn.begin(), syn.end(), d_syn);
     CK(h, cudaMemcpyAsync(d_res.p, res.data(), sizeof(float) * res.size(), cudaMemcpyHostToDevice, h->stream));
 
-    // reverse sweep, segment by segment, recomputing each segment forward
-    float* tp[18];
-    for (int k = 0; k < 18; ++k) tp[k] = (float*)tmp[k].p;
-    double* gp[3] = {(double*)gb[0].p, (double*)gb[1].p, (double*)gb[2].p};
+    // reverse sweep, segment by segment: replay the segment forward from its
+    // checkpoint (velocities and stencil sums of every step kept), then run
+    // its reverse steps
+    float* const* tp = tmp.data();
     const float* mat[3] = {h->mat[0], h->mat[1], h->mat[2]};
-    int lo[3], hi[3];
-    for (int a = 0; a < 3; ++a) {
-        lo[a] = h->L.H;
-        hi[a] = h->L.n[a] - 1 - h->L.H;
-    }
     const float dt_h = (float)(h->cfg.dt / h->cfg.h);
-    // stress fields of a state in the order xx, xy, xz, yy, yz, zz
-    static const int sidx[6] = {B2R_F_SXX, B2R_F_SXY, B2R_F_SXZ, B2R_F_SYY, B2R_F_SYZ, B2R_F_SZZ};
+    const EqwpStagParams sp = stag_params(h);
+    float* const* sp6 = srep.data();
     for (long long sgi = (long long)nseg - 1; sgi >= 0; --sgi) {
         const int n0 = (int)sgi * K;
         const int n1 = std::min(nsteps, n0 + K);
-        for (int f = 0; f < 9; ++f) {
-            CK(h, cudaMemcpyAsync(h->fld[f], ckpt[sgi * 9 + f].p, fb, cudaMemcpyDeviceToDevice, h->stream));
-            CK(h, cudaMemcpyAsync(replay[f].p, h->fld[f], fb, cudaMemcpyDeviceToDevice, h->stream));
-        }
-        h->ts = n0;
+        // v^{n0+k}: the checkpoint's velocities for k = 0, replay slot k after
+        auto vslot = [&](int k, int f) -> float* {
+            return k == 0 ? ckpt[sgi * 9 + B2R_F_VX + f] : vrep[(size_t)k * 3 + f];
+        };
+        for (int f = 0; f < 6; ++f)
+            CK(h, cudaMemcpyAsync(sp6[f], ckpt[sgi * 9 + B2R_F_SXX + f], fb, cudaMemcpyDeviceToDevice,
+                                  h->stream));
         for (int n = n0; n < n1; ++n) {
-            if ((st = substep(h, 0)) != B2R_OK) return st;
-            h->ts++;
-            const size_t k = (size_t)(n + 1 - n0);
-            for (int f = 0; f < 9; ++f)
-                CK(h, cudaMemcpyAsync(replay[k * 9 + f].p, h->fld[f], fb, cudaMemcpyDeviceToDevice, h->stream));
+            const int k = n - n0;
+            const float* vin[3] = {vslot(k, 0), vslot(k, 1), vslot(k, 2)};
+            float* vout[3] = {vslot(k + 1, 0), vslot(k + 1, 1), vslot(k + 1, 2)};
+            float* const* acc = &arep[(size_t)k * 3];
+            CK(h, launch_eqwp_stag_step_replay(vin, sp6, vout, acc, h->mat, h->L, n, sp, h->stream));
         }
         for (int n = n1 - 1; n >= n0; --n) {
+            const int k = n - n0;
             CK(h, adjoint_inject(tp[1], didx, nrec, (const float*)d_res.p + (size_t)n * nrec, h->stream));
-            const size_t kv = (size_t)(n + 1 - n0), ks = (size_t)(n - n0);
-            const float* fv[3] = {(const float*)replay[kv * 9 + 0].p, (const float*)replay[kv * 9 + 1].p,
-                                  (const float*)replay[kv * 9 + 2].p};
-            const float* fs[6];
-            for (int j = 0; j < 6; ++j) fs[j] = (const float*)replay[ks * 9 + sidx[j]].p;
-            CK(h, adjoint_step(tp, fv, fs, mat, gp, h->L, dt_h, lo, hi, h->stream));
+            const float* vn[3] = {vslot(k, 0), vslot(k, 1), vslot(k, 2)};
+            const float* an[3] = {arep[(size_t)k * 3], arep[(size_t)k * 3 + 1], arep[(size_t)k * 3 + 2]};
+            CK(h, adjoint_step(tp, vn, an, mat, gp, h->L, dt_h, n == 0, h->stream));
         }
     }
     // gradients out (interior cells, x fastest), g_rho = -g_b / rho^2

@@ -7,6 +7,9 @@ namespace b2r {
 struct FieldPtrs {
     float* p[10];   // vx, vy, vz, sxx, sxy, sxz, syy, syz, szz, disp
 };
+struct AccPtrs {
+    float* p[3];    // unscaled velocity-stage stencil sums ax, ay, az
+};
 struct MatPtrs {
     const float* p[3];   // lambda, mu, buoyancy
 };
@@ -32,15 +35,23 @@ cudaError_t launch_eqwp_ref_substep(float* const* fld, const BlockLayout& L, int
                                     const EqwpRefParams& p, cudaStream_t st);
 cudaError_t launch_eqwp_stag_substep(float* const* fld, float* const* mat, const BlockLayout& L,
                                      int step_i, int ts, const EqwpStagParams& p, cudaStream_t st);
+// One staggered time step for the adjoint's forward replay: velocities read
+// from v_in and written to v_out (with the stencil sums into acc), stresses s
+// (order sxx, sxy, sxz, syy, syz, szz) updated in place.  One block, R = 1.
+cudaError_t launch_eqwp_stag_step_replay(const float* const* v_in, float* const* s, float* const* v_out,
+                                         float* const* acc, float* const* mat, const BlockLayout& L,
+                                         int ts, const EqwpStagParams& p, cudaStream_t st);
 
 // adjoint.cu: receiver sampling / injection and one reverse step of the
 // staggered scheme (tmp = vb[3], sb[6], q[6], w[3]; stress order xx, xy, xz,
-// yy, yz, zz), gradients in FP64.
+// yy, yz, zz; v_n = forward v^n, acc_n = forward stencil sums of step n;
+// last = step 0, whose stress-side half has no earlier step to feed),
+// gradients in FP64.
 cudaError_t adjoint_sample(const float* vy, const long long* d_idx, int nrec, float* out, cudaStream_t st);
 cudaError_t adjoint_inject(float* vby, const long long* d_idx, int nrec, const float* res, cudaStream_t st);
-cudaError_t adjoint_step(float* const* tmp, const float* const* fwd_v, const float* const* fwd_s,
+cudaError_t adjoint_step(float* const* tmp, const float* const* v_n, const float* const* acc_n,
                          const float* const* mat, double* const* g, const BlockLayout& L, float dt_h,
-                         const int lo[3], const int hi[3], cudaStream_t st);
+                         bool last, cudaStream_t st);
 cudaError_t adjoint_grad_out(const double* g, const float* buoy, int rho, const BlockLayout& L,
                              double* out, cudaStream_t st);
 

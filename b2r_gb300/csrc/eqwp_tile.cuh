@@ -1,0 +1,282 @@
+// eqwp_tile.cuh -- tile machinery shared by the elastic-wave stage kernels
+// (eqwp.cu) and their adjoints (adjoint.cu): thread = 4 consecutive x cells
+// (one float4) of one row, CTA = 32 x 8 threads = a 128 x 8 tile marching z
+// over a chunk; x neighbours as float4 row segments through L1, z
+// neighbours in 5-plane float4 register queues; the staggered and collocated
+// 4th-order first differences of the 4 cells.
+#pragma once
+#include "b2r_common.cuh"
+
+namespace b2r {
+namespace eqk {
+
+// Thread = 4 consecutive x cells (one float4) of one row; CTA = 32 x 8
+// threads = a 128 x 8 tile; z marched over a chunk.
+constexpr int kBX = 32, kBY = 8, kTXc = 4 * kBX;
+#ifndef B2R_EQWP_MINB
+#define B2R_EQWP_MINB 2   // resident CTAs per SM the register budget is fitted to
+#endif
+
+enum { VX, VY, VZ, SXX, SXY, SXZ, SYY, SYZ, SZZ, DISP };
+
+__device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+__device__ __forceinline__ float4 ldw4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ float cmp(const float4& v, int j)
+{
+    return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
+}
+
+// 12 cells x-4 .. x+7 of a row around the thread's 4 cells
+struct Row12 {
+    float v[12];
+    __device__ __forceinline__ void load(const float* p)
+    {
+        const float4 a = ld4(p - 4), b = ld4(p), c = ld4(p + 4);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+        v[8] = c.x; v[9] = c.y; v[10] = c.z; v[11] = c.w;
+    }
+};
+
+// five planes z-2 .. z+2 of the thread's 4 cells
+struct Q5v {
+    float4 m2, m1, c, p1, p2;
+    __device__ __forceinline__ void shift(float4 nv)
+    {
+        m2 = m1; m1 = c; c = p1; p1 = p2; p2 = nv;
+    }
+};
+
+struct Win {
+    int lo[3], hi[3];
+    int zs, ze;
+    bool ok;
+};
+
+__device__ __forceinline__ Win window(const BlockLayout& L, int blk, int zc, int nzc, int shrink)
+{
+    Win w;
+    const int edge = edge_bits(L, blk);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) stage_region(L, edge, a, shrink, w.lo[a], w.hi[a]);
+    const int nz_out = w.hi[2] - w.lo[2] + 1;
+    const int per = (nz_out + nzc - 1) / nzc;
+    w.zs = w.lo[2] + zc * per;
+    w.ze = min(w.hi[2], w.zs + per - 1);
+    w.ok = nz_out > 0 && w.zs <= w.ze;
+    return w;
+}
+
+// Common prologue: this thread's cells, their x mask, the row base pointer offset.
+struct Cell {
+    int blk, y, xb;             // block, row, block x of the first of the 4 cells
+    bool vx[4], any, all;
+    long long base;             // element offset of (xb, y, 0) in the field buffers
+};
+
+__device__ __forceinline__ bool cell_setup(const BlockLayout& L, const Win& w, int blk, Cell& c)
+{
+    const int xs0 = ((L.xoff + 2) & ~3) + blockIdx.x * kTXc + 4 * threadIdx.x;
+    c.blk = blk;
+    c.xb = xs0 - L.xoff;
+    c.y = 2 + blockIdx.y * kBY + threadIdx.y;
+    if (!w.ok || c.y < w.lo[1] || c.y > w.hi[1]) return false;
+    c.any = false;
+    c.all = true;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        c.vx[j] = c.xb + j >= w.lo[0] && c.xb + j <= w.hi[0];
+        c.any |= c.vx[j];
+        c.all &= c.vx[j];
+    }
+    c.base = (long long)blk * L.bstride + (long long)c.y * L.P + xs0;
+    return c.any;
+}
+
+// Read-modify-write of the thread's 4 cells, split so that every load of an
+// iteration is issued before any store (the field pointers may alias as far
+// as the compiler knows, so a fused load-add-store per field would serialise
+// one DRAM round trip per field).
+__device__ __forceinline__ float4 rd4(const float* f, const Cell& c)
+{
+    if (c.all) return ldw4(f);
+    float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (c.vx[0]) o.x = f[0];
+    if (c.vx[1]) o.y = f[1];
+    if (c.vx[2]) o.z = f[2];
+    if (c.vx[3]) o.w = f[3];
+    return o;
+}
+// The add is an explicit round-to-nearest add, so that no kernel variant
+// contracts it with the product that formed d: every variant storing the
+// same update stores the same bits.  Returns the stored values.
+__device__ __forceinline__ float4 wr4(float* f, const Cell& c, float4 o, const float (&d)[4])
+{
+    o.x = __fadd_rn(o.x, d[0]);
+    o.y = __fadd_rn(o.y, d[1]);
+    o.z = __fadd_rn(o.z, d[2]);
+    o.w = __fadd_rn(o.w, d[3]);
+    if (c.all) {
+        *reinterpret_cast<float4*>(f) = o;
+    } else {
+        if (c.vx[0]) f[0] = o.x;
+        if (c.vx[1]) f[1] = o.y;
+        if (c.vx[2]) f[2] = o.z;
+        if (c.vx[3]) f[3] = o.w;
+    }
+    return o;
+}
+
+// d/dx of the 4 cells from a 12-cell row, d/dy from rows +-1, +-2, d/dz from a queue
+__device__ __forceinline__ float dcx(const Row12& r, int j, float a, float b)
+{
+    return a * (r.v[6 + j] - r.v[2 + j]) + b * (r.v[5 + j] - r.v[3 + j]);
+}
+__device__ __forceinline__ float dc4(const float4& m2, const float4& m1, const float4& p1,
+                                     const float4& p2, int j, float a, float b)
+{
+    return a * (cmp(p2, j) - cmp(m2, j)) + b * (cmp(p1, j) - cmp(m1, j));
+}
+
+// forward difference at i+1/2 and backward at i-1/2, 4th order (9/8, -1/24)
+__device__ __forceinline__ float dpx(const Row12& r, int j)
+{
+    return 1.125f * (r.v[5 + j] - r.v[4 + j]) - (1.f / 24.f) * (r.v[6 + j] - r.v[3 + j]);
+}
+__device__ __forceinline__ float dmx(const Row12& r, int j)
+{
+    return 1.125f * (r.v[4 + j] - r.v[3 + j]) - (1.f / 24.f) * (r.v[5 + j] - r.v[2 + j]);
+}
+// rows/planes -2..+2 around the cell: Dp uses -1..+2, Dm uses -2..+1
+__device__ __forceinline__ float dp4(const float4& m1, const float4& c, const float4& p1,
+                                     const float4& p2, int j)
+{
+    return 1.125f * (cmp(p1, j) - cmp(c, j)) - (1.f / 24.f) * (cmp(p2, j) - cmp(m1, j));
+}
+__device__ __forceinline__ float dm4(const float4& m2, const float4& m1, const float4& c,
+                                     const float4& p1, int j)
+{
+    return 1.125f * (cmp(c, j) - cmp(m1, j)) - (1.f / 24.f) * (cmp(p1, j) - cmp(m2, j));
+}
+
+// Velocity-stage operator of the staggered scheme on six stress-like fields
+// (xx, xy, xz, yy, yz, zz, each already offset to the thread's row):
+//   ax = Dp_x xx + Dm_y xy + Dm_z xz
+//   ay = Dm_x xy + Dp_y yy + Dm_z yz
+//   az = Dm_x xz + Dm_y yz + Dp_z zz
+// z neighbours come from register queues advanced one plane per eval().
+struct VelOp {
+    const float *xx, *xy, *xz, *yy, *yz, *zz;
+    Q5v qxz, qyz, qzz;
+    __device__ __forceinline__ void begin(int zs, long long S)
+    {
+        const long long o = (long long)(zs - 2) * S;
+        qxz.m1 = ld4(xz + o); qyz.m1 = ld4(yz + o); qzz.m1 = ld4(zz + o);
+        qxz.c = ld4(xz + o + S); qyz.c = ld4(yz + o + S); qzz.c = ld4(zz + o + S);
+        qxz.p1 = ld4(xz + o + 2 * S); qyz.p1 = ld4(yz + o + 2 * S); qzz.p1 = ld4(zz + o + 2 * S);
+        qxz.p2 = ld4(xz + o + 3 * S); qyz.p2 = ld4(yz + o + 3 * S); qzz.p2 = ld4(zz + o + 3 * S);
+    }
+    // o: element offset of plane z; planes must be visited in increasing z
+    __device__ __forceinline__ void eval(long long o, long long P, long long S, float (&ax)[4],
+                                         float (&ay)[4], float (&az)[4])
+    {
+        qxz.shift(ld4(xz + o + 2 * S));
+        qyz.shift(ld4(yz + o + 2 * S));
+        qzz.shift(ld4(zz + o + 2 * S));
+        Row12 rxx, rxy, rxz;
+        rxx.load(xx + o);
+        rxy.load(xy + o);
+        rxz.load(xz + o);
+        const float4 xym2 = ld4(xy + o - 2 * P), xym1 = ld4(xy + o - P), xyp1 = ld4(xy + o + P);
+        const float4 yym1 = ld4(yy + o - P), yyc = ld4(yy + o), yyp1 = ld4(yy + o + P), yyp2 = ld4(yy + o + 2 * P);
+        const float4 yzm2 = ld4(yz + o - 2 * P), yzm1 = ld4(yz + o - P), yzp1 = ld4(yz + o + P);
+        const float4 xyc = make_float4(rxy.v[4], rxy.v[5], rxy.v[6], rxy.v[7]);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            ax[j] = dpx(rxx, j) + dm4(xym2, xym1, xyc, xyp1, j) + dm4(qxz.m2, qxz.m1, qxz.c, qxz.p1, j);
+            ay[j] = dmx(rxy, j) + dp4(yym1, yyc, yyp1, yyp2, j) + dm4(qyz.m2, qyz.m1, qyz.c, qyz.p1, j);
+            az[j] = dmx(rxz, j) + dm4(yzm2, yzm1, qyz.c, yzp1, j) + dp4(qzz.m1, qzz.c, qzz.p1, qzz.p2, j);
+        }
+    }
+};
+
+// Stress-stage (strain) operator of the staggered scheme on three
+// velocity-like fields x, y, z:
+//   e[0] = Dm_x x, e[1] = Dm_y y, e[2] = Dm_z z,
+//   e[3] = Dp_y x + Dp_x y, e[4] = Dp_z x + Dp_x z, e[5] = Dp_z y + Dp_y z
+struct StrOp {
+    const float *x, *y, *z;
+    Q5v qx, qy, qz;
+    __device__ __forceinline__ void begin(int zs, long long S)
+    {
+        const long long o = (long long)(zs - 2) * S;
+        qx.m1 = ld4(x + o); qy.m1 = ld4(y + o); qz.m1 = ld4(z + o);
+        qx.c = ld4(x + o + S); qy.c = ld4(y + o + S); qz.c = ld4(z + o + S);
+        qx.p1 = ld4(x + o + 2 * S); qy.p1 = ld4(y + o + 2 * S); qz.p1 = ld4(z + o + 2 * S);
+        qx.p2 = ld4(x + o + 3 * S); qy.p2 = ld4(y + o + 3 * S); qz.p2 = ld4(z + o + 3 * S);
+    }
+    __device__ __forceinline__ void eval(long long o, long long P, long long S, float (&e)[6][4])
+    {
+        qx.shift(ld4(x + o + 2 * S));
+        qy.shift(ld4(y + o + 2 * S));
+        qz.shift(ld4(z + o + 2 * S));
+        Row12 rx, ry, rz;
+        rx.load(x + o);
+        ry.load(y + o);
+        rz.load(z + o);
+        const float4 xc = make_float4(rx.v[4], rx.v[5], rx.v[6], rx.v[7]);
+        const float4 yc = make_float4(ry.v[4], ry.v[5], ry.v[6], ry.v[7]);
+        const float4 zc = make_float4(rz.v[4], rz.v[5], rz.v[6], rz.v[7]);
+        const float4 xm1 = ld4(x + o - P), xp1 = ld4(x + o + P), xp2 = ld4(x + o + 2 * P);
+        const float4 ym2 = ld4(y + o - 2 * P), ym1 = ld4(y + o - P), yp1 = ld4(y + o + P);
+        const float4 zm1 = ld4(z + o - P), zp1 = ld4(z + o + P), zp2 = ld4(z + o + 2 * P);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            e[0][j] = dmx(rx, j);
+            e[1][j] = dm4(ym2, ym1, yc, yp1, j);
+            e[2][j] = dm4(qz.m2, qz.m1, qz.c, qz.p1, j);
+            e[3][j] = dp4(xm1, xc, xp1, xp2, j) + dpx(ry, j);
+            e[4][j] = dp4(qx.m1, qx.c, qx.p1, qx.p2, j) + dpx(rz, j);
+            e[5][j] = dp4(qy.m1, qy.c, qy.p1, qy.p2, j) + dp4(zm1, zc, zp1, zp2, j);
+        }
+    }
+};
+
+// masked store of 4 values (the lanes of the window)
+__device__ __forceinline__ void st4(float* f, const Cell& c, const float (&v)[4])
+{
+    if (c.all) {
+        *reinterpret_cast<float4*>(f) = make_float4(v[0], v[1], v[2], v[3]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (c.vx[j]) f[j] = v[j];
+    }
+}
+
+struct Grid {
+    dim3 g;
+    int nzc;
+};
+
+inline Grid stage_grid(const BlockLayout& L)
+{
+    Grid r;
+    const int xs_begin = (L.xoff + 2) & ~3;
+    const int xs_end = L.xoff + L.n[0] - 2;               // exclusive
+    const int tx = (xs_end - xs_begin + kTXc - 1) / kTXc;
+    const int ty = (L.n[1] - 4 + kBY - 1) / kBY;
+    const long long tiles = (long long)tx * ty * L.nblk;
+    const long long want = 152LL * 8 * 3;
+    int nzc = (int)((want + tiles - 1) / tiles);
+    int maxc = (L.n[2] - 4) / 16;
+    if (maxc < 1) maxc = 1;
+    if (nzc > maxc) nzc = maxc;
+    if (nzc < 1) nzc = 1;
+    r.nzc = nzc;
+    r.g = dim3(tx, ty, L.nblk * nzc);
+    return r;
+}
+
+}  // namespace eqk
+}  // namespace b2r

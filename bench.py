@@ -451,6 +451,13 @@ def run_adjoint(args, wl):
         t0 = time.perf_counter()
         d.eqwp_record(n, rec)
         fwd_ms.append((time.perf_counter() - t0) * 1e3)
+    # one untimed gradient: allocates the workspace the timed calls reuse
+    for f in range(9):
+        d.upload(zero, field=f)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d.eqwp_misfit_gradient(n, rec, d_obs, ckpt_every=wl["ckpt"])
+    first_ms = (time.perf_counter() - t0) * 1e3
     clocks = ClockSampler(0)
     clocks.start()
     l0 = b2r.kernel_launches()
@@ -482,6 +489,7 @@ def run_adjoint(args, wl):
             "config": {"workload": args.workload, "env": list(env), "time_steps": n,
                        "receivers": len(rec), "checkpoint_every": wl["ckpt"],
                        "forward_ms": round(fms, 1), "gradient_ms": round(gms, 1),
+                       "first_gradient_ms": round(first_ms, 1),
                        "gradient_over_forward": round(gms / fms, 3), "misfit": J,
                        "l2": "inputs larger than L2"},
             "e2e": None, "gpu_launches": int(launches),
