@@ -88,12 +88,13 @@ struct AdjS {
 // operator is minus the velocity-stage operator), then w = b * vb and
 // g_b += k * (D s^n) . vb on the window.
 __global__ void __launch_bounds__(kBX * kBY, B2R_EQWP_MINB)
-adj_velocity_kernel(AdjV A, const BlockLayout L, int nzc)
+adj_velocity_kernel(AdjV A, const BlockLayout L, Tiles T)
 {
+    const int nzc = T.nzc;
     const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
     const Win w = window(L, blk, zc, nzc, 2);
     Cell c;
-    if (!cell_setup(L, w, blk, c)) return;
+    if (!cell_setup(L, w, blk, c, T.x0, T.y0)) return;
     const long long P = L.P, S = L.plane;
     VelOp op;
     op.xx = A.q[0] + c.base;
@@ -143,12 +144,13 @@ adj_velocity_kernel(AdjV A, const BlockLayout L, int nzc)
 // of step n-1:  sb -= k * E w  (D^T = -E), then q = C(lambda, mu) * sb on
 // the window.
 __global__ void __launch_bounds__(kBX * kBY, B2R_EQWP_MINB)
-adj_stress_kernel(AdjS A, const BlockLayout L, int nzc)
+adj_stress_kernel(AdjS A, const BlockLayout L, Tiles T)
 {
+    const int nzc = T.nzc;
     const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
     const Win w = window(L, blk, zc, nzc, 4);
     Cell c;
-    if (!cell_setup(L, w, blk, c)) return;
+    if (!cell_setup(L, w, blk, c, T.x0, T.y0)) return;
     const long long P = L.P, S = L.plane;
     StrOp ow;
     ow.x = A.w[0] + c.base;
@@ -191,12 +193,13 @@ adj_stress_kernel(AdjS A, const BlockLayout L, int nzc)
 // lambda / mu gradients of the stress stage of step n-1 on the window:
 // g_lambda += k * tr(E v^n) tr(sb),  g_mu += k * (2 e_ii sb_ii + gamma_ij sb_ij)
 __global__ void __launch_bounds__(kBX * kBY, B2R_EQWP_MINB)
-adj_grad_lm_kernel(AdjS A, const BlockLayout L, int nzc)
+adj_grad_lm_kernel(AdjS A, const BlockLayout L, Tiles T)
 {
+    const int nzc = T.nzc;
     const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
     const Win w = window(L, blk, zc, nzc, 4);
     Cell c;
-    if (!cell_setup(L, w, blk, c)) return;
+    if (!cell_setup(L, w, blk, c, T.x0, T.y0)) return;
     const long long P = L.P, S = L.plane;
     StrOp ov;
     ov.x = A.v[0] + c.base;
@@ -337,12 +340,12 @@ cudaError_t adjoint_step(float* const* tmp, const float* const* v_n, const float
     T.g_lam = g[0];
     T.g_mu = g[1];
     T.k = dt_h;
-    const Grid gr = stage_grid(L);
-    adj_velocity_kernel<<<gr.g, dim3(kBX, kBY), 0, st>>>(V, L, gr.nzc);
+    const Grid ga = stage_grid(L, 2), gb = stage_grid(L, 4);
+    adj_velocity_kernel<<<ga.g, dim3(kBX, kBY), 0, st>>>(V, L, ga.t);
     count_launches(1);
     if (!last) {
-        adj_stress_kernel<<<gr.g, dim3(kBX, kBY), 0, st>>>(T, L, gr.nzc);
-        adj_grad_lm_kernel<<<gr.g, dim3(kBX, kBY), 0, st>>>(T, L, gr.nzc);
+        adj_stress_kernel<<<gb.g, dim3(kBX, kBY), 0, st>>>(T, L, gb.t);
+        adj_grad_lm_kernel<<<gb.g, dim3(kBX, kBY), 0, st>>>(T, L, gb.t);
         count_launches(2);
     }
     return cudaGetLastError();

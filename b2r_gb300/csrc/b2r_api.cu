@@ -208,16 +208,20 @@ b2r_status exchange_all(b2r_handle* h, bool staged)
         }
         bounce = h->bounce;
     }
+    // unstaged: one launch copying every halo cell from its owner block
+    const bool gather = !staged && (long long)nf * L.nblk <= 65535;
     if (h->cell_bytes == 1) {
         FieldSet<uint8_t> fs{};
         fs.p[0] = static_cast<uint8_t*>(h->buf[h->cur]);
-        CK(h, launch_halo_exchange<uint8_t>(fs, 1, L, static_cast<uint8_t*>(bounce), h->stream));
+        if (gather) CK(h, launch_halo_gather<uint8_t>(fs, 1, L, h->stream));
+        else CK(h, launch_halo_exchange<uint8_t>(fs, 1, L, static_cast<uint8_t*>(bounce), h->stream));
     } else {
         FieldSet<float> fs{};
         if (nf == 1) fs.p[0] = static_cast<float*>(h->buf[h->cur]);
         else
             for (int f = 0; f < nf; ++f) fs.p[f] = h->fld[f];
-        CK(h, launch_halo_exchange<float>(fs, nf, L, static_cast<float*>(bounce), h->stream));
+        if (gather) CK(h, launch_halo_gather<float>(fs, nf, L, h->stream));
+        else CK(h, launch_halo_exchange<float>(fs, nf, L, static_cast<float*>(bounce), h->stream));
     }
     return B2R_OK;
 }

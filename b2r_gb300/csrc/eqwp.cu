@@ -30,12 +30,13 @@ using namespace eqk;
 
 // ------------------------------------------------------------ REF (collocated FD4)
 __global__ void __launch_bounds__(kBX * kBY, B2R_EQWP_MINB)
-eqwp_ref_stress(FieldPtrs F, const BlockLayout L, int step_i, int nzc, EqwpRefParams p)
+eqwp_ref_stress(FieldPtrs F, const BlockLayout L, int step_i, Tiles T, EqwpRefParams p)
 {
+    const int nzc = T.nzc;
     const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
     const Win w = window(L, blk, zc, nzc, 4 * step_i + 2);
     Cell c;
-    if (!cell_setup(L, w, blk, c)) return;
+    if (!cell_setup(L, w, blk, c, T.x0, T.y0)) return;
     const long long P = L.P, S = L.plane;
     const float* vx = F.p[VX] + c.base;
     const float* vy = F.p[VY] + c.base;
@@ -96,12 +97,13 @@ eqwp_ref_stress(FieldPtrs F, const BlockLayout L, int step_i, int nzc, EqwpRefPa
 }
 
 __global__ void __launch_bounds__(kBX * kBY, B2R_EQWP_MINB)
-eqwp_ref_velocity(FieldPtrs F, const BlockLayout L, int step_i, int nzc, EqwpRefParams p, int ts)
+eqwp_ref_velocity(FieldPtrs F, const BlockLayout L, int step_i, Tiles T, EqwpRefParams p, int ts)
 {
+    const int nzc = T.nzc;
     const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
     const Win w = window(L, blk, zc, nzc, 4 * step_i + 4);
     Cell c;
-    if (!cell_setup(L, w, blk, c)) return;
+    if (!cell_setup(L, w, blk, c, T.x0, T.y0)) return;
     const long long P = L.P, S = L.plane;
     const float* sxx = F.p[SXX] + c.base;
     const float* sxy = F.p[SXY] + c.base;
@@ -167,13 +169,14 @@ eqwp_ref_velocity(FieldPtrs F, const BlockLayout L, int step_i, int nzc, EqwpRef
 // uses for the buoyancy gradient.
 template <bool ACC>
 __global__ void __launch_bounds__(kBX * kBY, B2R_EQWP_MINB)
-eqwp_stag_velocity(FieldPtrs F, FieldPtrs O, MatPtrs M, const BlockLayout L, int step_i, int nzc,
+eqwp_stag_velocity(FieldPtrs F, FieldPtrs O, MatPtrs M, const BlockLayout L, int step_i, Tiles T,
                    EqwpStagParams p, AccPtrs A)
 {
+    const int nzc = T.nzc;
     const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
     const Win w = window(L, blk, zc, nzc, 4 * step_i + 2);
     Cell c;
-    if (!cell_setup(L, w, blk, c)) return;
+    if (!cell_setup(L, w, blk, c, T.x0, T.y0)) return;
     const long long P = L.P, S = L.plane;
     VelOp op;
     op.xx = F.p[SXX] + c.base;
@@ -213,13 +216,14 @@ eqwp_stag_velocity(FieldPtrs F, FieldPtrs O, MatPtrs M, const BlockLayout L, int
 }
 
 __global__ void __launch_bounds__(kBX * kBY, B2R_EQWP_MINB)
-eqwp_stag_stress(FieldPtrs F, FieldPtrs O, MatPtrs M, const BlockLayout L, int step_i, int nzc,
+eqwp_stag_stress(FieldPtrs F, FieldPtrs O, MatPtrs M, const BlockLayout L, int step_i, Tiles T,
                  EqwpStagParams p, float src_amp)
 {
+    const int nzc = T.nzc;
     const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
     const Win w = window(L, blk, zc, nzc, 4 * step_i + 4);
     Cell c;
-    if (!cell_setup(L, w, blk, c)) return;
+    if (!cell_setup(L, w, blk, c, T.x0, T.y0)) return;
     const long long P = L.P, S = L.plane;
     StrOp op;
     op.x = F.p[VX] + c.base;
@@ -306,9 +310,9 @@ cudaError_t launch_eqwp_ref_substep(float* const* fld, const BlockLayout& L, int
 {
     FieldPtrs F{};
     for (int f = 0; f < 10; ++f) F.p[f] = fld[f];
-    const Grid g = stage_grid(L);
-    eqwp_ref_stress<<<g.g, dim3(kBX, kBY), 0, st>>>(F, L, step_i, g.nzc, p);
-    eqwp_ref_velocity<<<g.g, dim3(kBX, kBY), 0, st>>>(F, L, step_i, g.nzc, p, ts);
+    const Grid ga = stage_grid(L, 4 * step_i + 2), gb = stage_grid(L, 4 * step_i + 4);
+    eqwp_ref_stress<<<ga.g, dim3(kBX, kBY), 0, st>>>(F, L, step_i, ga.t, p);
+    eqwp_ref_velocity<<<gb.g, dim3(kBX, kBY), 0, st>>>(F, L, step_i, gb.t, p, ts);
     count_launches(2);
     return cudaGetLastError();
 }
@@ -320,11 +324,11 @@ cudaError_t launch_eqwp_stag_substep(float* const* fld, float* const* mat, const
     for (int f = 0; f < 9; ++f) F.p[f] = fld[f];
     MatPtrs M{};
     for (int m = 0; m < 3; ++m) M.p[m] = mat[m];
-    const Grid g = stage_grid(L);
+    const Grid ga = stage_grid(L, 4 * step_i + 2), gb = stage_grid(L, 4 * step_i + 4);
     float amp = 0.f;
     if (p.src_host && ts >= 0 && ts < p.src_len) amp = p.src_host[ts];
-    eqwp_stag_velocity<false><<<g.g, dim3(kBX, kBY), 0, st>>>(F, F, M, L, step_i, g.nzc, p, AccPtrs{});
-    eqwp_stag_stress<<<g.g, dim3(kBX, kBY), 0, st>>>(F, F, M, L, step_i, g.nzc, p, amp);
+    eqwp_stag_velocity<false><<<ga.g, dim3(kBX, kBY), 0, st>>>(F, F, M, L, step_i, ga.t, p, AccPtrs{});
+    eqwp_stag_stress<<<gb.g, dim3(kBX, kBY), 0, st>>>(F, F, M, L, step_i, gb.t, p, amp);
     count_launches(2);
     return cudaGetLastError();
 }
@@ -343,12 +347,12 @@ cudaError_t launch_eqwp_stag_step_replay(const float* const* v_in, float* const*
     for (int m = 0; m < 3; ++m) M.p[m] = mat[m];
     AccPtrs A{};
     for (int a = 0; a < 3; ++a) A.p[a] = acc[a];
-    const Grid g = stage_grid(L);
+    const Grid ga = stage_grid(L, 2), gb = stage_grid(L, 4);
     float amp = 0.f;
     if (p.src_host && ts >= 0 && ts < p.src_len) amp = p.src_host[ts];
-    eqwp_stag_velocity<true><<<g.g, dim3(kBX, kBY), 0, st>>>(F, O, M, L, 0, g.nzc, p, A);
+    eqwp_stag_velocity<true><<<ga.g, dim3(kBX, kBY), 0, st>>>(F, O, M, L, 0, ga.t, p, A);
     // the stress stage reads the new velocities and updates the stresses in place
-    eqwp_stag_stress<<<g.g, dim3(kBX, kBY), 0, st>>>(O, O, M, L, 0, g.nzc, p, amp);
+    eqwp_stag_stress<<<gb.g, dim3(kBX, kBY), 0, st>>>(O, O, M, L, 0, gb.t, p, amp);
     count_launches(2);
     return cudaGetLastError();
 }

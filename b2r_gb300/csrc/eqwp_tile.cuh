@@ -5,6 +5,8 @@
 // neighbours in 5-plane float4 register queues; the staggered and collocated
 // 4th-order first differences of the 4 cells.
 #pragma once
+#include <algorithm>
+
 #include "b2r_common.cuh"
 
 namespace b2r {
@@ -74,12 +76,12 @@ struct Cell {
     long long base;             // element offset of (xb, y, 0) in the field buffers
 };
 
-__device__ __forceinline__ bool cell_setup(const BlockLayout& L, const Win& w, int blk, Cell& c)
+__device__ __forceinline__ bool cell_setup(const BlockLayout& L, const Win& w, int blk, Cell& c, int x0, int y0)
 {
-    const int xs0 = ((L.xoff + 2) & ~3) + blockIdx.x * kTXc + 4 * threadIdx.x;
+    const int xs0 = x0 + blockIdx.x * kTXc + 4 * threadIdx.x;
     c.blk = blk;
     c.xb = xs0 - L.xoff;
-    c.y = 2 + blockIdx.y * kBY + threadIdx.y;
+    c.y = y0 + blockIdx.y * kBY + threadIdx.y;
     if (!w.ok || c.y < w.lo[1] || c.y > w.hi[1]) return false;
     c.any = false;
     c.all = true;
@@ -254,26 +256,45 @@ __device__ __forceinline__ void st4(float* f, const Cell& c, const float (&v)[4]
     }
 }
 
-struct Grid {
-    dim3 g;
-    int nzc;
+// Tile origin of a stage launch: the first tile starts at the lowest window
+// cell of any block (x rounded down to a float4 boundary), so that no tile
+// column or row lies wholly outside every window.
+struct Tiles {
+    int nzc;    // z chunks per block
+    int x0;     // storage x of the first tile column (multiple of 4)
+    int y0;     // first row
 };
 
-inline Grid stage_grid(const BlockLayout& L)
+struct Grid {
+    dim3 g;
+    Tiles t;
+};
+
+inline Grid stage_grid(const BlockLayout& L, int shrink)
 {
+    int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-1, -1, -1};
+    for (int b = 0; b < L.nblk; ++b) {
+        const int e = edge_bits(L, b);
+        for (int a = 0; a < 3; ++a) {
+            int l, h;
+            stage_region(L, e, a, shrink, l, h);
+            lo[a] = std::min(lo[a], l);
+            hi[a] = std::max(hi[a], h);
+        }
+    }
     Grid r;
-    const int xs_begin = (L.xoff + 2) & ~3;
-    const int xs_end = L.xoff + L.n[0] - 2;               // exclusive
-    const int tx = (xs_end - xs_begin + kTXc - 1) / kTXc;
-    const int ty = (L.n[1] - 4 + kBY - 1) / kBY;
+    r.t.x0 = (L.xoff + lo[0]) & ~3;
+    r.t.y0 = lo[1];
+    const int tx = std::max(1, (L.xoff + hi[0] + 1 - r.t.x0 + kTXc - 1) / kTXc);
+    const int ty = std::max(1, (hi[1] + 1 - lo[1] + kBY - 1) / kBY);
     const long long tiles = (long long)tx * ty * L.nblk;
     const long long want = 152LL * 8 * 3;
     int nzc = (int)((want + tiles - 1) / tiles);
-    int maxc = (L.n[2] - 4) / 16;
+    int maxc = (hi[2] - lo[2] + 1) / 16;
     if (maxc < 1) maxc = 1;
     if (nzc > maxc) nzc = maxc;
     if (nzc < 1) nzc = 1;
-    r.nzc = nzc;
+    r.t.nzc = nzc;
     r.g = dim3(tx, ty, L.nblk * nzc);
     return r;
 }

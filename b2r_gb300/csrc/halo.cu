@@ -13,6 +13,9 @@
 // Slab extents per axis follow the reference: x slabs span interior y,z; y
 // slabs full padded x and interior z; z slabs full padded x and y.  One
 // launch covers all blocks, both sides and up to kMaxFields fields.
+#include <algorithm>
+#include <type_traits>
+
 #include "b2r_common.cuh"
 #include "halo.h"
 
@@ -178,6 +181,63 @@ __global__ void gather_kernel(T* __restrict__ dom, const T* __restrict__ blocks,
     }
 }
 
+// ---------------------------------------------------------------- one-launch exchange
+// On one GPU every block can read every other block, so each halo cell can
+// be copied straight from the block that owns it: the halo shell of a block
+// splits into 26 regions (faces, edges, corners), region (dx, dy, dz) being
+// the interior slab of neighbour (bx+dx, by+dy, bz+dz) that borders it.  The
+// X -> Y -> Z sequence of the reference delivers exactly these values
+// (edges and corners arrive in two or three hops from the same owners), so
+// one launch replaces three, with no ordering between the regions.  Halo
+// cells without an owner (domain boundary, not periodic) keep their values.
+struct HaloDirs {
+    int n;                  // regions with a possible owner
+    int cta0[27];           // first CTA of region k (cta0[n] = total CTAs)
+    int d[26][3];           // direction
+    int ex[26], ey[26], ez[26];   // extent: x in vectors, y, z in cells
+    int dst[26][3], src[26][3];   // origins (cells) in the block and in the owner
+    int vb;                 // vector bytes
+};
+
+template <int VB>
+__global__ void __launch_bounds__(256)
+halo_gather_kernel(FieldSet<uint8_t> fs, const BlockLayout L, int cb, const HaloDirs hd)
+{
+    typedef typename std::conditional<VB == 16, uint4,
+            typename std::conditional<VB == 8, uint2,
+            typename std::conditional<VB == 4, uint32_t,
+            typename std::conditional<VB == 2, uint16_t, uint8_t>::type>::type>::type>::type V;
+    const int blk = blockIdx.y % L.nblk;
+    uint8_t* base = fs.p[blockIdx.y / L.nblk];
+    int k = 0;
+    while (k + 1 < hd.n && (int)blockIdx.x >= hd.cta0[k + 1]) ++k;
+    const int b[3] = {blk % L.nb[0], (blk / L.nb[0]) % L.nb[1], blk / (L.nb[0] * L.nb[1])};
+    int o[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        o[a] = b[a] + hd.d[k][a];
+        if (o[a] < 0 || o[a] >= L.nb[a]) {
+            if (!L.periodic) return;
+            o[a] = (o[a] + L.nb[a]) % L.nb[a];
+        }
+    }
+    const int oblk = o[0] + L.nb[0] * (o[1] + L.nb[1] * o[2]);
+    const long long rowb = (long long)L.P * cb, planeb = (long long)L.plane * cb;
+    uint8_t* dst = base + ((long long)blk * L.bstride + L.xoff + hd.dst[k][0]) * cb +
+                   hd.dst[k][1] * rowb + hd.dst[k][2] * planeb;
+    const uint8_t* src = base + ((long long)oblk * L.bstride + L.xoff + hd.src[k][0]) * cb +
+                         hd.src[k][1] * rowb + hd.src[k][2] * planeb;
+    const unsigned ex = hd.ex[k], ey = hd.ey[k];
+    const unsigned total = ex * ey * (unsigned)hd.ez[k];
+    const unsigned nct = hd.cta0[k + 1] - hd.cta0[k];
+    for (unsigned e = (blockIdx.x - hd.cta0[k]) * blockDim.x + threadIdx.x; e < total; e += nct * blockDim.x) {
+        const unsigned vx = e % ex, r = e / ex;
+        const unsigned y = r % ey, z = r / ey;
+        const long long off = (long long)vx * VB + y * rowb + z * planeb;
+        *reinterpret_cast<V*>(dst + off) = *reinterpret_cast<const V*>(src + off);
+    }
+}
+
 inline int grid_for(long long work, int threads)
 {
     long long g = (work + threads - 1) / threads;
@@ -215,6 +275,59 @@ cudaError_t launch_halo_exchange(const FieldSet<T>& fs, int nfields, const Block
     return cudaSuccess;
 }
 
+template <typename T>
+cudaError_t launch_halo_gather(const FieldSet<T>& fs, int nfields, const BlockLayout& L, cudaStream_t st)
+{
+    if (L.nblk == 1 && !L.periodic) return cudaSuccess;   // all halos are shell
+    const int cb = (int)sizeof(T);
+    // widest vector that every region row start and length is a multiple of
+    int vb = 16;
+    while (vb > cb && ((L.H * cb) % vb || (L.B[0] * cb) % vb || (L.xoff * cb) % vb)) vb >>= 1;
+    if (vb < cb) vb = cb;
+    HaloDirs hd{};
+    hd.vb = vb;
+    const long long per_cta = 256LL * 4;    // vectors per CTA
+    int ctas = 0;
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int d[3] = {dx, dy, dz};
+                if (!dx && !dy && !dz) continue;
+                bool any = true;
+                for (int a = 0; a < 3; ++a)
+                    if (d[a] && L.nb[a] == 1 && !L.periodic) any = false;
+                if (!any) continue;
+                const int k = hd.n++;
+                int ext[3];
+                for (int a = 0; a < 3; ++a) {
+                    hd.d[k][a] = d[a];
+                    ext[a] = d[a] ? L.H : L.B[a];
+                    hd.dst[k][a] = d[a] < 0 ? 0 : (d[a] == 0 ? L.H : L.H + L.B[a]);
+                    hd.src[k][a] = d[a] < 0 ? L.B[a] : L.H;
+                }
+                hd.ex[k] = ext[0] * cb / vb;
+                hd.ey[k] = ext[1];
+                hd.ez[k] = ext[2];
+                const long long nv = (long long)hd.ex[k] * ext[1] * ext[2];
+                hd.cta0[k] = ctas;
+                ctas += (int)std::max(1LL, std::min<long long>((nv + per_cta - 1) / per_cta, 4096));
+            }
+    hd.cta0[hd.n] = ctas;
+    if (hd.n == 0) return cudaSuccess;
+    FieldSet<uint8_t> fb{};
+    for (int f = 0; f < nfields; ++f) fb.p[f] = reinterpret_cast<uint8_t*>(fs.p[f]);
+    const dim3 grid((unsigned)ctas, (unsigned)(nfields * L.nblk));
+    switch (vb) {
+    case 16: halo_gather_kernel<16><<<grid, 256, 0, st>>>(fb, L, cb, hd); break;
+    case 8: halo_gather_kernel<8><<<grid, 256, 0, st>>>(fb, L, cb, hd); break;
+    case 4: halo_gather_kernel<4><<<grid, 256, 0, st>>>(fb, L, cb, hd); break;
+    case 2: halo_gather_kernel<2><<<grid, 256, 0, st>>>(fb, L, cb, hd); break;
+    default: halo_gather_kernel<1><<<grid, 256, 0, st>>>(fb, L, cb, hd); break;
+    }
+    count_launches(1);
+    return cudaGetLastError();
+}
+
 size_t halo_bounce_elems(const BlockLayout& L)
 {
     size_t m = 0;
@@ -249,6 +362,9 @@ template cudaError_t launch_halo_exchange<float>(const FieldSet<float>&, int, co
                                                  float*, cudaStream_t);
 template cudaError_t launch_halo_exchange<uint8_t>(const FieldSet<uint8_t>&, int,
                                                    const BlockLayout&, uint8_t*, cudaStream_t);
+template cudaError_t launch_halo_gather<float>(const FieldSet<float>&, int, const BlockLayout&, cudaStream_t);
+template cudaError_t launch_halo_gather<uint8_t>(const FieldSet<uint8_t>&, int, const BlockLayout&,
+                                                 cudaStream_t);
 template cudaError_t launch_scatter<float>(const float*, float*, const BlockLayout&, int, cudaStream_t);
 template cudaError_t launch_scatter<uint8_t>(const uint8_t*, uint8_t*, const BlockLayout&, int,
                                              cudaStream_t);

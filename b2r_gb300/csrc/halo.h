@@ -18,6 +18,10 @@ template <typename T>
 cudaError_t launch_halo_exchange(const FieldSet<T>& fs, int nfields, const BlockLayout& L,
                                  T* bounce, cudaStream_t st);
 size_t halo_bounce_elems(const BlockLayout& L);
+// The same boundary update in one launch: every halo cell copied from the
+// block owning it (26 face / edge / corner regions per block).
+template <typename T>
+cudaError_t launch_halo_gather(const FieldSet<T>& fs, int nfields, const BlockLayout& L, cudaStream_t st);
 
 // Dense domain array (shell > 0: with a fixed shell of that depth; periodic
 // layouts: bare torus) -> every padded block, halos included.
