@@ -187,30 +187,24 @@ eqwp_stag_velocity(FieldPtrs F, FieldPtrs O, MatPtrs M, const BlockLayout L, int
     op.zz = F.p[SZZ] + c.base;
     op.begin(w.zs, S);
     const float* buoy = M.p[2] + c.base;
-    const float k = p.dt * p.inv_h;
     for (int z = w.zs; z <= w.ze; ++z) {
         const long long o = (long long)z * S;
-        float ax[4], ay[4], az[4];
-        op.eval(o, P, S, ax, ay, az);
+        float a[3][4];
+        op.eval(o, P, S, a[0], a[1], a[2]);
         const float4 bb = ld4(buoy + o);
         float4 old[3];
 #pragma unroll
         for (int f = 0; f < 3; ++f) old[f] = rd4(F.p[VX + f] + c.base + o, c);
-        float dvx[4], dvy[4], dvz[4];
+        float nv[3][4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const float kb = k * cmp(bb, j);
-            dvx[j] = kb * ax[j];
-            dvy[j] = kb * ay[j];
-            dvz[j] = kb * az[j];
-        }
-        wr4(O.p[VX] + c.base + o, c, old[0], dvx);
-        wr4(O.p[VY] + c.base + o, c, old[1], dvy);
-        wr4(O.p[VZ] + c.base + o, c, old[2], dvz);
+        for (int f = 0; f < 3; ++f)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) nv[f][j] = vel_update(cmp(old[f], j), a[f][j], p.dt, p.inv_h, cmp(bb, j));
+#pragma unroll
+        for (int f = 0; f < 3; ++f) st4(O.p[VX + f] + c.base + o, c, nv[f]);
         if (ACC) {
-            st4(A.p[0] + c.base + o, c, ax);
-            st4(A.p[1] + c.base + o, c, ay);
-            st4(A.p[2] + c.base + o, c, az);
+#pragma unroll
+            for (int f = 0; f < 3; ++f) st4(A.p[f] + c.base + o, c, a[f]);
         }
     }
 }
@@ -232,13 +226,12 @@ eqwp_stag_stress(FieldPtrs F, FieldPtrs O, MatPtrs M, const BlockLayout L, int s
     op.begin(w.zs, S);
     const float* lam = M.p[0] + c.base;
     const float* mu = M.p[1] + c.base;
-    const float k = p.dt * p.inv_h;
     // source cell of this block, in block coordinates
     const int b0 = blk % L.nb[0], b1 = (blk / L.nb[0]) % L.nb[1], b2 = blk / (L.nb[0] * L.nb[1]);
     const int sx = p.src[0] - b0 * L.B[0] + L.H, sy = p.src[1] - b1 * L.B[1] + L.H,
               sz = p.src[2] - b2 * L.B[2] + L.H;
     const bool srow = (c.y == sy) && sx >= c.xb && sx < c.xb + 4;
-    // updated fields in the order of the strain components e[0..5]
+    // updated fields in the order of stress_update: xx, yy, zz, xy, xz, yz
     static constexpr int kOut[6] = {SXX, SYY, SZZ, SXY, SXZ, SYZ};
     for (int z = w.zs; z <= w.ze; ++z) {
         const long long o = (long long)z * S;
@@ -249,29 +242,24 @@ eqwp_stag_stress(FieldPtrs F, FieldPtrs O, MatPtrs M, const BlockLayout L, int s
         float4 old[6];
 #pragma unroll
         for (int f = 0; f < 6; ++f) old[f] = rd4(F.p[kOut[f]] + c.base + o, c);
-        float d[6][4];
+        float ns[6][4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const float exx = e[0][j], eyy = e[1][j], ezz = e[2][j];
-            const float l = cmp(l4, j), m = cmp(m4, j);
-            const float l2m = l + 2.f * m;
-            float axx = k * (l2m * exx + l * (eyy + ezz));
-            float ayy = k * (l2m * eyy + l * (exx + ezz));
-            float azz = k * (l2m * ezz + l * (exx + eyy));
+            const StressIn in{e[0][j], e[1][j], e[2][j], e[3][j], e[4][j], e[5][j]};
+            float sv[6];
+#pragma unroll
+            for (int f = 0; f < 6; ++f) sv[f] = cmp(old[f], j);
+            stress_update(in, p.dt, p.inv_h, cmp(l4, j), cmp(m4, j), sv);
             if (src_here && c.xb + j == sx) {
-                axx += src_amp;
-                ayy += src_amp;
-                azz += src_amp;
+                sv[0] = __fadd_rn(sv[0], src_amp);
+                sv[1] = __fadd_rn(sv[1], src_amp);
+                sv[2] = __fadd_rn(sv[2], src_amp);
             }
-            d[0][j] = axx;
-            d[1][j] = ayy;
-            d[2][j] = azz;
-            d[3][j] = k * m * e[3][j];
-            d[4][j] = k * m * e[4][j];
-            d[5][j] = k * m * e[5][j];
+#pragma unroll
+            for (int f = 0; f < 6; ++f) ns[f][j] = sv[f];
         }
 #pragma unroll
-        for (int f = 0; f < 6; ++f) wr4(O.p[kOut[f]] + c.base + o, c, old[f], d[f]);
+        for (int f = 0; f < 6; ++f) st4(O.p[kOut[f]] + c.base + o, c, ns[f]);
     }
 }
 

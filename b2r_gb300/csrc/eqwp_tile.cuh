@@ -140,25 +140,61 @@ __device__ __forceinline__ float dc4(const float4& m2, const float4& m1, const f
     return a * (cmp(p2, j) - cmp(m2, j)) + b * (cmp(p1, j) - cmp(m1, j));
 }
 
-// forward difference at i+1/2 and backward at i-1/2, 4th order (9/8, -1/24)
+// Staggered 4th-order differences, forward Dp at i+1/2 and backward Dm at
+// i-1/2: c1 (f1 - f0) + c2 (f2 - f-1), c1 = 9/8, c2 = -1/24.  Every
+// operation of the staggered scheme is an explicitly rounded intrinsic, in
+// the order of the FP32 oracle, so no kernel variant contracts differently
+// and all of them (two stage kernels, the fused step, the replay) give the
+// same bits.
+constexpr float kC1 = 9.f / 8.f, kC2 = -1.f / 24.f;
+__device__ __forceinline__ float sdiff(float a1, float a0, float b1, float b0)
+{
+    return __fadd_rn(__fmul_rn(kC1, __fsub_rn(a1, a0)), __fmul_rn(kC2, __fsub_rn(b1, b0)));
+}
 __device__ __forceinline__ float dpx(const Row12& r, int j)
 {
-    return 1.125f * (r.v[5 + j] - r.v[4 + j]) - (1.f / 24.f) * (r.v[6 + j] - r.v[3 + j]);
+    return sdiff(r.v[5 + j], r.v[4 + j], r.v[6 + j], r.v[3 + j]);
 }
 __device__ __forceinline__ float dmx(const Row12& r, int j)
 {
-    return 1.125f * (r.v[4 + j] - r.v[3 + j]) - (1.f / 24.f) * (r.v[5 + j] - r.v[2 + j]);
+    return sdiff(r.v[4 + j], r.v[3 + j], r.v[5 + j], r.v[2 + j]);
 }
 // rows/planes -2..+2 around the cell: Dp uses -1..+2, Dm uses -2..+1
 __device__ __forceinline__ float dp4(const float4& m1, const float4& c, const float4& p1,
                                      const float4& p2, int j)
 {
-    return 1.125f * (cmp(p1, j) - cmp(c, j)) - (1.f / 24.f) * (cmp(p2, j) - cmp(m1, j));
+    return sdiff(cmp(p1, j), cmp(c, j), cmp(p2, j), cmp(m1, j));
 }
 __device__ __forceinline__ float dm4(const float4& m2, const float4& m1, const float4& c,
                                      const float4& p1, int j)
 {
-    return 1.125f * (cmp(c, j) - cmp(m1, j)) - (1.f / 24.f) * (cmp(p1, j) - cmp(m2, j));
+    return sdiff(cmp(c, j), cmp(m1, j), cmp(p1, j), cmp(m2, j));
+}
+__device__ __forceinline__ float add3(float a, float b, float c) { return __fadd_rn(__fadd_rn(a, b), c); }
+
+// Velocity and stress updates of the staggered scheme from the raw stencil
+// sums (a = D s, e = E v), dt, 1/h and the material, as the oracle rounds
+// them:  v + (dt b)(a / h);  s_ii + dt (l2m e_ii + lambda (e_jj + e_kk));
+// s_ij + (dt mu)(e_ij / h).
+__device__ __forceinline__ float vel_update(float v, float a, float dt, float ih, float b)
+{
+    return __fadd_rn(v, __fmul_rn(__fmul_rn(dt, b), __fmul_rn(a, ih)));
+}
+struct StressIn {
+    float exx, eyy, ezz, gxy, gxz, gyz;   // raw stencil sums (not yet / h)
+};
+__device__ __forceinline__ void stress_update(const StressIn& e, float dt, float ih, float lam, float mu,
+                                              float (&s)[6])   // xx, yy, zz, xy, xz, yz; in / out
+{
+    const float exx = __fmul_rn(e.exx, ih), eyy = __fmul_rn(e.eyy, ih), ezz = __fmul_rn(e.ezz, ih);
+    const float l2m = __fadd_rn(lam, __fmul_rn(2.f, mu));
+    s[0] = __fadd_rn(s[0], __fmul_rn(dt, __fadd_rn(__fmul_rn(l2m, exx), __fmul_rn(lam, __fadd_rn(eyy, ezz)))));
+    s[1] = __fadd_rn(s[1], __fmul_rn(dt, __fadd_rn(__fmul_rn(l2m, eyy), __fmul_rn(lam, __fadd_rn(exx, ezz)))));
+    s[2] = __fadd_rn(s[2], __fmul_rn(dt, __fadd_rn(__fmul_rn(l2m, ezz), __fmul_rn(lam, __fadd_rn(exx, eyy)))));
+    const float dm = __fmul_rn(dt, mu);
+    s[3] = __fadd_rn(s[3], __fmul_rn(dm, __fmul_rn(e.gxy, ih)));
+    s[4] = __fadd_rn(s[4], __fmul_rn(dm, __fmul_rn(e.gxz, ih)));
+    s[5] = __fadd_rn(s[5], __fmul_rn(dm, __fmul_rn(e.gyz, ih)));
 }
 
 // Velocity-stage operator of the staggered scheme on six stress-like fields
@@ -195,9 +231,9 @@ struct VelOp {
         const float4 xyc = make_float4(rxy.v[4], rxy.v[5], rxy.v[6], rxy.v[7]);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            ax[j] = dpx(rxx, j) + dm4(xym2, xym1, xyc, xyp1, j) + dm4(qxz.m2, qxz.m1, qxz.c, qxz.p1, j);
-            ay[j] = dmx(rxy, j) + dp4(yym1, yyc, yyp1, yyp2, j) + dm4(qyz.m2, qyz.m1, qyz.c, qyz.p1, j);
-            az[j] = dmx(rxz, j) + dm4(yzm2, yzm1, qyz.c, yzp1, j) + dp4(qzz.m1, qzz.c, qzz.p1, qzz.p2, j);
+            ax[j] = add3(dpx(rxx, j), dm4(xym2, xym1, xyc, xyp1, j), dm4(qxz.m2, qxz.m1, qxz.c, qxz.p1, j));
+            ay[j] = add3(dmx(rxy, j), dp4(yym1, yyc, yyp1, yyp2, j), dm4(qyz.m2, qyz.m1, qyz.c, qyz.p1, j));
+            az[j] = add3(dmx(rxz, j), dm4(yzm2, yzm1, qyz.c, yzp1, j), dp4(qzz.m1, qzz.c, qzz.p1, qzz.p2, j));
         }
     }
 };
@@ -237,9 +273,9 @@ struct StrOp {
             e[0][j] = dmx(rx, j);
             e[1][j] = dm4(ym2, ym1, yc, yp1, j);
             e[2][j] = dm4(qz.m2, qz.m1, qz.c, qz.p1, j);
-            e[3][j] = dp4(xm1, xc, xp1, xp2, j) + dpx(ry, j);
-            e[4][j] = dp4(qx.m1, qx.c, qx.p1, qx.p2, j) + dpx(rz, j);
-            e[5][j] = dp4(qy.m1, qy.c, qy.p1, qy.p2, j) + dp4(zm1, zc, zp1, zp2, j);
+            e[3][j] = __fadd_rn(dp4(xm1, xc, xp1, xp2, j), dpx(ry, j));
+            e[4][j] = __fadd_rn(dp4(qx.m1, qx.c, qx.p1, qx.p2, j), dpx(rz, j));
+            e[5][j] = __fadd_rn(dp4(qy.m1, qy.c, qy.p1, qy.p2, j), dp4(zm1, zc, zp1, zp2, j));
         }
     }
 };

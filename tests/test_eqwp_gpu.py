@@ -99,3 +99,5 @@ def test_eqwp_stag_matches_oracle(b2r, orc, blocks, R):
         r32, r64 = rel_l2(got[k], f[k]), rel_l2(got[k], f64[k])
         print(f"{NAMES[k]} blocks={blocks} R={R}: vs FP32 {r32:.2e}, vs FP64 {r64:.2e}")
         assert r32 <= TOL, NAMES[k]
+        # every operation is rounded as the FP32 oracle rounds it
+        assert np.array_equal(got[k], f[k]), NAMES[k]
