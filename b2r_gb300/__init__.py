@@ -205,8 +205,10 @@ class Domain:
         """Replay whole periods from CUDA graphs (needs a non-default stream)."""
         _check(lib().b2r_set_graphs(self.h, 1 if enable else 0), self.h)
 
-    def set_tuning(self, zchunk=None, ctas_per_sm=None, pdl=None, tblock=None, zchunk2=None):
-        for key, v in ((1, zchunk), (2, ctas_per_sm), (3, pdl), (4, tblock), (5, zchunk2)):
+    def set_tuning(self, zchunk=None, ctas_per_sm=None, pdl=None, tblock=None, zchunk2=None,
+                   eqwp_fused=None):
+        for key, v in ((1, zchunk), (2, ctas_per_sm), (3, pdl), (4, tblock), (5, zchunk2),
+                       (6, eqwp_fused)):
             if v is not None:
                 _check(lib().b2r_set_tuning(self.h, key, int(v)), self.h)
 

@@ -40,6 +40,12 @@ struct b2r_handle {
     // elastic wave: fields and material
     float* fld[kMaxFields] = {};
     int nfld = 0;
+    // staggered model: the second field set of the one-pass step (v^n, s^n
+    // -> v^{n+1}, s^{n+1} out of place) and tensor maps of both sets'
+    // stresses; fld is always the current set
+    float* fld2[kMaxFields] = {};
+    StressMaps smaps[2];
+    bool eqwp_fused = false;   // two-pass by default: faster on this GPU so far
     float* mat[3] = {};
     std::vector<float> src;     // per-step source increment of sxx/syy/szz (STAG)
     void* staging = nullptr;
@@ -284,6 +290,13 @@ b2r_status substep(b2r_handle* h, int i)
     }
     case B2R_MODEL_EQWP_STAG: {
         const EqwpStagParams p = stag_params(h);
+        if (h->eqwp_fused) {
+            CK(h, launch_eqwp_stag_fused(h->smaps[0], h->fld, h->fld2, h->fld2 + B2R_F_SXX, h->mat, h->L, i,
+                                         (int)h->ts, p, h->d_status, h->stream));
+            for (int f = 0; f < h->nfld; ++f) std::swap(h->fld[f], h->fld2[f]);
+            std::swap(h->smaps[0], h->smaps[1]);
+            return B2R_OK;
+        }
         CK(h, launch_eqwp_stag_substep(h->fld, h->mat, h->L, i, (int)h->ts, p, h->stream));
         return B2R_OK;
     }
@@ -489,6 +502,16 @@ b2r_status b2r_create(const b2r_config* cfg, b2r_handle** out)
                     return bail(fail(nullptr, B2R_ERR_OOM, "cudaMalloc of %zu bytes failed", fb));
                 cudaMemset(h->mat[m], 0, fb);
             }
+            for (int f = 0; f < h->nfld; ++f) {
+                if (cudaMalloc(&h->fld2[f], fb) != cudaSuccess)
+                    return bail(fail(nullptr, B2R_ERR_OOM, "cudaMalloc of %zu bytes failed", fb));
+                cudaMemset(h->fld2[f], 0, fb);
+            }
+            const int box = eqwp_fused_box();
+            for (int f = 0; f < 6; ++f)
+                if (!make_block_tmap(&h->smaps[0].m[f], h->fld[B2R_F_SXX + f], h->L, 4, box, box, 1) ||
+                    !make_block_tmap(&h->smaps[1].m[f], h->fld2[B2R_F_SXX + f], h->L, 4, box, box, 1))
+                    return bail(fail(nullptr, B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed"));
         }
     }
     if (cudaDeviceSynchronize() != cudaSuccess)
@@ -504,8 +527,10 @@ b2r_status b2r_destroy(b2r_handle* h)
     if (h->adj_ws) cudaFree(h->adj_ws);
     for (int b = 0; b < 2; ++b)
         if (h->buf[b]) cudaFree(h->buf[b]);
-    for (int f = 0; f < kMaxFields; ++f)
+    for (int f = 0; f < kMaxFields; ++f) {
         if (h->fld[f]) cudaFree(h->fld[f]);
+        if (h->fld2[f]) cudaFree(h->fld2[f]);
+    }
     for (int m = 0; m < 3; ++m)
         if (h->mat[m]) cudaFree(h->mat[m]);
     if (h->staging) cudaFree(h->staging);
@@ -588,6 +613,9 @@ b2r_status b2r_upload(b2r_handle* h, int field, const void* src, int src_is_devi
     if (!eq)  // both ping-pong buffers carry the shell (heat-3D.cu:591-592)
         CK(h, cudaMemcpyAsync(h->buf[1 - h->cur], h->buf[h->cur], field_bytes(h),
                               cudaMemcpyDeviceToDevice, h->stream));
+    else if (!is_mat && h->fld2[field])   // so do both staggered field sets
+        CK(h, cudaMemcpyAsync(h->fld2[field], h->fld[field], field_bytes(h), cudaMemcpyDeviceToDevice,
+                              h->stream));
     h->ts = 0;
     h->halos_fresh = true;
     return B2R_OK;
@@ -737,6 +765,7 @@ b2r_status b2r_set_tuning(b2r_handle* h, int key, int value)
     case B2R_TUNE_PDL: h->tune.pdl = value != 0; break;
     case B2R_TUNE_TBLOCK: h->tune.tblock = value; break;
     case B2R_TUNE_ZCHUNK2: h->tune.zchunk2 = value; break;
+    case B2R_TUNE_EQWP_FUSED: h->eqwp_fused = value != 0; break;
     default: return fail(h, B2R_ERR_ARG, "unknown tuning key %d", key);
     }
     drop_graphs(h);

@@ -42,6 +42,19 @@ cudaError_t launch_eqwp_stag_step_replay(const float* const* v_in, float* const*
                                          float* const* acc, float* const* mat, const BlockLayout& L,
                                          int ts, const EqwpStagParams& p, cudaStream_t st);
 
+// eqwp_fused.cu: one staggered time step in one pass, v^n, s^n -> v^{n+1},
+// s^{n+1} (out of place).  maps: tensor maps of the six s^n fields (xx, xy,
+// xz, yy, yz, zz) with boxes of eqwp_fused_box()^2 cells; sout in the same
+// order.  status receives DEV_TIMEOUT if a bounded wait gave up.
+struct StressMaps {
+    CUtensorMap m[6];
+};
+size_t eqwp_fused_smem();
+int eqwp_fused_box();
+cudaError_t launch_eqwp_stag_fused(const StressMaps& maps, const float* const* vin, float* const* vout,
+                                   float* const* sout, float* const* mat, const BlockLayout& L, int step_i,
+                                   int ts, const EqwpStagParams& p, int* status, cudaStream_t st);
+
 // adjoint.cu: receiver sampling / injection and one reverse step of the
 // staggered scheme (tmp = vb[3], sb[6], q[6], w[3]; stress order xx, xy, xz,
 // yy, yz, zz; v_n = forward v^n, acc_n = forward stencil sums of step n;

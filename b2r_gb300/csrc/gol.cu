@@ -122,9 +122,11 @@ cudaError_t launch_gol_substep(const uint8_t* in, uint8_t* out, const BlockLayou
     const int rows = L.n[1] - 2;
     const int nty = (rows + kRY * kGolWarps - 1) / (kRY * kGolWarps);
     const long long tiles = (long long)ntx * nty * L.nblk;
-    const long long want = 152LL * 16 * 2;
+    // small blocks are latency bound (a generation of a 136^3 block is a few
+    // microseconds of data): short z chunks, many CTAs
+    const long long want = 152LL * 12;
     int nzc = (int)((want + tiles - 1) / tiles);
-    const int maxc = (L.n[2] - 2) / 16 > 0 ? (L.n[2] - 2) / 16 : 1;
+    const int maxc = (L.n[2] - 2) / 4 > 0 ? (L.n[2] - 2) / 4 : 1;
     if (nzc > maxc) nzc = maxc;
     if (nzc < 1) nzc = 1;
     dim3 grid(ntx, nty, L.nblk * nzc);

@@ -119,7 +119,9 @@ enum {
     B2R_TUNE_CTAS_PER_SM = 2,  /* 0 = one CTA per unit, k = persistent k CTAs per SM */
     B2R_TUNE_PDL = 3,          /* programmatic dependent launch on / off */
     B2R_TUNE_TBLOCK = 4,       /* time steps per HBM pass: 2 (radius 1, default) or 1 */
-    B2R_TUNE_ZCHUNK2 = 5       /* planes per work unit of the two-step sweep (0 = 16) */
+    B2R_TUNE_ZCHUNK2 = 5,      /* planes per work unit of the two-step sweep (0 = 16) */
+    B2R_TUNE_EQWP_FUSED = 6    /* staggered elastic wave: 1 = one-pass step, 0 = the velocity
+                                  and stress stages as two passes (default); bit-identical */
 };
 b2r_status b2r_set_tuning(b2r_handle* h, int key, int value);
 /* Time every schedule candidate (z-chunk length x persistent CTAs per SM x

@@ -69,8 +69,9 @@ def ricker(n, dt, f0, amp):
     return amp * (1 - 2 * a) * np.exp(-a)
 
 
+@pytest.mark.parametrize("fused", [True, False])
 @pytest.mark.parametrize("blocks,R", [((1, 1, 1), 1), ((2, 2, 1), 2), ((2, 1, 2), 1)])
-def test_eqwp_stag_matches_oracle(b2r, orc, blocks, R):
+def test_eqwp_stag_matches_oracle(b2r, orc, blocks, R, fused):
     env = (48, 40, 32)
     nsteps = 40
     h = 10.0
@@ -79,6 +80,7 @@ def test_eqwp_stag_matches_oracle(b2r, orc, blocks, R):
     src = (env[0] // 2, env[1] // 2, env[2] // 2)
     amps = ricker(nsteps, dt, 10.0, 1e6 * dt).astype(np.float32)
     with b2r.Domain(b2r.MODEL_EQWP_STAG, env, blocks=blocks, R=R, D=2, dt=dt, h=h, src=src) as d:
+        d.set_tuning(eqwp_fused=fused)
         for m, name in enumerate(["lambda", "mu", "buoy"]):
             d.upload(mat[m].astype(np.float32), field=name)
         zero = np.zeros(d.domain_shape, np.float32)
@@ -101,3 +103,32 @@ def test_eqwp_stag_matches_oracle(b2r, orc, blocks, R):
         assert r32 <= TOL, NAMES[k]
         # every operation is rounded as the FP32 oracle rounds it
         assert np.array_equal(got[k], f[k]), NAMES[k]
+
+
+@pytest.mark.parametrize("env,blocks,R", [((150, 90, 70), (3, 2, 1), 2), ((97, 61, 131), (1, 1, 1), 1),
+                                          ((64, 64, 64), (2, 2, 2), 3)])
+def test_eqwp_stag_one_pass_equals_two_pass(b2r, env, blocks, R):
+    """The one-pass step against the two stage kernels, on sizes that leave
+    ragged tiles and z chunks; both round every operation the same way."""
+    nsteps = 2 * R + 1
+    h = 10.0
+    mat = layered(env)
+    dt = 0.5 * h / (4000 * np.sqrt(3) * (9 / 8 + 1 / 24))
+    src = (env[0] // 3, env[1] // 2, env[2] // 2)
+    amps = ricker(nsteps, dt, 10.0, 1e6 * dt).astype(np.float32)
+    rng = np.random.default_rng(11)
+    outs = []
+    for fused in (False, True):
+        with b2r.Domain(b2r.MODEL_EQWP_STAG, env, blocks=blocks, R=R, D=2, dt=dt, h=h, src=src) as d:
+            d.set_tuning(eqwp_fused=fused)
+            for m, name in enumerate(["lambda", "mu", "buoy"]):
+                d.upload(mat[m].astype(np.float32), field=name)
+            rng = np.random.default_rng(11)
+            for k in range(9):
+                d.upload(rng.standard_normal(d.domain_shape).astype(np.float32), field=k)
+            d.set_source(amps)
+            d.step(nsteps)
+            outs.append([d.download(field=k) for k in range(9)])
+            d.synchronize()
+    for k in range(9):
+        assert np.array_equal(outs[0][k], outs[1][k]), NAMES[k]
