@@ -184,6 +184,19 @@ bool heat_fuse_ok(const b2r_handle* h, int i)
     return i + 1 < h->cfg.R;
 }
 
+// Game of Life generations that one pass may advance from sub-step i with
+// `left` steps to go: up to the period's end (no exchange in between), or
+// unbounded when the exchange is empty; 1 = the one-generation kernel, the
+// default (faster on 128^3 blocks so far; tblock >= 4 selects the
+// several-generation pass).
+int gol_pass_gens(const b2r_handle* h, int i, int left)
+{
+    if (h->cfg.model != B2R_MODEL_GOL || h->tune.tblock < 4) return 1;
+    int g = std::min(left, gol_max_generations_per_pass());
+    if (!(h->L.nblk == 1 && !h->L.periodic)) g = std::min(g, h->cfg.R - i);
+    return std::max(g, 1);
+}
+
 b2r_status check_status(b2r_handle* h)
 {
     int s = 0;
@@ -328,7 +341,14 @@ b2r_status advance(b2r_handle* h, int n)
         if (i == 0 && !h->halos_fresh)
             if ((st = exchange_all(h, false)) != B2R_OK) return st;
         h->halos_fresh = false;
-        if (n - s >= 2 && heat_fuse_ok(h, i)) {
+        const int gg = gol_pass_gens(h, i, n - s);
+        if (gg >= 2) {
+            CK(h, launch_gol_period(static_cast<const uint8_t*>(h->buf[h->cur]),
+                                    static_cast<uint8_t*>(h->buf[1 - h->cur]), h->L, i, gg, h->stream));
+            h->cur = 1 - h->cur;
+            h->ts += gg;
+            s += gg;
+        } else if (n - s >= 2 && heat_fuse_ok(h, i)) {
             if ((st = substep2(h, i)) != B2R_OK) return st;
             h->ts += 2;
             s += 2;

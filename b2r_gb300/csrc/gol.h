@@ -9,4 +9,11 @@ namespace b2r {
 cudaError_t launch_gol_substep(const uint8_t* in, uint8_t* out, const BlockLayout& L, int step_i,
                                cudaStream_t st);
 
+// ng (1 .. gol_max_generations_per_pass()) generations of sub-steps i0 ..
+// i0 + ng - 1 in one pass, in -> out.  Only the window of the last of them
+// is written to `out`.
+cudaError_t launch_gol_period(const uint8_t* in, uint8_t* out, const BlockLayout& L, int i0, int ng,
+                              cudaStream_t st);
+int gol_max_generations_per_pass();
+
 }  // namespace b2r

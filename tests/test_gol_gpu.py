@@ -12,10 +12,12 @@ def bernoulli(env, p, seed):
 
 @pytest.mark.parametrize("env,blocks,R", [((64, 64, 64), (2, 2, 2), 4), ((64, 48, 40), (1, 1, 1), 1),
                                           ((70, 36, 50), (2, 3, 1), 2), ((33, 17, 9), (1, 1, 1), 3)])
-def test_gol_periodic_bit_exact_every_period(b2r, orc, env, blocks, R):
+@pytest.mark.parametrize("tblock", [2, 4])
+def test_gol_periodic_bit_exact_every_period(b2r, orc, env, blocks, R, tblock):
     dom = bernoulli(env, 0.3, 2)
     ref = dom.copy()
     with b2r.Domain(b2r.MODEL_GOL, env, blocks=blocks, R=R, D=1, boundary=b2r.BC_PERIODIC) as d:
+        d.set_tuning(tblock=tblock)
         d.upload(dom)
         for period in range(3):
             d.step(R)
@@ -67,3 +69,24 @@ def test_gol_3D_gpu_main_block_entry(b2r, orc, R):
     # the valid interior after R generations is bit-exact
     s = (slice(R, -R),) * 3
     assert np.array_equal(got[s], a[s])
+
+
+@pytest.mark.parametrize("env,blocks,R,steps", [((300, 40, 30), (1, 1, 1), 1, 9), ((260, 70, 33), (2, 1, 1), 3, 7)])
+def test_gol_multi_generation_pass(b2r, orc, env, blocks, R, steps):
+    """Several generations per pass (wide rows split into x tiles, ragged
+    tails) against one generation per pass and the oracle."""
+    dom = np.zeros(tuple(e + 2 for e in env[::-1]), np.uint8)
+    dom[1:-1, 1:-1, 1:-1] = bernoulli(env, 0.3, 9)
+    outs = []
+    for tb in (1, 4):
+        with b2r.Domain(b2r.MODEL_GOL, env, blocks=blocks, R=R, D=1) as d:
+            d.set_tuning(tblock=tb)
+            d.upload(dom)
+            d.step(steps)
+            outs.append(d.download())
+    assert np.array_equal(outs[0], outs[1])
+    a, b = dom.copy(), dom.copy()
+    for _ in range(steps):
+        orc.gol_substep(a, b, 0, 1, 63)
+        a, b = b, a
+    assert np.array_equal(outs[1], a)
