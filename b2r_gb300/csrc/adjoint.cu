@@ -341,11 +341,11 @@ cudaError_t adjoint_step(float* const* tmp, const float* const* v_n, const float
     T.g_mu = g[1];
     T.k = dt_h;
     const Grid ga = stage_grid(L, 2), gb = stage_grid(L, 4);
-    adj_velocity_kernel<<<ga.g, dim3(kBX, kBY), 0, st>>>(V, L, ga.t);
+    adj_velocity_kernel<<<ga.g, ga.b, 0, st>>>(V, L, ga.t);
     count_launches(1);
     if (!last) {
-        adj_stress_kernel<<<gb.g, dim3(kBX, kBY), 0, st>>>(T, L, gb.t);
-        adj_grad_lm_kernel<<<gb.g, dim3(kBX, kBY), 0, st>>>(T, L, gb.t);
+        adj_stress_kernel<<<gb.g, gb.b, 0, st>>>(T, L, gb.t);
+        adj_grad_lm_kernel<<<gb.g, gb.b, 0, st>>>(T, L, gb.t);
         count_launches(2);
     }
     return cudaGetLastError();

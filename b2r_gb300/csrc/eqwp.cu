@@ -299,8 +299,8 @@ cudaError_t launch_eqwp_ref_substep(float* const* fld, const BlockLayout& L, int
     FieldPtrs F{};
     for (int f = 0; f < 10; ++f) F.p[f] = fld[f];
     const Grid ga = stage_grid(L, 4 * step_i + 2), gb = stage_grid(L, 4 * step_i + 4);
-    eqwp_ref_stress<<<ga.g, dim3(kBX, kBY), 0, st>>>(F, L, step_i, ga.t, p);
-    eqwp_ref_velocity<<<gb.g, dim3(kBX, kBY), 0, st>>>(F, L, step_i, gb.t, p, ts);
+    eqwp_ref_stress<<<ga.g, ga.b, 0, st>>>(F, L, step_i, ga.t, p);
+    eqwp_ref_velocity<<<gb.g, gb.b, 0, st>>>(F, L, step_i, gb.t, p, ts);
     count_launches(2);
     return cudaGetLastError();
 }
@@ -315,8 +315,8 @@ cudaError_t launch_eqwp_stag_substep(float* const* fld, float* const* mat, const
     const Grid ga = stage_grid(L, 4 * step_i + 2), gb = stage_grid(L, 4 * step_i + 4);
     float amp = 0.f;
     if (p.src_host && ts >= 0 && ts < p.src_len) amp = p.src_host[ts];
-    eqwp_stag_velocity<false><<<ga.g, dim3(kBX, kBY), 0, st>>>(F, F, M, L, step_i, ga.t, p, AccPtrs{});
-    eqwp_stag_stress<<<gb.g, dim3(kBX, kBY), 0, st>>>(F, F, M, L, step_i, gb.t, p, amp);
+    eqwp_stag_velocity<false><<<ga.g, ga.b, 0, st>>>(F, F, M, L, step_i, ga.t, p, AccPtrs{});
+    eqwp_stag_stress<<<gb.g, gb.b, 0, st>>>(F, F, M, L, step_i, gb.t, p, amp);
     count_launches(2);
     return cudaGetLastError();
 }
@@ -338,9 +338,9 @@ cudaError_t launch_eqwp_stag_step_replay(const float* const* v_in, float* const*
     const Grid ga = stage_grid(L, 2), gb = stage_grid(L, 4);
     float amp = 0.f;
     if (p.src_host && ts >= 0 && ts < p.src_len) amp = p.src_host[ts];
-    eqwp_stag_velocity<true><<<ga.g, dim3(kBX, kBY), 0, st>>>(F, O, M, L, 0, ga.t, p, A);
+    eqwp_stag_velocity<true><<<ga.g, ga.b, 0, st>>>(F, O, M, L, 0, ga.t, p, A);
     // the stress stage reads the new velocities and updates the stresses in place
-    eqwp_stag_stress<<<gb.g, dim3(kBX, kBY), 0, st>>>(O, O, M, L, 0, gb.t, p, amp);
+    eqwp_stag_stress<<<gb.g, gb.b, 0, st>>>(O, O, M, L, 0, gb.t, p, amp);
     count_launches(2);
     return cudaGetLastError();
 }

@@ -14,7 +14,7 @@ namespace eqk {
 
 // Thread = 4 consecutive x cells (one float4) of one row; CTA = 32 x 8
 // threads = a 128 x 8 tile; z marched over a chunk.
-constexpr int kBX = 32, kBY = 8, kTXc = 4 * kBX;
+constexpr int kBX = 32, kBY = 8;
 #ifndef B2R_EQWP_MINB
 #define B2R_EQWP_MINB 2   // resident CTAs per SM the register budget is fitted to
 #endif
@@ -78,10 +78,10 @@ struct Cell {
 
 __device__ __forceinline__ bool cell_setup(const BlockLayout& L, const Win& w, int blk, Cell& c, int x0, int y0)
 {
-    const int xs0 = x0 + blockIdx.x * kTXc + 4 * threadIdx.x;
+    const int xs0 = x0 + blockIdx.x * (4 * blockDim.x) + 4 * threadIdx.x;
     c.blk = blk;
     c.xb = xs0 - L.xoff;
-    c.y = y0 + blockIdx.y * kBY + threadIdx.y;
+    c.y = y0 + blockIdx.y * blockDim.y + threadIdx.y;
     if (!w.ok || c.y < w.lo[1] || c.y > w.hi[1]) return false;
     c.any = false;
     c.all = true;
@@ -301,8 +301,10 @@ struct Tiles {
     int y0;     // first row
 };
 
+// A launch: grid, CTA shape (kBX * kBY threads: 32 x 8, 16 x 16 or 8 x 32,
+// tiles of 128, 64 or 32 cells by 8, 16 or 32 rows) and tile origin.
 struct Grid {
-    dim3 g;
+    dim3 g, b;
     Tiles t;
 };
 
@@ -321,8 +323,21 @@ inline Grid stage_grid(const BlockLayout& L, int shrink)
     Grid r;
     r.t.x0 = (L.xoff + lo[0]) & ~3;
     r.t.y0 = lo[1];
-    const int tx = std::max(1, (L.xoff + hi[0] + 1 - r.t.x0 + kTXc - 1) / kTXc);
-    const int ty = std::max(1, (hi[1] + 1 - lo[1] + kBY - 1) / kBY);
+    // tile width: the fewest computed cells per row, narrower tiles paying a
+    // little for their larger x halo
+    const int W = std::max(1, L.xoff + hi[0] + 1 - r.t.x0);
+    int tw = 4 * kBX;
+    double best = 1e300;
+    for (int c = 4 * kBX; c >= kBX; c /= 2) {
+        const double cost = (double)((W + c - 1) / c) * c * (c == 4 * kBX ? 1.0 : (c == 2 * kBX ? 1.03 : 1.08));
+        if (cost < best - 1e-9) {
+            best = cost;
+            tw = c;
+        }
+    }
+    r.b = dim3(tw / 4, kBX * kBY / (tw / 4));
+    const int tx = std::max(1, (W + tw - 1) / tw);
+    const int ty = std::max(1, (hi[1] + 1 - lo[1] + (int)r.b.y - 1) / (int)r.b.y);
     const long long tiles = (long long)tx * ty * L.nblk;
     const long long want = 152LL * 8 * 3;
     int nzc = (int)((want + tiles - 1) / tiles);
