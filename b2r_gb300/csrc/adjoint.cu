@@ -29,6 +29,11 @@ namespace {
 
 using namespace eqk;
 
+// L2 prefetch distance of the reverse kernels (planes; 0 = none)
+#ifndef B2R_ADJ_PREFETCH
+#define B2R_ADJ_PREFETCH 1
+#endif
+
 // FP64 gradient cells of a thread, loaded before and stored after the
 // field stores of an iteration (32-byte aligned: the first cell of a thread
 // is a multiple of 4 elements from the buffer base)
@@ -106,6 +111,24 @@ adj_velocity_kernel(AdjV A, const BlockLayout L, Tiles T)
     op.begin(w.zs, S);
     for (int z = w.zs; z <= w.ze; ++z) {
         const long long o = (long long)z * S + c.base;
+        if (B2R_ADJ_PREFETCH > 0) {
+            const long long oa = ahead(L, z, B2R_ADJ_PREFETCH, w.ze) + c.base,
+                            oq = ahead(L, z, 2 + B2R_ADJ_PREFETCH, w.ze + 2);
+            pf_l2(op.xz + oq);
+            pf_l2(op.yz + oq);
+            pf_l2(op.zz + oq);
+            pf_l2(op.xx + oq - 2 * S);
+            pf_l2(op.xy + oq - 2 * S);
+            pf_l2(op.yy + oq - 2 * S);
+            pf_l2(A.buoy + oa);
+#pragma unroll
+            for (int f = 0; f < 3; ++f) {
+                pf_l2(A.vb[f] + oa);
+                pf_l2(A.acc[f] + oa);
+            }
+            pf_l2(reinterpret_cast<const float*>(A.g_b + oa));
+            pf_l2(reinterpret_cast<const float*>(A.g_b + oa) + 4);
+        }
         float a[3][4];
         op.eval(o - c.base, P, S, a[0], a[1], a[2]);
         const float4 bb = ld4(A.buoy + o);
@@ -159,6 +182,17 @@ adj_stress_kernel(AdjS A, const BlockLayout L, Tiles T)
     ow.begin(w.zs, S);
     for (int z = w.zs; z <= w.ze; ++z) {
         const long long o = (long long)z * S + c.base;
+        if (B2R_ADJ_PREFETCH > 0) {
+            const long long oa = ahead(L, z, B2R_ADJ_PREFETCH, w.ze) + c.base,
+                            oq = ahead(L, z, 2 + B2R_ADJ_PREFETCH, w.ze + 2);
+            pf_l2(ow.x + oq);
+            pf_l2(ow.y + oq);
+            pf_l2(ow.z + oq);
+            pf_l2(A.lam + oa);
+            pf_l2(A.mu + oa);
+#pragma unroll
+            for (int f = 0; f < 6; ++f) pf_l2(A.sb[f] + oa);
+        }
         float ew[6][4];
         ow.eval(o - c.base, P, S, ew);
         const float4 l4 = ld4(A.lam + o), m4 = ld4(A.mu + o);
@@ -208,6 +242,19 @@ adj_grad_lm_kernel(AdjS A, const BlockLayout L, Tiles T)
     ov.begin(w.zs, S);
     for (int z = w.zs; z <= w.ze; ++z) {
         const long long o = (long long)z * S + c.base;
+        if (B2R_ADJ_PREFETCH > 0) {
+            const long long oa = ahead(L, z, B2R_ADJ_PREFETCH, w.ze) + c.base,
+                            oq = ahead(L, z, 2 + B2R_ADJ_PREFETCH, w.ze + 2);
+            pf_l2(ov.x + oq);
+            pf_l2(ov.y + oq);
+            pf_l2(ov.z + oq);
+#pragma unroll
+            for (int f = 0; f < 6; ++f) pf_l2(A.sb[f] + oa);
+            pf_l2(reinterpret_cast<const float*>(A.g_lam + oa));
+            pf_l2(reinterpret_cast<const float*>(A.g_lam + oa) + 4);
+            pf_l2(reinterpret_cast<const float*>(A.g_mu + oa));
+            pf_l2(reinterpret_cast<const float*>(A.g_mu + oa) + 4);
+        }
         float ev[6][4];
         ov.eval(o - c.base, P, S, ev);
         float4 sb[6];

@@ -52,6 +52,15 @@ eqwp_ref_stress(FieldPtrs F, const BlockLayout L, int step_i, Tiles T, EqwpRefPa
     const float a = p.ca, b = p.cb;
     for (int z = w.zs; z <= w.ze; ++z) {
         const long long o = (long long)z * S;
+        if (B2R_EQWP_PREFETCH > 0) {
+            const long long oa = ahead(L, z, B2R_EQWP_PREFETCH, w.ze),
+                            oq = ahead(L, z, 2 + B2R_EQWP_PREFETCH, w.ze + 2);
+            pf_l2(vx + oq);
+            pf_l2(vy + oq);
+            pf_l2(vz + oq);
+#pragma unroll
+            for (int f = SXX; f <= SZZ; ++f) pf_l2(F.p[f] + c.base + oa);
+        }
         qx.shift(ld4(vx + o + 2 * S));
         qy.shift(ld4(vy + o + 2 * S));
         qz.shift(ld4(vz + o + 2 * S));
@@ -123,6 +132,19 @@ eqwp_ref_velocity(FieldPtrs F, const BlockLayout L, int step_i, Tiles T, EqwpRef
     const bool frow = (c.y == p.fy) && (ts < p.fsteps);
     for (int z = w.zs; z <= w.ze; ++z) {
         const long long o = (long long)z * S;
+        if (B2R_EQWP_PREFETCH > 0) {
+            const long long oa = ahead(L, z, B2R_EQWP_PREFETCH, w.ze),
+                            oq = ahead(L, z, 2 + B2R_EQWP_PREFETCH, w.ze + 2);
+            pf_l2(sxz + oq);
+            pf_l2(syz + oq);
+            pf_l2(szz + oq);
+            pf_l2(sxx + oa);
+            pf_l2(sxy + oa);
+            pf_l2(syy + oa);
+#pragma unroll
+            for (int f = VX; f <= VZ; ++f) pf_l2(F.p[f] + c.base + oa);
+            pf_l2(F.p[DISP] + c.base + oa);
+        }
         qxz.shift(ld4(sxz + o + 2 * S));
         qyz.shift(ld4(syz + o + 2 * S));
         qzz.shift(ld4(szz + o + 2 * S));
@@ -189,6 +211,19 @@ eqwp_stag_velocity(FieldPtrs F, FieldPtrs O, MatPtrs M, const BlockLayout L, int
     const float* buoy = M.p[2] + c.base;
     for (int z = w.zs; z <= w.ze; ++z) {
         const long long o = (long long)z * S;
+        if (B2R_EQWP_PREFETCH > 0) {
+            const long long oa = ahead(L, z, B2R_EQWP_PREFETCH, w.ze),
+                            oq = ahead(L, z, 2 + B2R_EQWP_PREFETCH, w.ze + 2);
+            pf_l2(op.xz + oq);
+            pf_l2(op.yz + oq);
+            pf_l2(op.zz + oq);
+            pf_l2(op.xx + oa);
+            pf_l2(op.xy + oa);
+            pf_l2(op.yy + oa);
+            pf_l2(buoy + oa);
+#pragma unroll
+            for (int f = 0; f < 3; ++f) pf_l2(F.p[VX + f] + c.base + oa);
+        }
         float a[3][4];
         op.eval(o, P, S, a[0], a[1], a[2]);
         const float4 bb = ld4(buoy + o);
@@ -235,6 +270,17 @@ eqwp_stag_stress(FieldPtrs F, FieldPtrs O, MatPtrs M, const BlockLayout L, int s
     static constexpr int kOut[6] = {SXX, SYY, SZZ, SXY, SXZ, SYZ};
     for (int z = w.zs; z <= w.ze; ++z) {
         const long long o = (long long)z * S;
+        if (B2R_EQWP_PREFETCH > 0) {
+            const long long oa = ahead(L, z, B2R_EQWP_PREFETCH, w.ze),
+                            oq = ahead(L, z, 2 + B2R_EQWP_PREFETCH, w.ze + 2);
+            pf_l2(op.x + oq);
+            pf_l2(op.y + oq);
+            pf_l2(op.z + oq);
+            pf_l2(lam + oa);
+            pf_l2(mu + oa);
+#pragma unroll
+            for (int f = 0; f < 6; ++f) pf_l2(F.p[kOut[f]] + c.base + oa);
+        }
         float e[6][4];
         op.eval(o, P, S, e);
         const float4 l4 = ld4(lam + o), m4 = ld4(mu + o);

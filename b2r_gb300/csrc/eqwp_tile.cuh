@@ -280,6 +280,24 @@ struct StrOp {
     }
 };
 
+// L2 prefetch of the thread's 16 bytes of a plane a few iterations ahead:
+// the z-marching stages are latency bound (each iteration waits on its own
+// first-touch DRAM loads), and a prefetch costs no register.
+#ifndef B2R_EQWP_PREFETCH
+#define B2R_EQWP_PREFETCH 1
+#endif
+__device__ __forceinline__ void pf_l2(const float* p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+// element offset of plane z + d, clamped to the last plane the CTA itself
+// reads (zlast): a prefetch past its own z chunk would fetch planes that
+// another CTA reads much later, and be evicted first
+__device__ __forceinline__ long long ahead(const BlockLayout& L, int z, int d, int zlast)
+{
+    return (long long)min(z + d, zlast) * L.plane;
+}
+
 // masked store of 4 values (the lanes of the window)
 __device__ __forceinline__ void st4(float* f, const Cell& c, const float (&v)[4])
 {
