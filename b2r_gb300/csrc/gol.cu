@@ -27,7 +27,6 @@ namespace {
 
 constexpr int kRY = 8;           // output rows per warp
 constexpr int kGolWarps = 4;     // warps per CTA, stacked in y
-constexpr int kOutWords = 30;    // output words per warp row
 
 __device__ __forceinline__ uint32_t ldw(const uint32_t* p) { return __ldg(p); }
 
@@ -42,11 +41,18 @@ __device__ __forceinline__ uint32_t life_rule(uint32_t cnt, uint32_t cur)
     return nxt & 0x01010101u;
 }
 
+// SEG = lanes per x segment: 32 (one segment per warp, 30 output words), or
+// 16 (two segments of 14 output words, stacked in y) when that wastes fewer
+// lanes on the row width (a 136-cell row is 34 words: 3 x 16 lanes instead
+// of 2 x 32).
+template <int SEG>
 __global__ void __launch_bounds__(32 * kGolWarps)
 gol_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out, const BlockLayout L,
            const int step_i, const int nzc)
 {
+    constexpr int kOut = SEG - 2, kSegs = 32 / SEG;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int l = lane & (SEG - 1), sg = lane / SEG;
     const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
     const int edge = edge_bits(L, blk);
     int lo[3], hi[3];
@@ -54,13 +60,14 @@ gol_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out, const Bloc
     for (int a = 0; a < 3; ++a) stage_region(L, edge, a, step_i + 1, lo[a], hi[a]);
 
     const int wb = (L.xoff + 1) >> 2;                       // first word with an updatable cell
-    const int w = wb + blockIdx.x * kOutWords + lane - 1;    // this lane's word (storage)
-    const int y0 = 1 + (blockIdx.y * kGolWarps + warp) * kRY;
+    const int w = wb + blockIdx.x * kOut + l - 1;           // this lane's word (storage)
+    const int wy0 = 1 + (blockIdx.y * kGolWarps + warp) * kSegs * kRY;   // first row of the warp
+    const int y0 = wy0 + sg * kRY;                           // first row of this lane's segment
     const int nz_out = hi[2] - lo[2] + 1;
     const int per = (nz_out + nzc - 1) / nzc;
     const int zs = lo[2] + zc * per;
     const int ze = min(hi[2], zs + per - 1);
-    if (nz_out <= 0 || zs > ze || y0 > hi[1]) return;       // warp-uniform
+    if (nz_out <= 0 || zs > ze || wy0 > hi[1]) return;      // warp-uniform
 
     // byte mask of cells of this word inside the x window
     const int xc = 4 * w - L.xoff;                          // block x of byte 0
@@ -68,7 +75,7 @@ gol_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out, const Bloc
 #pragma unroll
     for (int j = 0; j < 4; ++j)
         if (xc + j >= lo[0] && xc + j <= hi[0]) xmask |= 0xFFu << (8 * j);
-    const bool producer = lane >= 1 && lane <= kOutWords;
+    const bool producer = l >= 1 && l <= kOut;
 
     const int wpr = L.P >> 2;                               // words per row
     const uint32_t* inw = reinterpret_cast<const uint32_t*>(in + (long long)blk * L.bstride);
@@ -97,8 +104,8 @@ gol_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out, const Bloc
 #pragma unroll
         for (int r = 0; r < kRY; ++r) {
             const uint32_t v = s[r] + s[r + 1] + s[r + 2];          // 3 rows x 3 planes
-            const uint32_t vl = __shfl_up_sync(0xffffffffu, v, 1);
-            const uint32_t vr = __shfl_down_sync(0xffffffffu, v, 1);
+            const uint32_t vl = __shfl_up_sync(0xffffffffu, v, 1, SEG);
+            const uint32_t vr = __shfl_down_sync(0xffffffffu, v, 1, SEG);
             const uint32_t box = v + __funnelshift_l(vl, v, 8) + __funnelshift_r(v, vr, 8);
             const uint32_t cur = qb[r + 1];
             const uint32_t nxt = life_rule(box - cur, cur);
@@ -280,9 +287,12 @@ cudaError_t launch_gol_substep(const uint8_t* in, uint8_t* out, const BlockLayou
 {
     const int wb = (L.xoff + 1) >> 2;
     const int we = (L.xoff + L.n[0] - 2) >> 2;              // last word with an updatable cell
-    const int ntx = (we - wb + 1 + kOutWords - 1) / kOutWords;
+    const int nw = we - wb + 1;
+    const bool seg16 = ((nw + 13) / 14) * 16 < ((nw + 29) / 30) * 32;
+    const int out_words = seg16 ? 14 : 30, rows_per_warp = seg16 ? 2 * kRY : kRY;
+    const int ntx = (nw + out_words - 1) / out_words;
     const int rows = L.n[1] - 2;
-    const int nty = (rows + kRY * kGolWarps - 1) / (kRY * kGolWarps);
+    const int nty = (rows + rows_per_warp * kGolWarps - 1) / (rows_per_warp * kGolWarps);
     const long long tiles = (long long)ntx * nty * L.nblk;
     // small blocks are latency bound (a generation of a 136^3 block is a few
     // microseconds of data): short z chunks, many CTAs
@@ -292,7 +302,8 @@ cudaError_t launch_gol_substep(const uint8_t* in, uint8_t* out, const BlockLayou
     if (nzc > maxc) nzc = maxc;
     if (nzc < 1) nzc = 1;
     dim3 grid(ntx, nty, L.nblk * nzc);
-    gol_kernel<<<grid, 32 * kGolWarps, 0, st>>>(in, out, L, step_i, nzc);
+    if (seg16) gol_kernel<16><<<grid, 32 * kGolWarps, 0, st>>>(in, out, L, step_i, nzc);
+    else gol_kernel<32><<<grid, 32 * kGolWarps, 0, st>>>(in, out, L, step_i, nzc);
     count_launches(1);
     return cudaGetLastError();
 }
