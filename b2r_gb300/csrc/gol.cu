@@ -30,15 +30,18 @@ constexpr int kGolWarps = 4;     // warps per CTA, stacked in y
 
 __device__ __forceinline__ uint32_t ldw(const uint32_t* p) { return __ldg(p); }
 
-// Per-byte rule on counts (0..26) and current states (0/1).
+// Per-byte rule on counts (0..26) and current states (0/1), in plain 32-bit
+// logic: for a byte v < 128, (v + 0x7F) has bit 7 set iff v != 0, with no
+// carry into the next byte.  Survive: live and n >= 2 (bits 1..4 of n not
+// all zero) and n < 8 (bits 3..4 zero); birth: dead and n == 5.
 __device__ __forceinline__ uint32_t life_rule(uint32_t cnt, uint32_t cur)
 {
-    const uint32_t alive = cur * 0xFFu;                    // 0x00/0xFF per byte
-    const uint32_t le1 = __vcmpleu4(cnt, 0x01010101u);
-    const uint32_t ge8 = __vcmpgeu4(cnt, 0x08080808u);
-    const uint32_t eq5 = __vcmpeq4(cnt, 0x05050505u);
-    const uint32_t nxt = (alive & ~(le1 | ge8)) | (~alive & eq5);
-    return nxt & 0x01010101u;
+    const uint32_t ge2 = ((cnt & 0x1E1E1E1Eu) + 0x7F7F7F7Fu) & 0x80808080u;
+    const uint32_t ge8 = ((cnt & 0x18181818u) + 0x7F7F7F7Fu) & 0x80808080u;
+    const uint32_t ne5 = ((cnt ^ 0x05050505u) + 0x7F7F7F7Fu) & 0x80808080u;
+    const uint32_t cur7 = cur << 7;
+    const uint32_t nxt7 = (cur7 & ge2 & ~ge8) | (~cur7 & ~ne5 & 0x80808080u);
+    return nxt7 >> 7;
 }
 
 // SEG = lanes per x segment: 32 (one segment per warp, 30 output words), or
