@@ -29,7 +29,7 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libb2r.so")
 MODEL_HEAT, MODEL_GOL, MODEL_EQWP_REF, MODEL_EQWP_STAG = 1, 2, 3, 4
 BC_SHELL, BC_PERIODIC = 0, 1
 FIELDS = {"vx": 0, "vy": 1, "vz": 2, "sxx": 3, "sxy": 4, "sxz": 5, "syy": 6, "syz": 7,
-          "szz": 8, "disp": 9, "lambda": 16, "mu": 17, "buoy": 18}
+          "szz": 8, "disp": 9, "lambda": 16, "mu": 17, "buoy": 18, "kappa": 19}
 _STATUS = {0: "B2R_OK", 1: "B2R_ERR_ARG", 2: "B2R_ERR_CUDA", 3: "B2R_ERR_OOM",
            4: "B2R_ERR_TIMEOUT", 5: "B2R_ERR_STATE"}
 
@@ -96,6 +96,9 @@ def lib():
         "b2r_eqwp_misfit_gradient": ([vp, i, i, C.POINTER(C.c_int), C.POINTER(C.c_float), i,
                                       C.POINTER(d), C.POINTER(d), C.POINTER(d), C.POINTER(d),
                                       C.POINTER(C.c_float)], i),
+        "b2r_heat_record": ([vp, i, i, C.POINTER(C.c_int), C.POINTER(C.c_float)], i),
+        "b2r_heat_misfit_gradient": ([vp, i, i, C.POINTER(C.c_int), C.POINTER(C.c_float), i,
+                                      C.POINTER(d), C.POINTER(d), C.POINTER(C.c_float)], i),
         "b2r_batch_create": ([C.POINTER(BatchItem), i, C.POINTER(vp)], i),
         "b2r_batch_destroy": ([vp], i),
         "b2r_batch_last_error": ([], C.c_char_p),
@@ -275,6 +278,29 @@ class Domain:
         _check(lib().b2r_eqwp_record(self.h, nsteps, len(rec), rec.ctypes.data_as(C.POINTER(C.c_int)),
                                      out.ctypes.data_as(C.POINTER(C.c_float))), self.h)
         return out
+
+    def heat_record(self, nsteps, rec_xyz):
+        """u at receivers (global interior x, y, z) after every step of the
+        conductivity-scaled heat scheme: (nsteps, nrec)."""
+        rec = np.ascontiguousarray(rec_xyz, np.int32).reshape(-1, 3)
+        out = np.empty((nsteps, len(rec)), np.float32)
+        _check(lib().b2r_heat_record(self.h, nsteps, len(rec), rec.ctypes.data_as(C.POINTER(C.c_int)),
+                                     out.ctypes.data_as(C.POINTER(C.c_float))), self.h)
+        return out
+
+    def heat_misfit_gradient(self, nsteps, rec_xyz, d_obs, ckpt_every=50):
+        """(J, g_kappa, d_syn): the gradient is an env-shaped FP64 array (z, y, x)."""
+        rec = np.ascontiguousarray(rec_xyz, np.int32).reshape(-1, 3)
+        obs = np.ascontiguousarray(d_obs, np.float32)
+        g = np.empty(tuple(self.cfg.env)[::-1], np.float64)
+        J = C.c_double()
+        syn = np.empty((nsteps, len(rec)), np.float32)
+        dp = C.POINTER(C.c_double)
+        _check(lib().b2r_heat_misfit_gradient(
+            self.h, nsteps, len(rec), rec.ctypes.data_as(C.POINTER(C.c_int)),
+            obs.ctypes.data_as(C.POINTER(C.c_float)), ckpt_every, C.byref(J), g.ctypes.data_as(dp),
+            syn.ctypes.data_as(C.POINTER(C.c_float))), self.h)
+        return J.value, g, syn
 
     def eqwp_misfit_gradient(self, nsteps, rec_xyz, d_obs, ckpt_every=50):
         """(J, (g_lambda, g_mu, g_rho), d_syn): gradients are env-shaped FP64 arrays (z, y, x)."""

@@ -11,7 +11,7 @@ differences; the computation itself runs entirely in libb2r.
 import numpy as np
 import torch
 
-from . import MODEL_EQWP_STAG, Domain
+from . import MODEL_EQWP_STAG, MODEL_HEAT, Domain
 
 
 def _padded(a, H):
@@ -44,3 +44,29 @@ class EqwpMisfit(torch.autograd.Function):
     def backward(ctx, gJ):
         gl, gm, gr = ctx.saved_tensors
         return gJ * gl, gJ * gm, gJ * gr, None
+
+
+class HeatMisfit(torch.autograd.Function):
+    """``HeatMisfit.apply(kappa, problem)``: receiver misfit of the
+    conductivity-scaled heat scheme (b2r_heat_record) as a 0-d tensor, with
+    dJ/dkappa from the library's discrete adjoint (b2r_heat_misfit_gradient).
+    kappa: env-shaped (z, y, x) CPU tensor of the interior cells; problem:
+    dict with env, D, coef (alpha_dt, dx, dy, dz), u0 (domain array with its
+    D-deep shell), nsteps, rec, d_obs and optionally ckpt_every."""
+
+    @staticmethod
+    def forward(ctx, kappa, problem):
+        P = problem
+        a, dx, dy, dz = P["coef"]
+        with Domain(MODEL_HEAT, P["env"], D=P["D"], R=1, alpha_dt=a, dx=dx, dy=dy, dz=dz) as d:
+            d.upload(np.ascontiguousarray(_padded(kappa.detach().cpu().numpy(), P["D"]), np.float32),
+                     field="kappa")
+            d.upload(np.ascontiguousarray(P["u0"], np.float32))
+            J, g, _ = d.heat_misfit_gradient(P["nsteps"], P["rec"], P["d_obs"], P.get("ckpt_every", 50))
+        ctx.save_for_backward(torch.from_numpy(g))
+        return torch.tensor(J, dtype=torch.float64)
+
+    @staticmethod
+    def backward(ctx, gJ):
+        (g,) = ctx.saved_tensors
+        return gJ * g, None

@@ -151,6 +151,17 @@ size_t domain_cells(const b2r_handle* h)
     return c;
 }
 
+
+// the heat model's conductivity field, allocated on first use and set to 1
+b2r_status ensure_kappa(b2r_handle* h)
+{
+    if (h->mat[0]) return B2R_OK;
+    const size_t fb = field_bytes(h);
+    CK(h, cudaMalloc(&h->mat[0], fb));
+    CK(h, launch_fill(h->mat[0], fb / sizeof(float), 1.0f, h->stream));
+    return B2R_OK;
+}
+
 b2r_status ensure_staging(b2r_handle* h, size_t bytes)
 {
     if (h->staging_bytes >= bytes) return B2R_OK;
@@ -607,20 +618,28 @@ b2r_status b2r_upload(b2r_handle* h, int field, const void* src, int src_is_devi
 {
     if (!h || !src) return fail(h, B2R_ERR_ARG, "null argument");
     const bool eq = h->nfld > 0;
+    const bool is_kappa = field == B2R_F_KAPPA;
     const bool is_mat = eq && field >= B2R_F_LAMBDA && field <= B2R_F_BUOY;
-    if (!is_mat && (field < 0 || field >= (eq ? h->nfld : 1)))
+    if (is_kappa && h->cfg.model != B2R_MODEL_HEAT)
+        return fail(h, B2R_ERR_ARG, "the conductivity field exists only for the heat model");
+    if (!is_mat && !is_kappa && (field < 0 || field >= (eq ? h->nfld : 1)))
         return fail(h, B2R_ERR_ARG, "invalid field id %d", field);
     if (is_mat && h->cfg.model != B2R_MODEL_EQWP_STAG)
         return fail(h, B2R_ERR_ARG, "material fields exist only for the staggered model");
     const size_t bytes = domain_cells(h) * h->cell_bytes;
     const void* dsrc = src;
     b2r_status st;
+    if (is_kappa && (st = ensure_kappa(h)) != B2R_OK) return st;
     if (!src_is_device) {
         if ((st = ensure_staging(h, bytes)) != B2R_OK) return st;
         CK(h, cudaMemcpyAsync(h->staging, src, bytes, cudaMemcpyHostToDevice, h->stream));
         dsrc = h->staging;
     }
     void* dst;
+    if (is_kappa) {
+        CK(h, launch_scatter<float>(static_cast<const float*>(dsrc), h->mat[0], h->L, h->shell, h->stream));
+        return B2R_OK;
+    }
     if (is_mat) dst = h->mat[field - B2R_F_LAMBDA];
     else if (eq) dst = h->fld[field];
     else dst = h->buf[h->cur];
@@ -1075,6 +1094,145 @@ b2r_status b2r_eqwp_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const i
     CK(h, cudaStreamSynchronize(h->stream));
     h->ts = nsteps;
     h->halos_fresh = false;
+    return check_status(h);
+}
+
+namespace {
+
+b2r_status heat_adj_check(b2r_handle* h)
+{
+    if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
+    if (h->cfg.model != B2R_MODEL_HEAT) return fail(h, B2R_ERR_ARG, "the heat adjoint needs the heat model");
+    if (h->L.nblk != 1 || h->L.periodic)
+        return fail(h, B2R_ERR_ARG, "the heat adjoint runs on one block with a fixed shell");
+    return ensure_kappa(h);
+}
+
+HeatLap heat_lap_of(const b2r_handle* h)
+{
+    return heat_lap(h->cfg.D, h->cfg.alpha_dt, h->cfg.dx, h->cfg.dy, h->cfg.dz);
+}
+
+}  // namespace
+
+b2r_status b2r_heat_record(b2r_handle* h, int nsteps, int nrec, const int* rec_xyz, float* d_out)
+{
+    b2r_status st;
+    if ((st = heat_adj_check(h)) != B2R_OK) return st;
+    if (nsteps < 0 || nrec <= 0 || !rec_xyz || !d_out) return fail(h, B2R_ERR_ARG, "invalid receivers");
+    std::vector<long long> idx;
+    if ((st = rec_offsets(h, nrec, rec_xyz, idx)) != B2R_OK) return st;
+    DevBuf d_idx, d_rec;
+    CK(h, cudaMalloc(&d_idx.p, sizeof(long long) * nrec));
+    CK(h, cudaMalloc(&d_rec.p, sizeof(float) * (size_t)nrec * (nsteps > 0 ? nsteps : 1)));
+    CK(h, cudaMemcpyAsync(d_idx.p, idx.data(), sizeof(long long) * nrec, cudaMemcpyHostToDevice, h->stream));
+    const HeatLap c = heat_lap_of(h);
+    for (int n = 0; n < nsteps; ++n) {
+        float* in = static_cast<float*>(h->buf[h->cur]);
+        float* out = static_cast<float*>(h->buf[1 - h->cur]);
+        CK(h, launch_heat_kappa_step(in, out, h->mat[0], h->L, h->cfg.D, c, h->stream));
+        h->cur = 1 - h->cur;
+        CK(h, adjoint_sample(out, (const long long*)d_idx.p, nrec, (float*)d_rec.p + (size_t)n * nrec, h->stream));
+    }
+    h->ts += nsteps;
+    CK(h, cudaMemcpyAsync(d_out, d_rec.p, sizeof(float) * (size_t)nrec * nsteps, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return check_status(h);
+}
+
+b2r_status b2r_heat_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const int* rec_xyz,
+                                    const float* d_obs, int ckpt_every, double* misfit,
+                                    double* grad_kappa, float* d_syn)
+{
+    b2r_status st;
+    if ((st = heat_adj_check(h)) != B2R_OK) return st;
+    if (nsteps <= 0 || nrec <= 0 || !rec_xyz || !d_obs) return fail(h, B2R_ERR_ARG, "invalid receivers / steps");
+    const int K = ckpt_every > 0 ? ckpt_every : nsteps;
+    std::vector<long long> idx;
+    if ((st = rec_offsets(h, nrec, rec_xyz, idx)) != B2R_OK) return st;
+    const size_t fb = field_bytes(h);
+    const size_t nseg = (size_t)(nsteps + K - 1) / K;
+    // workspace on the handle: checkpoints, replay slots 1..K, lam, y, FP64 gradient
+    const size_t fba = (fb + 255) & ~(size_t)255;
+    const size_t gba = ((size_t)h->L.bstride * sizeof(double) + 255) & ~(size_t)255;
+    const size_t need = (nseg + (size_t)K + 1 + 2) * fba + gba;
+    if (h->adj_ws_bytes < need) {
+        if (h->adj_ws) cudaFree(h->adj_ws);
+        h->adj_ws = nullptr;
+        h->adj_ws_bytes = 0;
+        if (cudaMalloc(&h->adj_ws, need) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(h, B2R_ERR_OOM, "heat gradient needs %zu bytes of workspace", need);
+        }
+        h->adj_ws_bytes = need;
+    }
+    char* ws = static_cast<char*>(h->adj_ws);
+    std::vector<float*> ckpt(nseg), slot((size_t)K + 1);
+    for (auto& p : ckpt) p = reinterpret_cast<float*>(ws), ws += fba;
+    for (auto& p : slot) p = reinterpret_cast<float*>(ws), ws += fba;
+    float* lam = reinterpret_cast<float*>(ws);
+    ws += fba;
+    float* yb = reinterpret_cast<float*>(ws);
+    ws += fba;
+    double* g = reinterpret_cast<double*>(ws);
+    CK(h, cudaMemsetAsync(lam, 0, fb, h->stream));
+    CK(h, cudaMemsetAsync(yb, 0, fb, h->stream));
+    CK(h, cudaMemsetAsync(g, 0, (size_t)h->L.bstride * sizeof(double), h->stream));
+    // shell cells never change: every replay slot starts as the initial state
+    for (size_t k = 1; k < slot.size(); ++k)
+        CK(h, cudaMemcpyAsync(slot[k], h->buf[h->cur], fb, cudaMemcpyDeviceToDevice, h->stream));
+    DevBuf d_idx, d_rec, d_res;
+    CK(h, cudaMalloc(&d_idx.p, sizeof(long long) * nrec));
+    CK(h, cudaMalloc(&d_rec.p, sizeof(float) * (size_t)nrec * nsteps));
+    CK(h, cudaMalloc(&d_res.p, sizeof(float) * (size_t)nrec * nsteps));
+    CK(h, cudaMemcpyAsync(d_idx.p, idx.data(), sizeof(long long) * nrec, cudaMemcpyHostToDevice, h->stream));
+    const long long* didx = (const long long*)d_idx.p;
+    const HeatLap c = heat_lap_of(h);
+    const int D = h->cfg.D;
+
+    // forward with checkpoints and receiver samples
+    for (int n = 0; n < nsteps; ++n) {
+        float* in = static_cast<float*>(h->buf[h->cur]);
+        float* out = static_cast<float*>(h->buf[1 - h->cur]);
+        if (n % K == 0) CK(h, cudaMemcpyAsync(ckpt[n / K], in, fb, cudaMemcpyDeviceToDevice, h->stream));
+        CK(h, launch_heat_kappa_step(in, out, h->mat[0], h->L, D, c, h->stream));
+        h->cur = 1 - h->cur;
+        CK(h, adjoint_sample(out, didx, nrec, (float*)d_rec.p + (size_t)n * nrec, h->stream));
+    }
+    std::vector<float> syn((size_t)nrec * nsteps), res((size_t)nrec * nsteps);
+    CK(h, cudaMemcpyAsync(syn.data(), d_rec.p, sizeof(float) * syn.size(), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    double J = 0.0;
+    for (size_t i = 0; i < syn.size(); ++i) {
+        const double r = (double)syn[i] - (double)d_obs[i];
+        res[i] = (float)r;
+        J += 0.5 * r * r;
+    }
+    if (misfit) *misfit = J;
+    if (d_syn) std::copy(syn.begin(), syn.end(), d_syn);
+    CK(h, cudaMemcpyAsync(d_res.p, res.data(), sizeof(float) * res.size(), cudaMemcpyHostToDevice, h->stream));
+
+    // reverse sweep, segment by segment with recomputation
+    for (long long sgi = (long long)nseg - 1; sgi >= 0; --sgi) {
+        const int n0 = (int)sgi * K;
+        const int n1 = std::min(nsteps, n0 + K);
+        auto u_at = [&](int k) -> float* { return k == 0 ? ckpt[sgi] : slot[(size_t)k]; };
+        for (int n = n0; n < n1; ++n)
+            CK(h, launch_heat_kappa_step(u_at(n - n0), u_at(n - n0 + 1), h->mat[0], h->L, D, c, h->stream));
+        for (int n = n1 - 1; n >= n0; --n) {
+            CK(h, adjoint_inject(lam, didx, nrec, (const float*)d_res.p + (size_t)n * nrec, h->stream));
+            CK(h, launch_heat_adjoint_step(lam, yb, u_at(n - n0), h->mat[0], g, h->L, D, c, h->stream));
+        }
+    }
+    if (grad_kappa) {
+        const size_t ncell = (size_t)h->cfg.env[0] * h->cfg.env[1] * h->cfg.env[2];
+        DevBuf d_out;
+        CK(h, cudaMalloc(&d_out.p, ncell * sizeof(double)));
+        CK(h, adjoint_grad_out(g, nullptr, 0, h->L, (double*)d_out.p, h->stream));
+        CK(h, cudaMemcpyAsync(grad_kappa, d_out.p, ncell * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    }
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->ts = nsteps;
     return check_status(h);
 }
 

@@ -11,6 +11,22 @@ struct HeatCoef {
 };
 
 HeatCoef heat_coef(int D, double alpha_dt, double dx, double dy, double dz);
+
+// heat_adjoint.cu: the Laplacian of order 2D times alpha*dt/dx^2 per axis,
+// L u = w0*u + sum_k wx[k-1]*(u[x-k]+u[x+k]) + ...; the conductivity-scaled
+// step u' = u + kappa * L u on the interior window of one block, and one
+// reverse step of its adjoint (lam: adjoint of u^{n+1}, updated to that of
+// u^n; yb: scratch, zero outside the window; g += lam * L u^n in FP64).
+struct HeatLap {
+    float w0;
+    float wx[4], wy[4], wz[4];
+};
+HeatLap heat_lap(int D, double alpha_dt, double dx, double dy, double dz);
+cudaError_t launch_heat_kappa_step(const float* in, float* out, const float* kappa, const BlockLayout& L, int D,
+                                   const HeatLap& c, cudaStream_t st);
+cudaError_t launch_heat_adjoint_step(float* lam, float* yb, const float* u, const float* kappa, double* g,
+                                     const BlockLayout& L, int D, const HeatLap& c, cudaStream_t st);
+cudaError_t launch_fill(float* p, size_t n, float v, cudaStream_t st);
 // TMA box of one ring slot (cells): width and height for radius D.
 int heat_box_w();
 int heat_box_h(int D);

@@ -51,7 +51,9 @@ typedef enum { B2R_BC_SHELL = 0, B2R_BC_PERIODIC = 1 } b2r_boundary;
 enum {
     B2R_F_VX = 0, B2R_F_VY, B2R_F_VZ, B2R_F_SXX, B2R_F_SXY, B2R_F_SXZ,
     B2R_F_SYY, B2R_F_SYZ, B2R_F_SZZ, B2R_F_DISP,      /* 9: displacement (REF) */
-    B2R_F_LAMBDA = 16, B2R_F_MU = 17, B2R_F_BUOY = 18 /* material (STAG) */
+    B2R_F_LAMBDA = 16, B2R_F_MU = 17, B2R_F_BUOY = 18, /* material (STAG) */
+    B2R_F_KAPPA = 19                                   /* heat: conductivity of the
+                                                          differentiable form (default 1) */
 };
 
 typedef struct {
@@ -216,6 +218,25 @@ b2r_status b2r_eqwp_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const i
                                     const float* d_obs, int ckpt_every, double* misfit,
                                     double* grad_lambda, double* grad_mu, double* grad_rho,
                                     float* d_syn);
+
+/* ---- heat adjoint (no reference counterpart) ------------------------------ *
+ * The differentiable heat step scales the stencil of fdm_heat_diffuse_deltaD
+ * (heat-3D.cu:173-521) by a per-cell conductivity kappa (field
+ * B2R_F_KAPPA, 1 everywhere unless uploaded): u' = u + kappa * (L u) on the
+ * interior, with L the order-2D Laplacian times alpha*dt/dx^2 per axis.
+ * b2r_step keeps the plain scheme; these two calls use kappa.  One block,
+ * fixed shell (B2R_BC_SHELL), model B2R_MODEL_HEAT. */
+/* Forward nsteps from the current field, recording u at nrec receivers after
+ * every step into d_out[nsteps*nrec] (host). */
+b2r_status b2r_heat_record(b2r_handle* h, int nsteps, int nrec, const int* rec_xyz, float* d_out);
+/* Misfit J = 1/2 sum (d_syn - d_obs)^2 of that recording and dJ/dkappa per
+ * interior cell (host, env cells, x fastest, FP64), by the discrete adjoint
+ * backward in time with checkpoints every ckpt_every steps (<= 0: once) and
+ * recomputation in between; FP64 accumulation.  d_syn may be NULL.  The
+ * field ends in an unspecified state. */
+b2r_status b2r_heat_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const int* rec_xyz,
+                                    const float* d_obs, int ckpt_every, double* misfit,
+                                    double* grad_kappa, float* d_syn);
 
 /* ---- batched instances (no reference counterpart) ------------------------ */
 /* Many independent single-block heat domains of uneven sizes and stencil

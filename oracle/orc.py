@@ -300,3 +300,76 @@ def eqwp_stag_gradient(fields, mat, dt, dx, H, src_xyz, amps, rec, nsteps, d_obs
         eqwp_stag_adjoint_step(tmp, fv, fs, mat, g, dt / dx, lo, hi)
     g_rho = -g[2] * mat[2] ** 2
     return J, (g[0], g[1], g_rho), d, tmp
+
+
+# ---------------------------------------------------------------- heat adjoint
+# Differentiable heat step (new behaviour, no reference counterpart): the
+# stencil of fdm_heat_diffuse_deltaD (heat-3D.cu:15-28, weights of
+# heat-3D.cu:173-521) scaled per cell by a conductivity kappa,
+#   u^{n+1} = u^n + kappa * L u^n  on the interior window [D, n-1-D] (one block,
+# fixed shell), L u = w0 u + sum_k wx_k (u[x+k] + u[x-k]) + wy_k (...) + wz_k (...).
+_HEAT_CW = [[0, 0, 0, 0, 0],
+            [-2.0, 1.0, 0, 0, 0],
+            [-5.0 / 2.0, 4.0 / 3.0, -1.0 / 12.0, 0, 0],
+            [-49.0 / 18.0, 3.0 / 2.0, -3.0 / 20.0, 1.0 / 90.0, 0],
+            [-205.0 / 72.0, 8.0 / 5.0, -1.0 / 5.0, 8.0 / 315.0, -1.0 / 560.0]]
+
+
+def heat_lap_weights(D, alpha_dt, dx, dy, dz):
+    """(w0, wx[D], wy[D], wz[D]): the weights rounded to FP32 as the GPU holds
+    them, returned as FP64."""
+    wx, wy, wz = alpha_dt / (dx * dx), alpha_dt / (dy * dy), alpha_dt / (dz * dz)
+    f = lambda v: float(np.float32(v))
+    cw = _HEAT_CW[D]
+    return (f(cw[0] * (wx + wy + wz)), [f(wx * cw[k]) for k in range(1, D + 1)],
+            [f(wy * cw[k]) for k in range(1, D + 1)], [f(wz * cw[k]) for k in range(1, D + 1)])
+
+
+def heat_lap(u, D, w):
+    """L u on the window [D, n-1-D] of every axis (FP64)."""
+    w0, wx, wy, wz = w
+    nz, ny, nx = u.shape
+    c = (slice(D, nz - D), slice(D, ny - D), slice(D, nx - D))
+    out = w0 * u[c]
+    for k in range(1, D + 1):
+        out = out + wx[k - 1] * (u[D:nz - D, D:ny - D, D + k:nx - D + k] + u[D:nz - D, D:ny - D, D - k:nx - D - k])
+        out = out + wy[k - 1] * (u[D:nz - D, D + k:ny - D + k, D:nx - D] + u[D:nz - D, D - k:ny - D - k, D:nx - D])
+        out = out + wz[k - 1] * (u[D + k:nz - D + k, D:ny - D, D:nx - D] + u[D - k:nz - D - k, D:ny - D, D:nx - D])
+    return out
+
+
+def heat_kappa_record(u0, kappa, D, w, rec, nsteps):
+    """FP64 forward; rec: block coordinates (x, y, z).  (states, d[nsteps, nrec])."""
+    u = np.asarray(u0, np.float64).copy()
+    kap = np.asarray(kappa, np.float64)
+    nz, ny, nx = u.shape
+    c = (slice(D, nz - D), slice(D, ny - D), slice(D, nx - D))
+    states = [u.copy()]
+    d = np.zeros((nsteps, len(rec)))
+    for n in range(nsteps):
+        u[c] = u[c] + kap[c] * heat_lap(u, D, w)
+        for r, (x, y, z) in enumerate(rec):
+            d[n, r] = u[z, y, x]
+        states.append(u.copy())
+    return states, d
+
+
+def heat_kappa_gradient(u0, kappa, D, w, rec, nsteps, d_obs):
+    """FP64 misfit and dJ/dkappa (full block array, zero on the shell) by the
+    discrete adjoint; also returns the adjoint of u^0."""
+    states, d = heat_kappa_record(u0, kappa, D, w, rec, nsteps)
+    res = d - d_obs
+    J = 0.5 * float(np.sum(res * res))
+    kap = np.asarray(kappa, np.float64)
+    nz, ny, nx = kap.shape
+    c = (slice(D, nz - D), slice(D, ny - D), slice(D, nx - D))
+    lam = np.zeros(kap.shape)
+    g = np.zeros(kap.shape)
+    for n in range(nsteps - 1, -1, -1):
+        for r, (x, y, z) in enumerate(rec):
+            lam[z, y, x] += res[n, r]
+        g[c] += lam[c] * heat_lap(states[n], D, w)
+        y = np.zeros(kap.shape)
+        y[c] = kap[c] * lam[c]
+        lam[c] += heat_lap(y, D, w)
+    return J, g, d, lam
