@@ -109,6 +109,8 @@ def lib():
         "b2r_batch_lups": ([vp], C.c_int64),
         "b2r_batch_set_zchunk": ([vp, i], i),
         "b2r_batch_autotune": ([vp, vp, C.POINTER(C.c_int), C.POINTER(d)], i),
+        "b2r_batch_set_tile": ([vp, i], i),
+        "b2r_batch_tile": ([vp], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -378,6 +380,14 @@ class Batch:
 
     def set_zchunk(self, z):
         _bcheck(lib().b2r_batch_set_zchunk(self.h, int(z)))
+
+    def set_tile(self, width):
+        """Tile width of every instance: 128, 64, 32, or 0 for the mix's default."""
+        _bcheck(lib().b2r_batch_set_tile(self.h, int(width)))
+
+    @property
+    def tile(self):
+        return int(lib().b2r_batch_tile(self.h))
 
     def autotune(self):
         z = C.c_int()

@@ -36,13 +36,27 @@ struct RowsPerWarp {
     static constexpr int value = D <= 2 ? 2 : 1;
 };
 constexpr int cmax(int a, int b) { return a > b ? a : b; }
-constexpr int kSlot = cmax(cmax(heatk::Cfg<1, 2, kS>::SLOT, heatk::Cfg<2, 2, kS>::SLOT),
-                           cmax(heatk::Cfg<3, 1, kS>::SLOT, heatk::Cfg<4, 1, kS>::SLOT));
+// tile shapes: LPR lanes per row = 32, 16, 8 -> 128, 64, 32 cells wide
+template <int D, int LPR>
+using BCfg = heatk::Cfg<D, RowsPerWarp<D>::value, kS, 0, LPR>;
+template <int LPR>
+constexpr int slot_max()
+{
+    return cmax(cmax(BCfg<1, LPR>::SLOT, BCfg<2, LPR>::SLOT), cmax(BCfg<3, LPR>::SLOT, BCfg<4, LPR>::SLOT));
+}
+constexpr int kSlot = cmax(cmax(slot_max<32>(), slot_max<16>()), slot_max<8>());
 constexpr size_t kSmem = size_t(kS) * kSlot * sizeof(float) + kS * sizeof(uint64_t) + 16 + 128;
-constexpr int kBoxH[5] = {0, heatk::Cfg<1, 2, kS>::BH, heatk::Cfg<2, 2, kS>::BH,
-                          heatk::Cfg<3, 1, kS>::BH, heatk::Cfg<4, 1, kS>::BH};
-constexpr int kTileY[5] = {0, heatk::Cfg<1, 2, kS>::TY, heatk::Cfg<2, 2, kS>::TY,
-                           heatk::Cfg<3, 1, kS>::TY, heatk::Cfg<4, 1, kS>::TY};
+constexpr int kLpr[3] = {32, 16, 8};
+constexpr int kBoxH[5][3] = {{0, 0, 0},
+                             {BCfg<1, 32>::BH, BCfg<1, 16>::BH, BCfg<1, 8>::BH},
+                             {BCfg<2, 32>::BH, BCfg<2, 16>::BH, BCfg<2, 8>::BH},
+                             {BCfg<3, 32>::BH, BCfg<3, 16>::BH, BCfg<3, 8>::BH},
+                             {BCfg<4, 32>::BH, BCfg<4, 16>::BH, BCfg<4, 8>::BH}};
+constexpr int kTileY[5][3] = {{0, 0, 0},
+                              {BCfg<1, 32>::TY, BCfg<1, 16>::TY, BCfg<1, 8>::TY},
+                              {BCfg<2, 32>::TY, BCfg<2, 16>::TY, BCfg<2, 8>::TY},
+                              {BCfg<3, 32>::TY, BCfg<3, 16>::TY, BCfg<3, 8>::TY},
+                              {BCfg<4, 32>::TY, BCfg<4, 16>::TY, BCfg<4, 8>::TY}};
 
 struct InstDev {
     BlockLayout L;
@@ -78,7 +92,7 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
 #else
 #define B2R_UNIT_INLINE __forceinline__
 #endif
-template <int D>
+template <int D, int LPR>
 __device__ B2R_UNIT_INLINE bool run_unit(const BatchArgs& a, const InstDev& in, int k, int t, int u,
                                          heatk::Ring& rg)
 {
@@ -88,7 +102,7 @@ __device__ B2R_UNIT_INLINE bool run_unit(const BatchArgs& a, const InstDev& in, 
     const int zc = r / in.nty;
     const int zi0 = zc * in.Lz;
     const int zi1 = min(in.NZ, zi0 + in.Lz);
-    return heatk::sweep_unit<D, RowsPerWarp<D>::value, kS, kSlot>(
+    return heatk::sweep_unit<D, RowsPerWarp<D>::value, kS, kSlot, LPR>(
         &a.maps[2 * k + (t & 1)], in.buf[(t + 1) & 1], in.L, 0, in.C, 0, tx, ty, zi0, zi1, rg);
 }
 
@@ -116,6 +130,8 @@ __device__ __forceinline__ void decode(long long item, const long long* step_off
 #ifndef B2R_BATCH_MINB
 #define B2R_BATCH_MINB 2   // resident CTAs per SM the register budget is fitted to (no spills)
 #endif
+// LPR: tile shape of every instance of the launch (lanes per tile row)
+template <int LPR>
 __global__ void __launch_bounds__(kThreads, B2R_BATCH_MINB) batch_kernel(const BatchArgs a)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -176,10 +192,10 @@ __global__ void __launch_bounds__(kThreads, B2R_BATCH_MINB) batch_kernel(const B
         const InstDev& in = a.inst[k];
         bool ok;
         switch (in.D) {
-        case 1: ok = run_unit<1>(a, in, k, t, u, rg); break;
-        case 2: ok = run_unit<2>(a, in, k, t, u, rg); break;
-        case 3: ok = run_unit<3>(a, in, k, t, u, rg); break;
-        default: ok = run_unit<4>(a, in, k, t, u, rg); break;
+        case 1: ok = run_unit<1, LPR>(a, in, k, t, u, rg); break;
+        case 2: ok = run_unit<2, LPR>(a, in, k, t, u, rg); break;
+        case 3: ok = run_unit<3, LPR>(a, in, k, t, u, rg); break;
+        default: ok = run_unit<4, LPR>(a, in, k, t, u, rg); break;
         }
         if (!ok) {
             if (threadIdx.x == 0) report(a.status, DEV_TIMEOUT);
@@ -221,7 +237,8 @@ struct b2r_batch {
     int maxsteps = 0;
     long long total = 0;
     int lz_policy = 16;              // z chunk cap per unit (autotuned)
-    int grid = 0;
+    int shape = 0;                   // tile shape of every instance: index into kLpr (autotuned)
+    int grid[3] = {0, 0, 0};         // persistent grid per tile shape
     size_t smem = 0;                 // ring + schedule tables
     cudaGraphExec_t gexec = nullptr;
     cudaStream_t gstream = nullptr;
@@ -246,6 +263,60 @@ b2r_status bfail(b2r_status s, const char* msg, cudaError_t e = cudaSuccess)
     } while (0)
 
 inline int roundup(int v, int m) { return (v + m - 1) / m * m; }
+
+// cells one plane of an instance computes with tile shape s
+long long plane_cells(const b2r_batch* b, int k, int s)
+{
+    const InstDev& in = b->host[k];
+    const BlockLayout& L = in.L;
+    const int D = in.D;
+    const int X = L.xoff + L.n[0] - D - ((L.xoff + D) & ~3), Y = L.n[1] - 2 * D;
+    const int tw = 4 * kLpr[s], th = kTileY[D][s];
+    return (long long)((X + tw - 1) / tw) * tw * ((Y + th - 1) / th) * th;
+}
+
+// The tile shape for the whole mix: the fewest cells computed over every
+// instance's steps, narrow tiles paying a little for their wider skirt.
+int default_shape(const b2r_batch* b)
+{
+    static const double penalty[3] = {1.0, 1.03, 1.08};
+    int best = 0;
+    double bc = 1e300;
+    for (int s = 0; s < 3; ++s) {
+        double c = 0;
+        for (int k = 0; k < b->n; ++k)
+            c += (double)plane_cells(b, k, s) * b->host[k].NZ * b->host[k].nsteps;
+        c *= penalty[s];
+        if (c < bc - 1e-9) {
+            bc = c;
+            best = s;
+        }
+    }
+    return best;
+}
+
+b2r_status build_schedule(b2r_batch* b);
+
+// tile counts and tensor-map boxes of every instance for shape s
+b2r_status apply_shape(b2r_batch* b, int s)
+{
+    b->shape = s;
+    for (int k = 0; k < b->n; ++k) {
+        InstDev& in = b->host[k];
+        const BlockLayout& L = in.L;
+        const int D = in.D;
+        const int X = L.xoff + L.n[0] - D - ((L.xoff + D) & ~3), Y = L.n[1] - 2 * D;
+        const int tw = 4 * kLpr[s], th = kTileY[D][s];
+        in.ntx = (X + tw - 1) / tw;
+        in.nty = (Y + th - 1) / th;
+        for (int f = 0; f < 2; ++f)
+            if (!make_block_tmap(&b->maps[2 * k + f], in.buf[f], L, 4, tw + 8, kBoxH[D][s], 1))
+                return bfail(B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+    }
+    BCK(cudaMemcpy(b->d_maps, b->maps.data(), sizeof(CUtensorMap) * 2 * b->n, cudaMemcpyHostToDevice),
+        "copy tensor maps");
+    return build_schedule(b);
+}
 
 // schedule tables for the current Lz policy
 b2r_status build_schedule(b2r_batch* b)
@@ -294,7 +365,11 @@ b2r_status enqueue_run(b2r_batch* b, cudaStream_t st)
     a.maxsteps = b->maxsteps;
     a.ninst = b->n;
     a.total = b->total;
-    batch_kernel<<<b->grid, kThreads, b->smem, st>>>(a);
+    switch (b->shape) {
+    case 0: batch_kernel<32><<<b->grid[0], kThreads, b->smem, st>>>(a); break;
+    case 1: batch_kernel<16><<<b->grid[1], kThreads, b->smem, st>>>(a); break;
+    default: batch_kernel<8><<<b->grid[2], kThreads, b->smem, st>>>(a); break;
+    }
     BCK(cudaGetLastError(), "batch launch");
     return B2R_OK;
 }
@@ -354,17 +429,12 @@ b2r_status b2r_batch_create(const b2r_batch_item* items, int n, b2r_batch** out)
         in.D = D;
         in.nsteps = it.nsteps;
         in.C = heat_coef(D, it.alpha_dt, it.dx, it.dy, it.dz);
-        const int xs_begin = (L.xoff + D) & ~3;
-        in.ntx = (L.xoff + L.n[0] - D - xs_begin + heatk::kTX - 1) / heatk::kTX;
-        in.nty = (L.n[1] - 2 * D + kTileY[D] - 1) / kTileY[D];
         in.NZ = L.n[2] - 2 * D;
         const size_t fb = (size_t)L.bstride * sizeof(float);
         for (int s = 0; s < 2; ++s) {
             if (cudaMalloc(&in.buf[s], fb) != cudaSuccess)
                 return bail(bfail(B2R_ERR_OOM, "instance allocation failed"));
             cudaMemset(in.buf[s], 0, fb);
-            if (!make_block_tmap(&b->maps[2 * k + s], in.buf[s], L, 4, heatk::kTX + 8, kBoxH[D], 1))
-                return bail(bfail(B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed"));
         }
         b->maxsteps = std::max(b->maxsteps, it.nsteps);
     }
@@ -378,19 +448,24 @@ b2r_status b2r_batch_create(const b2r_batch_item* items, int n, b2r_batch** out)
         cudaMalloc(&b->d_status, sizeof(int)) != cudaSuccess)
         return bail(bfail(B2R_ERR_OOM, "batch table allocation failed"));
     cudaMemset(b->d_status, 0, sizeof(int));
-    if (cudaMemcpy(b->d_maps, b->maps.data(), sizeof(CUtensorMap) * 2 * n, cudaMemcpyHostToDevice) != cudaSuccess)
-        return bail(bfail(B2R_ERR_CUDA, "copy tensor maps"));
     // persistent grid: every resident slot
     b->smem = kSmem + sizeof(long long) * (b->maxsteps + 1 + n + 1) + sizeof(int) * (b->maxsteps + 1) + 16;
     if (b->smem > 200 * 1024) return bail(bfail(B2R_ERR_ARG, "too many time steps for the batch schedule"));
-    if (cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem) != cudaSuccess)
-        return bail(bfail(B2R_ERR_CUDA, "smem attribute"));
-    int dev = 0, sms = 0, occ = 0;
+    int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel, kThreads, b->smem);
-    b->grid = std::max(1, occ) * std::max(1, sms);
-    b2r_status st = build_schedule(b);
+    {
+        const void* fns[3] = {(const void*)batch_kernel<32>, (const void*)batch_kernel<16>,
+                              (const void*)batch_kernel<8>};
+        for (int s = 0; s < 3; ++s) {
+            int occ = 0;
+            if (cudaFuncSetAttribute(fns[s], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem) != cudaSuccess)
+                return bail(bfail(B2R_ERR_CUDA, "smem attribute"));
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fns[s], kThreads, b->smem);
+            b->grid[s] = std::max(1, occ) * std::max(1, sms);
+        }
+    }
+    b2r_status st = apply_shape(b, default_shape(b));
     if (st != B2R_OK) return bail(st);
     if (cudaDeviceSynchronize() != cudaSuccess) return bail(bfail(B2R_ERR_CUDA, "batch set-up failed"));
     *out = b;
@@ -522,9 +597,11 @@ b2r_status b2r_batch_autotune(b2r_batch* b, void* stream, int* best_zchunk, doub
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best = 1e30f;
-    int bestz = b->lz_policy;
+    int bestz = b->lz_policy, bests = b->shape;
     b2r_status s = B2R_OK;
-    for (int z : cands) {
+    for (int c = 0; c < 3 * 5 && s == B2R_OK; ++c) {
+        const int sh = c / 5, z = cands[c % 5];
+        if (sh != b->shape && (s = apply_shape(b, sh)) != B2R_OK) break;
         if ((s = b2r_batch_set_zchunk(b, z)) != B2R_OK) break;
         for (int k = 0; k < b->n; ++k)
             cudaMemcpyAsync(b->host[k].buf[0], save[k], (size_t)b->host[k].L.bstride * sizeof(float),
@@ -538,6 +615,7 @@ b2r_status b2r_batch_autotune(b2r_batch* b, void* stream, int* best_zchunk, doub
         if (ms < best) {
             best = ms;
             bestz = z;
+            bests = sh;
         }
     }
     cudaEventDestroy(e0);
@@ -551,7 +629,24 @@ b2r_status b2r_batch_autotune(b2r_batch* b, void* stream, int* best_zchunk, doub
     if (s != B2R_OK) return s;
     if (best_zchunk) *best_zchunk = bestz;
     if (best_ms) *best_ms = best;
+    if ((s = apply_shape(b, bests)) != B2R_OK) return s;
     return b2r_batch_set_zchunk(b, bestz);
 }
+
+b2r_status b2r_batch_set_tile(b2r_batch* b, int width)
+{
+    if (!b) return bfail(B2R_ERR_ARG, "null batch");
+    int s;
+    switch (width) {
+    case 0: s = default_shape(b); break;
+    case 128: s = 0; break;
+    case 64: s = 1; break;
+    case 32: s = 2; break;
+    default: return bfail(B2R_ERR_ARG, "tile width must be 128, 64, 32 or 0");
+    }
+    return apply_shape(b, s);
+}
+
+int b2r_batch_tile(const b2r_batch* b) { return b ? 4 * kLpr[b->shape] : 0; }
 
 }  // extern "C"

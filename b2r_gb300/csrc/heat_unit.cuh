@@ -23,11 +23,15 @@ constexpr int kTX = 128;     // tile width (cells): 32 lanes x float4
 constexpr int kWarps = 8;
 constexpr int kThreads = 32 * kWarps;
 
-// ring geometry for radius D, RY rows per warp, S slots of SLOT floats
-template <int D, int RY, int S, int SLOT_ = 0>
+// ring geometry for radius D, RY row slots per warp, S slots of SLOT floats,
+// LPR lanes per tile row: a tile is 4*LPR cells wide (128, 64 or 32) and a
+// warp covers 32/LPR rows per row slot
+template <int D, int RY, int S, int SLOT_ = 0, int LPR = 32>
 struct Cfg {
-    static constexpr int TY = kWarps * RY;
-    static constexpr int BW = kTX + 8;       // 4-cell skirt on both sides (D <= 4)
+    static constexpr int TXW = 4 * LPR;
+    static constexpr int RPW = 32 / LPR;
+    static constexpr int TY = kWarps * RY * RPW;
+    static constexpr int BW = TXW + 8;       // 4-cell skirt on both sides (D <= 4)
     static constexpr int BH = TY + 2 * D;
     static constexpr int PLANE = BW * BH;    // floats of one tile plane
     static constexpr int SLOT = SLOT_ > 0 ? SLOT_ : (PLANE + 31) / 32 * 32;   // 128-byte aligned
@@ -73,20 +77,23 @@ __device__ __forceinline__ void ring_drain(const Ring& rg)
 
 // Sweep one unit.  Returns false if a bounded wait gave up (all threads
 // agree: the decision is taken after a __syncthreads on a shared flag).
-template <int D, int RY, int S, int SLOT>
+template <int D, int RY, int S, int SLOT, int LPR = 32>
 __device__ __forceinline__ bool sweep_unit(const CUtensorMap* tmap, float* __restrict__ out,
                                            const BlockLayout& L, int step_i, const HeatCoef& C,
                                            int blk, int tx, int ty, int zi0, int zi1, Ring& rg)
 {
-    using G = Cfg<D, RY, S, SLOT>;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    using G = Cfg<D, RY, S, SLOT, LPR>;
+    constexpr int kTXW = G::TXW, kRPW = G::RPW;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int lane = (tid & 31) % LPR;        // x group of this thread in its row
+    const int sr = (tid & 31) / LPR;          // row of this thread within a row slot
     const int edge = edge_bits(L, blk);
     int lo[3], hi[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) stage_region(L, edge, a, D * (step_i + 1), lo[a], hi[a]);
-    const int xs0 = ((L.xoff + D) & ~3) + tx * kTX;      // storage x of tile column 0
+    const int xs0 = ((L.xoff + D) & ~3) + tx * kTXW;     // storage x of tile column 0
     const int y0 = D + ty * G::TY;                       // block y of tile row 0
-    if (xs0 - L.xoff > hi[0] || xs0 + kTX - 1 - L.xoff < lo[0]) return true;
+    if (xs0 - L.xoff > hi[0] || xs0 + kTXW - 1 - L.xoff < lo[0]) return true;
     if (y0 > hi[1] || y0 + G::TY - 1 < lo[1]) return true;
     const int zs = max(D + zi0, lo[2]);
     const int ze = min(D + zi1 - 1, hi[2]);
@@ -127,7 +134,7 @@ __device__ __forceinline__ bool sweep_unit(const CUtensorMap* tmap, float* __res
         for (int r2 = 0; r2 < RY; ++r2) {
 #pragma unroll
             for (int k = 0; k < 2 * D; ++k) q[r2][k] = q[r2][k + 1];
-            const int row = D + warp * RY + r2;
+            const int row = D + (warp * RY + r2) * kRPW + sr;
             q[r2][2 * D] = *reinterpret_cast<const float4*>(pl + row * G::BW + 4 + 4 * lane);
         }
         if (pr >= 2 * D && vx_any) {
@@ -135,9 +142,9 @@ __device__ __forceinline__ bool sweep_unit(const CUtensorMap* tmap, float* __res
             const float* pc = rg.smem + ((g - D) % S) * SLOT;
 #pragma unroll
             for (int r2 = 0; r2 < RY; ++r2) {
-                const int y = y0 + warp * RY + r2;
+                const int y = y0 + (warp * RY + r2) * kRPW + sr;
                 if (y < lo[1] || y > hi[1]) continue;
-                const int row = D + warp * RY + r2;
+                const int row = D + (warp * RY + r2) * kRPW + sr;
                 const float* prow = pc + row * G::BW + 4 * lane;
                 const float4 xl = *reinterpret_cast<const float4*>(prow);
                 const float4 c4 = q[r2][D];

@@ -344,6 +344,7 @@ def run_batch(args, wl):
     for i, a in enumerate(ins):
         bt.upload(i, a)
     tuned = bt.autotune()
+    tuned_tile = bt.tile
     lups = bt.lups
     for _ in range(args.warmup):
         bt.run()
@@ -398,7 +399,7 @@ def run_batch(args, wl):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded U[0,1))",
             "config": {"workload": args.workload, "instances": len(items), "lups_per_step": lups,
-                       "autotuned_zchunk": tuned[0],
+                       "autotuned_zchunk": tuned[0], "autotuned_tile_width": tuned_tile,
                        "sequential_plain_glups": round(seq, 3),
                        "batched_over_sequential": round(value / seq, 3),
                        "max_rel_l2_vs_sequential": max_rel,

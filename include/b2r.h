@@ -273,8 +273,15 @@ b2r_status b2r_batch_synchronize(b2r_batch* b, void* cuda_stream);
 int64_t b2r_batch_lups(const b2r_batch* b);
 /* Planes per work unit along z (0 = whole column). */
 b2r_status b2r_batch_set_zchunk(b2r_batch* b, int zchunk);
-/* Time whole runs with each z-chunk candidate (8, 16, 32, 64, whole column)
- * on the uploaded inputs, keep the fastest and restore the inputs. */
+/* Tile shape of every instance: 128 x 16, 64 x 32 or 32 x 64 cells (x by
+ * y, for D <= 2; half the rows for D >= 3), by width 128, 64 or 32; 0 picks
+ * the shape that computes the fewest cells over the whole mix (the default
+ * at creation).  b2r_batch_tile returns the current width. */
+b2r_status b2r_batch_set_tile(b2r_batch* b, int width);
+int b2r_batch_tile(const b2r_batch* b);
+/* Time whole runs with each tile shape x z-chunk candidate (8, 16, 32, 64,
+ * whole column) on the uploaded inputs, keep the fastest and restore the
+ * inputs. */
 b2r_status b2r_batch_autotune(b2r_batch* b, void* cuda_stream, int* best_zchunk, double* best_ms);
 
 #ifdef __cplusplus

@@ -27,13 +27,15 @@ def inputs(items, seed):
     return out
 
 
-@pytest.mark.parametrize("graph", [False, True])
-def test_batch_matches_plain_runs(b2r, orc, graph):
+@pytest.mark.parametrize("graph,tile", [(False, 0), (True, 0), (False, 128), (True, 64), (False, 32)])
+def test_batch_matches_plain_runs(b2r, orc, graph, tile):
     import torch
     items = mix(12, 1)
     ins = inputs(items, 2)
     s = torch.cuda.Stream()
     with b2r.Batch(items, stream=s) as bt:
+        bt.set_tile(tile)
+        assert bt.tile in (128, 64, 32)
         for i, a in enumerate(ins):
             bt.upload(i, a)
         bt.run(graph=graph)
