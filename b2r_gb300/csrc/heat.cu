@@ -41,6 +41,11 @@ struct HeatSched {
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;"); }
 
+// rows per warp of the delta-4 sweep (2 for the other radii)
+#ifndef B2R_HEAT4_RY
+#define B2R_HEAT4_RY 2
+#endif
+
 // resident CTAs per SM the register budget is fitted to, by stencil radius
 template <int D>
 struct MinBlocks {
@@ -145,7 +150,7 @@ cudaError_t launch_t(const CUtensorMap* tin, float* out, const BlockLayout& L, i
 
 }  // namespace
 
-int heat_box_h(int D) { return kWarps * 2 + 2 * D; }
+int heat_box_h(int D) { return kWarps * (D == 4 ? B2R_HEAT4_RY : 2) + 2 * D; }
 int heat_box_w() { return kTX + 8; }
 
 HeatCoef heat_coef(int D, double alpha_dt, double dx, double dy, double dz)
@@ -176,7 +181,7 @@ cudaError_t launch_heat_substep(const CUtensorMap* tin, float* out, const BlockL
     case 1: return launch_t<1, 2, 4>(tin, out, L, step_i, c, status, st, tune);
     case 2: return launch_t<2, 2, 5>(tin, out, L, step_i, c, status, st, tune);
     case 3: return launch_t<3, 2, 6>(tin, out, L, step_i, c, status, st, tune);
-    case 4: return launch_t<4, 2, 7>(tin, out, L, step_i, c, status, st, tune);
+    case 4: return launch_t<4, B2R_HEAT4_RY, 7>(tin, out, L, step_i, c, status, st, tune);
     default: return cudaErrorInvalidValue;
     }
 }

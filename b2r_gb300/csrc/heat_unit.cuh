@@ -126,13 +126,13 @@ __device__ __forceinline__ bool sweep_unit(const CUtensorMap* tmap, float* __res
     float4 q[RY][2 * D + 1];
     float* const outb = out + (long long)blk * L.bstride + xs0 + 4 * lane;
 
-    // unrolled by the queue depth for D <= 3, so the queue rotation becomes
-    // register renaming instead of 2D float4 moves per row and plane (at
-    // D = 4 the unrolled loop spills and runs slower)
+    // unrolled by the queue depth, so the queue rotation becomes register
+    // renaming instead of 2D float4 moves per row and plane (not at D = 4
+    // with two rows per warp, where the unrolled loop spills)
 #ifndef B2R_SWEEP_UNROLL
 #define B2R_SWEEP_UNROLL 1
 #endif
-    constexpr int kUnroll = (B2R_SWEEP_UNROLL && D <= 3) ? 2 * D + 1 : 1;
+    constexpr int kUnroll = (B2R_SWEEP_UNROLL && (D <= 3 || RY == 1)) ? 2 * D + 1 : 1;
 #pragma unroll kUnroll
     for (int pr = 0; pr < np; ++pr) {
         const unsigned g = gp + pr;
