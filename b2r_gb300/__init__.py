@@ -211,9 +211,9 @@ class Domain:
         _check(lib().b2r_set_graphs(self.h, 1 if enable else 0), self.h)
 
     def set_tuning(self, zchunk=None, ctas_per_sm=None, pdl=None, tblock=None, zchunk2=None,
-                   eqwp_fused=None):
+                   eqwp_fused=None, gol_bytes=None):
         for key, v in ((1, zchunk), (2, ctas_per_sm), (3, pdl), (4, tblock), (5, zchunk2),
-                       (6, eqwp_fused)):
+                       (6, eqwp_fused), (7, gol_bytes)):
             if v is not None:
                 _check(lib().b2r_set_tuning(self.h, key, int(v)), self.h)
 

@@ -46,6 +46,7 @@ struct b2r_handle {
     float* fld2[kMaxFields] = {};
     StressMaps smaps[2];
     bool eqwp_fused = false;   // two-pass by default: faster on this GPU so far
+    bool gol_bytes = false;    // Game of Life: byte-SWAR kernel instead of bit-sliced cells
     float* mat[3] = {};
     std::vector<float> src;     // per-step source increment of sxx/syy/szz (STAG)
     void* staging = nullptr;
@@ -303,8 +304,12 @@ b2r_status substep(b2r_handle* h, int i)
         h->cur = 1 - h->cur;
         return B2R_OK;
     case B2R_MODEL_GOL:
-        CK(h, launch_gol_substep(static_cast<const uint8_t*>(h->buf[h->cur]),
-                                 static_cast<uint8_t*>(h->buf[1 - h->cur]), h->L, i, h->stream));
+        if (h->gol_bytes)
+            CK(h, launch_gol_substep(static_cast<const uint8_t*>(h->buf[h->cur]),
+                                     static_cast<uint8_t*>(h->buf[1 - h->cur]), h->L, i, h->stream));
+        else
+            CK(h, launch_gol_bits_substep(static_cast<const uint8_t*>(h->buf[h->cur]),
+                                          static_cast<uint8_t*>(h->buf[1 - h->cur]), h->L, i, h->stream));
         h->cur = 1 - h->cur;
         return B2R_OK;
     case B2R_MODEL_EQWP_REF: {
@@ -805,6 +810,7 @@ b2r_status b2r_set_tuning(b2r_handle* h, int key, int value)
     case B2R_TUNE_TBLOCK: h->tune.tblock = value; break;
     case B2R_TUNE_ZCHUNK2: h->tune.zchunk2 = value; break;
     case B2R_TUNE_EQWP_FUSED: h->eqwp_fused = value != 0; break;
+    case B2R_TUNE_GOL_BYTES: h->gol_bytes = value != 0; break;
     default: return fail(h, B2R_ERR_ARG, "unknown tuning key %d", key);
     }
     drop_graphs(h);

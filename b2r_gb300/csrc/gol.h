@@ -16,4 +16,9 @@ cudaError_t launch_gol_period(const uint8_t* in, uint8_t* out, const BlockLayout
                               cudaStream_t st);
 int gol_max_generations_per_pass();
 
+// gol_bits.cu: the same generation as launch_gol_substep with bit-sliced
+// cells (32 per word), identical results.
+cudaError_t launch_gol_bits_substep(const uint8_t* in, uint8_t* out, const BlockLayout& L, int step_i,
+                                   cudaStream_t st);
+
 }  // namespace b2r

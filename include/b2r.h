@@ -125,8 +125,10 @@ enum {
                                   four generations (never across a halo exchange) per pass;
                                   1 = one step per pass */
     B2R_TUNE_ZCHUNK2 = 5,      /* planes per work unit of the two-step sweep (0 = 16) */
-    B2R_TUNE_EQWP_FUSED = 6    /* staggered elastic wave: 1 = one-pass step, 0 = the velocity
+    B2R_TUNE_EQWP_FUSED = 6,   /* staggered elastic wave: 1 = one-pass step, 0 = the velocity
                                   and stress stages as two passes (default); bit-identical */
+    B2R_TUNE_GOL_BYTES = 7     /* Game of Life one-generation kernel: 0 = bit-sliced cells
+                                  (default), 1 = four byte cells per word; identical results */
 };
 b2r_status b2r_set_tuning(b2r_handle* h, int key, int value);
 /* Time every schedule candidate (z-chunk length x persistent CTAs per SM x

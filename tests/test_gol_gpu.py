@@ -90,3 +90,29 @@ def test_gol_multi_generation_pass(b2r, orc, env, blocks, R, steps):
         orc.gol_substep(a, b, 0, 1, 63)
         a, b = b, a
     assert np.array_equal(outs[1], a)
+
+
+@pytest.mark.parametrize("env,blocks,R,periodic", [((64, 64, 64), (2, 2, 2), 4, True), ((300, 40, 30), (1, 1, 1), 1, False),
+                                                   ((33, 17, 9), (1, 1, 1), 2, True), ((520, 35, 20), (2, 1, 1), 3, False),
+                                                   ((70, 36, 50), (2, 3, 1), 2, True)])
+def test_gol_bit_sliced_equals_byte_kernel(b2r, orc, env, blocks, R, periodic):
+    """Bit-sliced cells (default) against four byte cells per word, on rows of
+    1 to 9 words per thread and tails that cut words."""
+    bc = b2r.BC_PERIODIC if periodic else b2r.BC_SHELL
+    if periodic:
+        dom = bernoulli(env, 0.3, 21)
+    else:
+        dom = np.zeros(tuple(e + 2 for e in env[::-1]), np.uint8)
+        dom[1:-1, 1:-1, 1:-1] = bernoulli(env, 0.3, 21)
+    outs = []
+    for gb in (1, 0):
+        with b2r.Domain(b2r.MODEL_GOL, env, blocks=blocks, R=R, D=1, boundary=bc) as d:
+            d.set_tuning(gol_bytes=gb)
+            d.upload(dom)
+            d.step(2 * R + 1)
+            outs.append(d.download())
+    assert np.array_equal(outs[0], outs[1])
+    if periodic:
+        ref = dom.copy()
+        orc.gol_run_periodic(ref, 2 * R + 1)
+        assert np.array_equal(outs[1], ref)
