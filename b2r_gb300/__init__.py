@@ -99,6 +99,7 @@ def lib():
         "b2r_heat_record": ([vp, i, i, C.POINTER(C.c_int), C.POINTER(C.c_float)], i),
         "b2r_heat_misfit_gradient": ([vp, i, i, C.POINTER(C.c_int), C.POINTER(C.c_float), i,
                                       C.POINTER(d), C.POINTER(d), C.POINTER(C.c_float)], i),
+        "b2r_selfcheck_bounded_wait": ([C.c_double, vp], i),
         "b2r_batch_create": ([C.POINTER(BatchItem), i, C.POINTER(vp)], i),
         "b2r_batch_destroy": ([vp], i),
         "b2r_batch_last_error": ([], C.c_char_p),

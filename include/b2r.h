@@ -286,6 +286,14 @@ int b2r_batch_tile(const b2r_batch* b);
  * inputs. */
 b2r_status b2r_batch_autotune(b2r_batch* b, void* cuda_stream, int* best_zchunk, double* best_ms);
 
+/* ---- diagnostics (no reference counterpart) ------------------------------- *
+ * Run the device-side failure path once: a one-CTA kernel waits with the
+ * library's bounded wait for an mbarrier phase that nothing completes, gives
+ * up after limit_ms (0 < limit_ms <= 10000), reports through a status word
+ * and exits.  Returns B2R_ERR_TIMEOUT when the path works; the context stays
+ * usable. */
+b2r_status b2r_selfcheck_bounded_wait(double limit_ms, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

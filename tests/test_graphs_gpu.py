@@ -37,3 +37,24 @@ def test_gol_graphs_bit_identical(b2r, orc):
     ref = dom.copy()
     orc.gol_run_periodic(ref, 73)
     assert np.array_equal(a, ref)
+
+
+def test_bounded_wait_reports_timeout_and_context_survives(b2r, orc):
+    """The device failure path: a wait that nothing completes gives up after
+    its limit and reports B2R_ERR_TIMEOUT; the next work on the GPU is right."""
+    import time
+    t0 = time.perf_counter()
+    st = b2r.lib().b2r_selfcheck_bounded_wait(50.0, None)
+    dt = time.perf_counter() - t0
+    assert st == 4, st                      # B2R_ERR_TIMEOUT
+    assert dt < 5.0
+    env = (40, 36, 32)
+    dom = np.zeros(tuple(e + 2 for e in env[::-1]), np.float32)
+    dom[1:-1, 1:-1, 1:-1] = np.random.default_rng(1).random(env[::-1], dtype=np.float32)
+    with b2r.Domain(b2r.MODEL_HEAT, env, D=1, alpha_dt=0.1) as d:
+        d.upload(dom)
+        d.step(6)
+        got = d.download()
+    ref = dom.copy()
+    orc.heat_run(ref, 1, 1, 6, 0.1, 1.0, 1.0, 1.0)
+    assert np.linalg.norm(got.astype(np.float64) - ref) / np.linalg.norm(ref) <= 1e-5
