@@ -326,6 +326,10 @@ struct Grid {
     Tiles t;
 };
 
+#ifndef B2R_EQWP_YHALO
+#define B2R_EQWP_YHALO 0    // cost of a re-read halo row against a computed row, percent (0 measured best)
+#endif
+
 inline Grid stage_grid(const BlockLayout& L, int shrink)
 {
     int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-1, -1, -1};
@@ -341,21 +345,28 @@ inline Grid stage_grid(const BlockLayout& L, int shrink)
     Grid r;
     r.t.x0 = (L.xoff + lo[0]) & ~3;
     r.t.y0 = lo[1];
-    // tile width: the fewest computed cells per row, narrower tiles paying a
-    // little for their larger x halo
+    // tile shape: tbx threads of 4 cells per row (8..32) by tby = 256 / tbx
+    // rows, the one that computes the fewest cells over the window, a tile
+    // paying for its y halo (two rows above and below are re-read) in
+    // proportion; CTAs need not be a multiple of 32 threads wide
     const int W = std::max(1, L.xoff + hi[0] + 1 - r.t.x0);
-    int tw = 4 * kBX;
+    const int Hy = std::max(1, hi[1] + 1 - lo[1]);
+    const int G4 = (W + 3) / 4;
+    int bx = kBX, by = kBY;
     double best = 1e300;
-    for (int c = 4 * kBX; c >= kBX; c /= 2) {
-        const double cost = (double)((W + c - 1) / c) * c * (c == 4 * kBX ? 1.0 : (c == 2 * kBX ? 1.03 : 1.08));
+    for (int c = 8; c <= kBX; ++c) {
+        const int rws = kBX * kBY / c;
+        const double cells = (double)((G4 + c - 1) / c) * c * 4 * ((Hy + rws - 1) / rws) * rws;
+        const double cost = cells * (1.0 + (B2R_EQWP_YHALO / 100.0) * 4.0 / rws);
         if (cost < best - 1e-9) {
             best = cost;
-            tw = c;
+            bx = c;
+            by = rws;
         }
     }
-    r.b = dim3(tw / 4, kBX * kBY / (tw / 4));
-    const int tx = std::max(1, (W + tw - 1) / tw);
-    const int ty = std::max(1, (hi[1] + 1 - lo[1] + (int)r.b.y - 1) / (int)r.b.y);
+    r.b = dim3(bx, by);
+    const int tx = std::max(1, (G4 + bx - 1) / bx);
+    const int ty = std::max(1, (Hy + by - 1) / by);
     const long long tiles = (long long)tx * ty * L.nblk;
     const long long want = 152LL * 8 * 3;
     int nzc = (int)((want + tiles - 1) / tiles);
