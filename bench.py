@@ -267,6 +267,24 @@ def config_of(args, wl):
             "parallelism": f"replicas x{args.gpus}", **({"tuning": tuning_of(args)} if args.tune else {})}
 
 
+# ------------------------------------------------------------------ ranks
+def max_over_ranks(ms, dev, world):
+    """The slowest rank's time (the job ends with it); world == 1: ms."""
+    if world <= 1:
+        return float(ms)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_glups(world, cells, steps, ms):
+    """Whole-job throughput of `world` independent replicas, each advancing
+    `cells` cells `steps` times, timed by the slowest rank (ms)."""
+    return world * cells * steps / (ms / 1000.0) / 1e9
+
+
 # ------------------------------------------------------------------ GPU side
 def make_domain(b2r, wl, stream):
     kw = dict(blocks=wl["blocks"], R=wl["R"], D=wl["D"], stream=stream,
@@ -591,11 +609,8 @@ def run_ours(args, wl):
     torch.cuda.synchronize(dev)
     barrier()
     clk = clocks.stop()
-    t = torch.tensor([total_ms], device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms = float(t.item()) / args.steps
-    value = world * cells * n / (ms / 1000.0) / 1e9
+    ms = max_over_ranks(total_ms, dev, world) / args.steps
+    value = replicas_glups(world, cells, n, ms)
 
     # ---- e2e through the C ABI with pinned host buffers
     e2e_val, h2d, d2h = None, 0, 0
@@ -610,11 +625,8 @@ def run_ours(args, wl):
             d.run_host(pin_in, n, pin_out)
         torch.cuda.synchronize(dev)
         barrier()
-        te = torch.tensor([(time.perf_counter() - t0) * 1000.0], device=dev)
-        if world > 1:
-            dist.all_reduce(te, op=dist.ReduceOp.MAX)
-        ems = float(te.item()) / args.steps
-        e2e_val = world * cells * n / (ems / 1000.0) / 1e9
+        ems = max_over_ranks((time.perf_counter() - t0) * 1000.0, dev, world) / args.steps
+        e2e_val = replicas_glups(world, cells, n, ems)
         h2d = d2h = host.nbytes
 
     # ---- roofline of the dominant kernel
