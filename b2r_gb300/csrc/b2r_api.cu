@@ -198,13 +198,13 @@ bool heat_fuse_ok(const b2r_handle* h, int i)
 
 // Game of Life generations that one pass may advance from sub-step i with
 // `left` steps to go: up to the period's end (no exchange in between), or
-// unbounded when the exchange is empty; 1 = the one-generation kernel, the
-// default (faster on 128^3 blocks so far; tblock >= 4 selects the
-// several-generation pass).
+// unbounded when the exchange is empty; 1 = the one-generation kernel.
+// Bit-sliced cells take several generations per pass by default (tblock >=
+// 2); byte cells only with tblock >= 4 (slower than one per pass so far).
 int gol_pass_gens(const b2r_handle* h, int i, int left)
 {
-    if (h->cfg.model != B2R_MODEL_GOL || h->tune.tblock < 4) return 1;
-    int g = std::min(left, gol_max_generations_per_pass());
+    if (h->cfg.model != B2R_MODEL_GOL || h->tune.tblock < (h->gol_bytes ? 4 : 2)) return 1;
+    int g = std::min(left, h->gol_bytes ? gol_max_generations_per_pass() : gol_bits_max_generations_per_pass());
     if (!(h->L.nblk == 1 && !h->L.periodic)) g = std::min(g, h->cfg.R - i);
     return std::max(g, 1);
 }
@@ -359,8 +359,12 @@ b2r_status advance(b2r_handle* h, int n)
         h->halos_fresh = false;
         const int gg = gol_pass_gens(h, i, n - s);
         if (gg >= 2) {
-            CK(h, launch_gol_period(static_cast<const uint8_t*>(h->buf[h->cur]),
-                                    static_cast<uint8_t*>(h->buf[1 - h->cur]), h->L, i, gg, h->stream));
+            if (h->gol_bytes)
+                CK(h, launch_gol_period(static_cast<const uint8_t*>(h->buf[h->cur]),
+                                        static_cast<uint8_t*>(h->buf[1 - h->cur]), h->L, i, gg, h->stream));
+            else
+                CK(h, launch_gol_bits_period(static_cast<const uint8_t*>(h->buf[h->cur]),
+                                             static_cast<uint8_t*>(h->buf[1 - h->cur]), h->L, i, gg, h->stream));
             h->cur = 1 - h->cur;
             h->ts += gg;
             s += gg;

@@ -187,6 +187,177 @@ gol_bits_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out, const
     }
 }
 
+
+// ---------------------------------------------------------------- several generations per pass
+// Up to kBMaxGen generations of one B2R period in one launch, on bit-sliced
+// cells.  A CTA owns a region of GW words of 32 cells (x; one halo word each
+// side), PR rows (ng halo rows each side) and a z chunk.  Generation g of a
+// plane (level g) is built from level g-1 planes z-1 .. z+1 held in a
+// 4-plane ring of bit words per level in shared memory; level g runs 2 planes
+// behind level g-1, so a time step reads only planes finished in earlier time
+// steps and needs one barrier.  A thread holds one word of 4 rows: z sums
+// from the ring, y sums in registers, x sums from the segment's neighbour
+// lanes by shuffles.  Level 0 is read (bytes packed to bits) once and the
+// last level written (unpacked) once per period.  Each level shrinks the
+// valid region by one cell per side as the period's windows do; cells
+// outside a sub-step's window keep their value.
+constexpr int kBMaxGen = 4;
+#ifndef B2R_GOLP_ROWS
+#define B2R_GOLP_ROWS 32     // output rows per band at most
+#endif
+#ifndef B2R_GOLP_CTAS
+#define B2R_GOLP_CTAS 8      // CTAs per SM the grid aims at
+#endif
+#ifndef B2R_GOLP_ZMIN
+#define B2R_GOLP_ZMIN 2      // z chunk of at least this many planes per generation
+#endif
+
+struct GolBitsPeriod {
+    int ng, i0;          // generations, first sub-step
+    int kx0, OW;         // first output word (32-byte units of the row) of tile 0, output words per tile
+    int y0, OR, PR;      // first output row, output rows per band, region rows (multiple of 4)
+    int nzc;
+};
+
+template <int GW>
+__global__ void __launch_bounds__(512)
+gol_bits_period_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out, const BlockLayout L,
+                       const GolBitsPeriod G)
+{
+    extern __shared__ uint32_t bsm[];
+    const int ng = G.ng, PR = G.PR;
+    constexpr int WP = GW;                       // words per ring row (the region's words)
+    const int RP = PR + 2;                       // padded rows (zero row each side)
+    const int plane_w = WP * RP;
+    uint32_t* ring = bsm;                        // [ng][4][RP][WP]: levels 0 .. ng-1
+    const int tid = threadIdx.x;
+    for (int i = tid; i < ng * 4 * plane_w; i += blockDim.x) bsm[i] = 0u;
+    __syncthreads();
+    const int w = tid % GW, yg = tid / GW;       // word of the region, group of 4 rows
+    const bool active = yg < PR / 4;
+
+    const int blk = blockIdx.z / G.nzc, zc = blockIdx.z % G.nzc;
+    const int edge = edge_bits(L, blk);
+    int lo[kBMaxGen + 1][3], hi[kBMaxGen + 1][3];
+#pragma unroll
+    for (int g = 1; g <= kBMaxGen; ++g)
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+            if (g <= ng) stage_region(L, edge, a, G.i0 + g, lo[g][a], hi[g][a]);
+    int flo[3], fhi[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) stage_region(L, edge, a, G.i0 + ng, flo[a], fhi[a]);
+    const int nzf = fhi[2] - flo[2] + 1;
+    const int per = (nzf + G.nzc - 1) / G.nzc;
+    const int zs = flo[2] + zc * per, ze = min(fhi[2], zs + per - 1);
+    if (nzf <= 0 || zs > ze) return;                               // uniform
+    const int kw = G.kx0 + blockIdx.x * G.OW - 1 + w;              // storage word of this lane
+    const int yb = G.y0 - ng + blockIdx.y * G.OR;                  // block row of region row 0
+    const int wpr = L.P >> 5;
+    const bool wload = active && kw >= 0 && kw < wpr;
+    const bool wout = active && w >= 1 && w <= G.OW && kw >= 0 && kw < wpr;
+    // window bits of this word for every level
+    uint32_t xm[kBMaxGen + 1];
+#pragma unroll
+    for (int g = 1; g <= kBMaxGen; ++g) {
+        xm[g] = 0u;
+        if (g <= ng) {
+            const int x0 = 32 * kw - L.xoff;
+            const int a = max(lo[g][0] - x0, 0), b = min(hi[g][0] - x0, 31);
+            if (a <= b) xm[g] = (b - a == 31) ? 0xFFFFFFFFu : (((1u << (b - a + 1)) - 1u) << a);
+        }
+    }
+    const uint8_t* inb = in + (long long)blk * L.bstride + 32LL * kw;
+    uint8_t* outb = out + (long long)blk * L.bstride + 32LL * kw;
+
+    // level-0 rows of the next plane, loaded one time step ahead
+    uint4 pa[4], pb[4];
+    auto load0 = [&](int z) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int y = yb + yg * 4 + k;
+            pa[k] = pb[k] = make_uint4(0u, 0u, 0u, 0u);
+            if (wload && z <= ze + ng && y >= 0 && y < L.n[1]) {
+                const uint4* s = reinterpret_cast<const uint4*>(inb + (long long)z * L.plane + (long long)y * L.P);
+                pa[k] = __ldg(s);
+                pb[k] = __ldg(s + 1);
+            }
+        }
+    };
+    load0(zs - ng);
+    const int nt = ze - zs + 3 * ng + 1;
+    for (int t = 0; t < nt; ++t) {
+        __syncthreads();
+        const int z0 = zs - ng + t;
+        if (active && z0 <= ze + ng) {
+            uint32_t* dst = ring + (z0 & 3) * plane_w + (yg * 4 + 1) * WP + w;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) dst[k * WP] = pack32(pa[k], pb[k]);
+        }
+        load0(z0 + 1);
+#pragma unroll
+        for (int g = 1; g <= kBMaxGen; ++g) {
+            const int zg = z0 - 2 * g;
+            // uniform over the CTA: every lane takes part in the shuffles
+            if (g > ng || zg < zs - (ng - g) || zg > ze + (ng - g)) continue;
+            const uint32_t* src = ring + (g - 1) * 4 * plane_w + (yg * 4) * WP + w;   // padded row yg*4 = row -1
+            const uint32_t* qa = src + ((zg - 1) & 3) * plane_w;
+            const uint32_t* qb = src + (zg & 3) * plane_w;
+            const uint32_t* qc = src + ((zg + 1) & 3) * plane_w;
+            uint32_t c0[6], c1[6], cur[4];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const uint32_t a = active ? qa[k * WP] : 0u, b = active ? qb[k * WP] : 0u,
+                               c = active ? qc[k * WP] : 0u;
+                c0[k] = xor3(a, b, c);
+                c1[k] = maj(a, b, c);
+                if (k >= 1 && k <= 4) cur[k - 1] = b;
+            }
+            const bool zin = zg >= lo[g][2] && zg <= hi[g][2];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t k1 = maj(c0[k], c0[k + 1], c0[k + 2]);
+                const uint32_t tt = xor3(c1[k], c1[k + 1], c1[k + 2]), d = maj(c1[k], c1[k + 1], c1[k + 2]);
+                const uint32_t e = tt & k1;
+                const uint32_t v0 = xor3(c0[k], c0[k + 1], c0[k + 2]), v1 = tt ^ k1, v2 = d ^ e, v3 = d & e;
+                const uint32_t p0 = __shfl_up_sync(0xffffffffu, v0, 1, GW), n0 = __shfl_down_sync(0xffffffffu, v0, 1, GW);
+                const uint32_t p1 = __shfl_up_sync(0xffffffffu, v1, 1, GW), n1 = __shfl_down_sync(0xffffffffu, v1, 1, GW);
+                const uint32_t p2 = __shfl_up_sync(0xffffffffu, v2, 1, GW), n2 = __shfl_down_sync(0xffffffffu, v2, 1, GW);
+                const uint32_t p3 = __shfl_up_sync(0xffffffffu, v3, 1, GW), n3 = __shfl_down_sync(0xffffffffu, v3, 1, GW);
+                const uint32_t l0 = __funnelshift_l(p0, v0, 1), r0 = __funnelshift_r(v0, n0, 1);
+                const uint32_t l1 = __funnelshift_l(p1, v1, 1), r1 = __funnelshift_r(v1, n1, 1);
+                const uint32_t l2 = __funnelshift_l(p2, v2, 1), r2 = __funnelshift_r(v2, n2, 1);
+                const uint32_t l3 = __funnelshift_l(p3, v3, 1), r3 = __funnelshift_r(v3, n3, 1);
+                const uint32_t s0 = xor3(l0, v0, r0), kk1 = maj(l0, v0, r0);
+                const uint32_t t1 = xor3(l1, v1, r1), m1 = maj(l1, v1, r1);
+                const uint32_t s1 = t1 ^ kk1, k2 = t1 & kk1;
+                const uint32_t t2 = xor3(l2, v2, r2), m2 = maj(l2, v2, r2);
+                const uint32_t s2 = xor3(t2, m1, k2), k3 = maj(t2, m1, k2);
+                const uint32_t t3 = xor3(l3, v3, r3), m3 = maj(l3, v3, r3);
+                const uint32_t s3 = xor3(t3, m2, k3), k4 = maj(t3, m2, k3);
+                const uint32_t s4 = m3 ^ k4;
+                const uint32_t born = ~s4 & ~s3 & s2 & ~s1 & s0;
+                const uint32_t surv = ~s4 & ((~s3 & (s2 | (s1 & s0))) | (s3 & ~s2 & ~s1 & ~s0));
+                const uint32_t c = cur[k];
+                const int r = yg * 4 + k, y = yb + r;
+                const uint32_t m = (zin && y >= lo[g][1] && y <= hi[g][1]) ? xm[g] : 0u;
+                const uint32_t nxt = (((c & surv) | (~c & born)) & m) | (c & ~m);
+                if (!active) continue;
+                if (g < ng) {
+                    ring[(g * 4 + (zg & 3)) * plane_w + (r + 1) * WP + w] = nxt;
+                } else if (wout && zg >= zs && zg <= ze && r >= ng && r < ng + G.OR && y >= flo[1] &&
+                           y <= fhi[1] && xm[g]) {
+                    uint4 a, b;
+                    unpack32(nxt, a, b);
+                    uint4* d = reinterpret_cast<uint4*>(outb + (long long)zg * L.plane + (long long)y * L.P);
+                    d[0] = a;
+                    d[1] = b;
+                }
+            }
+        }
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_gol_bits_substep(const uint8_t* in, uint8_t* out, const BlockLayout& L, int step_i,
@@ -227,6 +398,68 @@ cudaError_t launch_gol_bits_substep(const uint8_t* in, uint8_t* out, const Block
     case 8: gol_bits_kernel<8><<<grid, 32 * kBWarps, 0, st>>>(in, out, L, step_i, G); break;
     case 16: gol_bits_kernel<16><<<grid, 32 * kBWarps, 0, st>>>(in, out, L, step_i, G); break;
     default: gol_bits_kernel<32><<<grid, 32 * kBWarps, 0, st>>>(in, out, L, step_i, G); break;
+    }
+    count_launches(1);
+    return cudaGetLastError();
+}
+
+int gol_bits_max_generations_per_pass() { return kBMaxGen; }
+
+cudaError_t launch_gol_bits_period(const uint8_t* in, uint8_t* out, const BlockLayout& L, int i0, int ng,
+                                   cudaStream_t st)
+{
+    if (ng < 1 || ng > kBMaxGen) return cudaErrorInvalidValue;
+    int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-1, -1, -1};
+    for (int b = 0; b < L.nblk; ++b) {
+        const int e = edge_bits(L, b);
+        for (int a = 0; a < 3; ++a) {
+            int l, h;
+            stage_region(L, e, a, i0 + ng, l, h);
+            lo[a] = std::min(lo[a], l);
+            hi[a] = std::max(hi[a], h);
+        }
+    }
+    if (hi[0] < lo[0] || hi[1] < lo[1] || hi[2] < lo[2]) return cudaSuccess;
+    GolBitsPeriod G{};
+    G.ng = ng;
+    G.i0 = i0;
+    G.kx0 = (L.xoff + lo[0]) >> 5;
+    const int nwt = ((L.xoff + hi[0]) >> 5) - G.kx0 + 1;
+    int GW = 32;
+    for (int g : {8, 16, 32})
+        if (((nwt + g - 3) / (g - 2)) * g < ((nwt + GW - 3) / (GW - 2)) * GW) GW = g;
+    const int ntx = (nwt + GW - 3) / (GW - 2);
+    G.OW = GW - 2;
+    // bands of rows: at most B2R_GOLP_ROWS output rows, split evenly
+    const int H = hi[1] - lo[1] + 1;
+    const int nty = (H + B2R_GOLP_ROWS - 1) / B2R_GOLP_ROWS;
+    G.OR = (H + nty - 1) / nty;
+    G.PR = (G.OR + 2 * ng + 3) / 4 * 4;
+    if (GW * (G.PR / 4) > 512) G.PR = 512 / GW * 4, G.OR = G.PR - 2 * ng;
+    const int nty2 = (H + G.OR - 1) / G.OR;
+    G.y0 = lo[1];
+    const long long tiles = (long long)ntx * nty2 * L.nblk;
+    const int nz = hi[2] - lo[2] + 1;
+    int nzc = (int)std::max(1LL, (152LL * B2R_GOLP_CTAS + tiles - 1) / tiles);
+    nzc = std::min(nzc, std::max(1, nz / (B2R_GOLP_ZMIN * ng)));
+    G.nzc = nzc;
+    const size_t smem = (size_t)ng * 4 * GW * (G.PR + 2) * sizeof(uint32_t);
+    const int threads = (GW * (G.PR / 4) + 31) / 32 * 32;   // whole warps: every lane takes part in the shuffles
+    const dim3 grid(ntx, nty2, L.nblk * nzc);
+    static size_t attr[3] = {0, 0, 0};
+    const int gi = GW == 8 ? 0 : (GW == 16 ? 1 : 2);
+    if (smem > attr[gi]) {
+        const int bytes = (int)std::max<size_t>(smem, 48 * 1024);
+        cudaError_t e = GW == 8 ? cudaFuncSetAttribute(gol_bits_period_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)
+                      : GW == 16 ? cudaFuncSetAttribute(gol_bits_period_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)
+                                 : cudaFuncSetAttribute(gol_bits_period_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e != cudaSuccess) return e;
+        attr[gi] = (size_t)bytes;
+    }
+    switch (GW) {
+    case 8: gol_bits_period_kernel<8><<<grid, threads, smem, st>>>(in, out, L, G); break;
+    case 16: gol_bits_period_kernel<16><<<grid, threads, smem, st>>>(in, out, L, G); break;
+    default: gol_bits_period_kernel<32><<<grid, threads, smem, st>>>(in, out, L, G); break;
     }
     count_launches(1);
     return cudaGetLastError();

@@ -120,10 +120,10 @@ enum {
     B2R_TUNE_ZCHUNK = 1,       /* planes per work unit of the one-step sweep (0 = 16) */
     B2R_TUNE_CTAS_PER_SM = 2,  /* 0 = one CTA per unit, k = persistent k CTAs per SM */
     B2R_TUNE_PDL = 3,          /* programmatic dependent launch on / off */
-    B2R_TUNE_TBLOCK = 4,       /* time steps per HBM pass: >= 2 (default 2) lets heat of radius 1
-                                  take two steps per pass; >= 4 also lets Game of Life take up to
-                                  four generations (never across a halo exchange) per pass;
-                                  1 = one step per pass */
+    B2R_TUNE_TBLOCK = 4,       /* time steps per pass: >= 2 (default 2) lets heat of radius 1
+                                  take two steps per HBM pass and Game of Life (bit-sliced cells)
+                                  up to four generations per L2 pass, never across a halo
+                                  exchange; byte cells need >= 4; 1 = one step per pass */
     B2R_TUNE_ZCHUNK2 = 5,      /* planes per work unit of the two-step sweep (0 = 16) */
     B2R_TUNE_EQWP_FUSED = 6,   /* staggered elastic wave: 1 = one-pass step, 0 = the velocity
                                   and stress stages as two passes (default); bit-identical */

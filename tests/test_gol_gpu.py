@@ -12,7 +12,7 @@ def bernoulli(env, p, seed):
 
 @pytest.mark.parametrize("env,blocks,R", [((64, 64, 64), (2, 2, 2), 4), ((64, 48, 40), (1, 1, 1), 1),
                                           ((70, 36, 50), (2, 3, 1), 2), ((33, 17, 9), (1, 1, 1), 3)])
-@pytest.mark.parametrize("tblock", [2, 4])
+@pytest.mark.parametrize("tblock", [1, 2, 4])
 def test_gol_periodic_bit_exact_every_period(b2r, orc, env, blocks, R, tblock):
     dom = bernoulli(env, 0.3, 2)
     ref = dom.copy()
@@ -116,3 +116,21 @@ def test_gol_bit_sliced_equals_byte_kernel(b2r, orc, env, blocks, R, periodic):
         ref = dom.copy()
         orc.gol_run_periodic(ref, 2 * R + 1)
         assert np.array_equal(outs[1], ref)
+
+
+@pytest.mark.parametrize("env,blocks,R", [((64, 64, 64), (2, 2, 2), 4), ((100, 52, 40), (2, 1, 1), 3)])
+def test_gol_multi_generation_passes_agree(b2r, orc, env, blocks, R):
+    """Several generations per pass with bit-sliced and with byte cells,
+    against one generation per pass and the oracle (periodic)."""
+    dom = bernoulli(env, 0.3, 31)
+    outs = []
+    for gb, tb in ((0, 4), (1, 4), (0, 1)):
+        with b2r.Domain(b2r.MODEL_GOL, env, blocks=blocks, R=R, D=1, boundary=b2r.BC_PERIODIC) as d:
+            d.set_tuning(gol_bytes=gb, tblock=tb)
+            d.upload(dom)
+            d.step(2 * R)
+            outs.append(d.download())
+    ref = dom.copy()
+    orc.gol_run_periodic(ref, 2 * R)
+    for o in outs:
+        assert np.array_equal(o, ref)
