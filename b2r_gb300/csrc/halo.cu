@@ -190,23 +190,38 @@ __global__ void gather_kernel(T* __restrict__ dom, const T* __restrict__ blocks,
 // (edges and corners arrive in two or three hops from the same owners), so
 // one launch replaces three, with no ordering between the regions.  Halo
 // cells without an owner (domain boundary, not periodic) keep their values.
+// Each region's rows move in the widest vectors (16 down to the cell size)
+// that its row length and row starts allow.
 struct HaloDirs {
     int n;                  // regions with a possible owner
     int cta0[27];           // first CTA of region k (cta0[n] = total CTAs)
     int d[26][3];           // direction
     int ex[26], ey[26], ez[26];   // extent: x in vectors, y, z in cells
     int dst[26][3], src[26][3];   // origins (cells) in the block and in the owner
-    int vb;                 // vector bytes
+    int vb[26];                   // vector bytes of region k's rows
 };
 
+// copy ex x ey x ez vectors of VB bytes (rows of ex vectors), grid-stride
 template <int VB>
-__global__ void __launch_bounds__(256)
-halo_gather_kernel(FieldSet<uint8_t> fs, const BlockLayout L, int cb, const HaloDirs hd)
+__device__ __forceinline__ void copy_box(uint8_t* dst, const uint8_t* src, unsigned ex, unsigned ey,
+                                         unsigned total, long long rowb, long long planeb, unsigned e0,
+                                         unsigned stride)
 {
     typedef typename std::conditional<VB == 16, uint4,
             typename std::conditional<VB == 8, uint2,
             typename std::conditional<VB == 4, uint32_t,
             typename std::conditional<VB == 2, uint16_t, uint8_t>::type>::type>::type>::type V;
+    for (unsigned e = e0; e < total; e += stride) {
+        const unsigned vx = e % ex, r = e / ex;
+        const unsigned y = r % ey, z = r / ey;
+        const long long off = (long long)vx * VB + y * rowb + z * planeb;
+        *reinterpret_cast<V*>(dst + off) = *reinterpret_cast<const V*>(src + off);
+    }
+}
+
+__global__ void __launch_bounds__(256)
+halo_gather_kernel(FieldSet<uint8_t> fs, const BlockLayout L, int cb, const HaloDirs hd)
+{
     const int blk = blockIdx.y % L.nblk;
     uint8_t* base = fs.p[blockIdx.y / L.nblk];
     int k = 0;
@@ -230,11 +245,13 @@ halo_gather_kernel(FieldSet<uint8_t> fs, const BlockLayout L, int cb, const Halo
     const unsigned ex = hd.ex[k], ey = hd.ey[k];
     const unsigned total = ex * ey * (unsigned)hd.ez[k];
     const unsigned nct = hd.cta0[k + 1] - hd.cta0[k];
-    for (unsigned e = (blockIdx.x - hd.cta0[k]) * blockDim.x + threadIdx.x; e < total; e += nct * blockDim.x) {
-        const unsigned vx = e % ex, r = e / ex;
-        const unsigned y = r % ey, z = r / ey;
-        const long long off = (long long)vx * VB + y * rowb + z * planeb;
-        *reinterpret_cast<V*>(dst + off) = *reinterpret_cast<const V*>(src + off);
+    const unsigned e0 = (blockIdx.x - hd.cta0[k]) * blockDim.x + threadIdx.x, stride = nct * blockDim.x;
+    switch (hd.vb[k]) {   // uniform per CTA
+    case 16: copy_box<16>(dst, src, ex, ey, total, rowb, planeb, e0, stride); break;
+    case 8: copy_box<8>(dst, src, ex, ey, total, rowb, planeb, e0, stride); break;
+    case 4: copy_box<4>(dst, src, ex, ey, total, rowb, planeb, e0, stride); break;
+    case 2: copy_box<2>(dst, src, ex, ey, total, rowb, planeb, e0, stride); break;
+    default: copy_box<1>(dst, src, ex, ey, total, rowb, planeb, e0, stride); break;
     }
 }
 
@@ -280,12 +297,7 @@ cudaError_t launch_halo_gather(const FieldSet<T>& fs, int nfields, const BlockLa
 {
     if (L.nblk == 1 && !L.periodic) return cudaSuccess;   // all halos are shell
     const int cb = (int)sizeof(T);
-    // widest vector that every region row start and length is a multiple of
-    int vb = 16;
-    while (vb > cb && ((L.H * cb) % vb || (L.B[0] * cb) % vb || (L.xoff * cb) % vb)) vb >>= 1;
-    if (vb < cb) vb = cb;
     HaloDirs hd{};
-    hd.vb = vb;
     const long long per_cta = 256LL * 4;    // vectors per CTA
     int ctas = 0;
     for (int dz = -1; dz <= 1; ++dz)
@@ -305,6 +317,13 @@ cudaError_t launch_halo_gather(const FieldSet<T>& fs, int nfields, const BlockLa
                     hd.dst[k][a] = d[a] < 0 ? 0 : (d[a] == 0 ? L.H : L.H + L.B[a]);
                     hd.src[k][a] = d[a] < 0 ? L.B[a] : L.H;
                 }
+                // widest vector that the region's row length and both row starts are multiples of
+                int vb = 16;
+                while (vb > cb && ((ext[0] * cb) % vb || ((L.xoff + hd.dst[k][0]) * cb) % vb ||
+                                   ((L.xoff + hd.src[k][0]) * cb) % vb))
+                    vb >>= 1;
+                if (vb < cb) vb = cb;
+                hd.vb[k] = vb;
                 hd.ex[k] = ext[0] * cb / vb;
                 hd.ey[k] = ext[1];
                 hd.ez[k] = ext[2];
@@ -317,13 +336,7 @@ cudaError_t launch_halo_gather(const FieldSet<T>& fs, int nfields, const BlockLa
     FieldSet<uint8_t> fb{};
     for (int f = 0; f < nfields; ++f) fb.p[f] = reinterpret_cast<uint8_t*>(fs.p[f]);
     const dim3 grid((unsigned)ctas, (unsigned)(nfields * L.nblk));
-    switch (vb) {
-    case 16: halo_gather_kernel<16><<<grid, 256, 0, st>>>(fb, L, cb, hd); break;
-    case 8: halo_gather_kernel<8><<<grid, 256, 0, st>>>(fb, L, cb, hd); break;
-    case 4: halo_gather_kernel<4><<<grid, 256, 0, st>>>(fb, L, cb, hd); break;
-    case 2: halo_gather_kernel<2><<<grid, 256, 0, st>>>(fb, L, cb, hd); break;
-    default: halo_gather_kernel<1><<<grid, 256, 0, st>>>(fb, L, cb, hd); break;
-    }
+    halo_gather_kernel<<<grid, 256, 0, st>>>(fb, L, cb, hd);
     count_launches(1);
     return cudaGetLastError();
 }
