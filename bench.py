@@ -54,7 +54,7 @@ WORKLOADS = {
                      coef=(0.01, 1.0, 1.0, 0.5), bytes_per_cell=8, kernel="heat_sweep_kernel<1>"),
     # 3-D Game of Life, 256^3 torus, 2x2x2 subdomains, R = 4, 400 generations
     "gol_256": dict(model=2, env=(256, 256, 256), blocks=(2, 2, 2), R=4, D=1, sub_steps=400,
-                    bytes_per_cell=2, kernel="gol_kernel", periodic=True),
+                    bytes_per_cell=2, kernel="gol_bits_period_kernel", periodic=True),
     # 64 independent heat instances, edges U{32,48,..,192} per axis, D U{1..4},
     # steps U[50,500], seed 4, in one persistent launch replayed from a CUDA graph
     "batch64": dict(model=5, n=64, seed=4, env=(0, 0, 0), blocks=(1, 1, 1), R=1, D=0, sub_steps=0,
