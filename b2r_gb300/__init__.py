@@ -81,6 +81,7 @@ def lib():
         "b2r_step": ([vp, i], i),
         "b2r_set_graphs": ([vp, i], i),
         "b2r_set_tuning": ([vp, i, i], i),
+        "b2r_get_tuning": ([vp, i, C.POINTER(i)], i),
         "b2r_autotune": ([vp, i, C.POINTER(C.c_int), C.POINTER(d)], i),
         "b2r_run_host": ([vp, i, vp, i, vp], i),
         "b2r_time_step": ([vp], C.c_int64),
@@ -217,6 +218,16 @@ class Domain:
                        (6, eqwp_fused), (7, gol_bytes)):
             if v is not None:
                 _check(lib().b2r_set_tuning(self.h, key, int(v)), self.h)
+
+    def get_tuning(self):
+        """Every knob's current value (by the names set_tuning takes)."""
+        out = {}
+        for key, name in ((1, "zchunk"), (2, "ctas_per_sm"), (3, "pdl"), (4, "tblock"), (5, "zchunk2"),
+                          (6, "eqwp_fused"), (7, "gol_bytes")):
+            v = C.c_int()
+            _check(lib().b2r_get_tuning(self.h, key, C.byref(v)), self.h)
+            out[name] = v.value
+        return out
 
     def autotune(self, trial_steps=4):
         """Pick the fastest heat launch schedule; returns ({...}, ms per step)."""

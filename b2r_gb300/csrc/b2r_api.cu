@@ -821,6 +821,22 @@ b2r_status b2r_set_tuning(b2r_handle* h, int key, int value)
     return B2R_OK;
 }
 
+b2r_status b2r_get_tuning(const b2r_handle* h, int key, int* value)
+{
+    if (!h || !value) return fail(nullptr, B2R_ERR_ARG, "null argument");
+    switch (key) {
+    case B2R_TUNE_ZCHUNK: *value = h->tune.zchunk; break;
+    case B2R_TUNE_CTAS_PER_SM: *value = h->tune.ctas_per_sm; break;
+    case B2R_TUNE_PDL: *value = h->tune.pdl ? 1 : 0; break;
+    case B2R_TUNE_TBLOCK: *value = h->tune.tblock; break;
+    case B2R_TUNE_ZCHUNK2: *value = h->tune.zchunk2; break;
+    case B2R_TUNE_EQWP_FUSED: *value = h->eqwp_fused ? 1 : 0; break;
+    case B2R_TUNE_GOL_BYTES: *value = h->gol_bytes ? 1 : 0; break;
+    default: return fail(nullptr, B2R_ERR_ARG, "unknown tuning key %d", key);
+    }
+    return B2R_OK;
+}
+
 b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* best_ms)
 {
     if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
@@ -861,7 +877,7 @@ b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* bes
     struct Cand { int tb, zc2, zc, cp, pdl; };
     std::vector<Cand> cands;
     if (h->cfg.D == 1)
-        for (int z2 : {0, 16, 32, 64}) cands.push_back({2, z2, 0, 0, 1});
+        for (int z2 : {4, 8, 16, 32, 64}) cands.push_back({2, z2, 0, 0, 1});
     for (int pdl = 0; pdl < 2; ++pdl)
         for (int zc : zchunks)
             for (int cp : persist)

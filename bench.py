@@ -568,6 +568,12 @@ def run_ours(args, wl):
         d.set_tuning(**tune)
     host = load_inputs(d, wl, torch, dev)
     d.synchronize()
+    # heat: the library's autotuner picks the launch schedule for this shape
+    # (timed on the live field, which it restores); not part of the timing
+    tuned = None
+    if wl["model"] == 1 and not tune:
+        d.autotune(trial_steps=4)
+        tuned = {k: v for k, v in d.get_tuning().items() if k in ("zchunk", "ctas_per_sm", "pdl", "tblock", "zchunk2")}
     n = wl["sub_steps"]
     cells = wl["env"][0] * wl["env"][1] * wl["env"][2]
     small = config_of(args, wl)["l2"] != "inputs larger than L2"
@@ -675,7 +681,7 @@ def run_ours(args, wl):
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "u8" if wl["model"] == 2 else "f32",
                 "data": "synthetic (seeded U[0,1) / Bernoulli(0.3) / layered model)",
-                "config": config_of(args, wl),
+                "config": {**config_of(args, wl), **({"autotuned": tuned} if tuned else {})},
                 "e2e": ({"value": round(e2e_val, 3), "unit": "GLUPS", "h2d_bytes_per_step": h2d,
                          "d2h_bytes_per_step": d2h} if e2e_val is not None else None),
                 "gpu_launches": int(launches),

@@ -131,6 +131,8 @@ enum {
                                   (default), 1 = four byte cells per word; identical results */
 };
 b2r_status b2r_set_tuning(b2r_handle* h, int key, int value);
+/* Current value of a knob (after b2r_autotune: the schedule it picked). */
+b2r_status b2r_get_tuning(const b2r_handle* h, int key, int* value);
 /* Time every schedule candidate (z-chunk length x persistent CTAs per SM x
  * programmatic dependent launch) for trial_steps time steps on the live
  * fields, keep the fastest, restore the fields and the time step.  Results
