@@ -92,6 +92,7 @@ def lib():
                                   C.POINTER(d)], i),
         "b2r_gol_3D_gpu_main": ([vp, i, C.c_char_p, i, i, i, vp, C.POINTER(d)], i),
         "b2r_eqwp_gpu_main": ([vp, i, i, C.POINTER(d)], i),
+        "b2r_write_block_data": ([vp, i, i, i, C.c_char_p, i, C.c_char_p, i], i),
         "b2r_kernel_launches": ([], C.c_int64),
         "b2r_eqwp_record": ([vp, i, i, C.POINTER(C.c_int), C.POINTER(C.c_float)], i),
         "b2r_eqwp_misfit_gradient": ([vp, i, i, C.POINTER(C.c_int), C.POINTER(C.c_float), i,
@@ -120,6 +121,17 @@ def lib():
         fn.restype = res
     _lib = L
     return L
+
+
+def read_block_data_bin(path):
+    """(nz, ny, nx) float32 array of a file in the reference's block data
+    format: int32[3] {Ngx, Ngy, Ngz}, then Ngx*Ngy*Ngz floats, x fastest."""
+    raw = open(path, "rb").read()
+    nx, ny, nz = np.frombuffer(raw[:12], np.int32)
+    cells = np.frombuffer(raw[12:], np.float32)
+    if cells.size != int(nx) * int(ny) * int(nz):
+        raise ValueError("%s: header %dx%dx%d does not match %d cells" % (path, nx, ny, nz, cells.size))
+    return cells.reshape(int(nz), int(ny), int(nx))
 
 
 def _check(st, handle=None):
@@ -213,9 +225,9 @@ class Domain:
         _check(lib().b2r_set_graphs(self.h, 1 if enable else 0), self.h)
 
     def set_tuning(self, zchunk=None, ctas_per_sm=None, pdl=None, tblock=None, zchunk2=None,
-                   eqwp_fused=None, gol_bytes=None):
+                   eqwp_fused=None, gol_bytes=None, adj_fused=None):
         for key, v in ((1, zchunk), (2, ctas_per_sm), (3, pdl), (4, tblock), (5, zchunk2),
-                       (6, eqwp_fused), (7, gol_bytes)):
+                       (6, eqwp_fused), (7, gol_bytes), (8, adj_fused)):
             if v is not None:
                 _check(lib().b2r_set_tuning(self.h, key, int(v)), self.h)
 
@@ -223,7 +235,7 @@ class Domain:
         """Every knob's current value (by the names set_tuning takes)."""
         out = {}
         for key, name in ((1, "zchunk"), (2, "ctas_per_sm"), (3, "pdl"), (4, "tblock"), (5, "zchunk2"),
-                          (6, "eqwp_fused"), (7, "gol_bytes")):
+                          (6, "eqwp_fused"), (7, "gol_bytes"), (8, "adj_fused")):
             v = C.c_int()
             _check(lib().b2r_get_tuning(self.h, key, C.byref(v)), self.h)
             out[name] = v.value
@@ -263,6 +275,18 @@ class Domain:
                 for bx in range(nb[0]):
                     res[(bx, by, bz)] = out[bx + nb[0] * (by + nb[1] * bz)]
         return res
+
+    def write_block_data(self, field=0, block=0, time_step=None, directory=None, text=False):
+        """Write one padded block of a field as the reference's
+        write_block_data_bin / write_block_data (eqwp.cu:616-651) do: an
+        int32[3] {Ngx, Ngy, Ngz} header and the float cells (x fastest), or
+        comma-separated text, one line per row.  Returns the path written."""
+        ts = self.time_step if time_step is None else int(time_step)
+        buf = C.create_string_buffer(4096)
+        d = None if directory is None else os.fsencode(directory)
+        _check(lib().b2r_write_block_data(self.h, FIELDS.get(field, field), int(block), ts, d,
+                                          1 if text else 0, buf, len(buf)), self.h)
+        return buf.value.decode()
 
     def step(self, nsteps):
         _check(lib().b2r_step(self.h, int(nsteps)), self.h)

@@ -66,6 +66,23 @@ struct G4 {
 // sb component (xx, xy, xz, yy, yz, zz numbering) of each strain row of StrOp
 __device__ constexpr int kStrainS[6] = {0, 3, 5, 1, 2, 4};
 
+// lambda / mu gradient increments of one cell (lane j of the thread's 4),
+// explicitly rounded so that every kernel forming them gets the same bits:
+//   g_lambda += k tr(e) tr(sb),  g_mu += k (2 e_ii sb_ii + gamma_ij sb_ij)
+// (sb in strain-row order xx, yy, zz, xy, xz, yz; e = E v^n, raw sums)
+__device__ __forceinline__ void lm_increment(float k, const float4 (&sb)[6], const float (&ev)[6][4], int j,
+                                             double& gl, double& gm)
+{
+    const float sxx = cmp(sb[0], j), syy = cmp(sb[1], j), szz = cmp(sb[2], j);
+    const float sxy = cmp(sb[3], j), sxz = cmp(sb[4], j), syz = cmp(sb[5], j);
+    const float exx = ev[0][j], eyy = ev[1][j], ezz = ev[2][j];
+    const float tr = add3(sxx, syy, szz);
+    gl += (double)__fmul_rn(k, __fmul_rn(add3(exx, eyy, ezz), tr));
+    const float nrm = add3(__fmul_rn(exx, sxx), __fmul_rn(eyy, syy), __fmul_rn(ezz, szz));
+    const float shr = add3(__fmul_rn(ev[3][j], sxy), __fmul_rn(ev[4][j], sxz), __fmul_rn(ev[5][j], syz));
+    gm += (double)__fmul_rn(k, __fadd_rn(__fmul_rn(2.f, nrm), shr));
+}
+
 struct AdjV {
     const float* q[6];     // C*sb of the later step (xx, xy, xz, yy, yz, zz)
     float* vb[3];          // adjoint velocity, updated
@@ -264,15 +281,94 @@ adj_grad_lm_kernel(AdjS A, const BlockLayout L, Tiles T)
         gl.load(A.g_lam + o, c);
         gm.load(A.g_mu + o, c);
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const float sxx = cmp(sb[0], j), syy = cmp(sb[1], j), szz = cmp(sb[2], j);
-            const float sxy = cmp(sb[3], j), sxz = cmp(sb[4], j), syz = cmp(sb[5], j);
-            const float tr = sxx + syy + szz;
-            const float exx = ev[0][j], eyy = ev[1][j], ezz = ev[2][j];
-            gl.v[j] += (double)(A.k * ((exx + eyy + ezz) * tr));
-            gm.v[j] += (double)(A.k * (2.f * (exx * sxx + eyy * syy + ezz * szz) +
-                                       (ev[3][j] * sxy + ev[4][j] * sxz + ev[5][j] * syz)));
+        for (int j = 0; j < 4; ++j) lm_increment(A.k, sb, ev, j, gl.v[j], gm.v[j]);
+        gl.store(A.g_lam + o, c);
+        gm.store(A.g_mu + o, c);
+    }
+}
+
+// adj_stress_kernel and adj_grad_lm_kernel in one sweep: the updated sb
+// stays in registers for the lambda / mu gradients instead of being re-read
+// (68 + 92 -> 136 B per cell).  Two strain operators (w and v^n) are live,
+// so the register budget is fitted to one CTA per SM unless
+// B2R_ADJ_FUSED_MINB says otherwise.
+#ifndef B2R_ADJ_FUSED_MINB
+#define B2R_ADJ_FUSED_MINB 1
+#endif
+__global__ void __launch_bounds__(kBX * kBY, B2R_ADJ_FUSED_MINB)
+adj_stress_lm_kernel(AdjS A, const BlockLayout L, Tiles T)
+{
+    const int nzc = T.nzc;
+    const int blk = blockIdx.z / nzc, zc = blockIdx.z % nzc;
+    const Win w = window(L, blk, zc, nzc, 4);
+    Cell c;
+    if (!cell_setup(L, w, blk, c, T.x0, T.y0)) return;
+    const long long P = L.P, S = L.plane;
+    StrOp ow, ov;
+    ow.x = A.w[0] + c.base;
+    ow.y = A.w[1] + c.base;
+    ow.z = A.w[2] + c.base;
+    ov.x = A.v[0] + c.base;
+    ov.y = A.v[1] + c.base;
+    ov.z = A.v[2] + c.base;
+    ow.begin(w.zs, S);
+    ov.begin(w.zs, S);
+    for (int z = w.zs; z <= w.ze; ++z) {
+        const long long o = (long long)z * S + c.base;
+        if (B2R_ADJ_PREFETCH > 0) {
+            const long long oa = ahead(L, z, B2R_ADJ_PREFETCH, w.ze) + c.base,
+                            oq = ahead(L, z, 2 + B2R_ADJ_PREFETCH, w.ze + 2);
+#pragma unroll
+            for (int f = 0; f < 3; ++f) {
+                pf_l2(A.w[f] + c.base + oq);
+                pf_l2(A.v[f] + c.base + oq);
+            }
+            pf_l2(A.lam + oa);
+            pf_l2(A.mu + oa);
+#pragma unroll
+            for (int f = 0; f < 6; ++f) pf_l2(A.sb[f] + oa);
+            pf_l2(reinterpret_cast<const float*>(A.g_lam + oa));
+            pf_l2(reinterpret_cast<const float*>(A.g_lam + oa) + 4);
+            pf_l2(reinterpret_cast<const float*>(A.g_mu + oa));
+            pf_l2(reinterpret_cast<const float*>(A.g_mu + oa) + 4);
         }
+        float ew[6][4];
+        ow.eval(o - c.base, P, S, ew);
+        const float4 l4 = ld4(A.lam + o), m4 = ld4(A.mu + o);
+        float4 sb[6];
+#pragma unroll
+        for (int f = 0; f < 6; ++f) sb[f] = rd4(A.sb[kStrainS[f]] + o, c);
+        float d[6][4];
+#pragma unroll
+        for (int f = 0; f < 6; ++f)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) d[f][j] = -(A.k * ew[f][j]);
+#pragma unroll
+        for (int f = 0; f < 6; ++f) sb[f] = wr4(A.sb[kStrainS[f]] + o, c, sb[f], d[f]);
+        float qv[6][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const float l = cmp(l4, j), m = cmp(m4, j);
+            const float sxx = cmp(sb[0], j), syy = cmp(sb[1], j), szz = cmp(sb[2], j);
+            const float tr = sxx + syy + szz;
+            qv[0][j] = 2.f * m * sxx + l * tr;
+            qv[1][j] = 2.f * m * syy + l * tr;
+            qv[2][j] = 2.f * m * szz + l * tr;
+            qv[3][j] = m * cmp(sb[3], j);
+            qv[4][j] = m * cmp(sb[4], j);
+            qv[5][j] = m * cmp(sb[5], j);
+        }
+#pragma unroll
+        for (int f = 0; f < 6; ++f) st4(A.q[kStrainS[f]] + o, c, qv[f]);
+        // lambda / mu gradients of the stress stage of step n-1 from the sb
+        // just stored, exactly as adj_grad_lm_kernel forms them
+        float ev[6][4];
+        ov.eval(o - c.base, P, S, ev);
+        G4 gl, gm;
+        gl.load(A.g_lam + o, c);
+        gm.load(A.g_mu + o, c);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) lm_increment(A.k, sb, ev, j, gl.v[j], gm.v[j]);
         gl.store(A.g_lam + o, c);
         gm.store(A.g_mu + o, c);
     }
@@ -359,11 +455,12 @@ cudaError_t adjoint_inject(float* vby, const long long* d_idx, int nrec, const f
 }
 
 // Reverse step n: q (from the later step) -> vb, w, g_b; then, unless n is
-// the first step, w -> sb, q for step n-1, g_lambda, g_mu.  tmp = vb[3],
+// the first step, w -> sb, q for step n-1, g_lambda, g_mu (one sweep when
+// fused, else the stress kernel and the gradient kernel).  tmp = vb[3],
 // sb[6], q[6], w[3]; v_n = forward v^n, acc_n = forward D s^n.
 cudaError_t adjoint_step(float* const* tmp, const float* const* v_n, const float* const* acc_n,
                          const float* const* mat, double* const* g, const BlockLayout& L, float dt_h,
-                         bool last, cudaStream_t st)
+                         bool last, bool fused, cudaStream_t st)
 {
     AdjV V;
     AdjS T;
@@ -391,9 +488,14 @@ cudaError_t adjoint_step(float* const* tmp, const float* const* v_n, const float
     adj_velocity_kernel<<<ga.g, ga.b, 0, st>>>(V, L, ga.t);
     count_launches(1);
     if (!last) {
-        adj_stress_kernel<<<gb.g, gb.b, 0, st>>>(T, L, gb.t);
-        adj_grad_lm_kernel<<<gb.g, gb.b, 0, st>>>(T, L, gb.t);
-        count_launches(2);
+        if (fused) {
+            adj_stress_lm_kernel<<<gb.g, gb.b, 0, st>>>(T, L, gb.t);
+            count_launches(1);
+        } else {
+            adj_stress_kernel<<<gb.g, gb.b, 0, st>>>(T, L, gb.t);
+            adj_grad_lm_kernel<<<gb.g, gb.b, 0, st>>>(T, L, gb.t);
+            count_launches(2);
+        }
     }
     return cudaGetLastError();
 }

@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <new>
 #include <map>
 #include <mutex>
@@ -47,6 +48,7 @@ struct b2r_handle {
     StressMaps smaps[2];
     bool eqwp_fused = false;   // two-pass by default: faster on this GPU so far
     bool gol_bytes = false;    // Game of Life: byte-SWAR kernel instead of bit-sliced cells
+    bool adj_fused = true;     // adjoint: stress adjoint + lambda/mu gradients in one sweep
     float* mat[3] = {};
     std::vector<float> src;     // per-step source increment of sxx/syy/szz (STAG)
     void* staging = nullptr;
@@ -815,6 +817,7 @@ b2r_status b2r_set_tuning(b2r_handle* h, int key, int value)
     case B2R_TUNE_ZCHUNK2: h->tune.zchunk2 = value; break;
     case B2R_TUNE_EQWP_FUSED: h->eqwp_fused = value != 0; break;
     case B2R_TUNE_GOL_BYTES: h->gol_bytes = value != 0; break;
+    case B2R_TUNE_ADJ_FUSED: h->adj_fused = value != 0; break;
     default: return fail(h, B2R_ERR_ARG, "unknown tuning key %d", key);
     }
     drop_graphs(h);
@@ -832,6 +835,7 @@ b2r_status b2r_get_tuning(const b2r_handle* h, int key, int* value)
     case B2R_TUNE_ZCHUNK2: *value = h->tune.zchunk2; break;
     case B2R_TUNE_EQWP_FUSED: *value = h->eqwp_fused ? 1 : 0; break;
     case B2R_TUNE_GOL_BYTES: *value = h->gol_bytes ? 1 : 0; break;
+    case B2R_TUNE_ADJ_FUSED: *value = h->adj_fused ? 1 : 0; break;
     default: return fail(nullptr, B2R_ERR_ARG, "unknown tuning key %d", key);
     }
     return B2R_OK;
@@ -1104,7 +1108,7 @@ b2r_status b2r_eqwp_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const i
             CK(h, adjoint_inject(tp[1], didx, nrec, (const float*)d_res.p + (size_t)n * nrec, h->stream));
             const float* vn[3] = {vslot(k, 0), vslot(k, 1), vslot(k, 2)};
             const float* an[3] = {arep[(size_t)k * 3], arep[(size_t)k * 3 + 1], arep[(size_t)k * 3 + 2]};
-            CK(h, adjoint_step(tp, vn, an, mat, gp, h->L, dt_h, n == 0, h->stream));
+            CK(h, adjoint_step(tp, vn, an, mat, gp, h->L, dt_h, n == 0, h->adj_fused, h->stream));
         }
     }
     // gradients out (interior cells, x fastest), g_rho = -g_b / rho^2
@@ -1401,6 +1405,64 @@ b2r_status b2r_gol_3D_gpu_main(uint8_t* h_in, int R, const char* edge_flag, int 
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (gpu_seconds) *gpu_seconds = ms / 1000.0;
+    return B2R_OK;
+}
+
+b2r_status b2r_write_block_data(b2r_handle* h, int field, int block, int time_step, const char* dir,
+                                int text, char* path_out, int path_cap)
+{
+    if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
+    if (h->cfg.model == B2R_MODEL_GOL) return fail(h, B2R_ERR_ARG, "block data files hold float cells");
+    if (block < 0 || block >= h->L.nblk) return fail(h, B2R_ERR_ARG, "block %d outside 0..%d", block, h->L.nblk - 1);
+    static const char* const eq_names[10] = {"vx", "vy", "vz", "sxx", "sxy", "sxz",
+                                             "syy", "syz", "szz", "displacement"};
+    const char* name = nullptr;
+    const void* src = nullptr;
+    if (h->cfg.model == B2R_MODEL_HEAT) {
+        if (field == 0) {
+            name = "u";
+            src = h->buf[h->cur];
+        } else if (field == B2R_F_KAPPA && h->mat[0]) {
+            name = "kappa";
+            src = h->mat[0];
+        }
+    } else if (field >= 0 && field < h->nfld) {
+        name = eq_names[field];
+        src = h->fld[field];
+    } else if (field >= B2R_F_LAMBDA && field <= B2R_F_BUOY && h->mat[0]) {
+        static const char* const mat_names[3] = {"lambda", "mu", "buoyancy"};
+        name = mat_names[field - B2R_F_LAMBDA];
+        src = h->mat[field - B2R_F_LAMBDA];
+    }
+    if (!src) return fail(h, B2R_ERR_ARG, "field %d has no data on this handle", field);
+    const BlockLayout& L = h->L;
+    std::string path = dir && dir[0] ? std::string(dir) + "/" : std::string();
+    path += name;
+    if (block > 0) path += "-b" + std::to_string(block);
+    path += "-" + std::to_string(time_step) + (text ? ".txt" : ".bin");
+    const size_t ncell = (size_t)L.n[0] * L.n[1] * L.n[2];
+    std::vector<float> cells(ncell);
+    const float* blk = static_cast<const float*>(src) + (size_t)block * L.bstride + L.xoff;
+    CK(h, cudaMemcpy2DAsync(cells.data(), L.n[0] * sizeof(float), blk, L.P * sizeof(float),
+                            L.n[0] * sizeof(float), (size_t)L.n[1] * L.n[2], cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    std::ofstream out(path, std::ios::binary);
+    if (!out) return fail(h, B2R_ERR_ARG, "cannot open %s", path.c_str());
+    if (text) {
+        for (int z = 0; z < L.n[2]; ++z)
+            for (int y = 0; y < L.n[1]; ++y) {
+                const float* row = cells.data() + ((size_t)z * L.n[1] + y) * L.n[0];
+                for (int x = 0; x < L.n[0]; ++x) out << row[x] << ",";
+                out << "\n";
+            }
+    } else {
+        const int32_t hdr[3] = {L.n[0], L.n[1], L.n[2]};
+        out.write(reinterpret_cast<const char*>(hdr), sizeof(hdr));
+        out.write(reinterpret_cast<const char*>(cells.data()), (std::streamsize)(ncell * sizeof(float)));
+    }
+    out.close();
+    if (!out) return fail(h, B2R_ERR_ARG, "writing %s failed", path.c_str());
+    if (path_out && path_cap > 0) std::snprintf(path_out, (size_t)path_cap, "%s", path.c_str());
     return B2R_OK;
 }
 

@@ -64,7 +64,7 @@ cudaError_t adjoint_sample(const float* vy, const long long* d_idx, int nrec, fl
 cudaError_t adjoint_inject(float* vby, const long long* d_idx, int nrec, const float* res, cudaStream_t st);
 cudaError_t adjoint_step(float* const* tmp, const float* const* v_n, const float* const* acc_n,
                          const float* const* mat, double* const* g, const BlockLayout& L, float dt_h,
-                         bool last, cudaStream_t st);
+                         bool last, bool fused, cudaStream_t st);
 cudaError_t adjoint_grad_out(const double* g, const float* buoy, int rho, const BlockLayout& L,
                              double* out, cudaStream_t st);
 

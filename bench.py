@@ -480,6 +480,9 @@ def run_adjoint(args, wl):
     d_obs = d.eqwp_record(n, rec)
     d.close()
     d, zero = domain(model(0.0))
+    tune = tuning_of(args)
+    if tune:
+        d.set_tuning(**tune)
     torch.cuda.synchronize()
     fwd_ms = []
     for _ in range(max(1, args.warmup // 2)):
@@ -528,7 +531,7 @@ def run_adjoint(args, wl):
                        "forward_ms": round(fms, 1), "gradient_ms": round(gms, 1),
                        "first_gradient_ms": round(first_ms, 1),
                        "gradient_over_forward": round(gms / fms, 3), "misfit": J,
-                       "l2": "inputs larger than L2"},
+                       "l2": "inputs larger than L2", **({"tuning": tune} if tune else {})},
             "e2e": None, "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "achieved": round(wl["bytes_per_cell"] * value, 1),
                          "peak": peak, "unit": "GB/s",

@@ -127,8 +127,11 @@ enum {
     B2R_TUNE_ZCHUNK2 = 5,      /* planes per work unit of the two-step sweep (0 = 16) */
     B2R_TUNE_EQWP_FUSED = 6,   /* staggered elastic wave: 1 = one-pass step, 0 = the velocity
                                   and stress stages as two passes (default); bit-identical */
-    B2R_TUNE_GOL_BYTES = 7     /* Game of Life one-generation kernel: 0 = bit-sliced cells
+    B2R_TUNE_GOL_BYTES = 7,    /* Game of Life one-generation kernel: 0 = bit-sliced cells
                                   (default), 1 = four byte cells per word; identical results */
+    B2R_TUNE_ADJ_FUSED = 8     /* elastic-wave adjoint: 1 = the stress adjoint and the lambda /
+                                  mu gradients in one sweep (default), 0 = two kernels;
+                                  bit-identical */
 };
 b2r_status b2r_set_tuning(b2r_handle* h, int key, int value);
 /* Current value of a knob (after b2r_autotune: the schedule it picked). */
@@ -205,6 +208,17 @@ b2r_status b2r_heat_3D_gpu_main_noalloc(const float* d_in, float* d_out, int R, 
  * the handle's fields (model B2R_MODEL_EQWP_REF), ts = the outer time step
  * (selects the body force, eqwp.cu:135).  Does not exchange halos. */
 b2r_status b2r_eqwp_gpu_main(b2r_handle* h, int ts, int R, double* gpu_seconds);
+/* write_block_data_bin / write_block_data (eqwp.cu:616-651): one padded
+ * block of a float field (halos included, Ngx*Ngy*Ngz cells, x fastest) to
+ * <dir>/<name>-<time_step>.bin as an int32[3] {Ngx, Ngy, Ngz} header and the
+ * cells, or with text != 0 to <dir>/<name>-<time_step>.txt as "v," per cell
+ * and one line per row.  name is "displacement" for B2R_F_DISP (the
+ * reference's file) and otherwise the field's own name (u, kappa, vx .. szz,
+ * lambda, mu, buoyancy); a block other than 0 appends "-b<block>".  dir NULL
+ * is the working directory.  The path written is copied to path_out (may be
+ * NULL) of path_cap bytes.  Game-of-Life cells are bytes: B2R_ERR_ARG. */
+b2r_status b2r_write_block_data(b2r_handle* h, int field, int block, int time_step, const char* dir,
+                                int text, char* path_out, int path_cap);
 
 /* ---- adjoint of the staggered elastic wave (no reference counterpart) ---- */
 /* Forward nsteps from the current fields and record vy at nrec receivers

@@ -124,3 +124,20 @@ def test_autograd_matches_central_differences(b2r):
         gnorm = float(sum(((g * sc) ** 2).sum() for g, sc in
                           zip((lam.grad, mu.grad, rho.grad), scale)) ** 0.5)
         assert abs(fd - an) <= 1e-3 * max(abs(an), gnorm), trial
+
+
+def test_fused_stress_gradient_sweep_changes_no_bits(b2r):
+    """The stress adjoint with the lambda / mu gradients in one sweep and as
+    two kernels give the same bits."""
+    P = problem(env=(22, 18, 20), nsteps=24)
+    d_obs = observed(b2r, P)
+    mat = layered(P["env"])
+    res = []
+    for fused in (1, 0):
+        with gpu_domain(b2r, P, mat) as d:
+            d.set_tuning(adj_fused=fused)
+            assert d.get_tuning()["adj_fused"] == fused
+            res.append(d.eqwp_misfit_gradient(P["nsteps"], P["rec"], d_obs, ckpt_every=8))
+    assert res[0][0] == res[1][0]
+    for a, b in zip(res[0][1], res[1][1]):
+        assert np.array_equal(a, b)
