@@ -49,6 +49,7 @@ struct b2r_handle {
     bool eqwp_fused = false;   // two-pass by default: faster on this GPU so far
     bool gol_bytes = false;    // Game of Life: byte-SWAR kernel instead of bit-sliced cells
     bool adj_fused = true;     // adjoint: stress adjoint + lambda/mu gradients in one sweep
+    bool gol_push = false;     // Game of Life: period-end passes fill the next period's halos (opt-in: slower so far)
     float* mat[3] = {};
     std::vector<float> src;     // per-step source increment of sxx/syy/szz (STAG)
     void* staging = nullptr;
@@ -360,16 +361,22 @@ b2r_status advance(b2r_handle* h, int n)
             if ((st = exchange_all(h, false)) != B2R_OK) return st;
         h->halos_fresh = false;
         const int gg = gol_pass_gens(h, i, n - s);
+        // a bit-sliced pass that ends a period stores the next period's halos
+        // itself, so that period starts without the gather
+        const bool push = gg >= 2 && !h->gol_bytes && h->gol_push && i + gg == h->cfg.R &&
+                          (h->L.nblk > 1 || h->L.periodic);
         if (gg >= 2) {
             if (h->gol_bytes)
                 CK(h, launch_gol_period(static_cast<const uint8_t*>(h->buf[h->cur]),
                                         static_cast<uint8_t*>(h->buf[1 - h->cur]), h->L, i, gg, h->stream));
             else
                 CK(h, launch_gol_bits_period(static_cast<const uint8_t*>(h->buf[h->cur]),
-                                             static_cast<uint8_t*>(h->buf[1 - h->cur]), h->L, i, gg, h->stream));
+                                             static_cast<uint8_t*>(h->buf[1 - h->cur]), h->L, i, gg, push,
+                                             h->stream));
             h->cur = 1 - h->cur;
             h->ts += gg;
             s += gg;
+            h->halos_fresh = push;
         } else if (n - s >= 2 && heat_fuse_ok(h, i)) {
             if ((st = substep2(h, i)) != B2R_OK) return st;
             h->ts += 2;
@@ -818,6 +825,7 @@ b2r_status b2r_set_tuning(b2r_handle* h, int key, int value)
     case B2R_TUNE_EQWP_FUSED: h->eqwp_fused = value != 0; break;
     case B2R_TUNE_GOL_BYTES: h->gol_bytes = value != 0; break;
     case B2R_TUNE_ADJ_FUSED: h->adj_fused = value != 0; break;
+    case B2R_TUNE_GOL_PUSH: h->gol_push = value != 0; break;
     default: return fail(h, B2R_ERR_ARG, "unknown tuning key %d", key);
     }
     drop_graphs(h);
@@ -836,6 +844,7 @@ b2r_status b2r_get_tuning(const b2r_handle* h, int key, int* value)
     case B2R_TUNE_EQWP_FUSED: *value = h->eqwp_fused ? 1 : 0; break;
     case B2R_TUNE_GOL_BYTES: *value = h->gol_bytes ? 1 : 0; break;
     case B2R_TUNE_ADJ_FUSED: *value = h->adj_fused ? 1 : 0; break;
+    case B2R_TUNE_GOL_PUSH: *value = h->gol_push ? 1 : 0; break;
     default: return fail(nullptr, B2R_ERR_ARG, "unknown tuning key %d", key);
     }
     return B2R_OK;

@@ -21,9 +21,11 @@ int gol_max_generations_per_pass();
 cudaError_t launch_gol_bits_substep(const uint8_t* in, uint8_t* out, const BlockLayout& L, int step_i,
                                    cudaStream_t st);
 // ng generations (sub-steps i0 .. i0+ng-1) in one pass on bit-sliced cells;
-// only the window of the last one is written to `out`.
+// only the window of the last one is written to `out`.  push_halos (a pass
+// that ends a period) also copies the new band cells into the neighbour
+// blocks' halos of `out`, as the next period's halo gather would.
 cudaError_t launch_gol_bits_period(const uint8_t* in, uint8_t* out, const BlockLayout& L, int i0, int ng,
-                                   cudaStream_t st);
+                                   bool push_halos, cudaStream_t st);
 int gol_bits_max_generations_per_pass();
 
 }  // namespace b2r

@@ -217,7 +217,64 @@ struct GolBitsPeriod {
     int kx0, OW;         // first output word (32-byte units of the row) of tile 0, output words per tile
     int y0, OR, PR;      // first output row, output rows per band, region rows (multiple of 4)
     int nzc;
+    int push;            // the pass ends a period: push band cells into the neighbours' halos
 };
+
+// The halo exchange folded into the pass that ends a period: after its
+// output is stored, each CTA copies the part of its output box that the
+// halo gather (halo.cu) would send to the neighbour blocks.  Region d of
+// block t is owner t + d's cells p with p_a in [B_a, B_a + H) for d_a < 0,
+// [H, 2H) for d_a > 0 and any interior p_a for d_a = 0, stored at p + d B;
+// no region crosses a non-periodic domain edge.  Every row piece moves in
+// the widest vector that its length and both starts allow.
+__device__ __forceinline__ void push_box(const BlockLayout& L, int blk, uint8_t* out, const int (&blo)[3],
+                                         const int (&bhi)[3])
+{
+    const int H = L.H;
+    const int bc[3] = {blk % L.nb[0], (blk / L.nb[0]) % L.nb[1], blk / (L.nb[0] * L.nb[1])};
+    for (int r = 0; r < 27; ++r) {
+        const int d[3] = {r % 3 - 1, (r / 3) % 3 - 1, r / 9 - 1};
+        if (r == 13) continue;
+        int lo[3], hi[3], t[3];
+        bool ok = true;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const int sl = d[q] < 0 ? L.B[q] : H, sh = d[q] < 0 ? L.B[q] + H - 1 : (d[q] > 0 ? 2 * H - 1 : H + L.B[q] - 1);
+            lo[q] = max(sl, blo[q]);
+            hi[q] = min(sh, bhi[q]);
+            ok = ok && lo[q] <= hi[q];
+            t[q] = bc[q] - d[q];
+            if (t[q] < 0 || t[q] >= L.nb[q]) {
+                if (!L.periodic) ok = false;
+                t[q] = (t[q] + L.nb[q]) % L.nb[q];
+            }
+        }
+        if (!ok) continue;     // uniform over the CTA
+        const long long tb = t[0] + (long long)L.nb[0] * (t[1] + L.nb[1] * t[2]);
+        const long long so = (long long)blk * L.bstride + L.xoff + lo[0];
+        const long long doff = tb * L.bstride - (long long)blk * L.bstride +
+                               (long long)d[2] * L.B[2] * L.plane + (long long)d[1] * L.B[1] * L.P + d[0] * L.B[0];
+        const int len = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+        int vb = 16;
+        while (vb > 1 && ((len % vb) || (so % vb) || ((so + doff) % vb))) vb >>= 1;
+        const int nv = len / vb;
+        const int total = nv * ny * nz;
+        for (int e = threadIdx.x; e < total; e += blockDim.x) {
+            const int v = e % nv, rr = e / nv;
+            const int y = lo[1] + rr % ny, z = lo[2] + rr / ny;
+            const long long s0 = so + (long long)z * L.plane + (long long)y * L.P + (long long)v * vb;
+            uint8_t* dp = out + s0 + doff;
+            const uint8_t* sp = out + s0;
+            switch (vb) {
+            case 16: *reinterpret_cast<uint4*>(dp) = __ldcg(reinterpret_cast<const uint4*>(sp)); break;
+            case 8: *reinterpret_cast<uint2*>(dp) = __ldcg(reinterpret_cast<const uint2*>(sp)); break;
+            case 4: *reinterpret_cast<uint32_t*>(dp) = __ldcg(reinterpret_cast<const unsigned int*>(sp)); break;
+            case 2: *reinterpret_cast<uint16_t*>(dp) = __ldcg(reinterpret_cast<const unsigned short*>(sp)); break;
+            default: *dp = __ldcg(reinterpret_cast<const unsigned char*>(sp)); break;
+            }
+        }
+    }
+}
 
 template <int GW>
 __global__ void __launch_bounds__(512)
@@ -356,6 +413,20 @@ gol_bits_period_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out
             }
         }
     }
+    if (G.push) {
+        // the pass ends a period: copy this CTA's band cells, just written
+        // and still in L2, into the neighbours' halos
+        __syncthreads();
+        int box_lo[3], box_hi[3];
+        const int kwa = G.kx0 + blockIdx.x * G.OW;
+        box_lo[0] = max(32 * kwa - L.xoff, flo[0]);
+        box_hi[0] = min(32 * (kwa + G.OW) - L.xoff - 1, fhi[0]);
+        box_lo[1] = max(yb + ng, flo[1]);
+        box_hi[1] = min(yb + ng + G.OR - 1, fhi[1]);
+        box_lo[2] = zs;
+        box_hi[2] = ze;
+        push_box(L, blk, out, box_lo, box_hi);
+    }
 }
 
 }  // namespace
@@ -406,7 +477,7 @@ cudaError_t launch_gol_bits_substep(const uint8_t* in, uint8_t* out, const Block
 int gol_bits_max_generations_per_pass() { return kBMaxGen; }
 
 cudaError_t launch_gol_bits_period(const uint8_t* in, uint8_t* out, const BlockLayout& L, int i0, int ng,
-                                   cudaStream_t st)
+                                   bool push_halos, cudaStream_t st)
 {
     if (ng < 1 || ng > kBMaxGen) return cudaErrorInvalidValue;
     int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-1, -1, -1};
@@ -423,6 +494,7 @@ cudaError_t launch_gol_bits_period(const uint8_t* in, uint8_t* out, const BlockL
     GolBitsPeriod G{};
     G.ng = ng;
     G.i0 = i0;
+    G.push = push_halos ? 1 : 0;
     G.kx0 = (L.xoff + lo[0]) >> 5;
     const int nwt = ((L.xoff + hi[0]) >> 5) - G.kx0 + 1;
     int GW = 32;

@@ -129,9 +129,13 @@ enum {
                                   and stress stages as two passes (default); bit-identical */
     B2R_TUNE_GOL_BYTES = 7,    /* Game of Life one-generation kernel: 0 = bit-sliced cells
                                   (default), 1 = four byte cells per word; identical results */
-    B2R_TUNE_ADJ_FUSED = 8     /* elastic-wave adjoint: 1 = the stress adjoint and the lambda /
+    B2R_TUNE_ADJ_FUSED = 8,    /* elastic-wave adjoint: 1 = the stress adjoint and the lambda /
                                   mu gradients in one sweep (default), 0 = two kernels;
                                   bit-identical */
+    B2R_TUNE_GOL_PUSH = 9      /* Game of Life: 1 = a several-generation pass that ends a period
+                                  also fills the next period's halos, so no gather runs between
+                                  periods; 0 = the gather (default, faster on this GPU so far);
+                                  identical results */
 };
 b2r_status b2r_set_tuning(b2r_handle* h, int key, int value);
 /* Current value of a knob (after b2r_autotune: the schedule it picked). */
