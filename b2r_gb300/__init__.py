@@ -84,6 +84,7 @@ def lib():
         "b2r_get_tuning": ([vp, i, C.POINTER(i)], i),
         "b2r_autotune": ([vp, i, C.POINTER(C.c_int), C.POINTER(d)], i),
         "b2r_run_host": ([vp, i, vp, i, vp], i),
+        "b2r_run_host_batch": ([vp, i, C.POINTER(vp), C.POINTER(vp), i, i], i),
         "b2r_time_step": ([vp], C.c_int64),
         "b2r_set_source": ([vp, C.POINTER(C.c_float), i], i),
         "b2r_boundary_updating_direct": ([vp, i, i], i),
@@ -296,6 +297,22 @@ class Domain:
         po, _ = _ptr(host_out)
         _check(lib().b2r_run_host(self.h, FIELDS.get(field, field), pi, int(nsteps), po), self.h)
         return host_out
+
+    def run_host_batch(self, host_ins, nsteps, host_outs, field=0):
+        """run_host over several independent inputs, the copies of the next
+        input and the previous result overlapping the stepping."""
+        if len(host_ins) != len(host_outs):
+            raise ValueError("one output per input")
+        n = len(host_ins)
+        need = int(np.prod(self.domain_shape)) * np.dtype(self.dtype).itemsize
+        for a in list(host_ins) + list(host_outs):
+            nb = a.nbytes if isinstance(a, np.ndarray) else a.numel() * a.element_size()
+            if nb != need:
+                raise ValueError("every buffer holds %d bytes (the domain array), got %d" % (need, nb))
+        pi = (C.c_void_p * max(n, 1))(*[_ptr(a)[0].value for a in host_ins])
+        po = (C.c_void_p * max(n, 1))(*[_ptr(a)[0].value for a in host_outs])
+        _check(lib().b2r_run_host_batch(self.h, FIELDS.get(field, field), pi, po, n, int(nsteps)), self.h)
+        return host_outs
 
     def set_source(self, amps):
         a = np.ascontiguousarray(amps, np.float32)

@@ -54,6 +54,12 @@ struct b2r_handle {
     std::vector<float> src;     // per-step source increment of sxx/syy/szz (STAG)
     void* staging = nullptr;
     size_t staging_bytes = 0;
+    // pipelined host runs: two input and two output device buffers, a copy
+    // stream per direction, and the events that order them
+    void* pipe[4] = {};
+    size_t pipe_bytes = 0;
+    cudaStream_t cin = nullptr, cout = nullptr;
+    cudaEvent_t ev[4][2] = {};   // [in ready, input consumed, output gathered, output copied][slot]
     void* bounce = nullptr;
     size_t bounce_bytes = 0;
     int* d_status = nullptr;
@@ -583,6 +589,13 @@ b2r_status b2r_destroy(b2r_handle* h)
     for (int m = 0; m < 3; ++m)
         if (h->mat[m]) cudaFree(h->mat[m]);
     if (h->staging) cudaFree(h->staging);
+    for (void* p : h->pipe)
+        if (p) cudaFree(p);
+    for (auto& e2 : h->ev)
+        for (cudaEvent_t e : e2)
+            if (e) cudaEventDestroy(e);
+    if (h->cin) cudaStreamDestroy(h->cin);
+    if (h->cout) cudaStreamDestroy(h->cout);
     if (h->bounce) cudaFree(h->bounce);
     if (h->d_status) cudaFree(h->d_status);
     delete h;
@@ -782,6 +795,73 @@ b2r_status b2r_run_host(b2r_handle* h, int field, const void* host_in, int nstep
     if ((st = b2r_upload(h, field, host_in, 0)) != B2R_OK) return st;
     if ((st = b2r_step(h, nsteps)) != B2R_OK) return st;
     if ((st = b2r_download(h, field, host_out, 0)) != B2R_OK) return st;
+    return check_status(h);
+}
+
+// Pipelined b2r_run_host over `count` independent inputs: while problem i
+// steps on the handle's stream, the input of problem i+1 is copied in on one
+// copy stream and the result of problem i-1 copied out on the other.
+b2r_status b2r_run_host_batch(b2r_handle* h, int field, const void* const* host_in, void* const* host_out,
+                              int count, int nsteps)
+{
+    if (!h || !host_in || !host_out || count < 0) return fail(h, B2R_ERR_ARG, "invalid argument");
+    if (h->nfld > 0) return fail(h, B2R_ERR_ARG, "pipelined host runs cover the heat and Game-of-Life models");
+    if (field != 0) return fail(h, B2R_ERR_ARG, "invalid field id %d", field);
+    for (int i = 0; i < count; ++i)
+        if (!host_in[i] || !host_out[i]) return fail(h, B2R_ERR_ARG, "null buffer for problem %d", i);
+    const size_t bytes = domain_cells(h) * h->cell_bytes;
+    if (h->pipe_bytes < bytes) {
+        for (void*& p : h->pipe) {
+            if (p) cudaFree(p);
+            p = nullptr;
+        }
+        h->pipe_bytes = 0;
+        for (void*& p : h->pipe) CK(h, cudaMalloc(&p, bytes));
+        h->pipe_bytes = bytes;
+    }
+    if (!h->cin) {
+        CK(h, cudaStreamCreateWithFlags(&h->cin, cudaStreamNonBlocking));
+        CK(h, cudaStreamCreateWithFlags(&h->cout, cudaStreamNonBlocking));
+        for (auto& e2 : h->ev)
+            for (cudaEvent_t& e : e2) CK(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    enum { IN_READY, IN_FREE, OUT_READY, OUT_FREE };
+    void* const* in = h->pipe;
+    void* const* out = h->pipe + 2;
+    // nothing is pending from an earlier call: every wait below refers to an
+    // event recorded in this call or never recorded (a no-op)
+    CK(h, cudaStreamSynchronize(h->cin));
+    CK(h, cudaStreamSynchronize(h->cout));
+    for (auto& e2 : h->ev)
+        for (cudaEvent_t& e : e2) {
+            cudaEventDestroy(e);
+            CK(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        }
+    if (count > 0) {
+        CK(h, cudaMemcpyAsync(in[0], host_in[0], bytes, cudaMemcpyHostToDevice, h->cin));
+        CK(h, cudaEventRecord(h->ev[IN_READY][0], h->cin));
+    }
+    b2r_status st;
+    for (int i = 0; i < count; ++i) {
+        const int k = i & 1, k1 = (i + 1) & 1;
+        if (i + 1 < count) {   // next input, once problem i-1 has consumed that slot
+            CK(h, cudaStreamWaitEvent(h->cin, h->ev[IN_FREE][k1], 0));
+            CK(h, cudaMemcpyAsync(in[k1], host_in[i + 1], bytes, cudaMemcpyHostToDevice, h->cin));
+            CK(h, cudaEventRecord(h->ev[IN_READY][k1], h->cin));
+        }
+        CK(h, cudaStreamWaitEvent(h->stream, h->ev[IN_READY][k], 0));
+        if ((st = b2r_upload(h, field, in[k], 1)) != B2R_OK) return st;
+        CK(h, cudaEventRecord(h->ev[IN_FREE][k], h->stream));
+        if ((st = b2r_step(h, nsteps)) != B2R_OK) return st;
+        CK(h, cudaStreamWaitEvent(h->stream, h->ev[OUT_FREE][k], 0));   // result of problem i-2 copied out
+        if ((st = b2r_download(h, field, out[k], 1)) != B2R_OK) return st;
+        CK(h, cudaEventRecord(h->ev[OUT_READY][k], h->stream));
+        CK(h, cudaStreamWaitEvent(h->cout, h->ev[OUT_READY][k], 0));
+        CK(h, cudaMemcpyAsync(host_out[i], out[k], bytes, cudaMemcpyDeviceToHost, h->cout));
+        CK(h, cudaEventRecord(h->ev[OUT_FREE][k], h->cout));
+    }
+    CK(h, cudaStreamSynchronize(h->cout));
+    CK(h, cudaStreamSynchronize(h->stream));
     return check_status(h);
 }
 
