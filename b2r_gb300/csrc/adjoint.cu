@@ -417,28 +417,6 @@ inline int grid_for(long long work)
 }  // namespace
 
 // ---------------------------------------------------------------- driver
-// All device buffers of one gradient computation.
-struct AdjointRun {
-    BlockLayout L;
-    size_t fb = 0;
-    std::vector<float*> ckpt;        // 9 fields per checkpoint
-    std::vector<float*> replay;      // 9 fields per replayed state
-    float* tmp[18] = {};             // vb(3) sb(6) q(6) w(3)
-    double* g[3] = {};
-    long long* d_idx = nullptr;
-    float* d_rec = nullptr;          // nsteps*nrec synthetic data
-    float* d_res = nullptr;          // nsteps*nrec residual
-    ~AdjointRun()
-    {
-        for (float* p : ckpt) cudaFree(p);
-        for (float* p : replay) cudaFree(p);
-        for (float* p : tmp) if (p) cudaFree(p);
-        for (double* p : g) if (p) cudaFree(p);
-        if (d_idx) cudaFree(d_idx);
-        if (d_rec) cudaFree(d_rec);
-        if (d_res) cudaFree(d_res);
-    }
-};
 
 cudaError_t adjoint_sample(const float* vy, const long long* d_idx, int nrec, float* out, cudaStream_t st)
 {
