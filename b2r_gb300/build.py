@@ -1,7 +1,9 @@
 """Build libb2r.so in-tree for sm_103a (GB300).
 
 Each translation unit of csrc/ is compiled by nvcc in parallel and linked
-into b2r_gb300/libb2r.so.  No torch, no cmake.  Used by
+into b2r_gb300/libb2r.so; host/b2r_main.cpp (the simulation main over the C
+ABI) is compiled by the host C++ compiler into b2r_gb300/b2r_main.  No
+torch, no cmake.  Used by
 __graft_entry__.build() here and on the GPU host.
 """
 import concurrent.futures as cf
@@ -13,6 +15,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libb2r.so")
+MAIN_SRC = os.path.join(HERE, "host", "b2r_main.cpp")
+MAIN = os.path.join(HERE, "b2r_main")
+CXX = os.environ.get("CXX", "g++")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
@@ -52,7 +57,22 @@ def build(verbose_ptxas=False, force=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_main(force)
     return LIB
+
+
+def build_main(force=False):
+    """The C++ host program (b2r.cpp's main over the C ABI), linked to
+    libb2r.so beside it."""
+    if not force and os.path.exists(MAIN) and os.path.getmtime(MAIN) > max(
+            os.path.getmtime(MAIN_SRC), os.path.getmtime(LIB)):
+        return MAIN
+    cmd = [CXX, "-std=c++17", "-O2", "-Wall", "-I", os.path.join(HERE, "..", "include"), MAIN_SRC,
+           "-L", HERE, "-lb2r", "-Wl,-rpath,$ORIGIN", "-o", MAIN]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"b2r_main build failed:\n{r.stdout}\n{r.stderr}")
+    return MAIN
 
 
 if __name__ == "__main__":

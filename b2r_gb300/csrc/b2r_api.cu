@@ -65,6 +65,8 @@ struct b2r_handle {
     int* d_status = nullptr;
     long long ts = 0;
     bool halos_fresh = false;
+    unsigned xmask = 0;          // fields exchanged by the caller at time step xts
+    long long xts = -1;
     // CUDA graphs of whole periods (heat, GoL on a non-default stream)
     bool graphs = true;
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};   // by ping-pong buffer at start
@@ -873,13 +875,28 @@ b2r_status b2r_set_source(b2r_handle* h, const float* amps, int n)
     return B2R_OK;
 }
 
+// A caller that exchanges every field at a period start (b2r.cpp:197-206)
+// leaves the halos fresh: the next b2r_step starts without its own exchange.
+static b2r_status note_exchange(b2r_handle* h, int field, b2r_status st)
+{
+    if (st != B2R_OK || h->ts % h->cfg.R != 0) return st;
+    if (h->xts != h->ts) {
+        h->xmask = 0;
+        h->xts = h->ts;
+    }
+    h->xmask |= 1u << field;
+    const int nf = (h->cfg.model == B2R_MODEL_EQWP_REF || h->cfg.model == B2R_MODEL_EQWP_STAG) ? h->nfld : 1;
+    if (h->xmask == (nf >= 32 ? ~0u : (1u << nf) - 1u)) h->halos_fresh = true;
+    return st;
+}
+
 b2r_status b2r_boundary_updating_direct(b2r_handle* h, int time_step, int field)
 {
     (void)time_step;
     if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
     if (field < 0 || field >= (h->nfld > 0 ? h->nfld : 1))
         return fail(h, B2R_ERR_ARG, "invalid field id %d", field);
-    return exchange_one(h, field, false);
+    return note_exchange(h, field, exchange_one(h, field, false));
 }
 
 b2r_status b2r_boundary_updating(b2r_handle* h, int time_step, int field)
@@ -888,7 +905,7 @@ b2r_status b2r_boundary_updating(b2r_handle* h, int time_step, int field)
     if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
     if (field < 0 || field >= (h->nfld > 0 ? h->nfld : 1))
         return fail(h, B2R_ERR_ARG, "invalid field id %d", field);
-    return exchange_one(h, field, true);
+    return note_exchange(h, field, exchange_one(h, field, true));
 }
 
 // ---------------------------------------------------------------- autotuning
