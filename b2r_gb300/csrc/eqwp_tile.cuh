@@ -326,6 +326,12 @@ struct Grid {
     Tiles t;
 };
 
+#ifndef B2R_EQWP_CTAS
+#define B2R_EQWP_CTAS 24    // CTAs per SM a stage launch aims at (z chunks of the tiles)
+#endif
+#ifndef B2R_EQWP_ZMIN
+#define B2R_EQWP_ZMIN 16    // planes per z chunk at least
+#endif
 #ifndef B2R_EQWP_YHALO
 #define B2R_EQWP_YHALO 0    // cost of a re-read halo row against a computed row, percent (0 measured best)
 #endif
@@ -368,9 +374,9 @@ inline Grid stage_grid(const BlockLayout& L, int shrink)
     const int tx = std::max(1, (G4 + bx - 1) / bx);
     const int ty = std::max(1, (Hy + by - 1) / by);
     const long long tiles = (long long)tx * ty * L.nblk;
-    const long long want = 152LL * 8 * 3;
+    const long long want = 152LL * B2R_EQWP_CTAS;
     int nzc = (int)((want + tiles - 1) / tiles);
-    int maxc = (hi[2] - lo[2] + 1) / 16;
+    int maxc = (hi[2] - lo[2] + 1) / B2R_EQWP_ZMIN;
     if (maxc < 1) maxc = 1;
     if (nzc > maxc) nzc = maxc;
     if (nzc < 1) nzc = 1;

@@ -532,7 +532,8 @@ def run_adjoint(args, wl):
                        "receivers": len(rec), "checkpoint_every": wl["ckpt"],
                        "forward_ms": round(fms, 1), "gradient_ms": round(gms, 1),
                        "first_gradient_ms": round(first_ms, 1),
-                       "gradient_over_forward": round(gms / fms, 3), "misfit": J,
+                       "gradient_over_forward": round(gms / fms, 3),
+                       "reverse_over_forward": round((gms - fms) / fms, 3), "misfit": J,
                        "l2": "inputs larger than L2", **({"tuning": tune} if tune else {})},
             "e2e": None, "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "achieved": round(wl["bytes_per_cell"] * value, 1),
