@@ -47,9 +47,12 @@ __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.lau
 #endif
 
 // resident CTAs per SM the register budget is fitted to, by stencil radius
+#ifndef B2R_HEAT4_MINB
+#define B2R_HEAT4_MINB 2
+#endif
 template <int D>
 struct MinBlocks {
-    static constexpr int value = D == 1 ? 5 : (D == 2 ? 3 : 2);
+    static constexpr int value = D == 1 ? 5 : (D == 2 ? 3 : (D == 3 ? 2 : B2R_HEAT4_MINB));
 };
 
 template <int D, int RY, int S>

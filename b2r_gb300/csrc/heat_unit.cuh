@@ -132,7 +132,10 @@ __device__ __forceinline__ bool sweep_unit(const CUtensorMap* tmap, float* __res
 #ifndef B2R_SWEEP_UNROLL
 #define B2R_SWEEP_UNROLL 1
 #endif
-    constexpr int kUnroll = (B2R_SWEEP_UNROLL && (D <= 3 || RY == 1)) ? 2 * D + 1 : 1;
+#ifndef B2R_HEAT4_UNROLL
+#define B2R_HEAT4_UNROLL 0
+#endif
+    constexpr int kUnroll = (B2R_SWEEP_UNROLL && (D <= 3 || RY == 1 || B2R_HEAT4_UNROLL)) ? 2 * D + 1 : 1;
 #pragma unroll kUnroll
     for (int pr = 0; pr < np; ++pr) {
         const unsigned g = gp + pr;
