@@ -4,7 +4,7 @@ Each translation unit of csrc/ is compiled by nvcc in parallel and linked
 into b2r_gb300/libb2r.so; host/b2r_main.cpp (the simulation main over the C
 ABI) is compiled by the host C++ compiler into b2r_gb300/b2r_main.  No
 torch, no cmake.  Used by
-__graft_entry__.build() here and on the GPU host.
+__graft_entry__.build() on every machine (nvcc compiles without a GPU).
 """
 import concurrent.futures as cf
 import glob

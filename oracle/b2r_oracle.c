@@ -1,7 +1,8 @@
 /*
  * b2r_oracle.c -- CPU restatement of the B2R stencil hot path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the CUDA path, never part of it.
+ * TEST INFRASTRUCTURE ONLY: what the tests compare the CUDA path against,
+ * never part of it.
  * Built with -ffp-contract=off so that float and double expressions are
  * evaluated exactly as written on x86-64 and on aarch64 alike (the
  * reference's CPU build has no FMA contraction on x86-64 either).

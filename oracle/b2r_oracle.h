@@ -1,8 +1,8 @@
 /*
  * b2r_oracle.h -- CPU restatement of the B2R stencil hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA
- * implementation in b2r_gb300/csrc; only tests/, __graft_entry__.smoke() and
+ * TEST INFRASTRUCTURE ONLY.  The tests compare the CUDA implementation in
+ * b2r_gb300/csrc against this library; only tests/, __graft_entry__.smoke() and
  * bench.py's CPU-baseline leg may load it.  The product path never calls it.
  *
  * Storage convention (identical to the reference, heat-3D.cpp:42-45):

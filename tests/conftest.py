@@ -22,7 +22,7 @@ def orc():
 
 @pytest.fixture(scope="session")
 def b2r():
-    """The product package; on a GPU host the library must load (no fallback)."""
+    """The product package; on a machine with a GPU the library must load (no fallback)."""
     import b2r_gb300
     b2r_gb300.lib()
     return b2r_gb300

@@ -1,7 +1,7 @@
 """GPU parity of the heat kernels (delta1-4) against the oracle.
 
 Tolerance: FP32 on the GPU vs the oracle's FP32-storage restatement of the
-reference arithmetic: relative L2 <= 1e-5 (the benchmark spec's bound).  The
+reference arithmetic: relative L2 <= 1e-5 (the bound for FP32 work).  The
 oracle itself is bit-exact to the reference's heat_3D_cpu_main (see
 test_oracle.py), so the chain GPU ~ oracle == reference holds.  Each case also
 reports the error against the FP64 run of the same scheme.

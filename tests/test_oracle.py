@@ -1,4 +1,5 @@
-"""CPU tests of the oracle: pinned to the reference, then used as the checker.
+"""CPU tests of the oracle: pinned to the reference, then used as the reference
+for the GPU tests.
 
 * bit-exact against the golden fixtures produced by the reference's own
   heat_3D_cpu_main (tests/golden/gen_golden.py);
