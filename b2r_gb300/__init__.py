@@ -243,11 +243,13 @@ class Domain:
         return out
 
     def autotune(self, trial_steps=4):
-        """Pick the fastest heat launch schedule; returns ({...}, ms per step)."""
+        """Pick the fastest launch schedule / kernel choice for this shape
+        (heat, Game of Life, staggered elastic wave); returns (the chosen
+        knobs as get_tuning names them, ms per step or -1 when cached)."""
         best = (C.c_int * 3)()
         ms = C.c_double()
         _check(lib().b2r_autotune(self.h, trial_steps, best, C.byref(ms)), self.h)
-        return {"zchunk": best[0], "ctas_per_sm": best[1], "pdl": best[2]}, ms.value
+        return self.get_tuning(), ms.value
 
     def synchronize(self):
         _check(lib().b2r_synchronize(self.h), self.h)

@@ -947,11 +947,139 @@ b2r_status b2r_get_tuning(const b2r_handle* h, int key, int* value)
     return B2R_OK;
 }
 
+// Game of Life and the staggered elastic wave: the same timed search over
+// their kernel choices -- generations per pass, bit-sliced or byte cells and
+// the period-end halo fill (GoL); the one-pass or two-pass step (elastic
+// wave).  Trials run on the live fields, which are restored afterwards.
+struct KnobSet {
+    int tblock, gol_bytes, gol_push, eqwp_fused;
+};
+static std::map<TuneKey, KnobSet> g_knob_cache;
+
+static void apply_knobs(b2r_handle* h, const KnobSet& k)
+{
+    h->tune.tblock = k.tblock;
+    h->gol_bytes = k.gol_bytes != 0;
+    h->gol_push = k.gol_push != 0;
+    h->eqwp_fused = k.eqwp_fused != 0;
+}
+
+static b2r_status autotune_knobs(b2r_handle* h, int trial_steps, int best[3], double* best_ms)
+{
+    auto report = [&](const KnobSet& k, double ms) {
+        if (best) {
+            best[0] = k.tblock;
+            best[1] = h->cfg.model == B2R_MODEL_GOL ? k.gol_bytes : k.eqwp_fused;
+            best[2] = k.gol_push;
+        }
+        if (best_ms) *best_ms = ms;
+    };
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_knob_cache.find(key_of(h));
+        if (it != g_knob_cache.end()) {
+            apply_knobs(h, it->second);
+            report(it->second, -1.0);
+            drop_graphs(h);
+            return B2R_OK;
+        }
+    }
+    std::vector<KnobSet> cands;
+    const KnobSet cur{h->tune.tblock, h->gol_bytes, h->gol_push, h->eqwp_fused};
+    if (h->cfg.model == B2R_MODEL_GOL) {
+        for (int tb : {1, 2, 4})
+            for (int bytes = 0; bytes < 2; ++bytes)
+                for (int push = 0; push < 2; ++push)
+                    if (!push || (tb >= 2 && !bytes)) cands.push_back({tb, bytes, push, cur.eqwp_fused});
+    } else {
+        for (int fused = 0; fused < 2; ++fused) cands.push_back({cur.tblock, cur.gol_bytes, cur.gol_push, fused});
+    }
+    // the state the trials overwrite: the current buffer (GoL) or every
+    // field of the current set with the set's pointers (elastic wave)
+    const size_t fb = field_bytes(h);
+    const bool eq = h->nfld > 0;
+    const int nsave = eq ? h->nfld : 1;
+    std::vector<void*> save((size_t)nsave, nullptr);
+    float* save_fld[kMaxFields];
+    float* save_fld2[kMaxFields];
+    StressMaps save_smaps[2] = {h->smaps[0], h->smaps[1]};
+    std::memcpy(save_fld, h->fld, sizeof save_fld);
+    std::memcpy(save_fld2, h->fld2, sizeof save_fld2);
+    auto release = [&]() {
+        for (void* p : save)
+            if (p) cudaFree(p);
+    };
+    for (int f = 0; f < nsave; ++f) {
+        if (cudaMalloc(&save[(size_t)f], fb) != cudaSuccess) {
+            cudaGetLastError();
+            release();
+            return fail(h, B2R_ERR_OOM, "autotuning needs %zu bytes to keep the fields", fb * nsave);
+        }
+        const void* src = eq ? (const void*)h->fld[f] : h->buf[h->cur];
+        CK(h, cudaMemcpyAsync(save[(size_t)f], src, fb, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    const int save_cur = h->cur;
+    const long long save_ts = h->ts;
+    const bool save_fresh = h->halos_fresh;
+    // trials run as the stepping will (graph replay included, each
+    // candidate's graphs captured in its warm run) and over whole periods:
+    // a single period would not show what a choice costs at period ends
+    const int trial = h->cfg.model == B2R_MODEL_GOL ? std::max(trial_steps, 16 * h->cfg.R) : trial_steps;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    KnobSet bestK = cur;
+    float bestMs = 1e30f;
+    b2r_status st = B2R_OK;
+    for (const KnobSet& k : cands) {
+        apply_knobs(h, k);
+        drop_graphs(h);
+        if ((st = b2r_step(h, trial)) != B2R_OK) break;   // warm (captures graphs)
+        cudaEventRecord(e0, h->stream);
+        if ((st = b2r_step(h, trial)) != B2R_OK) break;
+        cudaEventRecord(e1, h->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < bestMs) {
+            bestMs = ms;
+            bestK = k;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::memcpy(h->fld, save_fld, sizeof save_fld);
+    std::memcpy(h->fld2, save_fld2, sizeof save_fld2);
+    h->smaps[0] = save_smaps[0];
+    h->smaps[1] = save_smaps[1];
+    h->cur = save_cur;
+    h->ts = save_ts;
+    h->halos_fresh = save_fresh;
+    for (int f = 0; f < nsave; ++f) {
+        void* dst = eq ? (void*)h->fld[f] : h->buf[h->cur];
+        cudaMemcpyAsync(dst, save[(size_t)f], fb, cudaMemcpyDeviceToDevice, h->stream);
+    }
+    cudaStreamSynchronize(h->stream);
+    release();
+    apply_knobs(h, st == B2R_OK ? bestK : cur);
+    drop_graphs(h);
+    if (st != B2R_OK) return st;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_knob_cache[key_of(h)] = bestK;
+    }
+    report(bestK, bestMs / trial);
+    return check_status(h);
+}
+
 b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* best_ms)
 {
     if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
-    if (h->cfg.model != B2R_MODEL_HEAT) return fail(h, B2R_ERR_ARG, "autotuning covers the heat sweep");
     if (trial_steps < 1) trial_steps = 4;
+    if (h->cfg.model == B2R_MODEL_GOL || h->cfg.model == B2R_MODEL_EQWP_STAG)
+        return autotune_knobs(h, trial_steps, best, best_ms);
+    if (h->cfg.model != B2R_MODEL_HEAT)
+        return fail(h, B2R_ERR_ARG, "autotuning covers heat, Game of Life and the staggered elastic wave");
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         auto it = g_tune_cache.find(key_of(h));

@@ -574,12 +574,15 @@ def run_ours(args, wl):
         d.set_tuning(**tune)
     host = load_inputs(d, wl, torch, dev)
     d.synchronize()
-    # heat: the library's autotuner picks the launch schedule for this shape
-    # (timed on the live field, which it restores); not part of the timing
+    # the library's autotuner picks the launch schedule / kernel choice for
+    # this shape (timed on the live fields, which it restores); not part of
+    # the timing
     tuned = None
-    if wl["model"] == 1 and not tune:
+    knobs = {1: ("zchunk", "ctas_per_sm", "pdl", "tblock", "zchunk2"),
+             2: ("tblock", "gol_bytes", "gol_push"), 4: ("eqwp_fused",)}
+    if wl["model"] in knobs and not tune:
         d.autotune(trial_steps=4)
-        tuned = {k: v for k, v in d.get_tuning().items() if k in ("zchunk", "ctas_per_sm", "pdl", "tblock", "zchunk2")}
+        tuned = {k: v for k, v in d.get_tuning().items() if k in knobs[wl["model"]]}
     n = wl["sub_steps"]
     cells = wl["env"][0] * wl["env"][1] * wl["env"][2]
     small = config_of(args, wl)["l2"] != "inputs larger than L2"

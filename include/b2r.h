@@ -140,12 +140,16 @@ enum {
 b2r_status b2r_set_tuning(b2r_handle* h, int key, int value);
 /* Current value of a knob (after b2r_autotune: the schedule it picked). */
 b2r_status b2r_get_tuning(const b2r_handle* h, int key, int* value);
-/* Time every schedule candidate (z-chunk length x persistent CTAs per SM x
- * programmatic dependent launch) for trial_steps time steps on the live
- * fields, keep the fastest, restore the fields and the time step.  Results
- * are cached per (model, D, block size, block count) for the process and
- * applied to later handles of the same shape.  best[3] (may be NULL) gets
- * {zchunk, ctas_per_sm, pdl}; *best_ms the time per step (-1 if cached). */
+/* Time every schedule candidate for trial_steps time steps on the live
+ * fields, keep the fastest, restore the fields and the time step.  Heat:
+ * time steps per pass x z-chunk length x persistent CTAs per SM x
+ * programmatic dependent launch, best[3] = {zchunk, ctas_per_sm, pdl}.
+ * Game of Life: generations per pass x bit-sliced / byte cells x period-end
+ * halo fill, best = {tblock, gol_bytes, gol_push}.  Staggered elastic wave:
+ * one-pass or two-pass step, best = {tblock, eqwp_fused, 0}.  Results are
+ * cached per (model, D, block size, block count) for the process and
+ * applied to later handles of the same shape.  best may be NULL; *best_ms
+ * gets the time per step (-1 if cached). */
 b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* best_ms);
 /* Upload, b2r_step, download: the whole job through host buffers. */
 b2r_status b2r_run_host(b2r_handle* h, int field, const void* host_in, int nsteps,

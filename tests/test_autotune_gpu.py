@@ -44,3 +44,44 @@ def test_schedules_bit_identical(b2r, zchunk, cps, pdl):
             d.step(6)
             res.append(d.download())
     assert np.array_equal(res[0], res[1])
+
+
+@pytest.mark.parametrize("model", ["gol", "stag"])
+def test_knob_autotune_keeps_state_and_bits(b2r, model):
+    """Game of Life and the staggered elastic wave: the autotuner times their
+    kernel choices on the live fields, restores them and changes no bits."""
+    import torch
+    rng = np.random.default_rng(5)
+    if model == "gol":
+        env, kw = (64, 64, 64), dict(blocks=(2, 2, 2), R=4, D=1, boundary=b2r.BC_PERIODIC)
+        m = b2r.MODEL_GOL
+        init = {0: (rng.random(env[::-1]) < 0.3).astype(np.uint8)}
+    else:
+        env, kw = (64, 48, 40), dict(blocks=(2, 1, 1), R=2, D=2, dt=1e-3, h=10.0, src=(30, 20, 18))
+        m = b2r.MODEL_EQWP_STAG
+        shape = tuple(e + 4 for e in env[::-1])
+        init = {"lambda": np.full(shape, 2e10, np.float32), "mu": np.full(shape, 1e10, np.float32),
+                "buoy": np.full(shape, 1 / 2400.0, np.float32)}
+        for k in range(9):
+            a = np.zeros(shape, np.float32)
+            a[2:-2, 2:-2, 2:-2] = ((rng.random(env[::-1]) - 0.5) * 1e-2).astype(np.float32)
+            init[k] = a
+    outs = []
+    for tune in (False, True):
+        s = torch.cuda.Stream()
+        with b2r.Domain(m, env, stream=s, **kw) as d:
+            for f, a in init.items():
+                d.upload(a, field=f)
+            d.step(4)
+            if tune:
+                best, ms = d.autotune(2)
+                assert d.time_step == 4
+                if model == "gol":
+                    assert best["tblock"] in (1, 2, 4) and best["gol_bytes"] in (0, 1)
+                else:
+                    assert best["eqwp_fused"] in (0, 1)
+            d.step(6)
+            outs.append([d.download(field=f) for f in (range(9) if model == "stag" else [0])])
+            d.synchronize()
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
