@@ -1243,21 +1243,26 @@ b2r_status b2r_eqwp_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const i
     // (9 fields each), the replayed velocities v^{n0+k} (k = 1..K; k = 0 is
     // the checkpoint) and stencil sums of a segment, the replay's stresses,
     // the adjoint fields and the FP64 gradients
+    // Two replay buffers when the workspace fits: segment s-1 is replayed
+    // on a second stream while segment s runs its reverse steps.
     const size_t gbytes = (size_t)h->L.bstride * sizeof(double);
     const size_t nf_ckpt = nseg * 9, nf_v = (size_t)(K + 1) * 3, nf_a = (size_t)K * 3;
-    const size_t nfields = nf_ckpt + nf_v + nf_a + 6 + 18;
     const size_t fba = (fb + 255) & ~(size_t)255, gba = (gbytes + 255) & ~(size_t)255;
-    const size_t need = nfields * fba + 3 * gba;
-    if (h->adj_ws_bytes < need) {
+    int nbuf = nseg > 1 ? 2 : 1;
+    for (;; --nbuf) {
+        const size_t nfields = nf_ckpt + nbuf * (nf_v + nf_a + 6) + 18;
+        const size_t need = nfields * fba + 3 * gba;
+        if (h->adj_ws_bytes >= need) break;
         if (h->adj_ws) cudaFree(h->adj_ws);
         h->adj_ws = nullptr;
         h->adj_ws_bytes = 0;
-        if (cudaMalloc(&h->adj_ws, need) != cudaSuccess) {
-            cudaGetLastError();
-            h->adj_ws = nullptr;
-            return fail(h, B2R_ERR_OOM, "misfit gradient needs %zu bytes of workspace", need);
+        if (cudaMalloc(&h->adj_ws, need) == cudaSuccess) {
+            h->adj_ws_bytes = need;
+            break;
         }
-        h->adj_ws_bytes = need;
+        cudaGetLastError();
+        h->adj_ws = nullptr;
+        if (nbuf == 1) return fail(h, B2R_ERR_OOM, "misfit gradient needs %zu bytes of workspace", need);
     }
     char* ws = static_cast<char*>(h->adj_ws);
     auto carve = [&](size_t n, std::vector<float*>& out) {
@@ -1266,9 +1271,9 @@ b2r_status b2r_eqwp_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const i
     };
     std::vector<float*> ckpt, vrep, arep, srep, tmp;
     carve(nf_ckpt, ckpt);
-    carve(nf_v, vrep);
-    carve(nf_a, arep);
-    carve(6, srep);
+    carve(nf_v * nbuf, vrep);   // buffer b: entries [b * nf_v, (b + 1) * nf_v)
+    carve(nf_a * nbuf, arep);
+    carve(6 * (size_t)nbuf, srep);
     carve(18, tmp);
     double* gp[3];
     for (int m = 0; m < 3; ++m, ws += gba) {
@@ -1312,38 +1317,80 @@ b2r_status b2r_eqwp_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const i
     if (d_syn) std::copy(syn.begin(), syn.end(), d_syn);
     CK(h, cudaMemcpyAsync(d_res.p, res.data(), sizeof(float) * res.size(), cudaMemcpyHostToDevice, h->stream));
 
-    // reverse sweep, segment by segment: replay the segment forward from its
-    // checkpoint (velocities and stencil sums of every step kept), then run
-    // its reverse steps
+    // reverse sweep, segment by segment: each segment is replayed forward
+    // from its checkpoint into replay buffer sgi % nbuf (velocities and
+    // stencil sums of every step kept), then its reverse steps run.  With two
+    // buffers the replay of the segment below runs on a second stream while
+    // this segment's reverse steps run; the results are the same bits.
     float* const* tp = tmp.data();
     const float* mat[3] = {h->mat[0], h->mat[1], h->mat[2]};
     const float dt_h = (float)(h->cfg.dt / h->cfg.h);
     const EqwpStagParams sp = stag_params(h);
-    float* const* sp6 = srep.data();
+    struct AuxStream {
+        cudaStream_t s = nullptr;
+        cudaEvent_t start = nullptr, rep[2] = {}, rev[2] = {};
+        ~AuxStream()
+        {
+            for (cudaEvent_t e : {start, rep[0], rep[1], rev[0], rev[1]})
+                if (e) cudaEventDestroy(e);
+            if (s) cudaStreamDestroy(s);
+        }
+    } ax;
+    cudaStream_t aux = h->stream;
+    if (nbuf == 2) {
+        CK(h, cudaStreamCreateWithFlags(&ax.s, cudaStreamNonBlocking));
+        for (cudaEvent_t* e : {&ax.start, &ax.rep[0], &ax.rep[1], &ax.rev[0], &ax.rev[1]})
+            CK(h, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+        aux = ax.s;
+        CK(h, cudaEventRecord(ax.start, h->stream));   // the forward and the residual are in place
+        CK(h, cudaStreamWaitEvent(aux, ax.start, 0));
+    }
+    // v^{n0+k} of segment sgi: the checkpoint's velocities for k = 0, replay
+    // slot k of the segment's buffer after
+    auto vslot = [&](long long sgi, int k, int f) -> float* {
+        return k == 0 ? ckpt[sgi * 9 + B2R_F_VX + f] : vrep[(size_t)(sgi % nbuf) * nf_v + (size_t)k * 3 + f];
+    };
+    auto aslot = [&](long long sgi, int k) -> float* const* {
+        return &arep[(size_t)(sgi % nbuf) * nf_a + (size_t)k * 3];
+    };
+    auto replay = [&](long long sgi, cudaStream_t st) -> b2r_status {
+        const int n0 = (int)sgi * K, n1 = std::min(nsteps, n0 + K);
+        float* const* s6 = srep.data() + 6 * (sgi % nbuf);
+        for (int f = 0; f < 6; ++f)
+            CK(h, cudaMemcpyAsync(s6[f], ckpt[sgi * 9 + B2R_F_SXX + f], fb, cudaMemcpyDeviceToDevice, st));
+        for (int n = n0; n < n1; ++n) {
+            const int k = n - n0;
+            const float* vin[3] = {vslot(sgi, k, 0), vslot(sgi, k, 1), vslot(sgi, k, 2)};
+            float* vout[3] = {vslot(sgi, k + 1, 0), vslot(sgi, k + 1, 1), vslot(sgi, k + 1, 2)};
+            CK(h, launch_eqwp_stag_step_replay(vin, s6, vout, aslot(sgi, k), h->mat, h->L, n, sp, st));
+        }
+        return B2R_OK;
+    };
+    if ((st = replay((long long)nseg - 1, aux)) != B2R_OK) return st;
+    if (nbuf == 2) CK(h, cudaEventRecord(ax.rep[(nseg - 1) % 2], aux));
     for (long long sgi = (long long)nseg - 1; sgi >= 0; --sgi) {
         const int n0 = (int)sgi * K;
         const int n1 = std::min(nsteps, n0 + K);
-        // v^{n0+k}: the checkpoint's velocities for k = 0, replay slot k after
-        auto vslot = [&](int k, int f) -> float* {
-            return k == 0 ? ckpt[sgi * 9 + B2R_F_VX + f] : vrep[(size_t)k * 3 + f];
-        };
-        for (int f = 0; f < 6; ++f)
-            CK(h, cudaMemcpyAsync(sp6[f], ckpt[sgi * 9 + B2R_F_SXX + f], fb, cudaMemcpyDeviceToDevice,
-                                  h->stream));
-        for (int n = n0; n < n1; ++n) {
-            const int k = n - n0;
-            const float* vin[3] = {vslot(k, 0), vslot(k, 1), vslot(k, 2)};
-            float* vout[3] = {vslot(k + 1, 0), vslot(k + 1, 1), vslot(k + 1, 2)};
-            float* const* acc = &arep[(size_t)k * 3];
-            CK(h, launch_eqwp_stag_step_replay(vin, sp6, vout, acc, h->mat, h->L, n, sp, h->stream));
+        if (nbuf == 2) {
+            CK(h, cudaStreamWaitEvent(h->stream, ax.rep[sgi % 2], 0));
+            if (sgi >= 1) {
+                const int b1 = (int)((sgi - 1) % 2);
+                // that buffer last served segment sgi + 1, whose reverse steps are queued
+                if (sgi + 1 < (long long)nseg) CK(h, cudaStreamWaitEvent(aux, ax.rev[b1], 0));
+                if ((st = replay(sgi - 1, aux)) != B2R_OK) return st;
+                CK(h, cudaEventRecord(ax.rep[b1], aux));
+            }
         }
         for (int n = n1 - 1; n >= n0; --n) {
             const int k = n - n0;
             CK(h, adjoint_inject(tp[1], didx, nrec, (const float*)d_res.p + (size_t)n * nrec, h->stream));
-            const float* vn[3] = {vslot(k, 0), vslot(k, 1), vslot(k, 2)};
-            const float* an[3] = {arep[(size_t)k * 3], arep[(size_t)k * 3 + 1], arep[(size_t)k * 3 + 2]};
+            const float* vn[3] = {vslot(sgi, k, 0), vslot(sgi, k, 1), vslot(sgi, k, 2)};
+            float* const* a = aslot(sgi, k);
+            const float* an[3] = {a[0], a[1], a[2]};
             CK(h, adjoint_step(tp, vn, an, mat, gp, h->L, dt_h, n == 0, h->adj_fused, h->stream));
         }
+        if (nbuf == 2) CK(h, cudaEventRecord(ax.rev[sgi % 2], h->stream));
+        else if (sgi >= 1 && (st = replay(sgi - 1, h->stream)) != B2R_OK) return st;
     }
     // gradients out (interior cells, x fastest), g_rho = -g_b / rho^2
     double* outs[3] = {grad_lambda, grad_mu, grad_rho};
