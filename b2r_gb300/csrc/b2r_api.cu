@@ -122,6 +122,17 @@ b2r_status fail(b2r_handle* h, b2r_status s, const char* fmt, ...)
                         "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
     } while (0)
 
+struct DevBuf {
+    void* p = nullptr;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf()
+    {
+        if (p) cudaFree(p);
+    }
+};
+
 inline int roundup(int v, int m) { return (v + m - 1) / m * m; }
 
 // cells consumed from the halo by one time step
@@ -999,20 +1010,24 @@ static b2r_status autotune_knobs(b2r_handle* h, int trial_steps, int best[3], do
     const size_t fb = field_bytes(h);
     const bool eq = h->nfld > 0;
     const int nsave = eq ? h->nfld : 1;
-    std::vector<void*> save((size_t)nsave, nullptr);
+    struct SaveBufs {
+        std::vector<void*> p;
+        ~SaveBufs()
+        {
+            for (void* q : p)
+                if (q) cudaFree(q);
+        }
+    } keep;
+    keep.p.assign((size_t)nsave, nullptr);
+    std::vector<void*>& save = keep.p;
     float* save_fld[kMaxFields];
     float* save_fld2[kMaxFields];
     StressMaps save_smaps[2] = {h->smaps[0], h->smaps[1]};
     std::memcpy(save_fld, h->fld, sizeof save_fld);
     std::memcpy(save_fld2, h->fld2, sizeof save_fld2);
-    auto release = [&]() {
-        for (void* p : save)
-            if (p) cudaFree(p);
-    };
     for (int f = 0; f < nsave; ++f) {
         if (cudaMalloc(&save[(size_t)f], fb) != cudaSuccess) {
             cudaGetLastError();
-            release();
             return fail(h, B2R_ERR_OOM, "autotuning needs %zu bytes to keep the fields", fb * nsave);
         }
         const void* src = eq ? (const void*)h->fld[f] : h->buf[h->cur];
@@ -1060,7 +1075,6 @@ static b2r_status autotune_knobs(b2r_handle* h, int trial_steps, int best[3], do
         cudaMemcpyAsync(dst, save[(size_t)f], fb, cudaMemcpyDeviceToDevice, h->stream);
     }
     cudaStreamSynchronize(h->stream);
-    release();
     apply_knobs(h, st == B2R_OK ? bestK : cur);
     drop_graphs(h);
     if (st != B2R_OK) return st;
@@ -1094,8 +1108,9 @@ b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* bes
     // keep the simulation state: trials run on the live buffers, which are
     // restored afterwards
     const size_t fb = field_bytes(h);
-    void* save = nullptr;
-    CK(h, cudaMalloc(&save, fb));
+    DevBuf keep;
+    CK(h, cudaMalloc(&keep.p, fb));
+    void* const save = keep.p;
     CK(h, cudaMemcpyAsync(save, h->buf[h->cur], fb, cudaMemcpyDeviceToDevice, h->stream));
     const int save_cur = h->cur;
     const long long save_ts = h->ts;
@@ -1149,7 +1164,6 @@ b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* bes
     h->graphs = save_graphs;
     cudaMemcpyAsync(h->buf[h->cur], save, fb, cudaMemcpyDeviceToDevice, h->stream);
     cudaStreamSynchronize(h->stream);
-    cudaFree(save);
     if (st != B2R_OK) return st;
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
@@ -1164,16 +1178,6 @@ b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* bes
 // ---------------------------------------------------------------- adjoint (staggered model)
 namespace {
 
-struct DevBuf {
-    void* p = nullptr;
-    DevBuf() = default;
-    DevBuf(const DevBuf&) = delete;
-    DevBuf& operator=(const DevBuf&) = delete;
-    ~DevBuf()
-    {
-        if (p) cudaFree(p);
-    }
-};
 
 b2r_status adj_check(b2r_handle* h)
 {
