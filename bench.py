@@ -14,7 +14,9 @@ value      GLUPS over all ranks, inputs resident in HBM (CUDA events on the
 e2e        the same metric through b2r_run_host_batch: pinned host input -> device,
            sub_steps time steps, device -> pinned host output, every step; the
            copies of the next step's input and the previous step's result
-           overlap the stepping (two copy streams).
+           overlap the stepping (two copy streams).  Elastic wave: every step
+           uploads and downloads each wavefield component through
+           Domain.upload / Domain.download (the material stays resident).
 roofline   dominant kernel: algorithmic bytes per launch (bytes_per_cell x
            cells swept by one launch) / average launch time, against the
            measured HBM copy bandwidth.
@@ -645,6 +647,32 @@ def run_ours(args, wl):
         ems = max_over_ranks((time.perf_counter() - t0) * 1000.0, dev, world) / args.steps
         e2e_val = replicas_glups(world, cells, n, ems)
         h2d = d2h = host.nbytes
+    elif wl["model"] in (3, 4):
+        # elastic wave: every step uploads the wavefield (its input; the
+        # material stays resident) from pinned host memory, runs the time
+        # steps and downloads the wavefield
+        nf = 10 if wl["model"] == 3 else 9
+        pin_in = torch.from_numpy(host).pin_memory()
+        pin_out = [torch.empty_like(pin_in).pin_memory() for _ in range(nf)]
+
+        def e2e_step():
+            for f in range(nf):
+                d.upload(pin_in, field=f)
+            d.step(n)
+            for f in range(nf):
+                d.download(pin_out[f], field=f)
+
+        e2e_step()                                    # warm
+        barrier()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize(dev)
+        barrier()
+        ems = max_over_ranks((time.perf_counter() - t0) * 1000.0, dev, world) / args.steps
+        e2e_val = replicas_glups(world, cells, n, ems)
+        h2d = d2h = nf * host.nbytes
 
     # ---- roofline of the dominant kernel
     peak, peak_src = measured_peak()
