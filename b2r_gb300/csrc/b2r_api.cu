@@ -383,7 +383,7 @@ b2r_status advance(b2r_handle* h, int n)
         // a bit-sliced pass that ends a period stores the next period's halos
         // itself, so that period starts without the gather
         const bool push = gg >= 2 && !h->gol_bytes && h->gol_push && i + gg == h->cfg.R &&
-                          (h->L.nblk > 1 || h->L.periodic);
+                          (h->L.nblk > 1 || h->L.periodic) && h->L.B[0] % 32 == 0;
         if (gg >= 2) {
             if (h->gol_bytes)
                 CK(h, launch_gol_period(static_cast<const uint8_t*>(h->buf[h->cur]),

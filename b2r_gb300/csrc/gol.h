@@ -22,8 +22,9 @@ cudaError_t launch_gol_bits_substep(const uint8_t* in, uint8_t* out, const Block
                                    cudaStream_t st);
 // ng generations (sub-steps i0 .. i0+ng-1) in one pass on bit-sliced cells;
 // only the window of the last one is written to `out`.  push_halos (a pass
-// that ends a period) also copies the new band cells into the neighbour
-// blocks' halos of `out`, as the next period's halo gather would.
+// that ends a period; block rows of a multiple of 32 cells) also copies the
+// new band cells into the neighbour blocks' halos of `out`, as the next
+// period's halo gather would.
 cudaError_t launch_gol_bits_period(const uint8_t* in, uint8_t* out, const BlockLayout& L, int i0, int ng,
                                    bool push_halos, cudaStream_t st);
 int gol_bits_max_generations_per_pass();

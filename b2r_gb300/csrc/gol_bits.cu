@@ -480,6 +480,10 @@ cudaError_t launch_gol_bits_period(const uint8_t* in, uint8_t* out, const BlockL
                                    bool push_halos, cudaStream_t st)
 {
     if (ng < 1 || ng > kBMaxGen) return cudaErrorInvalidValue;
+    // a block row that is not a multiple of 32 cells ends in a word that the
+    // pass stores whole, stale halo bytes included, which would race with
+    // the fill from the neighbour block
+    if (push_halos && L.B[0] % 32 != 0) return cudaErrorInvalidValue;
     int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-1, -1, -1};
     for (int b = 0; b < L.nblk; ++b) {
         const int e = edge_bits(L, b);

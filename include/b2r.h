@@ -134,8 +134,9 @@ enum {
                                   bit-identical */
     B2R_TUNE_GOL_PUSH = 9      /* Game of Life: 1 = a several-generation pass that ends a period
                                   also fills the next period's halos, so no gather runs between
-                                  periods; 0 = the gather (default, faster on this GPU so far);
-                                  identical results */
+                                  periods (block rows of a multiple of 32 cells; otherwise the
+                                  gather runs); 0 = the gather (default, faster on this GPU so
+                                  far); identical results */
 };
 b2r_status b2r_set_tuning(b2r_handle* h, int key, int value);
 /* Current value of a knob (after b2r_autotune: the schedule it picked). */
