@@ -180,3 +180,24 @@ def test_gol_halo_push_matches_gather(b2r, orc, env, blocks, R, periodic, graphs
             a, b = b, a
         ref = a
     assert np.array_equal(outs[0], ref)
+
+
+@pytest.mark.parametrize("env,blocks,R", [((80, 36, 20), (2, 3, 1), 2), ((64, 64, 64), (2, 2, 2), 4)])
+def test_gol_halo_push_repeatable(b2r, orc, env, blocks, R):
+    """Repeated runs with the halo fill requested give the oracle's bits
+    every time (rows of 40 cells fall back to the gather: a word across the
+    interior edge is stored whole and would race with the fill)."""
+    import torch
+    dom = bernoulli(env, 0.3, 12)
+    nsteps = 6 * R
+    ref = dom.copy()
+    orc.gol_run_periodic(ref, nsteps)
+    for _ in range(4):
+        s = torch.cuda.Stream()
+        with b2r.Domain(b2r.MODEL_GOL, env, blocks=blocks, R=R, D=1, boundary=b2r.BC_PERIODIC, stream=s) as d:
+            d.set_tuning(gol_push=1)
+            d.upload(dom)
+            d.step(nsteps)
+            out = d.download()
+            d.synchronize()
+        assert np.array_equal(out, ref)
