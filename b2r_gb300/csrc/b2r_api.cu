@@ -533,6 +533,7 @@ b2r_status b2r_create(const b2r_config* cfg, b2r_handle** out)
     b2r_status st = B2R_OK;
     auto bail = [&](b2r_status s) {
         b2r_destroy(h);
+        cudaGetLastError();   // a failed allocation must not surface in the caller's next launch check
         return s;
     };
     if (cudaMalloc(&h->d_status, sizeof(int)) != cudaSuccess)

@@ -58,3 +58,23 @@ def test_bounded_wait_reports_timeout_and_context_survives(b2r, orc):
     ref = dom.copy()
     orc.heat_run(ref, 1, 1, 6, 0.1, 1.0, 1.0, 1.0)
     assert np.linalg.norm(got.astype(np.float64) - ref) / np.linalg.norm(ref) <= 1e-5
+
+
+def test_oom_is_reported_and_the_context_stays_usable(b2r, orc):
+    """A domain larger than the GPU's memory is refused with B2R_ERR_OOM; the
+    next handle works (the failed allocation leaves no error behind)."""
+    with pytest.raises(b2r.B2RError) as ei:
+        b2r.Domain(b2r.MODEL_HEAT, (4800, 4800, 4800), D=1)
+    assert "B2R_ERR_OOM" in str(ei.value)
+    env = (40, 32, 24)
+    rng = np.random.default_rng(8)
+    dom = np.zeros(tuple(e + 2 for e in env[::-1]), np.float32)
+    dom[1:-1, 1:-1, 1:-1] = rng.random(env[::-1], dtype=np.float32)
+    with b2r.Domain(b2r.MODEL_HEAT, env, D=1, alpha_dt=0.1) as d:
+        d.upload(dom)
+        d.step(3)
+        got = d.download()
+        d.synchronize()
+    ref = dom.copy()
+    orc.heat_run(ref, 1, 1, 3, 0.1, 1.0, 1.0, 1.0)
+    assert float(np.linalg.norm(got.astype(np.float64) - ref) / np.linalg.norm(ref)) <= 1e-5
