@@ -117,9 +117,11 @@ b2r_status fail(b2r_handle* h, b2r_status s, const char* fmt, ...)
 #define CK(h, call)                                                                          \
     do {                                                                                     \
         cudaError_t e_ = (call);                                                             \
-        if (e_ != cudaSuccess)                                                               \
+        if (e_ != cudaSuccess) {                                                             \
+            cudaGetLastError(); /* a non-sticky error must not resurface in a later check */ \
             return fail(h, e_ == cudaErrorMemoryAllocation ? B2R_ERR_OOM : B2R_ERR_CUDA,     \
                         "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+        }                                                                                    \
     } while (0)
 
 struct DevBuf {
