@@ -259,7 +259,10 @@ b2r_status bfail(b2r_status s, const char* msg, cudaError_t e = cudaSuccess)
 #define BCK(call, msg)                                                                       \
     do {                                                                                     \
         cudaError_t e_ = (call);                                                             \
-        if (e_ != cudaSuccess) return bfail(e_ == cudaErrorMemoryAllocation ? B2R_ERR_OOM : B2R_ERR_CUDA, msg, e_); \
+        if (e_ != cudaSuccess) {                                                             \
+            cudaGetLastError(); /* a non-sticky error must not resurface in a later check */ \
+            return bfail(e_ == cudaErrorMemoryAllocation ? B2R_ERR_OOM : B2R_ERR_CUDA, msg, e_); \
+        }                                                                                    \
     } while (0)
 
 inline int roundup(int v, int m) { return (v + m - 1) / m * m; }
