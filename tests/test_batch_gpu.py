@@ -81,3 +81,31 @@ def test_batch_autotune_keeps_inputs(b2r):
             d.upload(ins[i])
             d.step(it["nsteps"])
             assert np.array_equal(got[i], d.download()), i
+
+
+def test_batches_with_different_schedules_coexist(b2r):
+    """A batch created after a larger one (longer schedule, more shared
+    memory) does not lower the kernel's shared-memory limit under it: both
+    run, concurrently, with their own results."""
+    import torch
+    big = mix(10, 7, max_steps=300)
+    small = mix(3, 8, max_steps=8)
+    ins_big, ins_small = inputs(big, 9), inputs(small, 10)
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    res = []
+    with b2r.Batch(big, stream=s1) as b1, b2r.Batch(small, stream=s2) as b2:
+        for bt, ins in ((b1, ins_big), (b2, ins_small)):
+            for i, a in enumerate(ins):
+                bt.upload(i, a)
+        b1.run()
+        b2.run()
+        b1.synchronize()
+        b2.synchronize()
+        res = [[b1.download(i) for i in range(len(big))], [b2.download(i) for i in range(len(small))]]
+    for items, ins, outs in ((big, ins_big, res[0]), (small, ins_small, res[1])):
+        for it, a, got in zip(items, ins, outs):
+            with b2r.Domain(b2r.MODEL_HEAT, it["env"], D=it["D"], alpha_dt=it["alpha_dt"]) as d:
+                d.upload(a)
+                d.step(it["nsteps"])
+                want = d.download()
+            assert np.array_equal(got, want)
