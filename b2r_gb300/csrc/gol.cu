@@ -16,6 +16,7 @@
 // byte, no carries), then the rule is applied to four cells at once with
 // byte-wise compares.  Every load is a coalesced 128-byte warp row; the
 // halo rows re-read by the next warp come from L1/L2.
+#include <mutex>
 #include <algorithm>
 
 #include "b2r_common.cuh"
@@ -355,6 +356,9 @@ cudaError_t launch_gol_period(const uint8_t* in, uint8_t* out, const BlockLayout
     constexpr int kNarrowT = 36 * kPGroups;
     const bool narrow = threads <= kNarrowT;
     static size_t attr[2] = {0, 0};
+    // raised only, under a lock: handles on other host threads share the limit
+    static std::mutex attr_mu;
+    std::lock_guard<std::mutex> attr_lock(attr_mu);
     if (smem > attr[narrow]) {
         const int bytes = (int)std::max<size_t>(smem, 48 * 1024);
         cudaError_t e = narrow ? cudaFuncSetAttribute(gol_period_kernel<kNarrowT, 2>,

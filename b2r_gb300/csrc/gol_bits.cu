@@ -17,6 +17,7 @@
 //     by one cell (funnel shifts) -> the 27-cell total T, 5 bits;
 //   * rule on T including the cell itself: live -> 3 <= T <= 8, dead ->
 //     T == 5.
+#include <mutex>
 #include <algorithm>
 
 #include "b2r_common.cuh"
@@ -524,6 +525,9 @@ cudaError_t launch_gol_bits_period(const uint8_t* in, uint8_t* out, const BlockL
     const dim3 grid(ntx, nty2, L.nblk * nzc);
     static size_t attr[3] = {0, 0, 0};
     const int gi = GW == 8 ? 0 : (GW == 16 ? 1 : 2);
+    // raised only, under a lock: handles on other host threads share the limit
+    static std::mutex attr_mu;
+    std::lock_guard<std::mutex> attr_lock(attr_mu);
     if (smem > attr[gi]) {
         const int bytes = (int)std::max<size_t>(smem, 48 * 1024);
         cudaError_t e = GW == 8 ? cudaFuncSetAttribute(gol_bits_period_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)
