@@ -78,3 +78,44 @@ def test_oom_is_reported_and_the_context_stays_usable(b2r, orc):
     ref = dom.copy()
     orc.heat_run(ref, 1, 1, 3, 0.1, 1.0, 1.0, 1.0)
     assert float(np.linalg.norm(got.astype(np.float64) - ref) / np.linalg.norm(ref)) <= 1e-5
+
+
+def test_handles_on_two_host_threads(b2r):
+    """One handle per host thread: heat and Game of Life stepped from two
+    threads at once give the bits of the same runs one after the other."""
+    import threading
+    import torch
+    rng = np.random.default_rng(13)
+    henv, genv = (64, 48, 80), (64, 64, 64)
+    hdom = np.zeros(tuple(e + 2 for e in henv[::-1]), np.float32)
+    hdom[1:-1, 1:-1, 1:-1] = rng.random(henv[::-1], dtype=np.float32)
+    gdom = (rng.random(genv[::-1]) < 0.3).astype(np.uint8)
+
+    def heat(out):
+        s = torch.cuda.Stream()
+        with b2r.Domain(b2r.MODEL_HEAT, henv, blocks=(2, 1, 2), R=2, D=1, alpha_dt=0.05, stream=s) as d:
+            d.upload(hdom)
+            d.step(41)
+            out.append(d.download())
+            d.synchronize()
+
+    def gol(out):
+        s = torch.cuda.Stream()
+        with b2r.Domain(b2r.MODEL_GOL, genv, blocks=(2, 2, 2), R=4, D=1, boundary=b2r.BC_PERIODIC,
+                        stream=s) as d:
+            d.upload(gdom)
+            d.step(42)
+            out.append(d.download())
+            d.synchronize()
+
+    ref_h, ref_g = [], []
+    heat(ref_h)
+    gol(ref_g)
+    got_h, got_g = [], []
+    threads = [threading.Thread(target=heat, args=(got_h,)), threading.Thread(target=gol, args=(got_g,))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert np.array_equal(got_h[0], ref_h[0])
+    assert np.array_equal(got_g[0], ref_g[0])
