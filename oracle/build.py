@@ -1,6 +1,8 @@
 """Build recipe for the oracle (test infrastructure only).
 
 * ``liborc.so``  -- the CPU restatement in b2r_oracle.c (always built).
+* ``_ref/eqwp_ref.cubin`` -- the reference's own eqwp.cu kernels, device
+  code only (oracle/refgpu.py runs them on the GPU as a second oracle).
 * ``_ref/libheat_ref.so`` -- the reference's own heat-3D.cpp compiled from
   its source tree, with a two-line config shim for its
   ``#include "../b2r_config.h"`` (heat-3D.cpp:16) and
@@ -55,6 +57,24 @@ def build_ref(force=False):
     return out
 
 
+def build_ref_cubin(force=False):
+    """Compile the reference's eqwp.cu, unmodified, into a cubin of its
+    device code for sm_103a (nvcc defaults otherwise, as the reference is
+    built); returns the path or None where the source tree is absent.  The
+    cubin is GPU code, so the prebuilt file serves the machine with the GPU."""
+    ref = os.path.join(REF_SRC, "eqwp.cu")
+    if not os.path.exists(ref):
+        return None
+    refdir = os.path.join(HERE, "_ref")
+    os.makedirs(refdir, exist_ok=True)
+    out = os.path.join(refdir, "eqwp_ref.cubin")
+    if force or not _newer(out, [ref, os.path.join(REF_SRC, "b2r_config.h")]):
+        subprocess.check_call([os.environ.get("NVCC", "nvcc"), "-cubin", "-gencode",
+                               "arch=compute_103a,code=sm_103a", "-O3", "-o", out, ref])
+    return out
+
+
 if __name__ == "__main__":
     print(build_oracle(force=True))
     print(build_ref(force=True))
+    print(build_ref_cubin(force=True))

@@ -1,0 +1,117 @@
+"""The reference's own elastic-wave CUDA kernels, run as a second oracle.
+
+TEST INFRASTRUCTURE ONLY: the GPU tests compare the library against these
+kernels; nothing in the product loads them.
+
+oracle/build.py compiles the reference's eqwp.cu (eqwp_fd4_stress and
+eqwp_fd4_v{x,y,z}, eqwp.cu:60-477) unmodified into oracle/_ref/eqwp_ref.cubin
+where the reference source tree is present; this module loads that cubin
+through the CUDA driver API in the process's current (PyTorch) context and
+drives it as eqwp_gpu_main does (eqwp.cu:661-688): per time step the stress
+kernel, then vx, vy (with the displacement) and vz, on 16 x 16 thread blocks
+over the padded block, R = 1.
+
+The kernels are correct only inside their envelope: R = 1 and a block of at
+most 16 rows (one thread-block tile in y) -- their y halo loads read row y-1
+into the slot of row y-2 (eqwp.cu:118-123), which with a single y tile is
+never executed.  run_reference refuses other shapes.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CUBIN = os.path.join(HERE, "_ref", "eqwp_ref.cubin")
+TILE = 16           # CUDA_BLOCK_SIZE (eqwp.cu:25)
+FRC_TIME = 50       # eqwp.cu:14
+
+# Itanium-mangled names of the reference's kernels (eqwp.cu:60,154,249,341)
+_NAMES = {
+    "stress": "_Z15eqwp_fd4_stressiiiPfS_S_S_S_S_S_S_S_i",
+    "vx": "_Z11eqwp_fd4_vxiiiPfS_S_S_P6float3iii",
+    "vy": "_Z11eqwp_fd4_vyiiiPfS_S_S_P6float3S_iii",
+    "vz": "_Z11eqwp_fd4_vziiiPfS_S_S_P6float3iii",
+}
+
+_mod = None
+
+
+def available():
+    return os.path.exists(CUBIN)
+
+
+def _driver():
+    cu = C.CDLL("libcuda.so.1")
+    cu.cuModuleLoadData.argtypes = [C.POINTER(C.c_void_p), C.c_void_p]
+    cu.cuModuleGetFunction.argtypes = [C.POINTER(C.c_void_p), C.c_void_p, C.c_char_p]
+    cu.cuLaunchKernel.argtypes = [C.c_void_p, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_uint, C.c_uint,
+                                  C.c_uint, C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]
+    return cu
+
+
+def _check(r, what):
+    if r != 0:
+        raise RuntimeError(f"{what} failed: CUresult {r}")
+
+
+def _load():
+    global _mod
+    if _mod is None:
+        import torch
+        torch.cuda.init()
+        torch.zeros(1, device="cuda")          # the primary context is current on this thread
+        cu = _driver()
+        data = open(CUBIN, "rb").read()
+        buf = C.create_string_buffer(data, len(data))
+        mod = C.c_void_p()
+        _check(cu.cuModuleLoadData(C.byref(mod), buf), "cuModuleLoadData")
+        fns = {}
+        for k, name in _NAMES.items():
+            f = C.c_void_p()
+            _check(cu.cuModuleGetFunction(C.byref(f), mod, name.encode()), "cuModuleGetFunction " + k)
+            fns[k] = f
+        _mod = (cu, mod, fns, buf)
+    return _mod
+
+
+def _launch(cu, f, grid, stream, *args):
+    vals = []
+    for a in args:
+        vals.append(C.c_int(a) if isinstance(a, int) else C.c_void_p(a.data_ptr()))
+    params = (C.c_void_p * len(vals))(*[C.cast(C.pointer(v), C.c_void_p) for v in vals])
+    _check(cu.cuLaunchKernel(f, grid[0], grid[1], 1, TILE, TILE, 1, 0, stream, params, None), "cuLaunchKernel")
+
+
+def reference_force(shape):
+    """f_init of eqwp_cuda_init (eqwp.cu:561-566): Ngx*Ngz float3, y = -1e4
+    on x in [Ngx/2, Ngx/2 + Ngx/10), z in [Ngz/2, Ngz/2 + Ngz/10)."""
+    ngz, _, ngx = shape
+    f = np.zeros((ngz, ngx, 3), np.float32)
+    f[ngz // 2:ngz // 2 + ngz // 10, ngx // 2:ngx // 2 + ngx // 10, 1] = -10000.0
+    return f
+
+
+def run_reference(fields, nsteps, ts0=0):
+    """fields: the 10 padded-block arrays (vx, vy, vz, sxx, sxy, sxz, syy, syz,
+    szz, displacement), each (Ngz, Ngy, Ngx) float32.  Returns them after
+    nsteps time steps of the reference kernels at R = 1."""
+    import torch
+    ngz, ngy, ngx = fields[0].shape
+    if ngy > TILE:
+        raise ValueError("the reference kernels are correct only within one %d-row tile in y" % TILE)
+    cu, _, fns, _ = _load()
+    dev = [torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda() for a in fields]
+    vx, vy, vz, sxx, sxy, sxz, syy, syz, szz, disp = dev
+    finit = torch.from_numpy(reference_force(fields[0].shape)).cuda()
+    grid = ((ngx + TILE - 1) // TILE, (ngy + TILE - 1) // TILE)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    R = 1
+    for n in range(nsteps):   # eqwp.cu:677-686 with b2r_i = 0
+        ts = ts0 + n
+        _launch(cu, fns["stress"], grid, stream, ngx, ngy, ngz, sxx, sxy, sxz, syy, syz, szz, vx, vy, vz, 0)
+        _launch(cu, fns["vx"], grid, stream, ngx, ngy, ngz, vx, sxx, sxy, sxz, finit, ts, 0, R)
+        _launch(cu, fns["vy"], grid, stream, ngx, ngy, ngz, vy, sxy, syy, syz, finit, disp, ts, 0, R)
+        _launch(cu, fns["vz"], grid, stream, ngx, ngy, ngz, vz, sxz, syz, szz, finit, ts, 0, R)
+    torch.cuda.synchronize()
+    return [t.cpu().numpy() for t in dev]
