@@ -217,7 +217,8 @@ gol_period_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out, con
 #pragma unroll
         for (int k = 0; k < kPRowsT; ++k) {
             const int y = yb + yg * kPRowsT + k;
-            pre[k] = (wload && z <= ze + ng && y >= 0 && y < L.n[1])
+            // planes and rows beyond the block read as dead (see gol_bits.cu)
+            pre[k] = (wload && z >= 0 && z <= ze + ng && z < L.n[2] && y >= 0 && y < L.n[1])
                          ? __ldg(inw + (long long)z * wplane + (long long)y * wpr + wx)
                          : 0u;
         }

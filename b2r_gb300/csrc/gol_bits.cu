@@ -335,7 +335,10 @@ gol_bits_period_kernel(const uint8_t* __restrict__ in, uint8_t* __restrict__ out
         for (int k = 0; k < 4; ++k) {
             const int y = yb + yg * 4 + k;
             pa[k] = pb[k] = make_uint4(0u, 0u, 0u, 0u);
-            if (wload && z <= ze + ng && y >= 0 && y < L.n[1]) {
+            // planes and rows beyond the block read as dead: they feed only
+            // cells outside the windows (a fixed shell shallower than the
+            // generations of the pass), which keep their values
+            if (wload && z >= 0 && z <= ze + ng && z < L.n[2] && y >= 0 && y < L.n[1]) {
                 const uint4* s = reinterpret_cast<const uint4*>(inb + (long long)z * L.plane + (long long)y * L.P);
                 pa[k] = __ldg(s);
                 pb[k] = __ldg(s + 1);

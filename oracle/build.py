@@ -1,8 +1,9 @@
 """Build recipe for the oracle (test infrastructure only).
 
 * ``liborc.so``  -- the CPU restatement in b2r_oracle.c (always built).
-* ``_ref/eqwp_ref.cubin`` -- the reference's own eqwp.cu kernels, device
-  code only (oracle/refgpu.py runs them on the GPU as a second oracle).
+* ``_ref/eqwp_ref.cubin``, ``_ref/gol_ref.cubin`` -- the reference's own
+  eqwp.cu and gol-3D.cu kernels, device code only (oracle/refgpu.py runs them
+  on the GPU as a second oracle).
 * ``_ref/libheat_ref.so`` -- the reference's own heat-3D.cpp compiled from
   its source tree, with a two-line config shim for its
   ``#include "../b2r_config.h"`` (heat-3D.cpp:16) and
@@ -58,20 +59,29 @@ def build_ref(force=False):
 
 
 def build_ref_cubin(force=False):
-    """Compile the reference's eqwp.cu, unmodified, into a cubin of its
-    device code for sm_103a (nvcc defaults otherwise, as the reference is
-    built); returns the path or None where the source tree is absent.  The
-    cubin is GPU code, so the prebuilt file serves the machine with the GPU."""
+    """Compile the reference's eqwp.cu and gol-3D.cu, unmodified, into cubins
+    of their device code for sm_103a (nvcc defaults otherwise, as the
+    reference is built; gol-3D.cu's host code calls cudaThreadSynchronize,
+    which CUDA 13 no longer declares, so that name is defined to its
+    successor on the command line).  Returns the eqwp cubin's path, or None
+    where the source tree is absent.  A cubin is GPU code, so the prebuilt
+    files serve the machine with the GPU."""
     ref = os.path.join(REF_SRC, "eqwp.cu")
     if not os.path.exists(ref):
         return None
     refdir = os.path.join(HERE, "_ref")
     os.makedirs(refdir, exist_ok=True)
-    out = os.path.join(refdir, "eqwp_ref.cubin")
-    if force or not _newer(out, [ref, os.path.join(REF_SRC, "b2r_config.h")]):
-        subprocess.check_call([os.environ.get("NVCC", "nvcc"), "-cubin", "-gencode",
-                               "arch=compute_103a,code=sm_103a", "-O3", "-o", out, ref])
-    return out
+    nvcc = os.environ.get("NVCC", "nvcc")
+    outs = []
+    for src, name, extra in (("eqwp.cu", "eqwp_ref.cubin", []),
+                             ("gol-3D.cu", "gol_ref.cubin", ["-DcudaThreadSynchronize=cudaDeviceSynchronize"])):
+        path = os.path.join(REF_SRC, src)
+        out = os.path.join(refdir, name)
+        if force or not _newer(out, [path, os.path.join(REF_SRC, "b2r_config.h")]):
+            subprocess.check_call([nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
+                                   *extra, "-o", out, path])
+        outs.append(out)
+    return outs[0]
 
 
 if __name__ == "__main__":

@@ -1,4 +1,5 @@
-"""The reference's own elastic-wave CUDA kernels, run as a second oracle.
+"""The reference's own elastic-wave and Game-of-Life CUDA kernels, run as a
+second oracle.
 
 TEST INFRASTRUCTURE ONLY: the GPU tests compare the library against these
 kernels; nothing in the product loads them.
@@ -9,9 +10,10 @@ where the reference source tree is present; this module loads that cubin
 through the CUDA driver API in the process's current (PyTorch) context and
 drives it as eqwp_gpu_main does (eqwp.cu:661-688): per time step the stress
 kernel, then vx, vy (with the displacement) and vz, on 16 x 16 thread blocks
-over the padded block, R = 1.
+over the padded block, R = 1; gol-3D.cu's gol_3d_kernel likewise
+(oracle/_ref/gol_ref.cubin, run_reference_gol).
 
-The kernels are correct only inside their envelope: R = 1 and a block of at
+The elastic-wave kernels are correct only inside their envelope: R = 1 and a block of at
 most 16 rows (one thread-block tile in y) -- their y halo loads read row y-1
 into the slot of row y-2 (eqwp.cu:118-123), which with a single y tile is
 never executed.  run_reference refuses other shapes.
@@ -34,11 +36,19 @@ _NAMES = {
     "vz": "_Z11eqwp_fd4_vziiiPfS_S_S_P6float3iii",
 }
 
-_mod = None
+GOL_CUBIN = os.path.join(HERE, "_ref", "gol_ref.cubin")
+GOL_TILE = 32       # CUDA_BLOCK_SIZE (gol-3D.cu:8)
+_GOL_NAME = "_Z13gol_3d_kernelPhS_iiii"   # gol_3d_kernel (gol-3D.cu:30)
+
+_mods = {}
 
 
 def available():
     return os.path.exists(CUBIN)
+
+
+def gol_available():
+    return os.path.exists(GOL_CUBIN)
 
 
 def _driver():
@@ -55,32 +65,31 @@ def _check(r, what):
         raise RuntimeError(f"{what} failed: CUresult {r}")
 
 
-def _load():
-    global _mod
-    if _mod is None:
+def _load(path, names):
+    if path not in _mods:
         import torch
         torch.cuda.init()
         torch.zeros(1, device="cuda")          # the primary context is current on this thread
         cu = _driver()
-        data = open(CUBIN, "rb").read()
+        data = open(path, "rb").read()
         buf = C.create_string_buffer(data, len(data))
         mod = C.c_void_p()
         _check(cu.cuModuleLoadData(C.byref(mod), buf), "cuModuleLoadData")
         fns = {}
-        for k, name in _NAMES.items():
+        for k, name in names.items():
             f = C.c_void_p()
             _check(cu.cuModuleGetFunction(C.byref(f), mod, name.encode()), "cuModuleGetFunction " + k)
             fns[k] = f
-        _mod = (cu, mod, fns, buf)
-    return _mod
+        _mods[path] = (cu, mod, fns, buf)
+    return _mods[path]
 
 
-def _launch(cu, f, grid, stream, *args):
+def _launch(cu, f, grid, stream, *args, tile=TILE):
     vals = []
     for a in args:
         vals.append(C.c_int(a) if isinstance(a, int) else C.c_void_p(a.data_ptr()))
     params = (C.c_void_p * len(vals))(*[C.cast(C.pointer(v), C.c_void_p) for v in vals])
-    _check(cu.cuLaunchKernel(f, grid[0], grid[1], 1, TILE, TILE, 1, 0, stream, params, None), "cuLaunchKernel")
+    _check(cu.cuLaunchKernel(f, grid[0], grid[1], 1, tile, tile, 1, 0, stream, params, None), "cuLaunchKernel")
 
 
 def reference_force(shape):
@@ -100,7 +109,7 @@ def run_reference(fields, nsteps, ts0=0):
     ngz, ngy, ngx = fields[0].shape
     if ngy > TILE:
         raise ValueError("the reference kernels are correct only within one %d-row tile in y" % TILE)
-    cu, _, fns, _ = _load()
+    cu, _, fns, _ = _load(CUBIN, _NAMES)
     dev = [torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda() for a in fields]
     vx, vy, vz, sxx, sxy, sxz, syy, syz, szz, disp = dev
     finit = torch.from_numpy(reference_force(fields[0].shape)).cuda()
@@ -115,3 +124,32 @@ def run_reference(fields, nsteps, ts0=0):
         _launch(cu, fns["vz"], grid, stream, ngx, ngy, ngz, vz, sxz, syz, szz, finit, ts, 0, R)
     torch.cuda.synchronize()
     return [t.cpu().numpy() for t in dev]
+
+
+def run_reference_gol(block, ngen):
+    """block: (Ngz, Ngy, Ngx) uint8 with a one-cell fixed shell.  Returns it
+    after ngen generations of the reference's gol_3d_kernel, one launch per
+    generation into a copy of its input (gol-3D.cu:124-129: "no rule fires"
+    keeps the cell), the shell restored after each one.  The kernel is
+    correct only where one 32 x 32 tile covers the block in x and y: its
+    behind/infront planes get no halo, and cells it does not update use an
+    unset neighbour count (gol-3D.cu:49,76-91), which writes undefined values
+    into the shell."""
+    import torch
+    ngz, ngy, ngx = block.shape
+    if ngx > GOL_TILE or ngy > GOL_TILE:
+        raise ValueError("the reference kernel is correct only within one %d x %d tile" % (GOL_TILE, GOL_TILE))
+    cu, _, fns, _ = _load(GOL_CUBIN, {"gol": _GOL_NAME})
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    cur = torch.from_numpy(np.ascontiguousarray(block, np.uint8)).cuda()
+    shell = torch.ones_like(cur, dtype=torch.bool)
+    shell[1:-1, 1:-1, 1:-1] = False
+    fixed = cur.clone()
+    for _ in range(ngen):
+        out = cur.clone()
+        _launch(cu, fns["gol"], (1, 1), stream, cur, out, ngx, ngy, ngz, 0, tile=GOL_TILE)
+        out[shell] = fixed[shell]
+        cur = out
+    torch.cuda.synchronize()
+    return cur.cpu().numpy()
+
