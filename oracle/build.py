@@ -1,8 +1,9 @@
 """Build recipe for the oracle (test infrastructure only).
 
 * ``liborc.so``  -- the CPU restatement in b2r_oracle.c (always built).
-* ``_ref/eqwp_ref.cubin``, ``_ref/gol_ref.cubin`` -- the reference's own
-  eqwp.cu and gol-3D.cu kernels, device code only (oracle/refgpu.py runs them
+* ``_ref/eqwp_ref.cubin``, ``_ref/gol_ref.cubin``, ``_ref/heat_ref.cubin``
+  -- the reference's own eqwp.cu, gol-3D.cu and heat-3D.cu kernels, device
+  code only (oracle/refgpu.py runs them
   on the GPU as a second oracle).
 * ``_ref/libheat_ref.so`` -- the reference's own heat-3D.cpp compiled from
   its source tree, with a two-line config shim for its
@@ -59,11 +60,12 @@ def build_ref(force=False):
 
 
 def build_ref_cubin(force=False):
-    """Compile the reference's eqwp.cu and gol-3D.cu, unmodified, into cubins
-    of their device code for sm_103a (nvcc defaults otherwise, as the
-    reference is built; gol-3D.cu's host code calls cudaThreadSynchronize,
-    which CUDA 13 no longer declares, so that name is defined to its
-    successor on the command line).  Returns the eqwp cubin's path, or None
+    """Compile the reference's eqwp.cu, gol-3D.cu and heat-3D.cu, unmodified,
+    into cubins of their device code for sm_103a (nvcc defaults otherwise,
+    as the reference is built; the host code of the last two calls
+    cudaThreadSynchronize, which CUDA 13 no longer declares, so that name is
+    defined to its successor on the command line; heat-3D.cu gets the
+    delta-1 config shim that its CPU build uses).  Returns the eqwp cubin's path, or None
     where the source tree is absent.  A cubin is GPU code, so the prebuilt
     files serve the machine with the GPU."""
     ref = os.path.join(REF_SRC, "eqwp.cu")
@@ -73,8 +75,14 @@ def build_ref_cubin(force=False):
     os.makedirs(refdir, exist_ok=True)
     nvcc = os.environ.get("NVCC", "nvcc")
     outs = []
+    sub = os.path.join(refdir, "incg", "sub")     # heat-3D.cu includes "../b2r_config.h"
+    os.makedirs(sub, exist_ok=True)
+    with open(os.path.join(refdir, "incg", "b2r_config.h"), "w") as f:
+        f.write("#pragma once\n#define B2R_D 1\ntypedef float CELL_DT;\n")
+    sync = "-DcudaThreadSynchronize=cudaDeviceSynchronize"
     for src, name, extra in (("eqwp.cu", "eqwp_ref.cubin", []),
-                             ("gol-3D.cu", "gol_ref.cubin", ["-DcudaThreadSynchronize=cudaDeviceSynchronize"])):
+                             ("gol-3D.cu", "gol_ref.cubin", [sync]),
+                             ("heat-3D.cu", "heat_ref.cubin", [sync, "-I", sub])):
         path = os.path.join(REF_SRC, src)
         out = os.path.join(refdir, name)
         if force or not _newer(out, [path, os.path.join(REF_SRC, "b2r_config.h")]):

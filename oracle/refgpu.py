@@ -1,5 +1,5 @@
-"""The reference's own elastic-wave and Game-of-Life CUDA kernels, run as a
-second oracle.
+"""The reference's own elastic-wave, Game-of-Life and heat CUDA kernels, run
+as a second oracle.
 
 TEST INFRASTRUCTURE ONLY: the GPU tests compare the library against these
 kernels; nothing in the product loads them.
@@ -10,8 +10,8 @@ where the reference source tree is present; this module loads that cubin
 through the CUDA driver API in the process's current (PyTorch) context and
 drives it as eqwp_gpu_main does (eqwp.cu:661-688): per time step the stress
 kernel, then vx, vy (with the displacement) and vz, on 16 x 16 thread blocks
-over the padded block, R = 1; gol-3D.cu's gol_3d_kernel likewise
-(oracle/_ref/gol_ref.cubin, run_reference_gol).
+over the padded block, R = 1; gol-3D.cu's gol_3d_kernel and heat-3D.cu's
+fdm_heat_diffuse_delta1 likewise (run_reference_gol, run_reference_heat).
 
 The elastic-wave kernels are correct only inside their envelope: R = 1 and a block of at
 most 16 rows (one thread-block tile in y) -- their y halo loads read row y-1
@@ -40,6 +40,10 @@ GOL_CUBIN = os.path.join(HERE, "_ref", "gol_ref.cubin")
 GOL_TILE = 32       # CUDA_BLOCK_SIZE (gol-3D.cu:8)
 _GOL_NAME = "_Z13gol_3d_kernelPhS_iiii"   # gol_3d_kernel (gol-3D.cu:30)
 
+HEAT_CUBIN = os.path.join(HERE, "_ref", "heat_ref.cubin")
+HEAT_TILE = 32      # CUDA_BLOCK_SIZE (heat-3D.cu:8)
+_HEAT_NAME = "_Z23fdm_heat_diffuse_delta1PfS_iiii"   # fdm_heat_diffuse_delta1 (heat-3D.cu:173)
+
 _mods = {}
 
 
@@ -49,6 +53,10 @@ def available():
 
 def gol_available():
     return os.path.exists(GOL_CUBIN)
+
+
+def heat_available():
+    return os.path.exists(HEAT_CUBIN)
 
 
 def _driver():
@@ -152,4 +160,24 @@ def run_reference_gol(block, ngen):
         cur = out
     torch.cuda.synchronize()
     return cur.cpu().numpy()
+
+
+def run_reference_heat(block, nsteps):
+    """block: (Ngz, Ngy, Ngx) float32 with a one-cell fixed shell.  Returns it
+    after nsteps steps of the reference's fdm_heat_diffuse_delta1 at R = 1
+    (its constants: alpha*dt = 0.01, dx = dy = 1, dz = 0.5, heat-3D.cu:9-13),
+    driven as heat_3D_gpu_main drives it (heat-3D.cu:583-642): both device
+    buffers start as the block, 32 x 32 thread blocks, ping-pong."""
+    import torch
+    ngz, ngy, ngx = block.shape
+    cu, _, fns, _ = _load(HEAT_CUBIN, {"heat": _HEAT_NAME})
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    a = torch.from_numpy(np.ascontiguousarray(block, np.float32)).cuda()
+    b = a.clone()
+    grid = ((ngx + HEAT_TILE - 1) // HEAT_TILE, (ngy + HEAT_TILE - 1) // HEAT_TILE)
+    for _ in range(nsteps):
+        _launch(cu, fns["heat"], grid, stream, a, b, ngx, ngy, ngz, 0, tile=HEAT_TILE)
+        a, b = b, a
+    torch.cuda.synchronize()
+    return a.cpu().numpy()
 
