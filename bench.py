@@ -249,6 +249,21 @@ def run_reference(args, wl):
         t_all += time.perf_counter() - t0
         vals.append(v)
     value = float(np.mean(vals))
+    # for context: the reference's own GPU kernel of the same path
+    # (fdm_heat_diffuse_delta1, compiled unmodified), device-resident
+    ref_gpu = None
+    if wl["model"] == 1 and D == 1:
+        try:
+            import torch
+            from oracle import refgpu
+            if torch.cuda.is_available() and refgpu.heat_available():
+                ms = refgpu.time_reference_heat(dom, wl["sub_steps"], reps=max(1, args.steps))
+                cells = env[0] * env[1] * env[2]
+                ref_gpu = {"value": round(cells * wl["sub_steps"] / (ms / 1e3) / 1e9, 3), "unit": "GLUPS",
+                           "kernel": "fdm_heat_diffuse_delta1 (heat-3D.cu:173), its own constants",
+                           "note": "the reference's CUDA kernel on this GPU, fields resident, no copies"}
+        except Exception as e:   # context only: never fails the reference line
+            ref_gpu = {"unavailable": str(e)[:200]}
     line = {"metric": "GLUPS", "value": round(value, 4), "unit": "GLUPS", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(1000 * t_all / args.steps, 3), "higher_is_better": True,
@@ -257,7 +272,8 @@ def run_reference(args, wl):
             "cpu_baseline": {"value": round(value, 4), "unit": "GLUPS", "cores": cores, "kind": kind,
                              "sample": sample},
             "e2e": {"value": round(value, 4), "unit": "GLUPS", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
+                    "d2h_bytes_per_step": 0},
+            **({"reference_gpu_kernel": ref_gpu} if ref_gpu else {})}
     print(json.dumps(line), flush=True)
 
 

@@ -181,3 +181,31 @@ def run_reference_heat(block, nsteps):
     torch.cuda.synchronize()
     return a.cpu().numpy()
 
+
+def time_reference_heat(block, nsteps, reps=3):
+    """Milliseconds per run of nsteps reference delta-1 steps on the device
+    (CUDA events, after one untimed run), the block resident in HBM."""
+    import torch
+    ngz, ngy, ngx = block.shape
+    cu, _, fns, _ = _load(HEAT_CUBIN, {"heat": _HEAT_NAME})
+    s = torch.cuda.current_stream()
+    stream = C.c_void_p(s.cuda_stream)
+    a = torch.from_numpy(np.ascontiguousarray(block, np.float32)).cuda()
+    b = a.clone()
+    grid = ((ngx + HEAT_TILE - 1) // HEAT_TILE, (ngy + HEAT_TILE - 1) // HEAT_TILE)
+
+    def run():
+        x, y = a, b
+        for _ in range(nsteps):
+            _launch(cu, fns["heat"], grid, stream, x, y, ngx, ngy, ngz, 0, tile=HEAT_TILE)
+            x, y = y, x
+
+    run()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        run()
+    e1.record(s)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
