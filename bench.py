@@ -215,6 +215,21 @@ def cpu_sample(wl, budget_s=10.0, nthreads=0, dom=None):
             steps += 1
         lups = steps * env[0] * env[1] * env[2]
         return lups / t / 1e9, "port", cores, f"{steps} generation(s) of the restated rule on the {env} torus"
+    if wl["model"] == 3:
+        # the reference's collocated model (eqwp.cu:60-477) restated, on a
+        # 128x128x64 sample with its two-cell shell and body force
+        n = (128 + 4, 128 + 4, 64 + 4)
+        f = [np.zeros(n[::-1], np.float32) for _ in range(10)]
+        force = dict(fy=n[1] - 7 - 2, fx0=n[0] // 2, fx1=n[0] // 2 + n[0] // 10, fz0=n[2] // 2,
+                     fz1=n[2] // 2 + n[2] // 10, fval=-1e4, fsteps=50)
+        steps, t = 0, 0.0
+        while t < budget_s or steps < 1:
+            t0 = time.perf_counter()
+            orc.eqwp_ref_substep(f, 0, 2, 63, steps, force)
+            t += time.perf_counter() - t0
+            steps += 1
+        return (steps * 128 * 128 * 64 / t / 1e9, "port", cores,
+                f"{steps} step(s) of the restated reference model on 128x128x64")
     # elastic wave: restated staggered step on a 128x128x64 sample
     n = (128 + 8, 128 + 8, 64 + 8)
     f = [np.zeros(n[::-1], np.float32) for _ in range(9)]
@@ -263,6 +278,20 @@ def run_reference(args, wl):
                            "kernel": "fdm_heat_diffuse_delta1 (heat-3D.cu:173), its own constants",
                            "note": "the reference's CUDA kernel on this GPU, fields resident, no copies"}
         except Exception as e:   # context only: never fails the reference line
+            ref_gpu = {"unavailable": str(e)[:200]}
+    if wl["model"] == 3:
+        try:
+            import torch
+            from oracle import refgpu
+            if torch.cuda.is_available() and refgpu.available():
+                shape = tuple(e + 4 for e in env[::-1])     # the reference block, R = 1
+                ms = refgpu.time_reference_eqwp(shape, wl["sub_steps"], reps=1)
+                cells = env[0] * env[1] * env[2]
+                ref_gpu = {"value": round(cells * wl["sub_steps"] / (ms / 1e3) / 1e9, 3), "unit": "GLUPS",
+                           "kernel": "eqwp_fd4_stress + eqwp_fd4_v{x,y,z} (eqwp.cu:60-477)",
+                           "note": "the reference's CUDA kernels on this GPU, fields resident; timing only "
+                                   "(beyond one 16-row tile in y their results are wrong at tile edges)"}
+        except Exception as e:
             ref_gpu = {"unavailable": str(e)[:200]}
     line = {"metric": "GLUPS", "value": round(value, 4), "unit": "GLUPS", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,

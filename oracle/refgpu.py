@@ -209,3 +209,37 @@ def time_reference_heat(block, nsteps, reps=3):
     e1.synchronize()
     return e0.elapsed_time(e1) / reps
 
+
+def time_reference_eqwp(shape, nsteps, reps=1):
+    """Milliseconds per run of nsteps reference elastic-wave steps (stress,
+    vx, vy, vz per step) on a zero block of the given (Ngz, Ngy, Ngx) shape
+    with the body force, fields resident (CUDA events, after one untimed
+    run).  Timing only: beyond one 16-row tile in y the kernels' results are
+    wrong at tile edges (eqwp.cu:118-123), their memory accesses stay inside
+    the block."""
+    import torch
+    ngz, ngy, ngx = shape
+    cu, _, fns, _ = _load(CUBIN, _NAMES)
+    s = torch.cuda.current_stream()
+    stream = C.c_void_p(s.cuda_stream)
+    f = [torch.zeros(shape, dtype=torch.float32, device="cuda") for _ in range(10)]
+    vx, vy, vz, sxx, sxy, sxz, syy, syz, szz, disp = f
+    finit = torch.from_numpy(reference_force(shape)).cuda()
+    grid = ((ngx + TILE - 1) // TILE, (ngy + TILE - 1) // TILE)
+
+    def run():
+        for ts in range(nsteps):
+            _launch(cu, fns["stress"], grid, stream, ngx, ngy, ngz, sxx, sxy, sxz, syy, syz, szz, vx, vy, vz, 0)
+            _launch(cu, fns["vx"], grid, stream, ngx, ngy, ngz, vx, sxx, sxy, sxz, finit, ts, 0, 1)
+            _launch(cu, fns["vy"], grid, stream, ngx, ngy, ngz, vy, sxy, syy, syz, finit, disp, ts, 0, 1)
+            _launch(cu, fns["vz"], grid, stream, ngx, ngy, ngz, vz, sxz, syz, szz, finit, ts, 0, 1)
+
+    run()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        run()
+    e1.record(s)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
