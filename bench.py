@@ -283,6 +283,20 @@ def run_reference(args, wl):
                            "note": "the reference's CUDA kernel on this GPU, fields resident, no copies"}
         except Exception as e:   # context only: never fails the reference line
             ref_gpu = {"unavailable": str(e)[:200]}
+    if wl["model"] == 2:
+        try:
+            import torch
+            from oracle import refgpu
+            if torch.cuda.is_available() and refgpu.gol_available():
+                shape = tuple(e + 2 for e in env[::-1])     # one block with a one-cell shell
+                ms = refgpu.time_reference_gol(shape, wl["sub_steps"], reps=1)
+                cells = env[0] * env[1] * env[2]
+                ref_gpu = {"value": round(cells * wl["sub_steps"] / (ms / 1e3) / 1e9, 3), "unit": "GLUPS",
+                           "kernel": "gol_3d_kernel (gol-3D.cu:30)",
+                           "note": "the reference's CUDA kernel on this GPU, one block, resident; timing only "
+                                   "(beyond one 32x32 tile its results are wrong at tile edges)"}
+        except Exception as e:
+            ref_gpu = {"unavailable": str(e)[:200]}
     if wl["model"] == 3:
         try:
             import torch

@@ -243,3 +243,34 @@ def time_reference_eqwp(shape, nsteps, reps=1):
     e1.synchronize()
     return e0.elapsed_time(e1) / reps
 
+
+def time_reference_gol(shape, ngen, reps=1):
+    """Milliseconds per run of ngen launches of the reference's
+    gol_3d_kernel on a random (Ngz, Ngy, Ngx) block, ping-pong as
+    gol_3D_gpu_main runs it (gol-3D.cu:124-145), resident (CUDA events,
+    after one untimed run).  Timing only: beyond one 32 x 32 tile its results
+    are wrong at tile edges; its memory accesses stay inside the block."""
+    import torch
+    ngz, ngy, ngx = shape
+    cu, _, fns, _ = _load(GOL_CUBIN, {"gol": _GOL_NAME})
+    s = torch.cuda.current_stream()
+    stream = C.c_void_p(s.cuda_stream)
+    a = (torch.rand(shape, device="cuda") < 0.3).to(torch.uint8)
+    b = a.clone()
+    grid = ((ngx + GOL_TILE - 1) // GOL_TILE, (ngy + GOL_TILE - 1) // GOL_TILE)
+
+    def run():
+        x, y = a, b
+        for _ in range(ngen):
+            _launch(cu, fns["gol"], grid, stream, x, y, ngx, ngy, ngz, 0, tile=GOL_TILE)
+            x, y = y, x
+
+    run()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(reps):
+        run()
+    e1.record(s)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
