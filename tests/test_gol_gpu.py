@@ -201,3 +201,28 @@ def test_gol_halo_push_repeatable(b2r, orc, env, blocks, R):
             out = d.download()
             d.synchronize()
         assert np.array_equal(out, ref)
+
+
+@pytest.mark.parametrize("env", [(30, 30, 40), (9, 7, 5), (65, 33, 17), (128, 20, 12)])
+@pytest.mark.parametrize("R,tblock", [(1, 2), (2, 4), (5, 2), (3, 1)])
+def test_gol_single_fixed_shell_block(b2r, orc, env, R, tblock):
+    """One block with a one-cell fixed shell (no exchange, so a pass may take
+    more generations than the shell is deep): every R and pass length
+    against the oracle."""
+    if R > min(env) // 2:
+        pytest.skip("R*D <= min(B)/2 (b2r.cpp:54)")
+    dom = np.zeros(tuple(e + 2 for e in env[::-1]), np.uint8)
+    dom[1:-1, 1:-1, 1:-1] = bernoulli(env, 0.35, 14)
+    dom[:, :, 0] = 1
+    nsteps = 11
+    with b2r.Domain(b2r.MODEL_GOL, env, D=1, R=R) as d:
+        d.set_tuning(tblock=tblock)
+        d.upload(dom)
+        d.step(nsteps)
+        got = d.download()
+        d.synchronize()
+    a, b = dom.copy(), dom.copy()
+    for _ in range(nsteps):
+        orc.gol_substep(a, b, 0, 1, 63)
+        a, b = b, a
+    assert np.array_equal(got, a)
