@@ -159,3 +159,24 @@ def test_two_step_sweep_bit_identical(b2r, orc, env, blocks, R, periodic):
         ref = dom.copy()
         orc.heat_run(ref, 1, 1, 11, 0.1, 1.0, 1.0, 1.0)
         assert rel_l2(outs[1], ref) <= TOL
+
+
+@pytest.mark.parametrize("env", [(64, 2, 48), (2, 40, 33), (37, 29, 2), (3, 3, 3)])
+@pytest.mark.parametrize("D", [1, 2])
+def test_heat_thin_domains(b2r, orc, env, D):
+    """Domains a few cells thick along one axis (TMA boxes larger than the
+    block, windows of one or two cells) against the oracle."""
+    if D > min(env) // 2:
+        pytest.skip("R*D <= min(B)/2 (b2r.cpp:54)")
+    rng = np.random.default_rng(15)
+    dom = np.zeros(tuple(e + 2 * D for e in env[::-1]), np.float32)
+    dom[D:-D, D:-D, D:-D] = rng.random(env[::-1], dtype=np.float32)
+    with b2r.Domain(b2r.MODEL_HEAT, env, D=D, R=1, alpha_dt=0.05) as d:
+        d.upload(dom)
+        d.step(7)
+        got = d.download()
+        d.synchronize()
+    ref = dom.copy()
+    orc.heat_run(ref, D, D, 7, 0.05, 1.0, 1.0, 1.0)
+    r = float(np.linalg.norm(got.astype(np.float64) - ref) / np.linalg.norm(ref))
+    assert r <= 1e-5
