@@ -109,3 +109,28 @@ def test_batches_with_different_schedules_coexist(b2r):
                 d.step(it["nsteps"])
                 want = d.download()
             assert np.array_equal(got, want)
+
+
+def test_batch_tiny_and_thin_instances(b2r):
+    """Instances smaller than one tile, and a few cells thick, next to a
+    larger one: each matches its own plain run."""
+    import torch
+    items = [dict(env=(5, 6, 7), D=1, nsteps=9), dict(env=(8, 8, 8), D=2, nsteps=4),
+             dict(env=(16, 3, 40), D=1, nsteps=12), dict(env=(96, 80, 64), D=3, nsteps=6),
+             dict(env=(2, 2, 2), D=1, nsteps=3)]
+    for it in items:
+        it.update(alpha_dt=0.03, dx=1.0, dy=1.0, dz=1.0)
+    ins = inputs(items, 16)
+    s = torch.cuda.Stream()
+    with b2r.Batch(items, stream=s) as bt:
+        for i, a in enumerate(ins):
+            bt.upload(i, a)
+        bt.run()
+        bt.synchronize()
+        outs = [bt.download(i) for i in range(len(items))]
+    for it, a, got in zip(items, ins, outs):
+        with b2r.Domain(b2r.MODEL_HEAT, it["env"], D=it["D"], alpha_dt=it["alpha_dt"]) as d:
+            d.upload(a)
+            d.step(it["nsteps"])
+            want = d.download()
+        assert np.array_equal(got, want), it
