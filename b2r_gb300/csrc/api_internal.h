@@ -1,0 +1,139 @@
+// api_internal.h -- what the translation units of the C ABI share: the
+// handle, the error helper and the period driver (b2r_api.cu); the
+// autotuners (api_tune.cu) and the adjoint drivers (api_adjoint.cu) use them.
+#pragma once
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <new>
+#include <map>
+#include <mutex>
+#include <algorithm>
+#include <string>
+#include <tuple>
+#include <vector>
+#include <cudaTypedefs.h>
+#include "b2r_common.cuh"
+#include "eqwp.h"
+#include "gol.h"
+#include "halo.h"
+#include "heat.h"
+
+using namespace b2r;
+
+struct b2r_handle {
+    b2r_config cfg{};
+    BlockLayout L{};
+    int cell_bytes = 4;
+    int shell = 1;              // depth of the fixed shell in domain arrays
+    cudaStream_t stream = nullptr;
+    // heat / GoL: one field, two ping-pong buffers
+    void* buf[2] = {nullptr, nullptr};
+    int cur = 0;
+    CUtensorMap tmap[2];
+    CUtensorMap tmap2[2];       // boxes of the two-step kernel (D = 1)
+    HeatCoef hc{};
+    HeatTune tune{};
+    // elastic wave: fields and material
+    float* fld[kMaxFields] = {};
+    int nfld = 0;
+    // staggered model: the second field set of the one-pass step (v^n, s^n
+    // -> v^{n+1}, s^{n+1} out of place) and tensor maps of both sets'
+    // stresses; fld is always the current set
+    float* fld2[kMaxFields] = {};
+    StressMaps smaps[2];
+    bool eqwp_fused = false;   // two-pass by default: faster on this GPU so far
+    bool gol_bytes = false;    // Game of Life: byte-SWAR kernel instead of bit-sliced cells
+    bool adj_fused = true;     // adjoint: stress adjoint + lambda/mu gradients in one sweep
+    bool gol_push = false;     // Game of Life: period-end passes fill the next period's halos (opt-in: slower so far)
+    float* mat[3] = {};
+    std::vector<float> src;     // per-step source increment of sxx/syy/szz (STAG)
+    void* staging = nullptr;
+    size_t staging_bytes = 0;
+    // pipelined host runs: two input and two output device buffers, a copy
+    // stream per direction, and the events that order them
+    void* pipe[4] = {};
+    size_t pipe_bytes = 0;
+    cudaStream_t cin = nullptr, cout = nullptr;
+    cudaEvent_t ev[4][2] = {};   // [in ready, input consumed, output gathered, output copied][slot]
+    void* bounce = nullptr;
+    size_t bounce_bytes = 0;
+    int* d_status = nullptr;
+    long long ts = 0;
+    bool halos_fresh = false;
+    unsigned xmask = 0;          // fields exchanged by the caller at time step xts
+    long long xts = -1;
+    // CUDA graphs of whole periods (heat, GoL on a non-default stream)
+    bool graphs = true;
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};   // by ping-pong buffer at start
+    bool gflip[2] = {false, false};                   // the graph ends on the other buffer
+    int gsteps = 0;                                   // time steps per graph launch
+    long long gkernels = 0;                           // kernels per graph launch
+    // misfit-gradient workspace (checkpoints, replay, adjoint fields, FP64
+    // gradients), kept for the next call on this handle
+    void* adj_ws = nullptr;
+    size_t adj_ws_bytes = 0;
+    std::string err;
+};
+
+namespace b2r_api __attribute__((visibility("hidden"))) {
+
+struct TuneKey {
+    int model, D, n0, n1, n2, nblk;
+    bool operator<(const TuneKey& o) const
+    {
+        return std::tie(model, D, n0, n1, n2, nblk) < std::tie(o.model, o.D, o.n0, o.n1, o.n2, o.nblk);
+    }
+};
+
+#define CK(h, call)                                                                          \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess) {                                                             \
+            cudaGetLastError(); /* a non-sticky error must not resurface in a later check */ \
+            return fail(h, e_ == cudaErrorMemoryAllocation ? B2R_ERR_OOM : B2R_ERR_CUDA,     \
+                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+        }                                                                                    \
+    } while (0)
+
+struct DevBuf {
+    void* p = nullptr;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf()
+    {
+        if (p) cudaFree(p);
+    }
+};
+
+inline int roundup(int v, int m) { return (v + m - 1) / m * m; }
+
+extern std::mutex g_tune_mu;
+extern std::map<TuneKey, HeatTune> g_tune_cache;
+TuneKey key_of(const b2r_handle* h);
+extern thread_local std::string g_err;
+b2r_status fail(b2r_handle* h, b2r_status s, const char* fmt, ...);
+int halo_per_step(const b2r_config& c);
+void fill_layout(BlockLayout& L, const int n[3], const int B[3], const int nb[3], int H, int cell_bytes,
+                 int periodic, int fixed_edge);
+size_t field_bytes(const b2r_handle* h);
+size_t domain_cells(const b2r_handle* h);
+b2r_status ensure_kappa(b2r_handle* h);
+b2r_status ensure_staging(b2r_handle* h, size_t bytes);
+b2r_status build_heat_maps(b2r_handle* h);
+bool heat_fuse_ok(const b2r_handle* h, int i);
+int gol_pass_gens(const b2r_handle* h, int i, int left);
+b2r_status check_status(b2r_handle* h);
+b2r_status exchange_all(b2r_handle* h, bool staged);
+b2r_status exchange_one(b2r_handle* h, int field, bool staged);
+EqwpStagParams stag_params(const b2r_handle* h);
+b2r_status substep(b2r_handle* h, int i);
+b2r_status substep2(b2r_handle* h, int i);
+void drop_graphs(b2r_handle* h);
+b2r_status advance(b2r_handle* h, int n);
+b2r_status capture_graph(b2r_handle* h, int c, int periods);
+
+}  // namespace b2r_api

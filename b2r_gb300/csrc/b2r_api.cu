@@ -1,96 +1,16 @@
 // b2r_api.cu -- the C ABI of libb2r (include/b2r.h): handles, geometry,
 // device memory of the resident subdomains, the period driver (halo
-// exchange + R sub-steps, b2r.cpp:179-221) and the reference-shaped per-block
-// entries (heat_3D_gpu_main, gol_3D_gpu_main, eqwp_gpu_main).
-#include <atomic>
-#include <cstdarg>
-#include <cstdio>
-#include <cstring>
-#include <fstream>
-#include <new>
-#include <map>
-#include <mutex>
-#include <algorithm>
-#include <string>
-#include <tuple>
-#include <vector>
+// exchange + R sub-steps, b2r.cpp:179-221), host runs and block data files,
+// and the reference-shaped per-block entries (heat_3D_gpu_main,
+// gol_3D_gpu_main, eqwp_gpu_main).  The tuning knobs and autotuners are in
+// api_tune.cu, the misfit-gradient drivers in api_adjoint.cu.
+#include "api_internal.h"
 
-#include <cudaTypedefs.h>
+namespace b2r_api {
 
-#include "b2r_common.cuh"
-#include "eqwp.h"
-#include "gol.h"
-#include "halo.h"
-#include "heat.h"
-
-using namespace b2r;
-
-struct b2r_handle {
-    b2r_config cfg{};
-    BlockLayout L{};
-    int cell_bytes = 4;
-    int shell = 1;              // depth of the fixed shell in domain arrays
-    cudaStream_t stream = nullptr;
-    // heat / GoL: one field, two ping-pong buffers
-    void* buf[2] = {nullptr, nullptr};
-    int cur = 0;
-    CUtensorMap tmap[2];
-    CUtensorMap tmap2[2];       // boxes of the two-step kernel (D = 1)
-    HeatCoef hc{};
-    HeatTune tune{};
-    // elastic wave: fields and material
-    float* fld[kMaxFields] = {};
-    int nfld = 0;
-    // staggered model: the second field set of the one-pass step (v^n, s^n
-    // -> v^{n+1}, s^{n+1} out of place) and tensor maps of both sets'
-    // stresses; fld is always the current set
-    float* fld2[kMaxFields] = {};
-    StressMaps smaps[2];
-    bool eqwp_fused = false;   // two-pass by default: faster on this GPU so far
-    bool gol_bytes = false;    // Game of Life: byte-SWAR kernel instead of bit-sliced cells
-    bool adj_fused = true;     // adjoint: stress adjoint + lambda/mu gradients in one sweep
-    bool gol_push = false;     // Game of Life: period-end passes fill the next period's halos (opt-in: slower so far)
-    float* mat[3] = {};
-    std::vector<float> src;     // per-step source increment of sxx/syy/szz (STAG)
-    void* staging = nullptr;
-    size_t staging_bytes = 0;
-    // pipelined host runs: two input and two output device buffers, a copy
-    // stream per direction, and the events that order them
-    void* pipe[4] = {};
-    size_t pipe_bytes = 0;
-    cudaStream_t cin = nullptr, cout = nullptr;
-    cudaEvent_t ev[4][2] = {};   // [in ready, input consumed, output gathered, output copied][slot]
-    void* bounce = nullptr;
-    size_t bounce_bytes = 0;
-    int* d_status = nullptr;
-    long long ts = 0;
-    bool halos_fresh = false;
-    unsigned xmask = 0;          // fields exchanged by the caller at time step xts
-    long long xts = -1;
-    // CUDA graphs of whole periods (heat, GoL on a non-default stream)
-    bool graphs = true;
-    cudaGraphExec_t gexec[2] = {nullptr, nullptr};   // by ping-pong buffer at start
-    bool gflip[2] = {false, false};                   // the graph ends on the other buffer
-    int gsteps = 0;                                   // time steps per graph launch
-    long long gkernels = 0;                           // kernels per graph launch
-    // misfit-gradient workspace (checkpoints, replay, adjoint fields, FP64
-    // gradients), kept for the next call on this handle
-    void* adj_ws = nullptr;
-    size_t adj_ws_bytes = 0;
-    std::string err;
-};
-
-namespace {
 
 // autotuning results per (model, D, block size, blocks), shared by handles
 
-struct TuneKey {
-    int model, D, n0, n1, n2, nblk;
-    bool operator<(const TuneKey& o) const
-    {
-        return std::tie(model, D, n0, n1, n2, nblk) < std::tie(o.model, o.D, o.n0, o.n1, o.n2, o.nblk);
-    }
-};
 std::mutex g_tune_mu;
 std::map<TuneKey, HeatTune> g_tune_cache;
 
@@ -114,28 +34,8 @@ b2r_status fail(b2r_handle* h, b2r_status s, const char* fmt, ...)
     return s;
 }
 
-#define CK(h, call)                                                                          \
-    do {                                                                                     \
-        cudaError_t e_ = (call);                                                             \
-        if (e_ != cudaSuccess) {                                                             \
-            cudaGetLastError(); /* a non-sticky error must not resurface in a later check */ \
-            return fail(h, e_ == cudaErrorMemoryAllocation ? B2R_ERR_OOM : B2R_ERR_CUDA,     \
-                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
-        }                                                                                    \
-    } while (0)
 
-struct DevBuf {
-    void* p = nullptr;
-    DevBuf() = default;
-    DevBuf(const DevBuf&) = delete;
-    DevBuf& operator=(const DevBuf&) = delete;
-    ~DevBuf()
-    {
-        if (p) cudaFree(p);
-    }
-};
 
-inline int roundup(int v, int m) { return (v + m - 1) / m * m; }
 
 // cells consumed from the halo by one time step
 int halo_per_step(const b2r_config& c)
@@ -452,7 +352,10 @@ b2r_status substep2(b2r_handle* h, int i)
     return B2R_OK;
 }
 
-}  // namespace
+}  // namespace b2r_api
+
+using namespace b2r_api;
+
 
 namespace b2r {
 
@@ -920,638 +823,6 @@ b2r_status b2r_boundary_updating(b2r_handle* h, int time_step, int field)
     if (field < 0 || field >= (h->nfld > 0 ? h->nfld : 1))
         return fail(h, B2R_ERR_ARG, "invalid field id %d", field);
     return note_exchange(h, field, exchange_one(h, field, true));
-}
-
-// ---------------------------------------------------------------- autotuning
-
-b2r_status b2r_set_tuning(b2r_handle* h, int key, int value)
-{
-    if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
-    switch (key) {
-    case B2R_TUNE_ZCHUNK: h->tune.zchunk = value; break;
-    case B2R_TUNE_CTAS_PER_SM: h->tune.ctas_per_sm = value; break;
-    case B2R_TUNE_PDL: h->tune.pdl = value != 0; break;
-    case B2R_TUNE_TBLOCK: h->tune.tblock = value; break;
-    case B2R_TUNE_ZCHUNK2: h->tune.zchunk2 = value; break;
-    case B2R_TUNE_EQWP_FUSED: h->eqwp_fused = value != 0; break;
-    case B2R_TUNE_GOL_BYTES: h->gol_bytes = value != 0; break;
-    case B2R_TUNE_ADJ_FUSED: h->adj_fused = value != 0; break;
-    case B2R_TUNE_GOL_PUSH: h->gol_push = value != 0; break;
-    default: return fail(h, B2R_ERR_ARG, "unknown tuning key %d", key);
-    }
-    drop_graphs(h);
-    return B2R_OK;
-}
-
-b2r_status b2r_get_tuning(const b2r_handle* h, int key, int* value)
-{
-    if (!h || !value) return fail(nullptr, B2R_ERR_ARG, "null argument");
-    switch (key) {
-    case B2R_TUNE_ZCHUNK: *value = h->tune.zchunk; break;
-    case B2R_TUNE_CTAS_PER_SM: *value = h->tune.ctas_per_sm; break;
-    case B2R_TUNE_PDL: *value = h->tune.pdl ? 1 : 0; break;
-    case B2R_TUNE_TBLOCK: *value = h->tune.tblock; break;
-    case B2R_TUNE_ZCHUNK2: *value = h->tune.zchunk2; break;
-    case B2R_TUNE_EQWP_FUSED: *value = h->eqwp_fused ? 1 : 0; break;
-    case B2R_TUNE_GOL_BYTES: *value = h->gol_bytes ? 1 : 0; break;
-    case B2R_TUNE_ADJ_FUSED: *value = h->adj_fused ? 1 : 0; break;
-    case B2R_TUNE_GOL_PUSH: *value = h->gol_push ? 1 : 0; break;
-    default: return fail(nullptr, B2R_ERR_ARG, "unknown tuning key %d", key);
-    }
-    return B2R_OK;
-}
-
-// Game of Life and the staggered elastic wave: the same timed search over
-// their kernel choices -- generations per pass, bit-sliced or byte cells and
-// the period-end halo fill (GoL); the one-pass or two-pass step (elastic
-// wave).  Trials run on the live fields, which are restored afterwards.
-struct KnobSet {
-    int tblock, gol_bytes, gol_push, eqwp_fused;
-};
-static std::map<TuneKey, KnobSet> g_knob_cache;
-
-static void apply_knobs(b2r_handle* h, const KnobSet& k)
-{
-    h->tune.tblock = k.tblock;
-    h->gol_bytes = k.gol_bytes != 0;
-    h->gol_push = k.gol_push != 0;
-    h->eqwp_fused = k.eqwp_fused != 0;
-}
-
-static b2r_status autotune_knobs(b2r_handle* h, int trial_steps, int best[3], double* best_ms)
-{
-    auto report = [&](const KnobSet& k, double ms) {
-        if (best) {
-            best[0] = k.tblock;
-            best[1] = h->cfg.model == B2R_MODEL_GOL ? k.gol_bytes : k.eqwp_fused;
-            best[2] = k.gol_push;
-        }
-        if (best_ms) *best_ms = ms;
-    };
-    {
-        std::lock_guard<std::mutex> lock(g_tune_mu);
-        auto it = g_knob_cache.find(key_of(h));
-        if (it != g_knob_cache.end()) {
-            apply_knobs(h, it->second);
-            report(it->second, -1.0);
-            drop_graphs(h);
-            return B2R_OK;
-        }
-    }
-    std::vector<KnobSet> cands;
-    const KnobSet cur{h->tune.tblock, h->gol_bytes, h->gol_push, h->eqwp_fused};
-    if (h->cfg.model == B2R_MODEL_GOL) {
-        for (int tb : {1, 2, 4})
-            for (int bytes = 0; bytes < 2; ++bytes)
-                for (int push = 0; push < 2; ++push)
-                    if (!push || (tb >= 2 && !bytes)) cands.push_back({tb, bytes, push, cur.eqwp_fused});
-    } else {
-        for (int fused = 0; fused < 2; ++fused) cands.push_back({cur.tblock, cur.gol_bytes, cur.gol_push, fused});
-    }
-    // the state the trials overwrite: the current buffer (GoL) or every
-    // field of the current set with the set's pointers (elastic wave)
-    const size_t fb = field_bytes(h);
-    const bool eq = h->nfld > 0;
-    const int nsave = eq ? h->nfld : 1;
-    struct SaveBufs {
-        std::vector<void*> p;
-        ~SaveBufs()
-        {
-            for (void* q : p)
-                if (q) cudaFree(q);
-        }
-    } keep;
-    keep.p.assign((size_t)nsave, nullptr);
-    std::vector<void*>& save = keep.p;
-    float* save_fld[kMaxFields];
-    float* save_fld2[kMaxFields];
-    StressMaps save_smaps[2] = {h->smaps[0], h->smaps[1]};
-    std::memcpy(save_fld, h->fld, sizeof save_fld);
-    std::memcpy(save_fld2, h->fld2, sizeof save_fld2);
-    for (int f = 0; f < nsave; ++f) {
-        if (cudaMalloc(&save[(size_t)f], fb) != cudaSuccess) {
-            cudaGetLastError();
-            return fail(h, B2R_ERR_OOM, "autotuning needs %zu bytes to keep the fields", fb * nsave);
-        }
-        const void* src = eq ? (const void*)h->fld[f] : h->buf[h->cur];
-        CK(h, cudaMemcpyAsync(save[(size_t)f], src, fb, cudaMemcpyDeviceToDevice, h->stream));
-    }
-    const int save_cur = h->cur;
-    const long long save_ts = h->ts;
-    const bool save_fresh = h->halos_fresh;
-    // trials run as the stepping will (graph replay included, each
-    // candidate's graphs captured in its warm run) and over whole periods:
-    // a single period would not show what a choice costs at period ends
-    const int trial = h->cfg.model == B2R_MODEL_GOL ? std::max(trial_steps, 16 * h->cfg.R) : trial_steps;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    KnobSet bestK = cur;
-    float bestMs = 1e30f;
-    b2r_status st = B2R_OK;
-    for (const KnobSet& k : cands) {
-        apply_knobs(h, k);
-        drop_graphs(h);
-        if ((st = b2r_step(h, trial)) != B2R_OK) break;   // warm (captures graphs)
-        cudaEventRecord(e0, h->stream);
-        if ((st = b2r_step(h, trial)) != B2R_OK) break;
-        cudaEventRecord(e1, h->stream);
-        cudaEventSynchronize(e1);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < bestMs) {
-            bestMs = ms;
-            bestK = k;
-        }
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    std::memcpy(h->fld, save_fld, sizeof save_fld);
-    std::memcpy(h->fld2, save_fld2, sizeof save_fld2);
-    h->smaps[0] = save_smaps[0];
-    h->smaps[1] = save_smaps[1];
-    h->cur = save_cur;
-    h->ts = save_ts;
-    h->halos_fresh = save_fresh;
-    for (int f = 0; f < nsave; ++f) {
-        void* dst = eq ? (void*)h->fld[f] : h->buf[h->cur];
-        cudaMemcpyAsync(dst, save[(size_t)f], fb, cudaMemcpyDeviceToDevice, h->stream);
-    }
-    cudaStreamSynchronize(h->stream);
-    apply_knobs(h, st == B2R_OK ? bestK : cur);
-    drop_graphs(h);
-    if (st != B2R_OK) return st;
-    {
-        std::lock_guard<std::mutex> lock(g_tune_mu);
-        g_knob_cache[key_of(h)] = bestK;
-    }
-    report(bestK, bestMs / trial);
-    return check_status(h);
-}
-
-b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* best_ms)
-{
-    if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
-    if (trial_steps < 1) trial_steps = 4;
-    if (h->cfg.model == B2R_MODEL_GOL || h->cfg.model == B2R_MODEL_EQWP_STAG)
-        return autotune_knobs(h, trial_steps, best, best_ms);
-    if (h->cfg.model != B2R_MODEL_HEAT)
-        return fail(h, B2R_ERR_ARG, "autotuning covers heat, Game of Life and the staggered elastic wave");
-    {
-        std::lock_guard<std::mutex> lock(g_tune_mu);
-        auto it = g_tune_cache.find(key_of(h));
-        if (it != g_tune_cache.end()) {
-            h->tune = it->second;
-            if (best) { best[0] = h->tune.zchunk; best[1] = h->tune.ctas_per_sm; best[2] = h->tune.pdl; }
-            if (best_ms) *best_ms = -1.0;
-            drop_graphs(h);
-            return B2R_OK;
-        }
-    }
-    // keep the simulation state: trials run on the live buffers, which are
-    // restored afterwards
-    const size_t fb = field_bytes(h);
-    DevBuf keep;
-    CK(h, cudaMalloc(&keep.p, fb));
-    void* const save = keep.p;
-    CK(h, cudaMemcpyAsync(save, h->buf[h->cur], fb, cudaMemcpyDeviceToDevice, h->stream));
-    const int save_cur = h->cur;
-    const long long save_ts = h->ts;
-    const bool save_fresh = h->halos_fresh;
-    const bool save_graphs = h->graphs;
-    h->graphs = false;
-    static const int zchunks[] = {0, 16, 32, 64, 128, 256};
-    static const int persist[] = {0, 1, 2, 3, 4, 5, 6};
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    HeatTune bestT = h->tune;
-    float bestMs = 1e30f;
-    b2r_status st = B2R_OK;
-    // candidates: the two-step sweep (radius 1) by z-chunk, then the one-step
-    // sweep by z-chunk x persistent CTAs per SM x PDL
-    struct Cand { int tb, zc2, zc, cp, pdl; };
-    std::vector<Cand> cands;
-    if (h->cfg.D == 1)
-        for (int z2 : {4, 8, 16, 32, 64}) cands.push_back({2, z2, 0, 0, 1});
-    for (int pdl = 0; pdl < 2; ++pdl)
-        for (int zc : zchunks)
-            for (int cp : persist)
-                if (zc <= h->L.n[2]) cands.push_back({1, 0, zc, cp, pdl});
-    for (const Cand& cd : cands)
-            {
-                if (st != B2R_OK) break;
-                h->tune.tblock = cd.tb;
-                h->tune.zchunk2 = cd.zc2;
-                h->tune.zchunk = cd.zc;
-                h->tune.ctas_per_sm = cd.cp;
-                h->tune.pdl = cd.pdl;
-                if ((st = b2r_step(h, 1)) != B2R_OK) break;       // warm
-                cudaEventRecord(e0, h->stream);
-                if ((st = b2r_step(h, trial_steps)) != B2R_OK) break;
-                cudaEventRecord(e1, h->stream);
-                cudaEventSynchronize(e1);
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, e0, e1);
-                if (ms < bestMs) {
-                    bestMs = ms;
-                    bestT = h->tune;
-                }
-            }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    h->tune = bestT;
-    h->cur = save_cur;
-    h->ts = save_ts;
-    h->halos_fresh = save_fresh;
-    h->graphs = save_graphs;
-    cudaMemcpyAsync(h->buf[h->cur], save, fb, cudaMemcpyDeviceToDevice, h->stream);
-    cudaStreamSynchronize(h->stream);
-    if (st != B2R_OK) return st;
-    {
-        std::lock_guard<std::mutex> lock(g_tune_mu);
-        g_tune_cache[key_of(h)] = bestT;
-    }
-    drop_graphs(h);
-    if (best) { best[0] = bestT.tblock == 2 ? bestT.zchunk2 : bestT.zchunk; best[1] = bestT.ctas_per_sm; best[2] = bestT.pdl; }
-    if (best_ms) *best_ms = bestMs / trial_steps;
-    return check_status(h);
-}
-
-// ---------------------------------------------------------------- adjoint (staggered model)
-namespace {
-
-
-b2r_status adj_check(b2r_handle* h)
-{
-    if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
-    if (h->cfg.model != B2R_MODEL_EQWP_STAG)
-        return fail(h, B2R_ERR_ARG, "the adjoint covers the staggered elastic-wave model");
-    if (h->L.nblk != 1 || h->cfg.R != 1)
-        return fail(h, B2R_ERR_ARG, "the adjoint runs on one block with R = 1");
-    return B2R_OK;
-}
-
-// receiver element offsets (global interior coordinates -> block storage)
-b2r_status rec_offsets(b2r_handle* h, int nrec, const int* rec_xyz, std::vector<long long>& idx)
-{
-    idx.resize(nrec);
-    for (int r = 0; r < nrec; ++r) {
-        int c[3];
-        for (int a = 0; a < 3; ++a) {
-            c[a] = rec_xyz[3 * r + a];
-            if (c[a] < 0 || c[a] >= h->cfg.env[a]) return fail(h, B2R_ERR_ARG, "receiver %d outside the domain", r);
-            c[a] += h->L.H;
-        }
-        idx[r] = (long long)c[2] * h->L.plane + (long long)c[1] * h->L.P + h->L.xoff + c[0];
-    }
-    return B2R_OK;
-}
-
-}  // namespace
-
-b2r_status b2r_eqwp_record(b2r_handle* h, int nsteps, int nrec, const int* rec_xyz, float* d_out)
-{
-    b2r_status st;
-    if ((st = adj_check(h)) != B2R_OK) return st;
-    if (nsteps < 0 || nrec <= 0 || !rec_xyz || !d_out) return fail(h, B2R_ERR_ARG, "invalid receivers");
-    std::vector<long long> idx;
-    if ((st = rec_offsets(h, nrec, rec_xyz, idx)) != B2R_OK) return st;
-    DevBuf d_idx, d_rec;
-    CK(h, cudaMalloc(&d_idx.p, sizeof(long long) * nrec));
-    CK(h, cudaMalloc(&d_rec.p, sizeof(float) * (size_t)nrec * (nsteps > 0 ? nsteps : 1)));
-    CK(h, cudaMemcpyAsync(d_idx.p, idx.data(), sizeof(long long) * nrec, cudaMemcpyHostToDevice, h->stream));
-    h->ts = 0;
-    for (int n = 0; n < nsteps; ++n) {
-        if ((st = substep(h, 0)) != B2R_OK) return st;
-        h->ts++;
-        CK(h, adjoint_sample(h->fld[B2R_F_VY], (const long long*)d_idx.p, nrec, (float*)d_rec.p + (size_t)n * nrec,
-                             h->stream));
-    }
-    CK(h, cudaMemcpyAsync(d_out, d_rec.p, sizeof(float) * (size_t)nrec * nsteps, cudaMemcpyDeviceToHost, h->stream));
-    CK(h, cudaStreamSynchronize(h->stream));
-    return check_status(h);
-}
-
-b2r_status b2r_eqwp_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const int* rec_xyz,
-                                    const float* d_obs, int ckpt_every, double* misfit,
-                                    double* grad_lambda, double* grad_mu, double* grad_rho,
-                                    float* d_syn)
-{
-    b2r_status st;
-    if ((st = adj_check(h)) != B2R_OK) return st;
-    if (nsteps <= 0 || nrec <= 0 || !rec_xyz || !d_obs) return fail(h, B2R_ERR_ARG, "invalid receivers / steps");
-    const int K = ckpt_every > 0 ? ckpt_every : nsteps;
-    std::vector<long long> idx;
-    if ((st = rec_offsets(h, nrec, rec_xyz, idx)) != B2R_OK) return st;
-    const size_t fb = field_bytes(h);
-    const size_t nseg = (size_t)(nsteps + K - 1) / K;
-    // workspace, carved from one allocation kept on the handle: checkpoints
-    // (9 fields each), the replayed velocities v^{n0+k} (k = 1..K; k = 0 is
-    // the checkpoint) and stencil sums of a segment, the replay's stresses,
-    // the adjoint fields and the FP64 gradients
-    // Two replay buffers when the workspace fits: segment s-1 is replayed
-    // on a second stream while segment s runs its reverse steps.
-    const size_t gbytes = (size_t)h->L.bstride * sizeof(double);
-    const size_t nf_ckpt = nseg * 9, nf_v = (size_t)(K + 1) * 3, nf_a = (size_t)K * 3;
-    const size_t fba = (fb + 255) & ~(size_t)255, gba = (gbytes + 255) & ~(size_t)255;
-    int nbuf = nseg > 1 ? 2 : 1;
-    for (;; --nbuf) {
-        const size_t nfields = nf_ckpt + nbuf * (nf_v + nf_a + 6) + 18;
-        const size_t need = nfields * fba + 3 * gba;
-        if (h->adj_ws_bytes >= need) break;
-        if (h->adj_ws) cudaFree(h->adj_ws);
-        h->adj_ws = nullptr;
-        h->adj_ws_bytes = 0;
-        if (cudaMalloc(&h->adj_ws, need) == cudaSuccess) {
-            h->adj_ws_bytes = need;
-            break;
-        }
-        cudaGetLastError();
-        h->adj_ws = nullptr;
-        if (nbuf == 1) return fail(h, B2R_ERR_OOM, "misfit gradient needs %zu bytes of workspace", need);
-    }
-    char* ws = static_cast<char*>(h->adj_ws);
-    auto carve = [&](size_t n, std::vector<float*>& out) {
-        out.resize(n);
-        for (size_t i = 0; i < n; ++i, ws += fba) out[i] = reinterpret_cast<float*>(ws);
-    };
-    std::vector<float*> ckpt, vrep, arep, srep, tmp;
-    carve(nf_ckpt, ckpt);
-    carve(nf_v * nbuf, vrep);   // buffer b: entries [b * nf_v, (b + 1) * nf_v)
-    carve(nf_a * nbuf, arep);
-    carve(6 * (size_t)nbuf, srep);
-    carve(18, tmp);
-    double* gp[3];
-    for (int m = 0; m < 3; ++m, ws += gba) {
-        gp[m] = reinterpret_cast<double*>(ws);
-        CK(h, cudaMemsetAsync(gp[m], 0, gbytes, h->stream));
-    }
-    DevBuf d_idx, d_rec, d_res;
-    // cells outside the update window never change: every replay slot starts
-    // as a copy of the initial state there
-    for (size_t k = 0; k < vrep.size(); ++k)
-        CK(h, cudaMemcpyAsync(vrep[k], h->fld[B2R_F_VX + k % 3], fb, cudaMemcpyDeviceToDevice, h->stream));
-    for (float* b : arep) CK(h, cudaMemsetAsync(b, 0, fb, h->stream));
-    for (float* b : tmp) CK(h, cudaMemsetAsync(b, 0, fb, h->stream));
-    CK(h, cudaMalloc(&d_idx.p, sizeof(long long) * nrec));
-    CK(h, cudaMalloc(&d_rec.p, sizeof(float) * (size_t)nrec * nsteps));
-    CK(h, cudaMalloc(&d_res.p, sizeof(float) * (size_t)nrec * nsteps));
-    CK(h, cudaMemcpyAsync(d_idx.p, idx.data(), sizeof(long long) * nrec, cudaMemcpyHostToDevice, h->stream));
-    const long long* didx = (const long long*)d_idx.p;
-
-    // forward with checkpoints every K steps and receiver samples
-    h->ts = 0;
-    for (int n = 0; n < nsteps; ++n) {
-        if (n % K == 0)
-            for (int f = 0; f < 9; ++f)
-                CK(h, cudaMemcpyAsync(ckpt[(n / K) * 9 + f], h->fld[f], fb, cudaMemcpyDeviceToDevice, h->stream));
-        if ((st = substep(h, 0)) != B2R_OK) return st;
-        h->ts++;
-        CK(h, adjoint_sample(h->fld[B2R_F_VY], didx, nrec, (float*)d_rec.p + (size_t)n * nrec, h->stream));
-    }
-    // misfit and residual (host, FP64)
-    std::vector<float> syn((size_t)nrec * nsteps), res((size_t)nrec * nsteps);
-    CK(h, cudaMemcpyAsync(syn.data(), d_rec.p, sizeof(float) * syn.size(), cudaMemcpyDeviceToHost, h->stream));
-    CK(h, cudaStreamSynchronize(h->stream));
-    double J = 0.0;
-    for (size_t i = 0; i < syn.size(); ++i) {
-        const double r = (double)syn[i] - (double)d_obs[i];
-        res[i] = (float)r;
-        J += 0.5 * r * r;
-    }
-    if (misfit) *misfit = J;
-    if (d_syn) std::copy(syn.begin(), syn.end(), d_syn);
-    CK(h, cudaMemcpyAsync(d_res.p, res.data(), sizeof(float) * res.size(), cudaMemcpyHostToDevice, h->stream));
-
-    // reverse sweep, segment by segment: each segment is replayed forward
-    // from its checkpoint into replay buffer sgi % nbuf (velocities and
-    // stencil sums of every step kept), then its reverse steps run.  With two
-    // buffers the replay of the segment below runs on a second stream while
-    // this segment's reverse steps run; the results are the same bits.
-    float* const* tp = tmp.data();
-    const float* mat[3] = {h->mat[0], h->mat[1], h->mat[2]};
-    const float dt_h = (float)(h->cfg.dt / h->cfg.h);
-    const EqwpStagParams sp = stag_params(h);
-    struct AuxStream {
-        cudaStream_t s = nullptr;
-        cudaEvent_t start = nullptr, rep[2] = {}, rev[2] = {};
-        ~AuxStream()
-        {
-            for (cudaEvent_t e : {start, rep[0], rep[1], rev[0], rev[1]})
-                if (e) cudaEventDestroy(e);
-            if (s) cudaStreamDestroy(s);
-        }
-    } ax;
-    cudaStream_t aux = h->stream;
-    if (nbuf == 2) {
-        CK(h, cudaStreamCreateWithFlags(&ax.s, cudaStreamNonBlocking));
-        for (cudaEvent_t* e : {&ax.start, &ax.rep[0], &ax.rep[1], &ax.rev[0], &ax.rev[1]})
-            CK(h, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
-        aux = ax.s;
-        CK(h, cudaEventRecord(ax.start, h->stream));   // the forward and the residual are in place
-        CK(h, cudaStreamWaitEvent(aux, ax.start, 0));
-    }
-    // v^{n0+k} of segment sgi: the checkpoint's velocities for k = 0, replay
-    // slot k of the segment's buffer after
-    auto vslot = [&](long long sgi, int k, int f) -> float* {
-        return k == 0 ? ckpt[sgi * 9 + B2R_F_VX + f] : vrep[(size_t)(sgi % nbuf) * nf_v + (size_t)k * 3 + f];
-    };
-    auto aslot = [&](long long sgi, int k) -> float* const* {
-        return &arep[(size_t)(sgi % nbuf) * nf_a + (size_t)k * 3];
-    };
-    auto replay = [&](long long sgi, cudaStream_t st) -> b2r_status {
-        const int n0 = (int)sgi * K, n1 = std::min(nsteps, n0 + K);
-        float* const* s6 = srep.data() + 6 * (sgi % nbuf);
-        for (int f = 0; f < 6; ++f)
-            CK(h, cudaMemcpyAsync(s6[f], ckpt[sgi * 9 + B2R_F_SXX + f], fb, cudaMemcpyDeviceToDevice, st));
-        for (int n = n0; n < n1; ++n) {
-            const int k = n - n0;
-            const float* vin[3] = {vslot(sgi, k, 0), vslot(sgi, k, 1), vslot(sgi, k, 2)};
-            float* vout[3] = {vslot(sgi, k + 1, 0), vslot(sgi, k + 1, 1), vslot(sgi, k + 1, 2)};
-            CK(h, launch_eqwp_stag_step_replay(vin, s6, vout, aslot(sgi, k), h->mat, h->L, n, sp, st));
-        }
-        return B2R_OK;
-    };
-    if ((st = replay((long long)nseg - 1, aux)) != B2R_OK) return st;
-    if (nbuf == 2) CK(h, cudaEventRecord(ax.rep[(nseg - 1) % 2], aux));
-    for (long long sgi = (long long)nseg - 1; sgi >= 0; --sgi) {
-        const int n0 = (int)sgi * K;
-        const int n1 = std::min(nsteps, n0 + K);
-        if (nbuf == 2) {
-            CK(h, cudaStreamWaitEvent(h->stream, ax.rep[sgi % 2], 0));
-            if (sgi >= 1) {
-                const int b1 = (int)((sgi - 1) % 2);
-                // that buffer last served segment sgi + 1, whose reverse steps are queued
-                if (sgi + 1 < (long long)nseg) CK(h, cudaStreamWaitEvent(aux, ax.rev[b1], 0));
-                if ((st = replay(sgi - 1, aux)) != B2R_OK) return st;
-                CK(h, cudaEventRecord(ax.rep[b1], aux));
-            }
-        }
-        for (int n = n1 - 1; n >= n0; --n) {
-            const int k = n - n0;
-            CK(h, adjoint_inject(tp[1], didx, nrec, (const float*)d_res.p + (size_t)n * nrec, h->stream));
-            const float* vn[3] = {vslot(sgi, k, 0), vslot(sgi, k, 1), vslot(sgi, k, 2)};
-            float* const* a = aslot(sgi, k);
-            const float* an[3] = {a[0], a[1], a[2]};
-            CK(h, adjoint_step(tp, vn, an, mat, gp, h->L, dt_h, n == 0, h->adj_fused, h->stream));
-        }
-        if (nbuf == 2) CK(h, cudaEventRecord(ax.rev[sgi % 2], h->stream));
-        else if (sgi >= 1 && (st = replay(sgi - 1, h->stream)) != B2R_OK) return st;
-    }
-    // gradients out (interior cells, x fastest), g_rho = -g_b / rho^2
-    double* outs[3] = {grad_lambda, grad_mu, grad_rho};
-    const size_t ncell = (size_t)h->cfg.env[0] * h->cfg.env[1] * h->cfg.env[2];
-    DevBuf d_out;
-    CK(h, cudaMalloc(&d_out.p, ncell * sizeof(double)));
-    for (int m = 0; m < 3; ++m) {
-        if (!outs[m]) continue;
-        CK(h, adjoint_grad_out(gp[m], h->mat[2], m == 2, h->L, (double*)d_out.p, h->stream));
-        CK(h, cudaMemcpyAsync(outs[m], d_out.p, ncell * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    }
-    CK(h, cudaStreamSynchronize(h->stream));
-    h->ts = nsteps;
-    h->halos_fresh = false;
-    return check_status(h);
-}
-
-namespace {
-
-b2r_status heat_adj_check(b2r_handle* h)
-{
-    if (!h) return fail(nullptr, B2R_ERR_ARG, "null handle");
-    if (h->cfg.model != B2R_MODEL_HEAT) return fail(h, B2R_ERR_ARG, "the heat adjoint needs the heat model");
-    if (h->L.nblk != 1 || h->L.periodic)
-        return fail(h, B2R_ERR_ARG, "the heat adjoint runs on one block with a fixed shell");
-    return ensure_kappa(h);
-}
-
-HeatLap heat_lap_of(const b2r_handle* h)
-{
-    return heat_lap(h->cfg.D, h->cfg.alpha_dt, h->cfg.dx, h->cfg.dy, h->cfg.dz);
-}
-
-}  // namespace
-
-b2r_status b2r_heat_record(b2r_handle* h, int nsteps, int nrec, const int* rec_xyz, float* d_out)
-{
-    b2r_status st;
-    if ((st = heat_adj_check(h)) != B2R_OK) return st;
-    if (nsteps < 0 || nrec <= 0 || !rec_xyz || !d_out) return fail(h, B2R_ERR_ARG, "invalid receivers");
-    std::vector<long long> idx;
-    if ((st = rec_offsets(h, nrec, rec_xyz, idx)) != B2R_OK) return st;
-    DevBuf d_idx, d_rec;
-    CK(h, cudaMalloc(&d_idx.p, sizeof(long long) * nrec));
-    CK(h, cudaMalloc(&d_rec.p, sizeof(float) * (size_t)nrec * (nsteps > 0 ? nsteps : 1)));
-    CK(h, cudaMemcpyAsync(d_idx.p, idx.data(), sizeof(long long) * nrec, cudaMemcpyHostToDevice, h->stream));
-    const HeatLap c = heat_lap_of(h);
-    for (int n = 0; n < nsteps; ++n) {
-        float* in = static_cast<float*>(h->buf[h->cur]);
-        float* out = static_cast<float*>(h->buf[1 - h->cur]);
-        CK(h, launch_heat_kappa_step(in, out, h->mat[0], h->L, h->cfg.D, c, h->stream));
-        h->cur = 1 - h->cur;
-        CK(h, adjoint_sample(out, (const long long*)d_idx.p, nrec, (float*)d_rec.p + (size_t)n * nrec, h->stream));
-    }
-    h->ts += nsteps;
-    CK(h, cudaMemcpyAsync(d_out, d_rec.p, sizeof(float) * (size_t)nrec * nsteps, cudaMemcpyDeviceToHost, h->stream));
-    CK(h, cudaStreamSynchronize(h->stream));
-    return check_status(h);
-}
-
-b2r_status b2r_heat_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const int* rec_xyz,
-                                    const float* d_obs, int ckpt_every, double* misfit,
-                                    double* grad_kappa, float* d_syn)
-{
-    b2r_status st;
-    if ((st = heat_adj_check(h)) != B2R_OK) return st;
-    if (nsteps <= 0 || nrec <= 0 || !rec_xyz || !d_obs) return fail(h, B2R_ERR_ARG, "invalid receivers / steps");
-    const int K = ckpt_every > 0 ? ckpt_every : nsteps;
-    std::vector<long long> idx;
-    if ((st = rec_offsets(h, nrec, rec_xyz, idx)) != B2R_OK) return st;
-    const size_t fb = field_bytes(h);
-    const size_t nseg = (size_t)(nsteps + K - 1) / K;
-    // workspace on the handle: checkpoints, replay slots 1..K, lam, y, FP64 gradient
-    const size_t fba = (fb + 255) & ~(size_t)255;
-    const size_t gba = ((size_t)h->L.bstride * sizeof(double) + 255) & ~(size_t)255;
-    const size_t need = (nseg + (size_t)K + 1 + 2) * fba + gba;
-    if (h->adj_ws_bytes < need) {
-        if (h->adj_ws) cudaFree(h->adj_ws);
-        h->adj_ws = nullptr;
-        h->adj_ws_bytes = 0;
-        if (cudaMalloc(&h->adj_ws, need) != cudaSuccess) {
-            cudaGetLastError();
-            return fail(h, B2R_ERR_OOM, "heat gradient needs %zu bytes of workspace", need);
-        }
-        h->adj_ws_bytes = need;
-    }
-    char* ws = static_cast<char*>(h->adj_ws);
-    std::vector<float*> ckpt(nseg), slot((size_t)K + 1);
-    for (auto& p : ckpt) p = reinterpret_cast<float*>(ws), ws += fba;
-    for (auto& p : slot) p = reinterpret_cast<float*>(ws), ws += fba;
-    float* lam = reinterpret_cast<float*>(ws);
-    ws += fba;
-    float* yb = reinterpret_cast<float*>(ws);
-    ws += fba;
-    double* g = reinterpret_cast<double*>(ws);
-    CK(h, cudaMemsetAsync(lam, 0, fb, h->stream));
-    CK(h, cudaMemsetAsync(yb, 0, fb, h->stream));
-    CK(h, cudaMemsetAsync(g, 0, (size_t)h->L.bstride * sizeof(double), h->stream));
-    // shell cells never change: every replay slot starts as the initial state
-    for (size_t k = 1; k < slot.size(); ++k)
-        CK(h, cudaMemcpyAsync(slot[k], h->buf[h->cur], fb, cudaMemcpyDeviceToDevice, h->stream));
-    DevBuf d_idx, d_rec, d_res;
-    CK(h, cudaMalloc(&d_idx.p, sizeof(long long) * nrec));
-    CK(h, cudaMalloc(&d_rec.p, sizeof(float) * (size_t)nrec * nsteps));
-    CK(h, cudaMalloc(&d_res.p, sizeof(float) * (size_t)nrec * nsteps));
-    CK(h, cudaMemcpyAsync(d_idx.p, idx.data(), sizeof(long long) * nrec, cudaMemcpyHostToDevice, h->stream));
-    const long long* didx = (const long long*)d_idx.p;
-    const HeatLap c = heat_lap_of(h);
-    const int D = h->cfg.D;
-
-    // forward with checkpoints and receiver samples
-    for (int n = 0; n < nsteps; ++n) {
-        float* in = static_cast<float*>(h->buf[h->cur]);
-        float* out = static_cast<float*>(h->buf[1 - h->cur]);
-        if (n % K == 0) CK(h, cudaMemcpyAsync(ckpt[n / K], in, fb, cudaMemcpyDeviceToDevice, h->stream));
-        CK(h, launch_heat_kappa_step(in, out, h->mat[0], h->L, D, c, h->stream));
-        h->cur = 1 - h->cur;
-        CK(h, adjoint_sample(out, didx, nrec, (float*)d_rec.p + (size_t)n * nrec, h->stream));
-    }
-    std::vector<float> syn((size_t)nrec * nsteps), res((size_t)nrec * nsteps);
-    CK(h, cudaMemcpyAsync(syn.data(), d_rec.p, sizeof(float) * syn.size(), cudaMemcpyDeviceToHost, h->stream));
-    CK(h, cudaStreamSynchronize(h->stream));
-    double J = 0.0;
-    for (size_t i = 0; i < syn.size(); ++i) {
-        const double r = (double)syn[i] - (double)d_obs[i];
-        res[i] = (float)r;
-        J += 0.5 * r * r;
-    }
-    if (misfit) *misfit = J;
-    if (d_syn) std::copy(syn.begin(), syn.end(), d_syn);
-    CK(h, cudaMemcpyAsync(d_res.p, res.data(), sizeof(float) * res.size(), cudaMemcpyHostToDevice, h->stream));
-
-    // reverse sweep, segment by segment with recomputation
-    for (long long sgi = (long long)nseg - 1; sgi >= 0; --sgi) {
-        const int n0 = (int)sgi * K;
-        const int n1 = std::min(nsteps, n0 + K);
-        auto u_at = [&](int k) -> float* { return k == 0 ? ckpt[sgi] : slot[(size_t)k]; };
-        for (int n = n0; n < n1; ++n)
-            CK(h, launch_heat_kappa_step(u_at(n - n0), u_at(n - n0 + 1), h->mat[0], h->L, D, c, h->stream));
-        for (int n = n1 - 1; n >= n0; --n) {
-            CK(h, adjoint_inject(lam, didx, nrec, (const float*)d_res.p + (size_t)n * nrec, h->stream));
-            CK(h, launch_heat_adjoint_step(lam, yb, u_at(n - n0), h->mat[0], g, h->L, D, c, h->stream));
-        }
-    }
-    if (grad_kappa) {
-        const size_t ncell = (size_t)h->cfg.env[0] * h->cfg.env[1] * h->cfg.env[2];
-        DevBuf d_out;
-        CK(h, cudaMalloc(&d_out.p, ncell * sizeof(double)));
-        CK(h, adjoint_grad_out(g, nullptr, 0, h->L, (double*)d_out.p, h->stream));
-        CK(h, cudaMemcpyAsync(grad_kappa, d_out.p, ncell * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    }
-    CK(h, cudaStreamSynchronize(h->stream));
-    h->ts = nsteps;
-    return check_status(h);
 }
 
 // ---------------------------------------------------------------- per-block entries
