@@ -46,3 +46,29 @@ def test_upload_fills_halos_like_exchange(b2r, orc):
     ref = orc.split_blocks(dom, blocks, R, periodic=True)
     for k in ref:
         assert np.array_equal(got[k], ref[k]), k
+
+
+@pytest.mark.parametrize("model,env,blocks,R,D,periodic", [
+    (1, (24, 16, 20), (2, 2, 2), 4, 1, False),    # R*D = min(B)/2 = 4
+    (1, (32, 16, 24), (2, 2, 2), 2, 2, True),     # R*D = 4 = 8/2
+    (2, (32, 32, 32), (2, 2, 2), 8, 1, True),     # R = 8 = 16/2
+])
+def test_boundary_updating_at_the_halo_limit(b2r, orc, model, env, blocks, R, D, periodic):
+    """Halos as deep as b2r.cpp:54 allows (R*D = min(B)/2), non-cubic."""
+    bc = b2r.BC_PERIODIC if periodic else b2r.BC_SHELL
+    with b2r.Domain(model, env, blocks=blocks, R=R, D=D, boundary=bc, alpha_dt=0.05) as d:
+        rng = np.random.default_rng(2)
+        if d.dtype == np.uint8:
+            dom = (rng.random(d.domain_shape) < 0.4).astype(np.uint8)
+        else:
+            dom = rng.random(d.domain_shape, dtype=np.float32)
+        d.upload(dom)
+        d.step(R)
+        before = d.download_blocks()
+        d.boundary_updating_direct(R, 0)
+        after = d.download_blocks()
+        d.synchronize()
+    ref = {k: v.copy() for k, v in before.items()}
+    orc.halo_exchange(ref, blocks, d.halo, periodic=periodic)
+    for k in ref:
+        assert np.array_equal(after[k], ref[k]), k
