@@ -22,7 +22,11 @@ def orc():
 
 @pytest.fixture(scope="session")
 def b2r():
-    """The product package; on a machine with a GPU the library must load (no fallback)."""
+    """The product package; on a machine with a GPU the library must load (no
+    fallback).  A fresh checkout compiles it (and the host program) first."""
     import b2r_gb300
+    from b2r_gb300 import build as pkg_build
+    if not os.path.exists(b2r_gb300.LIB_PATH) or not os.path.exists(pkg_build.MAIN):
+        pkg_build.build()
     b2r_gb300.lib()
     return b2r_gb300

@@ -17,25 +17,25 @@ def run(*args, cwd=None):
     return subprocess.run([MAIN, *map(str, args)], capture_output=True, text=True, cwd=cwd, timeout=600)
 
 
-def test_usage_without_four_arguments():
+def test_usage_without_four_arguments(b2r):
     r = run(1, 2, 2)
     assert r.returncode == 1
     assert "please set parameter B2R_B_R, BLOCK_DIM_(X,Y,Z)" in r.stdout
 
 
-def test_env_must_divide_by_blocks():
+def test_env_must_divide_by_blocks(b2r):
     r = run(1, 3, 1, 1, "--env", 64, 64, 64)
     assert r.returncode == 1
     assert "perfectly divisible" in r.stdout
 
 
-def test_halo_must_fit_the_block():
+def test_halo_must_fit_the_block(b2r):
     r = run(40, 1, 1, 1, "--env", 64, 64, 64)
     assert r.returncode == 1
     assert "R*D" in r.stdout
 
 
-def test_unknown_model():
+def test_unknown_model(b2r):
     r = run(1, 1, 1, 1, "--model", "nope")
     assert r.returncode == 1 and "unknown model" in r.stdout
 
@@ -48,7 +48,7 @@ def test_unknown_model():
     ("gol", 4, (2, 2, 2), (64, 64, 64), []),
     ("stag", 2, (2, 2, 1), (64, 64, 32), []),
 ])
-def test_main_runs_every_model(tmp_path, model, R, blocks, env, extra):
+def test_main_runs_every_model(b2r, tmp_path, model, R, blocks, env, extra):
     r = run(R, *blocks, "--model", model, "--env", *env, "--iters", 13, "--snapshot", tmp_path, *extra)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "13 Iterations with B2R_R=%d took" % R in r.stdout
