@@ -64,10 +64,17 @@ def lib():
 
 
 def ref_lib():
-    """The reference's own heat-3D.cpp, or None where it was not built."""
+    """The reference's own heat-3D.cpp (built on first use where its source
+    tree is present), or None."""
     global _ref
     if _ref is None:
         path = os.path.join(HERE, "_ref", "libheat_ref.so")
+        if not os.path.exists(path):
+            from . import build as _b
+            try:
+                path = _b.build_ref() or path
+            except Exception:
+                return None
         if not os.path.exists(path):
             return None
         try:
