@@ -141,20 +141,50 @@ def _check(st, handle=None):
         raise B2RError(st, msg.decode() if msg else "")
 
 
-def _ptr(a):
-    """(pointer, is_device) of a numpy array or a torch tensor."""
+def _ptr(a, need=None, itemsize=None):
+    """(pointer, is_device) of a C-contiguous numpy array or torch tensor.
+
+    need: the bytes the library reads or writes through the pointer; an
+    array of another size, element size or layout raises ValueError before
+    any copy (the library trusts the pointer for that many bytes)."""
     if isinstance(a, np.ndarray):
-        assert a.flags.c_contiguous
-        return C.c_void_p(a.ctypes.data), 0
-    # torch tensor
-    assert a.is_contiguous()
-    return C.c_void_p(a.data_ptr()), 1 if a.is_cuda else 0
+        contig, nbytes, isz = a.flags.c_contiguous, a.nbytes, a.itemsize
+        ptr, dev = a.ctypes.data, 0
+    elif hasattr(a, "data_ptr"):
+        contig, nbytes, isz = a.is_contiguous(), a.numel() * a.element_size(), a.element_size()
+        ptr, dev = a.data_ptr(), 1 if a.is_cuda else 0
+    else:
+        raise TypeError("expected a numpy array or a torch tensor, got %s" % type(a).__name__)
+    if not contig:
+        raise ValueError("the array must be C-contiguous")
+    if itemsize is not None and isz != itemsize:
+        raise ValueError("cells of %d bytes expected, got %d" % (itemsize, isz))
+    if need is not None and nbytes != need:
+        raise ValueError("the array must hold %d bytes, got %d" % (need, nbytes))
+    return C.c_void_p(ptr), dev
 
 
 def _ef(edge_flag):
+    """edge_flag[3] (one of -1, 0, 1 per axis) as the char[3] the library reads."""
     if edge_flag is None:
         return None
-    return bytes([(v + 256) % 256 for v in edge_flag])
+    ef = [int(v) for v in edge_flag]
+    if len(ef) != 3 or any(v not in (-1, 0, 1) for v in ef):
+        raise ValueError("edge_flag holds three values in {-1, 0, 1}, got %r" % (edge_flag,))
+    return bytes([(v + 256) % 256 for v in ef])
+
+
+def _block(h_in, dtype):
+    if not isinstance(h_in, np.ndarray) or h_in.dtype != dtype or h_in.ndim != 3 or not h_in.flags.c_contiguous:
+        raise ValueError("a C-contiguous 3-D %s numpy block (nz, ny, nx) expected" % np.dtype(dtype).name)
+    return h_in.shape
+
+
+def _traces(d_obs, nsteps, nrec):
+    obs = np.ascontiguousarray(d_obs, np.float32)
+    if obs.shape != (nsteps, nrec):
+        raise ValueError("d_obs must be (nsteps, nrec) = (%d, %d), got %s" % (nsteps, nrec, obs.shape))
+    return obs
 
 
 class Domain:
@@ -254,14 +284,23 @@ class Domain:
     def synchronize(self):
         _check(lib().b2r_synchronize(self.h), self.h)
 
+    @property
+    def _domain_bytes(self):
+        return int(np.prod(self.domain_shape)) * self.cell_bytes
+
+    def _field_cell_bytes(self, field):
+        # material and conductivity fields are float32 whatever the model's cells
+        return 4 if FIELDS.get(field, field) >= 16 else self.cell_bytes
+
     def upload(self, arr, field=0):
-        p, dev = _ptr(arr)
+        isz = self._field_cell_bytes(field)
+        p, dev = _ptr(arr, int(np.prod(self.domain_shape)) * isz, isz)
         _check(lib().b2r_upload(self.h, FIELDS.get(field, field), p, dev), self.h)
 
     def download(self, out=None, field=0):
         if out is None:
             out = np.empty(self.domain_shape, self.dtype)
-        p, dev = _ptr(out)
+        p, dev = _ptr(out, self._domain_bytes, self.cell_bytes)
         _check(lib().b2r_download(self.h, FIELDS.get(field, field), p, dev), self.h)
         return out
 
@@ -295,8 +334,8 @@ class Domain:
         _check(lib().b2r_step(self.h, int(nsteps)), self.h)
 
     def run_host(self, host_in, nsteps, host_out, field=0):
-        pi, _ = _ptr(host_in)
-        po, _ = _ptr(host_out)
+        pi, _ = _ptr(host_in, self._domain_bytes, self.cell_bytes)
+        po, _ = _ptr(host_out, self._domain_bytes, self.cell_bytes)
         _check(lib().b2r_run_host(self.h, FIELDS.get(field, field), pi, int(nsteps), po), self.h)
         return host_out
 
@@ -306,13 +345,9 @@ class Domain:
         if len(host_ins) != len(host_outs):
             raise ValueError("one output per input")
         n = len(host_ins)
-        need = int(np.prod(self.domain_shape)) * np.dtype(self.dtype).itemsize
-        for a in list(host_ins) + list(host_outs):
-            nb = a.nbytes if isinstance(a, np.ndarray) else a.numel() * a.element_size()
-            if nb != need:
-                raise ValueError("every buffer holds %d bytes (the domain array), got %d" % (need, nb))
-        pi = (C.c_void_p * max(n, 1))(*[_ptr(a)[0].value for a in host_ins])
-        po = (C.c_void_p * max(n, 1))(*[_ptr(a)[0].value for a in host_outs])
+        need = self._domain_bytes
+        pi = (C.c_void_p * max(n, 1))(*[_ptr(a, need, self.cell_bytes)[0].value for a in host_ins])
+        po = (C.c_void_p * max(n, 1))(*[_ptr(a, need, self.cell_bytes)[0].value for a in host_outs])
         _check(lib().b2r_run_host_batch(self.h, FIELDS.get(field, field), pi, po, n, int(nsteps)), self.h)
         return host_outs
 
@@ -348,7 +383,7 @@ class Domain:
     def heat_misfit_gradient(self, nsteps, rec_xyz, d_obs, ckpt_every=50):
         """(J, g_kappa, d_syn): the gradient is an env-shaped FP64 array (z, y, x)."""
         rec = np.ascontiguousarray(rec_xyz, np.int32).reshape(-1, 3)
-        obs = np.ascontiguousarray(d_obs, np.float32)
+        obs = _traces(d_obs, nsteps, len(rec))
         g = np.empty(tuple(self.cfg.env)[::-1], np.float64)
         J = C.c_double()
         syn = np.empty((nsteps, len(rec)), np.float32)
@@ -362,7 +397,7 @@ class Domain:
     def eqwp_misfit_gradient(self, nsteps, rec_xyz, d_obs, ckpt_every=50):
         """(J, (g_lambda, g_mu, g_rho), d_syn): gradients are env-shaped FP64 arrays (z, y, x)."""
         rec = np.ascontiguousarray(rec_xyz, np.int32).reshape(-1, 3)
-        obs = np.ascontiguousarray(d_obs, np.float32)
+        obs = _traces(d_obs, nsteps, len(rec))
         env = tuple(self.cfg.env)[::-1]
         g = [np.empty(env, np.float64) for _ in range(3)]
         J = C.c_double()
@@ -416,14 +451,19 @@ class Batch:
     def lups(self):
         return int(lib().b2r_batch_lups(self.h))
 
+    def _bytes(self, i):
+        if not 0 <= i < len(self.items):
+            raise IndexError("instance %d of %d" % (i, len(self.items)))
+        return int(np.prod(self.shape(i))) * 4
+
     def upload(self, i, arr):
-        p, dev = _ptr(arr)
+        p, dev = _ptr(arr, self._bytes(i), 4)
         _bcheck(lib().b2r_batch_upload(self.h, i, p, dev, self.stream))
 
     def download(self, i, out=None):
         if out is None:
             out = np.empty(self.shape(i), np.float32)
-        p, dev = _ptr(out)
+        p, dev = _ptr(out, self._bytes(i), 4)
         _bcheck(lib().b2r_batch_download(self.h, i, p, dev, self.stream))
         return out
 
@@ -476,8 +516,7 @@ def kernel_launches():
 def heat_3D_gpu_main(h_in, R, D=1, edge_flag=None, alpha_dt=0.1 * 0.1, dx=1.0, dy=1.0, dz=0.5,
                      stream=None):
     """heat-3D.cu:583 on a host float32 block (nz,ny,nx), in place; returns GPU seconds."""
-    assert h_in.dtype == np.float32 and h_in.flags.c_contiguous
-    nz, ny, nx = h_in.shape
+    nz, ny, nx = _block(h_in, np.float32)
     secs = C.c_double()
     s = getattr(stream, "cuda_stream", stream) or 0
     _check(lib().b2r_heat_3D_gpu_main(h_in.ctypes.data_as(C.c_void_p), R, D, _ef(edge_flag), nx,
@@ -488,8 +527,7 @@ def heat_3D_gpu_main(h_in, R, D=1, edge_flag=None, alpha_dt=0.1 * 0.1, dx=1.0, d
 
 def gol_3D_gpu_main(h_in, R, edge_flag=None, stream=None):
     """gol-3D.cu:119 on a host uint8 block (nz,ny,nx), in place; returns GPU seconds."""
-    assert h_in.dtype == np.uint8 and h_in.flags.c_contiguous
-    nz, ny, nx = h_in.shape
+    nz, ny, nx = _block(h_in, np.uint8)
     secs = C.c_double()
     s = getattr(stream, "cuda_stream", stream) or 0
     _check(lib().b2r_gol_3D_gpu_main(h_in.ctypes.data_as(C.c_void_p), R, _ef(edge_flag), nx, ny,

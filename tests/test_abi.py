@@ -50,3 +50,40 @@ def test_per_block_entry_rejects_bad_args(b2r):
     assert ei.value.status == 1
     with pytest.raises(b2r.B2RError):
         b2r.heat_3D_gpu_main(a, R=1, D=7)
+
+
+def test_wrapper_checks_host_buffers(b2r):
+    """The library trusts a host pointer for a fixed number of bytes, so the
+    Python face refuses arrays of another size, element size or layout
+    before any copy."""
+    import numpy as np
+    from b2r_gb300 import _ptr, _ef, _traces
+    a = np.zeros((4, 5, 6), np.float32)
+    assert _ptr(a, a.nbytes, 4)[1] == 0
+    with pytest.raises(ValueError, match="must hold"):
+        _ptr(a, a.nbytes + 4, 4)
+    with pytest.raises(ValueError, match="cells of 4 bytes"):
+        _ptr(a.astype(np.float64), a.nbytes * 2, 4)
+    with pytest.raises(ValueError, match="C-contiguous"):
+        _ptr(a[:, :, ::2])
+    with pytest.raises(TypeError):
+        _ptr([0.0] * 8)
+    assert _ef((-1, 0, 1)) == bytes([255, 0, 1])
+    for bad in ((0, 0), (0, 2, 0), (1, 1, 1, 1)):
+        with pytest.raises(ValueError, match="edge_flag"):
+            _ef(bad)
+    assert _traces(np.zeros((7, 3)), 7, 3).dtype == np.float32
+    with pytest.raises(ValueError, match="d_obs"):
+        _traces(np.zeros((7, 2)), 7, 3)
+
+
+def test_per_block_entries_check_the_block(b2r):
+    import numpy as np
+    for bad in (np.zeros((6, 6, 6), np.float64), np.zeros((6, 6), np.float32),
+                np.zeros((6, 6, 12), np.float32)[:, :, ::2]):
+        with pytest.raises(ValueError, match="numpy block"):
+            b2r.heat_3D_gpu_main(bad, R=1)
+    with pytest.raises(ValueError, match="numpy block"):
+        b2r.gol_3D_gpu_main(np.zeros((6, 6, 6), np.float32), R=1)
+    with pytest.raises(ValueError, match="edge_flag"):
+        b2r.heat_3D_gpu_main(np.zeros((8, 8, 8), np.float32), R=1, edge_flag=(0, 0))
