@@ -94,6 +94,11 @@ b2r_status b2r_geometry(const b2r_handle* h, int block_n[3], int* halo,
 int64_t b2r_cells(const b2r_handle* h);
 
 /* ---- data movement ------------------------------------------------------ */
+/* A domain array is domain_n[0]*domain_n[1]*domain_n[2] cells (x fastest) of
+ * cell_bytes each (b2r_geometry); the material and conductivity fields are
+ * float32 whatever the model's cells.  The library reads or writes exactly
+ * that many bytes through the pointer: a smaller buffer is the caller's bug,
+ * it cannot be detected here. */
 /* Load a domain array into every block (interiors, halos and shell).
  * src_is_device: 0 = host memory (pinned recommended), 1 = device memory.
  * Resets the time-step counter to 0. */
