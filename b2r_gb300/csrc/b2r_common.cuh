@@ -9,6 +9,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+#include <mutex>
+
 #include "../../include/b2r.h"
 
 namespace b2r {
@@ -150,5 +153,41 @@ void count_launches(long long n);
 // elem_bytes 4 (float) or 1 (uint8).  Returns false on failure.
 bool make_block_tmap(CUtensorMap* map, const void* base, const BlockLayout& L, int elem_bytes,
                      int box_x, int box_y, int box_z);
+
+// One-time launch setup of a kernel: raise its dynamic shared-memory limit
+// and read how many CTAs of `threads` threads fit per SM.  Host threads may
+// launch concurrently: the first caller does the setup under the lock and
+// publishes the result with a release store; a failed setup is not
+// published, so the next call tries again.
+struct KernelSetup {
+    std::mutex mu;
+    std::atomic<int> per_sm{0};   // 0 until the setup succeeded
+    int sms = 1;                  // written before per_sm is published
+};
+
+template <class Kernel>
+cudaError_t kernel_setup(KernelSetup& ks, Kernel kern, int threads, size_t smem, int* per_sm, int* total)
+{
+    int v = ks.per_sm.load(std::memory_order_acquire);
+    if (v == 0) {
+        std::lock_guard<std::mutex> lock(ks.mu);
+        v = ks.per_sm.load(std::memory_order_relaxed);
+        if (v == 0) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            int dev = 0, sms = 0, occ = 0;
+            if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+            if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, smem)) != cudaSuccess)
+                return e;
+            ks.sms = sms > 0 ? sms : 1;
+            v = occ > 0 ? occ : 1;
+            ks.per_sm.store(v, std::memory_order_release);
+        }
+    }
+    if (per_sm) *per_sm = v;
+    if (total) *total = v * ks.sms;
+    return cudaSuccess;
+}
 
 }  // namespace b2r

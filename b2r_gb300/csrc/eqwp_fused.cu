@@ -307,13 +307,8 @@ cudaError_t launch_eqwp_stag_fused(const StressMaps& maps, const float* const* v
                                    float* const* sout, float* const* mat, const BlockLayout& L, int step_i,
                                    int ts, const EqwpStagParams& p, int* status, cudaStream_t st)
 {
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(eqwp_stag_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kFusedSmem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
+    static KernelSetup setup;
+    if (cudaError_t e = kernel_setup(setup, eqwp_stag_fused, kFThreads, kFusedSmem, nullptr, nullptr)) return e;
     FusedArgs A{};
     for (int f = 0; f < 3; ++f) {
         A.vin[f] = vin[f];

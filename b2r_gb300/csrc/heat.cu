@@ -91,20 +91,10 @@ cudaError_t launch_t(const CUtensorMap* tin, float* out, const BlockLayout& L, i
 {
     using Cfg = heatk::Cfg<D, RY, S>;
     auto kern = heat_sweep_kernel<D, RY, S>;
-    static int resident = 0;    // CTAs resident on the whole GPU
-    static int resident_per_sm = 0;
-    if (resident == 0) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)Cfg::SMEM);
-        if (e != cudaSuccess) return e;
-        int dev = 0, sms = 0, occ = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreads, Cfg::SMEM);
-        if (e != cudaSuccess) return e;
-        resident_per_sm = occ > 0 ? occ : 1;
-        resident = resident_per_sm * (sms > 0 ? sms : 1);
-    }
+    static KernelSetup setup;
+    int resident = 0, resident_per_sm = 0;    // CTAs resident per SM / on the whole GPU
+    if (cudaError_t e = kernel_setup(setup, kern, kThreads, Cfg::SMEM, &resident_per_sm, &resident))
+        return e;
     HeatSched sch;
     const int xs_begin = (L.xoff + D) & ~3;
     const int xs_end = L.xoff + L.n[0] - D;              // exclusive

@@ -303,18 +303,9 @@ int heat2_box_h() { return kBoxH; }
 cudaError_t launch_heat_substep2(const CUtensorMap* tin, float* out, const BlockLayout& L, int step_i,
                                  const HeatCoef& c, int* status, cudaStream_t st, int zchunk)
 {
-    static int resident = 0;
-    if (resident == 0) {
-        cudaError_t e = cudaFuncSetAttribute(heat2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kSmem2);
-        if (e != cudaSuccess) return e;
-        int dev = 0, sms = 0, occ = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, heat2_kernel, kT2, kSmem2);
-        if (e != cudaSuccess) return e;
-        resident = (occ > 0 ? occ : 1) * (sms > 0 ? sms : 1);
-    }
+    static KernelSetup setup;
+    int resident = 0;                          // CTAs resident on the whole GPU
+    if (cudaError_t e = kernel_setup(setup, heat2_kernel, kT2, kSmem2, nullptr, &resident)) return e;
     H2Sched sch;
     sch.out0 = (L.xoff + 1) & ~3;                       // aligned float4 holding x = 1
     const int xend = L.xoff + L.n[0] - 1;               // storage x one past the last region cell

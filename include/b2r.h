@@ -19,6 +19,11 @@
  * for B2R_BC_SHELL it carries a fixed shell of `shell` = D cells around the
  * interior ((env+2D) cells per axis, e.g. 130^3 for a 128^3 heat interior);
  * for B2R_BC_PERIODIC it is the bare torus (env cells per axis).
+ *
+ * Threads: distinct handles (and batches) may be driven from distinct host
+ * threads at once, each on its own stream; the library's process-wide state
+ * (kernel setup, autotuner caches, the launch counter) is locked or atomic.
+ * One handle is not to be used by two threads at a time.
  */
 #ifndef B2R_H
 #define B2R_H

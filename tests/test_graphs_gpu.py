@@ -1,4 +1,6 @@
 """Periods replayed from CUDA graphs give the same bits as direct launches."""
+import os
+
 import numpy as np
 import pytest
 
@@ -119,3 +121,57 @@ def test_handles_on_two_host_threads(b2r):
         t.join()
     assert np.array_equal(got_h[0], ref_h[0])
     assert np.array_equal(got_g[0], ref_g[0])
+
+
+FIRST_USE_SCRIPT = r"""
+import sys, threading
+import os
+
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+import b2r_gb300 as b2r
+env = (48, 40, 32)
+cases = [dict(D=1), dict(D=2), dict(D=4), dict(D=1, R=2, blocks=(2, 1, 1)), dict(D=2, R=2, blocks=(1, 2, 1))]
+
+def start(c):
+    rng = np.random.default_rng(c["D"])
+    D = c["D"]
+    dom = np.zeros(tuple(e + 2 * D for e in env[::-1]), np.float32)
+    dom[D:-D, D:-D, D:-D] = rng.random(env[::-1], dtype=np.float32)
+    return dom
+
+def run(c, out, gate=None):
+    with b2r.Domain(b2r.MODEL_HEAT, env, alpha_dt=0.02, **c) as d:
+        d.upload(start(c))
+        d.synchronize()
+        if gate is not None:
+            gate.wait()
+        d.step(7)
+        out.append(d.download())
+        d.synchronize()
+
+gate = threading.Barrier(len(cases))
+outs = [[] for _ in cases]
+ths = [threading.Thread(target=run, args=(c, o, gate)) for c, o in zip(cases, outs)]
+for t in ths: t.start()
+for t in ths: t.join()
+for c, o in zip(cases, outs):
+    ref = []
+    run(c, ref)
+    assert len(o) == 1 and np.array_equal(o[0], ref[0]), c
+print("first-use threads ok")
+"""
+
+
+def test_first_launches_from_many_threads(b2r):
+    """Kernel setup (shared-memory limit, occupancy) happens on a kernel's
+    first launch: five threads of a fresh process making their first heat
+    launches at once (the two-step and one-step sweeps, several radii) get
+    the bits of the same runs made afterwards one at a time."""
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", FIRST_USE_SCRIPT, root], capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "first-use threads ok" in r.stdout
