@@ -587,24 +587,26 @@ b2r_status b2r_upload(b2r_handle* h, int field, const void* src, int src_is_devi
     }
     void* dst;
     if (is_kappa) {
-        CK(h, launch_scatter<float>(static_cast<const float*>(dsrc), h->mat[0], h->L, h->shell, h->stream));
+        CK(h, launch_scatter<float>(static_cast<const float*>(dsrc), h->mat[0], nullptr, h->L, h->shell,
+                                    h->stream));
         return B2R_OK;
     }
-    if (is_mat) dst = h->mat[field - B2R_F_LAMBDA];
-    else if (eq) dst = h->fld[field];
-    else dst = h->buf[h->cur];
+    void* dst2 = nullptr;   // written with the same cells in the same pass
+    if (is_mat) {
+        dst = h->mat[field - B2R_F_LAMBDA];
+    } else if (eq) {
+        dst = h->fld[field];
+        dst2 = h->fld2[field];   // both staggered field sets carry the shell
+    } else {
+        dst = h->buf[h->cur];
+        dst2 = h->buf[1 - h->cur];   // so do both ping-pong buffers (heat-3D.cu:591-592)
+    }
     if (h->cell_bytes == 1)
         CK(h, launch_scatter<uint8_t>(static_cast<const uint8_t*>(dsrc), static_cast<uint8_t*>(dst),
-                                      h->L, h->shell, h->stream));
+                                      static_cast<uint8_t*>(dst2), h->L, h->shell, h->stream));
     else
-        CK(h, launch_scatter<float>(static_cast<const float*>(dsrc), static_cast<float*>(dst), h->L,
-                                    h->shell, h->stream));
-    if (!eq)  // both ping-pong buffers carry the shell (heat-3D.cu:591-592)
-        CK(h, cudaMemcpyAsync(h->buf[1 - h->cur], h->buf[h->cur], field_bytes(h),
-                              cudaMemcpyDeviceToDevice, h->stream));
-    else if (!is_mat && h->fld2[field])   // so do both staggered field sets
-        CK(h, cudaMemcpyAsync(h->fld2[field], h->fld[field], field_bytes(h), cudaMemcpyDeviceToDevice,
-                              h->stream));
+        CK(h, launch_scatter<float>(static_cast<const float*>(dsrc), static_cast<float*>(dst),
+                                    static_cast<float*>(dst2), h->L, h->shell, h->stream));
     h->ts = 0;
     h->halos_fresh = true;
     return B2R_OK;

@@ -119,65 +119,121 @@ __global__ void halo_pack_kernel(FieldSet<T> fs, T* bounce, const BlockLayout L,
 }
 
 // domain array <-> blocks.  shell > 0: non-periodic domain with a `shell`
-// deep fixed shell; periodic: bare torus.
-template <typename T>
-__global__ void scatter_kernel(const T* __restrict__ dom, T* __restrict__ blocks,
-                               const BlockLayout L, int shell)
+// deep fixed shell; periodic: bare torus.  One warp per row of cells: the
+// row's source (scatter) or owner blocks (gather) are found once per row,
+// and the lanes walk x with kRowUnroll loads in flight before their stores,
+// so the copy runs at HBM speed without per-cell index divisions.
+constexpr int kRowWarps = 8;
+constexpr int kRowUnroll = 4;
+
+// a global coordinate at most one period outside [0, e) (the halo depth
+// never exceeds a block), wrapped onto the torus
+__device__ __forceinline__ int wrap_once(int g, int e)
 {
-    const int dn0 = L.nb[0] * L.B[0] + 2 * shell, dn1 = L.nb[1] * L.B[1] + 2 * shell;
-    const int dn2 = L.nb[2] * L.B[2] + 2 * shell;
-    const long long rowlen = L.n[0];
-    const long long total = rowlen * L.n[1] * L.n[2] * L.nblk;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-         e += (long long)gridDim.x * blockDim.x) {
-        const int x = (int)(e % rowlen);
-        long long r = e / rowlen;
+    return g < 0 ? g + e : (g >= e ? g - e : g);
+}
+
+// blocks2 (may be null): a second set of blocks that gets the same cells
+template <typename T>
+__global__ void __launch_bounds__(kRowWarps * 32)
+scatter_kernel(const T* __restrict__ dom, T* __restrict__ blocks, T* __restrict__ blocks2,
+               const BlockLayout L, int shell)
+{
+    const int lane = threadIdx.x & 31;
+    const int e0 = L.nb[0] * L.B[0], e1 = L.nb[1] * L.B[1], e2 = L.nb[2] * L.B[2];
+    const int dn0 = e0 + 2 * shell, dn1 = e1 + 2 * shell;
+    const long long nrows = (long long)L.n[1] * L.n[2] * L.nblk;
+    for (long long r = (long long)blockIdx.x * kRowWarps + (threadIdx.x >> 5); r < nrows;
+         r += (long long)gridDim.x * kRowWarps) {
         const int y = (int)(r % L.n[1]);
-        r /= L.n[1];
-        const int z = (int)(r % L.n[2]);
-        const int blk = (int)(r / L.n[2]);
+        const long long rz = r / L.n[1];
+        const int z = (int)(rz % L.n[2]);
+        const int blk = (int)(rz / L.n[2]);
         const int b0 = blk % L.nb[0], b1 = (blk / L.nb[0]) % L.nb[1], b2 = blk / (L.nb[0] * L.nb[1]);
-        int g0 = b0 * L.B[0] + x - L.H, g1 = b1 * L.B[1] + y - L.H, g2 = b2 * L.B[2] + z - L.H;
-        T v = T(0);
+        const int gx0 = b0 * L.B[0] - L.H;          // global x of block cell x = 0
+        int g1 = b1 * L.B[1] + y - L.H, g2 = b2 * L.B[2] + z - L.H;
+        // domain row, indexed by the global x (from -shell with a shell);
+        // no row: the block row lies outside the domain and its shell (zeros)
+        long long row = -1;
         if (L.periodic) {
-            const int e0 = L.nb[0] * L.B[0], e1 = L.nb[1] * L.B[1], e2 = L.nb[2] * L.B[2];
-            g0 = ((g0 % e0) + e0) % e0;
-            g1 = ((g1 % e1) + e1) % e1;
-            g2 = ((g2 % e2) + e2) % e2;
-            v = dom[((long long)g2 * e1 + g1) * e0 + g0];
-        } else {
-            g0 += shell; g1 += shell; g2 += shell;
-            if (g0 >= 0 && g0 < dn0 && g1 >= 0 && g1 < dn1 && g2 >= 0 && g2 < dn2)
-                v = dom[((long long)g2 * dn1 + g1) * dn0 + g0];
+            g1 = wrap_once(g1, e1);
+            g2 = wrap_once(g2, e2);
+            if ((unsigned)g1 < (unsigned)e1 && (unsigned)g2 < (unsigned)e2)
+                row = ((long long)g2 * e1 + g1) * e0;
+        } else if (g1 >= -shell && g1 < e1 + shell && g2 >= -shell && g2 < e2 + shell) {
+            row = ((long long)(g2 + shell) * dn1 + (g1 + shell)) * dn0 + shell;
         }
-        blocks[blk * L.bstride + (long long)z * L.plane + (long long)y * L.P + L.xoff + x] = v;
+        const long long o = blk * L.bstride + (long long)z * L.plane + (long long)y * L.P + L.xoff;
+        for (int xb = 0; xb < L.n[0]; xb += 32 * kRowUnroll) {
+            T v[kRowUnroll];
+#pragma unroll
+            for (int u = 0; u < kRowUnroll; ++u) {
+                const int x = xb + u * 32 + lane;
+                int g0 = gx0 + x;
+                bool in;
+                if (L.periodic) {
+                    g0 = wrap_once(g0, e0);
+                    in = (unsigned)g0 < (unsigned)e0;
+                } else {
+                    in = g0 >= -shell && g0 < e0 + shell;
+                }
+                v[u] = (row >= 0 && x < L.n[0] && in) ? dom[row + g0] : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < kRowUnroll; ++u) {
+                const int x = xb + u * 32 + lane;
+                if (x < L.n[0]) {
+                    blocks[o + x] = v[u];
+                    if (blocks2) blocks2[o + x] = v[u];
+                }
+            }
+        }
     }
 }
 
-template <typename T>
-__global__ void gather_kernel(T* __restrict__ dom, const T* __restrict__ blocks,
-                              const BlockLayout L, int shell)
+// owner block of global coordinate g along an axis (the shell belongs to
+// the edge blocks' halos)
+__device__ __forceinline__ int owner_of(int g, int B, int nb)
 {
+    int b = g >= 0 ? g / B : 0;
+    return b >= nb ? nb - 1 : b;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRowWarps * 32)
+gather_kernel(T* __restrict__ dom, const T* __restrict__ blocks, const BlockLayout L, int shell)
+{
+    const int lane = threadIdx.x & 31;
     const int dn0 = L.nb[0] * L.B[0] + 2 * shell, dn1 = L.nb[1] * L.B[1] + 2 * shell;
     const int dn2 = L.nb[2] * L.B[2] + 2 * shell;
-    const long long total = (long long)dn0 * dn1 * dn2;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-         e += (long long)gridDim.x * blockDim.x) {
-        const int d0 = (int)(e % dn0);
-        long long r = e / dn0;
-        const int d1 = (int)(r % dn1);
-        const int d2 = (int)(r / dn1);
-        const int g[3] = {d0 - shell, d1 - shell, d2 - shell};
-        int b[3], l[3];
-        for (int a = 0; a < 3; ++a) {
-            int bb = g[a] >= 0 ? g[a] / L.B[a] : -1;
-            bb = bb < 0 ? 0 : (bb >= L.nb[a] ? L.nb[a] - 1 : bb);
-            b[a] = bb;
-            l[a] = g[a] - bb * L.B[a] + L.H;
+    const long long nrows = (long long)dn1 * dn2;
+    for (long long r = (long long)blockIdx.x * kRowWarps + (threadIdx.x >> 5); r < nrows;
+         r += (long long)gridDim.x * kRowWarps) {
+        const int g1 = (int)(r % dn1) - shell, g2 = (int)(r / dn1) - shell;
+        const int bb1 = owner_of(g1, L.B[1], L.nb[1]), bb2 = owner_of(g2, L.B[2], L.nb[2]);
+        const int l1 = g1 - bb1 * L.B[1] + L.H, l2 = g2 - bb2 * L.B[2] + L.H;
+        const long long drow = r * dn0;
+        const long long o = (long long)l2 * L.plane + (long long)l1 * L.P + L.xoff;
+        const int blk_yz = L.nb[0] * (bb1 + L.nb[1] * bb2);
+        // the row's cells [lo, hi) are owned by x-block bb0 (block cell x = d0 - shell - bb0*B + H)
+        for (int bb0 = 0; bb0 < L.nb[0]; ++bb0) {
+            const int lo = bb0 == 0 ? 0 : shell + bb0 * L.B[0];
+            const int hi = bb0 == L.nb[0] - 1 ? dn0 : shell + (bb0 + 1) * L.B[0];
+            const long long srow = (long long)(blk_yz + bb0) * L.bstride + o + (L.H - shell - bb0 * L.B[0]);
+            for (int xb = lo; xb < hi; xb += 32 * kRowUnroll) {
+                T v[kRowUnroll];
+#pragma unroll
+                for (int u = 0; u < kRowUnroll; ++u) {
+                    const int d0 = xb + u * 32 + lane;
+                    v[u] = d0 < hi ? blocks[srow + d0] : T(0);
+                }
+#pragma unroll
+                for (int u = 0; u < kRowUnroll; ++u) {
+                    const int d0 = xb + u * 32 + lane;
+                    if (d0 < hi) dom[drow + d0] = v[u];
+                }
+            }
         }
-        const int blk = b[0] + L.nb[0] * (b[1] + L.nb[1] * b[2]);
-        dom[e] = blocks[blk * L.bstride + (long long)l[2] * L.plane + (long long)l[1] * L.P +
-                        L.xoff + l[0]];
     }
 }
 
@@ -353,10 +409,12 @@ size_t halo_bounce_elems(const BlockLayout& L)
 }
 
 template <typename T>
-cudaError_t launch_scatter(const T* dom, T* blocks, const BlockLayout& L, int shell, cudaStream_t st)
+cudaError_t launch_scatter(const T* dom, T* blocks, T* blocks2, const BlockLayout& L, int shell,
+                           cudaStream_t st)
 {
-    const long long total = (long long)L.n[0] * L.n[1] * L.n[2] * L.nblk;
-    scatter_kernel<T><<<grid_for(total, 256), 256, 0, st>>>(dom, blocks, L, shell);
+    const long long rows = (long long)L.n[1] * L.n[2] * L.nblk;
+    scatter_kernel<T><<<grid_for(rows * 32, kRowWarps * 32), kRowWarps * 32, 0, st>>>(dom, blocks, blocks2, L,
+                                                                                      shell);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -364,9 +422,8 @@ cudaError_t launch_scatter(const T* dom, T* blocks, const BlockLayout& L, int sh
 template <typename T>
 cudaError_t launch_gather(T* dom, const T* blocks, const BlockLayout& L, int shell, cudaStream_t st)
 {
-    const long long total = (long long)(L.nb[0] * L.B[0] + 2 * shell) *
-                            (L.nb[1] * L.B[1] + 2 * shell) * (L.nb[2] * L.B[2] + 2 * shell);
-    gather_kernel<T><<<grid_for(total, 256), 256, 0, st>>>(dom, blocks, L, shell);
+    const long long rows = (long long)(L.nb[1] * L.B[1] + 2 * shell) * (L.nb[2] * L.B[2] + 2 * shell);
+    gather_kernel<T><<<grid_for(rows * 32, kRowWarps * 32), kRowWarps * 32, 0, st>>>(dom, blocks, L, shell);
     count_launches(1);
     return cudaGetLastError();
 }
@@ -378,8 +435,8 @@ template cudaError_t launch_halo_exchange<uint8_t>(const FieldSet<uint8_t>&, int
 template cudaError_t launch_halo_gather<float>(const FieldSet<float>&, int, const BlockLayout&, cudaStream_t);
 template cudaError_t launch_halo_gather<uint8_t>(const FieldSet<uint8_t>&, int, const BlockLayout&,
                                                  cudaStream_t);
-template cudaError_t launch_scatter<float>(const float*, float*, const BlockLayout&, int, cudaStream_t);
-template cudaError_t launch_scatter<uint8_t>(const uint8_t*, uint8_t*, const BlockLayout&, int,
+template cudaError_t launch_scatter<float>(const float*, float*, float*, const BlockLayout&, int, cudaStream_t);
+template cudaError_t launch_scatter<uint8_t>(const uint8_t*, uint8_t*, uint8_t*, const BlockLayout&, int,
                                              cudaStream_t);
 template cudaError_t launch_gather<float>(float*, const float*, const BlockLayout&, int, cudaStream_t);
 template cudaError_t launch_gather<uint8_t>(uint8_t*, const uint8_t*, const BlockLayout&, int,

@@ -24,9 +24,10 @@ template <typename T>
 cudaError_t launch_halo_gather(const FieldSet<T>& fs, int nfields, const BlockLayout& L, cudaStream_t st);
 
 // Dense domain array (shell > 0: with a fixed shell of that depth; periodic
-// layouts: bare torus) -> every padded block, halos included.
+// layouts: bare torus) -> every padded block, halos included; blocks2, when
+// not null, is a second set of blocks written with the same cells.
 template <typename T>
-cudaError_t launch_scatter(const T* dom, T* blocks, const BlockLayout& L, int shell,
+cudaError_t launch_scatter(const T* dom, T* blocks, T* blocks2, const BlockLayout& L, int shell,
                            cudaStream_t st);
 // Blocks -> dense domain array (interiors from their owners, shell from the
 // edge blocks' halos, which are never updated).
