@@ -339,13 +339,21 @@ class Domain:
         _check(lib().b2r_run_host(self.h, FIELDS.get(field, field), pi, int(nsteps), po), self.h)
         return host_out
 
+    @property
+    def nfields(self):
+        """Fields of one problem: the wavefield components of the elastic
+        wave (ten with the displacement for the reference model), else one."""
+        return {MODEL_EQWP_REF: 10, MODEL_EQWP_STAG: 9}.get(self.cfg.model, 1)
+
     def run_host_batch(self, host_ins, nsteps, host_outs, field=0):
         """run_host over several independent inputs, the copies of the next
-        input and the previous result overlapping the stepping."""
+        input and the previous result overlapping the stepping.  Each input
+        and output holds the model's `nfields` domain arrays back to back
+        (shape (nfields, nz, ny, nx) for the elastic wave)."""
         if len(host_ins) != len(host_outs):
             raise ValueError("one output per input")
         n = len(host_ins)
-        need = self._domain_bytes
+        need = self._domain_bytes * self.nfields
         pi = (C.c_void_p * max(n, 1))(*[_ptr(a, need, self.cell_bytes)[0].value for a in host_ins])
         po = (C.c_void_p * max(n, 1))(*[_ptr(a, need, self.cell_bytes)[0].value for a in host_outs])
         _check(lib().b2r_run_host_batch(self.h, FIELDS.get(field, field), pi, po, n, int(nsteps)), self.h)

@@ -726,11 +726,14 @@ b2r_status b2r_run_host_batch(b2r_handle* h, int field, const void* const* host_
                               int count, int nsteps)
 {
     if (!h || !host_in || !host_out || count < 0) return fail(h, B2R_ERR_ARG, "invalid argument");
-    if (h->nfld > 0) return fail(h, B2R_ERR_ARG, "pipelined host runs cover the heat and Game-of-Life models");
     if (field != 0) return fail(h, B2R_ERR_ARG, "invalid field id %d", field);
     for (int i = 0; i < count; ++i)
         if (!host_in[i] || !host_out[i]) return fail(h, B2R_ERR_ARG, "null buffer for problem %d", i);
-    const size_t bytes = domain_cells(h) * h->cell_bytes;
+    // a problem is every field of the model, back to back in field-id order
+    // (the elastic wave's wavefield components; one field for heat and GoL)
+    const int nf = h->nfld > 0 ? h->nfld : 1;
+    const size_t fbytes = domain_cells(h) * h->cell_bytes;
+    const size_t bytes = fbytes * nf;
     if (h->pipe_bytes < bytes) {
         for (void*& p : h->pipe) {
             if (p) cudaFree(p);
@@ -771,11 +774,13 @@ b2r_status b2r_run_host_batch(b2r_handle* h, int field, const void* const* host_
             CK(h, cudaEventRecord(h->ev[IN_READY][k1], h->cin));
         }
         CK(h, cudaStreamWaitEvent(h->stream, h->ev[IN_READY][k], 0));
-        if ((st = b2r_upload(h, field, in[k], 1)) != B2R_OK) return st;
+        for (int f = 0; f < nf; ++f)
+            if ((st = b2r_upload(h, f, static_cast<const char*>(in[k]) + f * fbytes, 1)) != B2R_OK) return st;
         CK(h, cudaEventRecord(h->ev[IN_FREE][k], h->stream));
         if ((st = b2r_step(h, nsteps)) != B2R_OK) return st;
         CK(h, cudaStreamWaitEvent(h->stream, h->ev[OUT_FREE][k], 0));   // result of problem i-2 copied out
-        if ((st = b2r_download(h, field, out[k], 1)) != B2R_OK) return st;
+        for (int f = 0; f < nf; ++f)
+            if ((st = b2r_download(h, f, static_cast<char*>(out[k]) + f * fbytes, 1)) != B2R_OK) return st;
         CK(h, cudaEventRecord(h->ev[OUT_READY][k], h->stream));
         CK(h, cudaStreamWaitEvent(h->cout, h->ev[OUT_READY][k], 0));
         CK(h, cudaMemcpyAsync(host_out[i], out[k], bytes, cudaMemcpyDeviceToHost, h->cout));

@@ -165,11 +165,15 @@ b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* bes
 /* Upload, b2r_step, download: the whole job through host buffers. */
 b2r_status b2r_run_host(b2r_handle* h, int field, const void* host_in, int nsteps,
                         void* host_out);
-/* b2r_run_host over count independent inputs of the same shape (heat or
- * Game of Life, field 0): problem i is uploaded from host_in[i], stepped
- * nsteps times and downloaded to host_out[i], with the copy of the next input
- * and of the previous result overlapping the stepping (two copy streams, two
- * device buffers per direction).  Pinned host buffers make the copies
+/* b2r_run_host over count independent inputs of the same shape (field must
+ * be 0): problem i is uploaded from host_in[i], stepped nsteps times and
+ * downloaded to host_out[i], with the copy of the next input and of the
+ * previous result overlapping the stepping (two copy streams, two device
+ * buffers per direction).  A problem is every field of the model back to
+ * back in field-id order: one domain array for heat and Game of Life; the
+ * nine wavefield components (B2R_F_VX .. B2R_F_SZZ) of the staggered elastic
+ * wave, and those and the displacement (ten) of the reference model, whose
+ * material stays resident.  Pinned host buffers make the copies
  * asynchronous.  Returns when every result is on the host. */
 b2r_status b2r_run_host_batch(b2r_handle* h, int field, const void* const* host_in, void* const* host_out,
                               int count, int nsteps);
