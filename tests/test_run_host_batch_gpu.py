@@ -1,6 +1,7 @@
 """Pipelined host runs (b2r_run_host_batch): the same bits as one
-b2r_run_host per input, for heat and Game of Life, with the copies of the
-next input and the previous result overlapping the stepping."""
+b2r_run_host per input (heat, Game of Life) or as per-field uploads and
+downloads (the elastic wave, whose problem is the whole wavefield), with the
+copies of the next input and the previous result overlapping the stepping."""
 import numpy as np
 import pytest
 
