@@ -109,6 +109,36 @@ struct DevBuf {
     }
 };
 
+// Two timing events, destroyed on every return path.
+struct EventPair {
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    EventPair() = default;
+    EventPair(const EventPair&) = delete;
+    EventPair& operator=(const EventPair&) = delete;
+    cudaError_t create()
+    {
+        cudaError_t e = cudaEventCreate(&e0);
+        if (e != cudaSuccess) {
+            e0 = nullptr;
+            return e;
+        }
+        e = cudaEventCreate(&e1);
+        if (e != cudaSuccess) e1 = nullptr;
+        return e;
+    }
+    // seconds between the two recorded events (0 when unavailable)
+    double seconds() const
+    {
+        float ms = 0.f;
+        return cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess ? ms / 1000.0 : 0.0;
+    }
+    ~EventPair()
+    {
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    }
+};
+
 inline int roundup(int v, int m) { return (v + m - 1) / m * m; }
 
 extern std::mutex g_tune_mu;

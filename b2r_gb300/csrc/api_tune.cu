@@ -156,14 +156,19 @@ static b2r_status autotune_knobs(b2r_handle* h, int trial_steps, int best[3], do
     h->cur = save_cur;
     h->ts = save_ts;
     h->halos_fresh = save_fresh;
+    // restore every field even after a failed trial; report the first failure
+    cudaError_t rerr = cudaSuccess;
     for (int f = 0; f < nsave; ++f) {
         void* dst = eq ? (void*)h->fld[f] : h->buf[h->cur];
-        cudaMemcpyAsync(dst, save[(size_t)f], fb, cudaMemcpyDeviceToDevice, h->stream);
+        const cudaError_t e = cudaMemcpyAsync(dst, save[(size_t)f], fb, cudaMemcpyDeviceToDevice, h->stream);
+        if (rerr == cudaSuccess) rerr = e;
     }
-    cudaStreamSynchronize(h->stream);
+    const cudaError_t se = cudaStreamSynchronize(h->stream);
+    if (rerr == cudaSuccess) rerr = se;
     apply_knobs(h, st == B2R_OK ? bestK : cur);
     drop_graphs(h);
     if (st != B2R_OK) return st;
+    CK(h, rerr);
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         g_knob_cache[key_of(h)] = bestK;
@@ -221,26 +226,25 @@ b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* bes
         for (int zc : zchunks)
             for (int cp : persist)
                 if (zc <= h->L.n[2]) cands.push_back({1, 0, zc, cp, pdl});
-    for (const Cand& cd : cands)
-            {
-                if (st != B2R_OK) break;
-                h->tune.tblock = cd.tb;
-                h->tune.zchunk2 = cd.zc2;
-                h->tune.zchunk = cd.zc;
-                h->tune.ctas_per_sm = cd.cp;
-                h->tune.pdl = cd.pdl;
-                if ((st = b2r_step(h, 1)) != B2R_OK) break;       // warm
-                cudaEventRecord(e0, h->stream);
-                if ((st = b2r_step(h, trial_steps)) != B2R_OK) break;
-                cudaEventRecord(e1, h->stream);
-                cudaEventSynchronize(e1);
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, e0, e1);
-                if (ms < bestMs) {
-                    bestMs = ms;
-                    bestT = h->tune;
-                }
-            }
+    for (const Cand& cd : cands) {
+        if (st != B2R_OK) break;
+        h->tune.tblock = cd.tb;
+        h->tune.zchunk2 = cd.zc2;
+        h->tune.zchunk = cd.zc;
+        h->tune.ctas_per_sm = cd.cp;
+        h->tune.pdl = cd.pdl;
+        if ((st = b2r_step(h, 1)) != B2R_OK) break;       // warm
+        cudaEventRecord(e0, h->stream);
+        if ((st = b2r_step(h, trial_steps)) != B2R_OK) break;
+        cudaEventRecord(e1, h->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < bestMs) {
+            bestMs = ms;
+            bestT = h->tune;
+        }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     h->tune = bestT;
@@ -248,9 +252,12 @@ b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* bes
     h->ts = save_ts;
     h->halos_fresh = save_fresh;
     h->graphs = save_graphs;
-    cudaMemcpyAsync(h->buf[h->cur], save, fb, cudaMemcpyDeviceToDevice, h->stream);
-    cudaStreamSynchronize(h->stream);
+    // restore the field even after a failed trial; report the first failure
+    cudaError_t rerr = cudaMemcpyAsync(h->buf[h->cur], save, fb, cudaMemcpyDeviceToDevice, h->stream);
+    const cudaError_t se = cudaStreamSynchronize(h->stream);
+    if (rerr == cudaSuccess) rerr = se;
     if (st != B2R_OK) return st;
+    CK(h, rerr);
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         g_tune_cache[key_of(h)] = bestT;

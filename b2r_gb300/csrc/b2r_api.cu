@@ -758,7 +758,8 @@ b2r_status b2r_run_host_batch(b2r_handle* h, int field, const void* const* host_
     CK(h, cudaStreamSynchronize(h->cout));
     for (auto& e2 : h->ev)
         for (cudaEvent_t& e : e2) {
-            cudaEventDestroy(e);
+            if (e) cudaEventDestroy(e);
+            e = nullptr;
             CK(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         }
     if (count > 0) {
@@ -879,10 +880,11 @@ b2r_status b2r_heat_3D_gpu_main(float* h_in, int R, int D, const char* edge_flag
     cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
     const size_t fb = (size_t)L.bstride * sizeof(float);
     Scratch s;
-    int* d_status = nullptr;
+    DevBuf status_buf;
     CK(nullptr, cudaMalloc(&s.p[0], fb));
     CK(nullptr, cudaMalloc(&s.p[1], fb));
-    CK(nullptr, cudaMalloc(&d_status, sizeof(int)));
+    CK(nullptr, cudaMalloc(&status_buf.p, sizeof(int)));
+    int* d_status = static_cast<int*>(status_buf.p);
     CK(nullptr, cudaMemsetAsync(d_status, 0, sizeof(int), st));
     // host block (dense rows of Ngx) -> pitched device rows (heat-3D.cu:590-592)
     for (int b = 0; b < 2; ++b)
@@ -891,25 +893,19 @@ b2r_status b2r_heat_3D_gpu_main(float* h_in, int R, int D, const char* edge_flag
                                       cudaMemcpyHostToDevice, st));
     CUtensorMap tm[2];
     for (int b = 0; b < 2; ++b)
-        if (!make_block_tmap(&tm[b], s.p[b], L, 4, heat_box_w(), heat_box_h(D), 1)) {
-            cudaFree(d_status);
+        if (!make_block_tmap(&tm[b], s.p[b], L, 4, heat_box_w(), heat_box_h(D), 1))
             return fail(nullptr, B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed");
-        }
     const HeatCoef hc = heat_coef(D, alpha_dt, dx, dy, dz);
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    cudaEventRecord(e0, st);
+    EventPair ev;
+    CK(nullptr, ev.create());
+    CK(nullptr, cudaEventRecord(ev.e0, st));
     int cur = 0;
     for (int i = 0; i < R; ++i) {   // heat-3D.cu:602-628
         cudaError_t e = launch_heat_substep(&tm[cur], (float*)s.p[1 - cur], L, D, i, hc, d_status, st);
-        if (e != cudaSuccess) {
-            cudaFree(d_status);
-            return fail(nullptr, B2R_ERR_CUDA, "heat launch: %s", cudaGetErrorString(e));
-        }
+        if (e != cudaSuccess) return fail(nullptr, B2R_ERR_CUDA, "heat launch: %s", cudaGetErrorString(e));
         cur = 1 - cur;
     }
-    cudaEventRecord(e1, st);
+    CK(nullptr, cudaEventRecord(ev.e1, st));
     // planes [R*D, Ngz-R*D) back to the host (heat-3D.cu:633-635)
     const int zc = Ngz - 2 * H;
     CK(nullptr, cudaMemcpy2DAsync(h_in + (size_t)H * Ngx * Ngy, Ngx * sizeof(float),
@@ -918,12 +914,7 @@ b2r_status b2r_heat_3D_gpu_main(float* h_in, int R, int D, const char* edge_flag
     int dev_st = 0;
     CK(nullptr, cudaMemcpyAsync(&dev_st, d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(nullptr, cudaStreamSynchronize(st));
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaFree(d_status);
-    if (gpu_seconds) *gpu_seconds = ms / 1000.0;
+    if (gpu_seconds) *gpu_seconds = ev.seconds();
     if (dev_st != DEV_OK) return fail(nullptr, B2R_ERR_TIMEOUT, "device wait gave up (code %d)", dev_st);
     return B2R_OK;
 }
@@ -951,26 +942,21 @@ b2r_status b2r_gol_3D_gpu_main(uint8_t* h_in, int R, const char* edge_flag, int 
     for (int b = 0; b < 2; ++b)   // gol-3D.cu:126-129
         CK(nullptr, cudaMemcpy2DAsync((uint8_t*)s.p[b] + L.xoff, L.P, h_in, Ngx, Ngx,
                                       (size_t)Ngy * Ngz, cudaMemcpyHostToDevice, st));
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    cudaEventRecord(e0, st);
+    EventPair ev;
+    CK(nullptr, ev.create());
+    CK(nullptr, cudaEventRecord(ev.e0, st));
     int cur = 0;
     for (int i = 0; i < R; ++i) {  // gol-3D.cu:138-145
         cudaError_t e = launch_gol_substep((const uint8_t*)s.p[cur], (uint8_t*)s.p[1 - cur], L, i, st);
         if (e != cudaSuccess) return fail(nullptr, B2R_ERR_CUDA, "gol launch: %s", cudaGetErrorString(e));
         cur = 1 - cur;
     }
-    cudaEventRecord(e1, st);
+    CK(nullptr, cudaEventRecord(ev.e1, st));
     // whole block back (gol-3D.cu:149)
     CK(nullptr, cudaMemcpy2DAsync(h_in, Ngx, (uint8_t*)s.p[cur] + L.xoff, L.P, Ngx, (size_t)Ngy * Ngz,
                                   cudaMemcpyDeviceToHost, st));
     CK(nullptr, cudaStreamSynchronize(st));
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if (gpu_seconds) *gpu_seconds = ms / 1000.0;
+    if (gpu_seconds) *gpu_seconds = ev.seconds();
     return B2R_OK;
 }
 

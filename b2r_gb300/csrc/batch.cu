@@ -600,7 +600,17 @@ b2r_status b2r_batch_autotune(b2r_batch* b, void* stream, int* best_zchunk, doub
     if (!b) return bfail(B2R_ERR_ARG, "null batch");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // the runs overwrite the instance buffers: keep buffer 0 of every instance
-    std::vector<float*> save(b->n, nullptr);
+    // (freed on every return path)
+    struct SaveBufs {
+        std::vector<float*> p;
+        ~SaveBufs()
+        {
+            for (float* q : p)
+                if (q) cudaFree(q);
+        }
+    } saved;
+    saved.p.assign(b->n, nullptr);
+    std::vector<float*>& save = saved.p;
     for (int k = 0; k < b->n; ++k) {
         const size_t fb = (size_t)b->host[k].L.bstride * sizeof(float);
         BCK(cudaMalloc(&save[k], fb), "autotune save");
@@ -634,13 +644,18 @@ b2r_status b2r_batch_autotune(b2r_batch* b, void* stream, int* best_zchunk, doub
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    // restore every instance even after a failed trial; report the first failure
+    cudaError_t rerr = cudaSuccess;
     for (int k = 0; k < b->n; ++k) {
-        cudaMemcpyAsync(b->host[k].buf[0], save[k], (size_t)b->host[k].L.bstride * sizeof(float),
-                        cudaMemcpyDeviceToDevice, st);
+        const cudaError_t e = cudaMemcpyAsync(b->host[k].buf[0], save[k],
+                                              (size_t)b->host[k].L.bstride * sizeof(float),
+                                              cudaMemcpyDeviceToDevice, st);
+        if (rerr == cudaSuccess) rerr = e;
     }
-    cudaStreamSynchronize(st);
-    for (float* p : save) cudaFree(p);
+    const cudaError_t se = cudaStreamSynchronize(st);
+    if (rerr == cudaSuccess) rerr = se;
     if (s != B2R_OK) return s;
+    BCK(rerr, "restoring the instances after the trials");
     if (best_zchunk) *best_zchunk = bestz;
     if (best_ms) *best_ms = best;
     if ((s = apply_shape(b, bests)) != B2R_OK) return s;
