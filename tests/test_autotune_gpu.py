@@ -1,4 +1,6 @@
-"""The heat autotuner: picks a launch schedule, keeps the state, changes no bits."""
+"""The autotuners (heat schedules; Game-of-Life and staggered elastic-wave
+kernel choices): each picks a launch schedule, keeps the state and changes
+no bits."""
 import numpy as np
 import pytest
 

@@ -1,4 +1,6 @@
-"""Periods replayed from CUDA graphs give the same bits as direct launches."""
+"""Periods replayed from CUDA graphs give the same bits as direct launches;
+handles driven from several host threads at once (first launches included)
+give the bits of the same runs one after the other."""
 import os
 
 import numpy as np
