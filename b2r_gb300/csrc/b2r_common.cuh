@@ -154,39 +154,70 @@ void count_launches(long long n);
 bool make_block_tmap(CUtensorMap* map, const void* base, const BlockLayout& L, int elem_bytes,
                      int box_x, int box_y, int box_z);
 
-// One-time launch setup of a kernel: raise its dynamic shared-memory limit
-// and read how many CTAs of `threads` threads fit per SM.  Host threads may
-// launch concurrently: the first caller does the setup under the lock and
-// publishes the result with a release store; a failed setup is not
-// published, so the next call tries again.
+// One-time launch setup of a kernel on each device: raise its dynamic
+// shared-memory limit and read how many CTAs of `threads` threads fit per SM.
+// The function attribute belongs to the device that is current when it is
+// set, so the setup is kept per device (device ordinals below
+// kSetupDevices).  Host threads may launch concurrently: the first caller on
+// a device does the setup under the lock and publishes the result with a
+// release store; a failed setup is not published, so the next call tries
+// again.
+constexpr int kSetupDevices = 64;
 struct KernelSetup {
     std::mutex mu;
-    std::atomic<int> per_sm{0};   // 0 until the setup succeeded
-    int sms = 1;                  // written before per_sm is published
+    std::atomic<int> per_sm[kSetupDevices] = {};   // 0 until the setup on that device succeeded
+    int sms[kSetupDevices] = {};                   // written before per_sm[dev] is published
 };
 
 template <class Kernel>
 cudaError_t kernel_setup(KernelSetup& ks, Kernel kern, int threads, size_t smem, int* per_sm, int* total)
 {
-    int v = ks.per_sm.load(std::memory_order_acquire);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kSetupDevices) return cudaErrorInvalidDevice;
+    int v = ks.per_sm[dev].load(std::memory_order_acquire);
     if (v == 0) {
         std::lock_guard<std::mutex> lock(ks.mu);
-        v = ks.per_sm.load(std::memory_order_relaxed);
+        v = ks.per_sm[dev].load(std::memory_order_relaxed);
         if (v == 0) {
-            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
-            int dev = 0, sms = 0, occ = 0;
-            if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+            int sms = 0, occ = 0;
             if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
             if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, smem)) != cudaSuccess)
                 return e;
-            ks.sms = sms > 0 ? sms : 1;
+            ks.sms[dev] = sms > 0 ? sms : 1;
             v = occ > 0 ? occ : 1;
-            ks.per_sm.store(v, std::memory_order_release);
+            ks.per_sm[dev].store(v, std::memory_order_release);
         }
     }
     if (per_sm) *per_sm = v;
-    if (total) *total = v * ks.sms;
+    if (total) *total = v * ks.sms[dev];
+    return cudaSuccess;
+}
+
+// A dynamic shared-memory limit that several launch shapes of one kernel
+// share: only ever raised, per device (the attribute belongs to the device
+// that is current when it is set), under a lock (handles on several host
+// threads).
+struct SmemLimit {
+    std::mutex mu;
+    size_t bytes[kSetupDevices] = {};
+};
+
+inline cudaError_t raise_smem_limit(SmemLimit& s, const void* kern, size_t bytes)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kSetupDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(s.mu);
+    if (bytes > s.bytes[dev]) {
+        if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes)) != cudaSuccess)
+            return e;
+        s.bytes[dev] = bytes;
+    }
     return cudaSuccess;
 }
 

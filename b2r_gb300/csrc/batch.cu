@@ -461,20 +461,14 @@ b2r_status b2r_batch_create(const b2r_batch_item* items, int n, b2r_batch** out)
     {
         const void* fns[3] = {(const void*)batch_kernel<32>, (const void*)batch_kernel<16>,
                               (const void*)batch_kernel<8>};
-        // the limit is per function and process-wide: only ever raised, so
-        // that a batch with a smaller schedule does not lower it under one
-        // created before it
-        static std::mutex mu;
-        static size_t limit[3] = {0, 0, 0};
-        std::lock_guard<std::mutex> lock(mu);
+        // the limit is per function and device: only ever raised, so that a
+        // batch with a smaller schedule does not lower it under one created
+        // before it
+        static SmemLimit limit[3];
         for (int s = 0; s < 3; ++s) {
             int occ = 0;
-            if (b->smem > limit[s]) {
-                if (cudaFuncSetAttribute(fns[s], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem) !=
-                    cudaSuccess)
-                    return bail(bfail(B2R_ERR_CUDA, "smem attribute"));
-                limit[s] = b->smem;
-            }
+            if (raise_smem_limit(limit[s], fns[s], b->smem) != cudaSuccess)
+                return bail(bfail(B2R_ERR_CUDA, "smem attribute"));
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fns[s], kThreads, b->smem);
             b->grid[s] = std::max(1, occ) * std::max(1, sms);
         }

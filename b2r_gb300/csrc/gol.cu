@@ -356,19 +356,10 @@ cudaError_t launch_gol_period(const uint8_t* in, uint8_t* out, const BlockLayout
     // narrow regions: a variant with two resident CTAs per SM
     constexpr int kNarrowT = 36 * kPGroups;
     const bool narrow = threads <= kNarrowT;
-    static size_t attr[2] = {0, 0};
-    // raised only, under a lock: handles on other host threads share the limit
-    static std::mutex attr_mu;
-    std::lock_guard<std::mutex> attr_lock(attr_mu);
-    if (smem > attr[narrow]) {
-        const int bytes = (int)std::max<size_t>(smem, 48 * 1024);
-        cudaError_t e = narrow ? cudaFuncSetAttribute(gol_period_kernel<kNarrowT, 2>,
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)
-                               : cudaFuncSetAttribute(gol_period_kernel<kPMaxW * kPGroups, 1>,
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        if (e != cudaSuccess) return e;
-        attr[narrow] = (size_t)bytes;
-    }
+    static SmemLimit attr[2];
+    const void* kern = narrow ? (const void*)gol_period_kernel<kNarrowT, 2>
+                              : (const void*)gol_period_kernel<kPMaxW * kPGroups, 1>;
+    if (cudaError_t e = raise_smem_limit(attr[narrow], kern, std::max<size_t>(smem, 48 * 1024))) return e;
     if (narrow) gol_period_kernel<kNarrowT, 2><<<grid, threads, smem, st>>>(in, out, L, G);
     else gol_period_kernel<kPMaxW * kPGroups, 1><<<grid, threads, smem, st>>>(in, out, L, G);
     count_launches(1);

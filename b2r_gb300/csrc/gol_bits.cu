@@ -526,19 +526,13 @@ cudaError_t launch_gol_bits_period(const uint8_t* in, uint8_t* out, const BlockL
     const size_t smem = (size_t)ng * 4 * GW * (G.PR + 2) * sizeof(uint32_t);
     const int threads = (GW * (G.PR / 4) + 31) / 32 * 32;   // whole warps: every lane takes part in the shuffles
     const dim3 grid(ntx, nty2, L.nblk * nzc);
-    static size_t attr[3] = {0, 0, 0};
+    // raised only, per device, under a lock: handles on other host threads share the limit
+    static SmemLimit attr[3];
     const int gi = GW == 8 ? 0 : (GW == 16 ? 1 : 2);
-    // raised only, under a lock: handles on other host threads share the limit
-    static std::mutex attr_mu;
-    std::lock_guard<std::mutex> attr_lock(attr_mu);
-    if (smem > attr[gi]) {
-        const int bytes = (int)std::max<size_t>(smem, 48 * 1024);
-        cudaError_t e = GW == 8 ? cudaFuncSetAttribute(gol_bits_period_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)
-                      : GW == 16 ? cudaFuncSetAttribute(gol_bits_period_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)
-                                 : cudaFuncSetAttribute(gol_bits_period_kernel<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        if (e != cudaSuccess) return e;
-        attr[gi] = (size_t)bytes;
-    }
+    const void* kern = GW == 8 ? (const void*)gol_bits_period_kernel<8>
+                     : GW == 16 ? (const void*)gol_bits_period_kernel<16>
+                                : (const void*)gol_bits_period_kernel<32>;
+    if (cudaError_t e = raise_smem_limit(attr[gi], kern, std::max<size_t>(smem, 48 * 1024))) return e;
     switch (GW) {
     case 8: gol_bits_period_kernel<8><<<grid, threads, smem, st>>>(in, out, L, G); break;
     case 16: gol_bits_period_kernel<16><<<grid, threads, smem, st>>>(in, out, L, G); break;

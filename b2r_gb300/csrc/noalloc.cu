@@ -12,8 +12,11 @@
 //
 // Limits and sharing:
 // * each of the two ping-pong buffers holds at most kNoAllocCells cells in
-//   the library's padded layout (row pitch rounded up to 32 cells), i.e.
-//   blocks up to about 160^3; larger blocks are rejected with B2R_ERR_ARG;
+//   the library's padded layout (the same layout as b2r_heat_3D_gpu_main:
+//   rows padded to a multiple of 32 cells with at least 4 cells before the
+//   block and 8 after it), i.e. P * Ngy * Ngz <= 4,194,304 with P the padded
+//   row pitch -- cubes up to 147^3 at R*D = 1; larger blocks are rejected
+//   with B2R_ERR_ARG;
 // * the array (2 x 16 MiB + 256 B) is resident on every GPU that loads the
 //   library, until the process exits;
 // * every call on a device uses the same array and leaves its contents
@@ -21,14 +24,14 @@
 //   before reading them.  Calls that overlap on the GPU (other streams,
 //   other host threads) race on the array and must be serialised by the
 //   caller;
-// * the first call on each device looks up the array's device address
-//   (cudaGetSymbolAddress, with that device current); make that first call
-//   before any stream capture.
+// * every call looks up the array's device address on the current device
+//   (cudaGetSymbolAddress; cheap, and never stale after a context is torn
+//   down and re-created); the first call on a device also loads the
+//   library's device code there, so make that first call before any stream
+//   capture.
 #include <cstdio>
-#include <mutex>
 
-#include "b2r_common.cuh"
-#include "heat.h"
+#include "api_internal.h"
 
 namespace b2r {
 namespace {
@@ -39,26 +42,14 @@ constexpr size_t kStatusFloats = 64;                          // 256 B for the s
 // [buffer A | buffer B | status word]
 static __device__ __align__(256) float g_noalloc_scratch[2 * kNoAllocCells + kStatusFloats];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-void* g_scratch_ptr[kMaxDevices] = {};
-
-// Device address of the scratch array on the current device (set-up once
-// per device).  The host-side symbol is only a stand-in: kernels must get this.
+// Device address of the scratch array on the current device.  The host-side
+// symbol is only a stand-in: kernels must be given this address.
 cudaError_t scratch_address(void** out)
 {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        g_scratch_ptr[dev] = p;
-    }
-    *out = g_scratch_ptr[dev];
+    *out = p;
     return cudaSuccess;
 }
 
@@ -87,27 +78,10 @@ extern "C" b2r_status b2r_heat_3D_gpu_main_noalloc(const float* d_in, float* d_o
     if (R < 1) return nfail(B2R_ERR_ARG, "R must be >= 1");
     const int H = R * D;
     const int n[3] = {Ngx, Ngy, Ngz};
-    BlockLayout L{};
+    int B[3];
     for (int a = 0; a < 3; ++a) {
-        if (n[a] - 2 * H < 1) return nfail(B2R_ERR_ARG, "block too small for R*D");
-        L.n[a] = n[a];
-        L.B[a] = n[a] - 2 * H;
-        L.nb[a] = 1;
-    }
-    // the library's padded float layout (128-byte rows, >= 16 B pad each side)
-    L.nblk = 1;
-    L.H = H;
-    L.xoff = (H + 4 + 31) / 32 * 32 - H;
-    L.P = (L.xoff + Ngx + 4 + 31) / 32 * 32;
-    L.periodic = 0;
-    L.plane = (long long)L.P * Ngy;
-    L.bstride = L.plane * Ngz;
-    if ((size_t)L.bstride > kNoAllocCells) {
-        fprintf(stderr,
-                "b2r_heat_3D_gpu_main_noalloc: block %dx%dx%d needs %lld padded cells per buffer;"
-                " the no-allocation scratch holds %zu\n",
-                Ngx, Ngy, Ngz, L.bstride, kNoAllocCells);
-        return B2R_ERR_ARG;
+        B[a] = n[a] - 2 * H;
+        if (B[a] < 1) return nfail(B2R_ERR_ARG, "block too small for R*D");
     }
     int edge = 0;
     if (edge_flag)
@@ -116,7 +90,17 @@ extern "C" b2r_status b2r_heat_3D_gpu_main_noalloc(const float* d_in, float* d_o
             if (v < 0) edge |= 1 << (2 * a);
             if (v > 0) edge |= 1 << (2 * a + 1);
         }
-    L.fixed_edge = edge;
+    // the allocating entry's padded float layout (b2r_heat_3D_gpu_main)
+    const int nb[3] = {1, 1, 1};
+    BlockLayout L{};
+    b2r_api::fill_layout(L, n, B, nb, H, 4, 0, edge);
+    if ((size_t)L.bstride > kNoAllocCells) {
+        fprintf(stderr,
+                "b2r_heat_3D_gpu_main_noalloc: block %dx%dx%d needs %lld padded cells per buffer;"
+                " the no-allocation scratch holds %zu\n",
+                Ngx, Ngy, Ngz, L.bstride, kNoAllocCells);
+        return B2R_ERR_ARG;
+    }
 
     void* base = nullptr;
     cudaError_t e = scratch_address(&base);
