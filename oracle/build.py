@@ -1,10 +1,11 @@
 """Build recipe for the oracle (test infrastructure only).
 
 * ``liborc.so``  -- the CPU restatement in b2r_oracle.c (always built).
-* ``_ref/eqwp_ref.cubin``, ``_ref/gol_ref.cubin``, ``_ref/heat_ref.cubin``
-  -- the reference's own eqwp.cu, gol-3D.cu and heat-3D.cu kernels, device
-  code only (oracle/refgpu.py runs them
-  on the GPU as a second oracle).
+* ``_ref/eqwp_ref.cubin``, ``_ref/gol_ref.cubin``, ``_ref/heat_ref.cubin``,
+  ``_ref/heat_ref_d{2,3,4}.cubin`` -- the reference's own eqwp.cu, gol-3D.cu
+  and heat-3D.cu kernels, device code only, heat-3D.cu once per stencil
+  radius B2R_D (its shared tiles are sized by it, heat-3D.cu:175,252);
+  oracle/refgpu.py runs them on the GPU as a second oracle.
 * ``_ref/libheat_ref.so`` -- the reference's own heat-3D.cpp compiled from
   its source tree, with a two-line config shim for its
   ``#include "../b2r_config.h"`` (heat-3D.cpp:16) and
@@ -19,7 +20,10 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_SRC = os.environ.get("B2R_REFERENCE_SRC", "/root/reference")
+# the reference's source tree: B2R_REFERENCE_SRC, else a "reference" folder
+# beside this repository
+REF_SRC = os.environ.get("B2R_REFERENCE_SRC",
+                         os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 CFLAGS = ["-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared"]
 
 
@@ -75,14 +79,21 @@ def build_ref_cubin(force=False):
     os.makedirs(refdir, exist_ok=True)
     nvcc = os.environ.get("NVCC", "nvcc")
     outs = []
-    sub = os.path.join(refdir, "incg", "sub")     # heat-3D.cu includes "../b2r_config.h"
-    os.makedirs(sub, exist_ok=True)
-    with open(os.path.join(refdir, "incg", "b2r_config.h"), "w") as f:
-        f.write("#pragma once\n#define B2R_D 1\ntypedef float CELL_DT;\n")
     sync = "-DcudaThreadSynchronize=cudaDeviceSynchronize"
-    for src, name, extra in (("eqwp.cu", "eqwp_ref.cubin", []),
-                             ("gol-3D.cu", "gol_ref.cubin", [sync]),
-                             ("heat-3D.cu", "heat_ref.cubin", [sync, "-I", sub])):
+    jobs = [("eqwp.cu", "eqwp_ref.cubin", []), ("gol-3D.cu", "gol_ref.cubin", [sync])]
+    for D in (1, 2, 3, 4):
+        # heat-3D.cu includes "../b2r_config.h": one shim folder per radius
+        inc = os.path.join(refdir, "incg" if D == 1 else f"incg{D}")
+        sub = os.path.join(inc, "sub")
+        os.makedirs(sub, exist_ok=True)
+        shim = os.path.join(inc, "b2r_config.h")
+        text = f"#pragma once\n#define B2R_D {D}\ntypedef float CELL_DT;\n"
+        if not os.path.exists(shim) or open(shim).read() != text:
+            with open(shim, "w") as f:
+                f.write(text)
+        name = "heat_ref.cubin" if D == 1 else f"heat_ref_d{D}.cubin"
+        jobs.append(("heat-3D.cu", name, [sync, "-I", sub]))
+    for src, name, extra in jobs:
         path = os.path.join(REF_SRC, src)
         out = os.path.join(refdir, name)
         if force or not _newer(out, [path, os.path.join(REF_SRC, "b2r_config.h")]):

@@ -11,7 +11,10 @@ through the CUDA driver API in the process's current (PyTorch) context and
 drives it as eqwp_gpu_main does (eqwp.cu:661-688): per time step the stress
 kernel, then vx, vy (with the displacement) and vz, on 16 x 16 thread blocks
 over the padded block, R = 1; gol-3D.cu's gol_3d_kernel and heat-3D.cu's
-fdm_heat_diffuse_delta1 likewise (run_reference_gol, run_reference_heat).
+fdm_heat_diffuse_delta1 likewise (run_reference_gol, run_reference_heat),
+heat-3D.cu's fdm_heat_diffuse_delta2..4 from the cubins built at B2R_D = 2..4
+(run_reference_heat_d) and its edge-flag kernel
+fdm_heat_diffuse_delta1_verify at any R (run_reference_heat_verify).
 
 The elastic-wave kernels are correct only inside their envelope: R = 1 and a block of at
 most 16 rows (one thread-block tile in y) -- their y halo loads read row y-1
@@ -43,6 +46,16 @@ _GOL_NAME = "_Z13gol_3d_kernelPhS_iiii"   # gol_3d_kernel (gol-3D.cu:30)
 HEAT_CUBIN = os.path.join(HERE, "_ref", "heat_ref.cubin")
 HEAT_TILE = 32      # CUDA_BLOCK_SIZE (heat-3D.cu:8)
 _HEAT_NAME = "_Z23fdm_heat_diffuse_delta1PfS_iiii"   # fdm_heat_diffuse_delta1 (heat-3D.cu:173)
+# fdm_heat_diffuse_delta1_verify (heat-3D.cu:57): the edge-flag form of delta 1
+_HEAT_VERIFY_NAME = "_Z30fdm_heat_diffuse_delta1_verifyPfS_iiiiiiii"
+# fdm_heat_diffuse_delta2..4 (heat-3D.cu:250,337,432), one cubin per B2R_D
+_HEAT_D_NAMES = {2: "_Z23fdm_heat_diffuse_delta2PfS_iiii", 3: "_Z23fdm_heat_diffuse_delta3PfS_iiii",
+                 4: "_Z23fdm_heat_diffuse_delta4PfS_iiii"}
+
+
+def heat_d_cubin(D):
+    return HEAT_CUBIN if D == 1 else os.path.join(HERE, "_ref", f"heat_ref_d{D}.cubin")
+
 
 _mods = {}
 
@@ -57,6 +70,10 @@ def gol_available():
 
 def heat_available():
     return os.path.exists(HEAT_CUBIN)
+
+
+def heat_d_available(D):
+    return os.path.exists(heat_d_cubin(D))
 
 
 def _driver():
@@ -83,12 +100,13 @@ def _load(path, names):
         buf = C.create_string_buffer(data, len(data))
         mod = C.c_void_p()
         _check(cu.cuModuleLoadData(C.byref(mod), buf), "cuModuleLoadData")
-        fns = {}
-        for k, name in names.items():
+        _mods[path] = (cu, mod, {}, buf)
+    cu, mod, fns, _ = _mods[path]
+    for k, name in names.items():      # functions of the module looked up on first use
+        if k not in fns:
             f = C.c_void_p()
             _check(cu.cuModuleGetFunction(C.byref(f), mod, name.encode()), "cuModuleGetFunction " + k)
             fns[k] = f
-        _mods[path] = (cu, mod, fns, buf)
     return _mods[path]
 
 
@@ -180,6 +198,70 @@ def run_reference_heat(block, nsteps):
         a, b = b, a
     torch.cuda.synchronize()
     return a.cpu().numpy()
+
+
+def heat_d_envelope(shape, D):
+    """Whether fdm_heat_diffuse_delta<D> is correct on a (Ngz, Ngy, Ngx) block
+    at R = 1: one 32-row tile in y (its y halo loads read row y-1 into the
+    slot of row y-D, heat-3D.cu:304-309), and in x every thread that loads a
+    left halo of the last x tile updates its own cell (the loads sit under
+    the update test, heat-3D.cu:298-303) -- (Ngx-1-D) mod 32 >= D-1 -- or a
+    single x tile."""
+    ngz, ngy, ngx = shape
+    if ngy > HEAT_TILE:
+        return False
+    return ngx <= HEAT_TILE or (ngx - 1 - D) % HEAT_TILE >= D - 1
+
+
+def run_reference_heat_d(block, D, nsteps):
+    """block: (Ngz, Ngy, Ngx) float32 with a D-cell fixed shell.  Returns it
+    after nsteps steps of the reference's fdm_heat_diffuse_delta<D> (D = 2,
+    3, 4; 1 runs the delta-1 kernel) at R = 1 with its constants
+    (alpha*dt = 0.01, dx = dy = 1, dz = 0.5, heat-3D.cu:9-13), driven as
+    heat_3D_gpu_main drives it (heat-3D.cu:583-628): both device buffers
+    start as the block, 32 x 32 thread blocks, ping-pong.  Refuses blocks
+    outside the kernel's correct envelope (heat_d_envelope)."""
+    import torch
+    if D == 1:
+        return run_reference_heat(block, nsteps)
+    ngz, ngy, ngx = block.shape
+    if not heat_d_envelope(block.shape, D):
+        raise ValueError("fdm_heat_diffuse_delta%d is correct only within one 32-row y tile, "
+                         "with (Ngx-1-D) mod 32 >= D-1" % D)
+    cu, _, fns, _ = _load(heat_d_cubin(D), {"heat": _HEAT_D_NAMES[D]})
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    a = torch.from_numpy(np.ascontiguousarray(block, np.float32)).cuda()
+    b = a.clone()
+    grid = ((ngx + HEAT_TILE - 1) // HEAT_TILE, (ngy + HEAT_TILE - 1) // HEAT_TILE)
+    for _ in range(nsteps):
+        _launch(cu, fns["heat"], grid, stream, a, b, ngx, ngy, ngz, 0, tile=HEAT_TILE)
+        a, b = b, a
+    torch.cuda.synchronize()
+    return a.cpu().numpy()
+
+
+def run_reference_heat_verify(block, R, ef):
+    """heat_3D_gpu_main (heat-3D.cu:583-637) with the edge-flag kernel it
+    keeps commented out (fdm_heat_diffuse_delta1_verify, heat-3D.cu:57-158,
+    606): both device buffers start as the (Ngz, Ngy, Ngx) float32 block, R
+    ping-pong launches with b2r_i = 0..R-1 and ef = (xef, yef, zef) in
+    {-1, 0, 1}, then planes [R, Ngz-R) of the result replace the block's.
+    Any number of 32 x 32 tiles: the radius-1 halo loads are right."""
+    import torch
+    ngz, ngy, ngx = block.shape
+    cu, _, fns, _ = _load(HEAT_CUBIN, {"heat": _HEAT_NAME, "verify": _HEAT_VERIFY_NAME})
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    a = torch.from_numpy(np.ascontiguousarray(block, np.float32)).cuda()
+    b = a.clone()
+    grid = ((ngx + HEAT_TILE - 1) // HEAT_TILE, (ngy + HEAT_TILE - 1) // HEAT_TILE)
+    for i in range(R):
+        _launch(cu, fns["verify"], grid, stream, a, b, ngx, ngy, ngz, i, int(ef[0]), int(ef[1]), int(ef[2]), R,
+                tile=HEAT_TILE)
+        a, b = b, a
+    torch.cuda.synchronize()
+    out = np.array(block, np.float32, copy=True)
+    out[R:ngz - R] = a.cpu().numpy()[R:ngz - R]
+    return out
 
 
 def time_reference_heat(block, nsteps, reps=3):

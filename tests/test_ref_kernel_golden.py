@@ -74,3 +74,53 @@ def test_library_matches_reference_kernels(b2r):
         d.step(G.HEAT["nsteps"])
         h = d.download()
     assert rel_l2(h, NPZ["heat"]) <= 1e-5
+
+
+HEAT_NPZ = np.load(os.path.join(HERE, "golden", "ref_heat_kernels.npz"))
+
+
+def verify_edge(ef):
+    e = 0
+    for a in range(3):
+        e |= (1 << (2 * a)) if ef[a] < 0 else 0
+        e |= (1 << (2 * a + 1)) if ef[a] > 0 else 0
+    return e
+
+
+@pytest.mark.parametrize("D", [2, 3, 4])
+def test_oracle_heat_high_order_matches_reference_kernels(orc, D):
+    """The oracle's order-D restatement against fdm_heat_diffuse_delta<D>
+    (heat-3D.cu:250-521) inside its envelope: R = 1, one y tile."""
+    u = G.heat_d_input(D)
+    orc.heat_run(u, D, D, G.HEAT_D[D]["nsteps"], 0.01, 1.0, 1.0, 0.5)
+    assert rel_l2(u, HEAT_NPZ[f"heat_d{D}"]) <= 1e-5
+
+
+@pytest.mark.parametrize("k", [0, 1])
+def test_oracle_heat_edge_flags_match_reference_verify_kernel(orc, k):
+    """The oracle's fixed-shell window against fdm_heat_diffuse_delta1_verify
+    (heat-3D.cu:57-158) driven as heat_3D_gpu_main, R = 2 and 3."""
+    c = G.HEAT_VERIFY[k]
+    blk = G.heat_verify_input(k)
+    R = c["R"]
+    a, b = blk.copy(), blk.copy()
+    for i in range(R):
+        orc.heat_substep(a, b, 1, i, R, verify_edge(c["ef"]), **orc.REF_HEAT)
+        a, b = b, a
+    ref = blk.copy()
+    ref[R:-R] = a[R:-R]
+    assert rel_l2(ref, HEAT_NPZ[f"heat_verify{k}"]) <= 1e-5
+
+
+@pytest.mark.gpu
+def test_library_matches_reference_heat_kernels(b2r):
+    for D, c in G.HEAT_D.items():
+        with b2r.Domain(b2r.MODEL_HEAT, c["env"], D=D, R=1, alpha_dt=0.01, dx=1.0, dy=1.0, dz=0.5) as d:
+            d.upload(G.heat_d_input(D))
+            d.step(c["nsteps"])
+            h = d.download()
+        assert rel_l2(h, HEAT_NPZ[f"heat_d{D}"]) <= 1e-5, f"delta{D}"
+    for k, c in enumerate(G.HEAT_VERIFY):
+        blk = G.heat_verify_input(k)
+        b2r.heat_3D_gpu_main(blk, c["R"], D=1, edge_flag=c["ef"])
+        assert rel_l2(blk, HEAT_NPZ[f"heat_verify{k}"]) <= 1e-5, f"edge flags {c['ef']}"
