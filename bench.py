@@ -95,6 +95,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tune", default="",
                     help="launch-schedule knobs for Domain.set_tuning, e.g. eqwp_fused=1,tblock=4")
+    ap.add_argument("--no-secondary", dest="secondary", action="store_false",
+                    help="the default heat1_512 run on one GPU also measures the other configurations "
+                         "(under \"secondary\"); this flag skips them")
     return ap.parse_args()
 
 
@@ -377,26 +380,35 @@ def load_inputs(d, wl, torch, dev):
         for k in range(10):
             d.upload(zero, field=k)
         return zero
+    mat, amps = stag_model(d.domain_shape, d.cfg.dt, wl["sub_steps"] * 64)
+    for name, arr in zip(("lambda", "mu", "buoy"), mat):
+        d.upload(arr, field=name)
+    zero = np.zeros(d.domain_shape, np.float32)
+    for k in range(9):
+        d.upload(zero, field=k)
+    d.set_source(amps)
+    return zero
+
+
+def stag_model(shape, dt, nsrc):
+    """The staggered elastic-wave workload's material and source: 8 horizontal
+    layers (along y) with vp U[2000, 4000] m/s, vs = vp / sqrt(3), rho
+    U[2000, 2600] kg/m^3 from seed 3, on a domain array of numpy shape
+    (nz, ny, nx); the explosive Ricker source (10 Hz, delayed 1.2 / f0) for
+    nsrc steps of dt.  Returns ([lambda, mu, 1/rho] float32, amps float32)."""
     rng = np.random.default_rng(3)
     layers = 8
     vp_l = rng.uniform(2000, 4000, layers)
     rho_l = rng.uniform(2000, 2600, layers)
-    shape = d.domain_shape
     idx = np.minimum(np.arange(shape[1]) * layers // shape[1], layers - 1)
     vp = np.broadcast_to(vp_l[idx][None, :, None], shape)
     rho = np.broadcast_to(rho_l[idx][None, :, None], shape)
     mu = rho * (vp / 3 ** 0.5) ** 2
     lam = rho * vp ** 2 - 2 * mu
-    for name, arr in (("lambda", lam), ("mu", mu), ("buoy", 1.0 / rho)):
-        d.upload(np.ascontiguousarray(arr, np.float32), field=name)
-    zero = np.zeros(shape, np.float32)
-    for k in range(9):
-        d.upload(zero, field=k)
-    dt = d.cfg.dt
-    t = np.arange(wl["sub_steps"] * 64) * dt - 1.2 / 10.0
+    mat = [np.ascontiguousarray(arr, np.float32) for arr in (lam, mu, 1.0 / rho)]
+    t = np.arange(nsrc) * dt - 1.2 / 10.0
     a = (np.pi * 10.0 * t) ** 2
-    d.set_source((1e6 * dt * (1 - 2 * a) * np.exp(-a)).astype(np.float32))
-    return zero
+    return mat, (1e6 * dt * (1 - 2 * a) * np.exp(-a)).astype(np.float32)
 
 
 def batch_items(wl):
@@ -476,6 +488,22 @@ def run_batch(args, wl):
         max_rel = max(max_rel, float(np.linalg.norm(got[i].astype(np.float64) - plain) /
                                      np.linalg.norm(plain.astype(np.float64))))
     seq = lups / (seq_ms / 1e3) / 1e9
+    # the three instances with the fewest updates against the oracle (FP32, FP64)
+    from oracle import orc
+    small = sorted(range(len(items)), key=lambda i: int(np.prod(items[i]["env"])) * items[i]["nsteps"])[:3]
+    r32, r64 = 0.0, 0.0
+    for i in small:
+        it = items[i]
+        a32 = ins[i].copy()
+        orc.heat_run(a32, it["D"], it["D"], it["nsteps"], it["alpha_dt"], it["dx"], it["dy"], it["dz"])
+        a64 = ins[i].astype(np.float64)
+        orc.heat_run(a64, it["D"], it["D"], it["nsteps"], it["alpha_dt"], it["dx"], it["dy"], it["dz"])
+        r32, r64 = max(r32, rel_l2(got[i], a32)), max(r64, rel_l2(got[i], a64))
+    parity = {"instances": [dict(env=list(items[i]["env"]), D=items[i]["D"], nsteps=items[i]["nsteps"])
+                            for i in small],
+              "rel_l2_fp32": r32, "rel_l2_fp64": r64, "tolerance": 1e-5,
+              "max_rel_l2_vs_sequential": max_rel,
+              "oracle": "oracle/b2r_oracle.c heat restatement (FP32, FP64), worst of the three"}
     peak, peak_src = measured_peak()
     achieved = wl["bytes_per_cell"] * lups / (ms / 1e3) / 1e9
     bt.close()
@@ -493,8 +521,8 @@ def run_batch(args, wl):
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_src,
                          "kernel": "batch_kernel", "note": "8 B per lattice-site update, whole run"},
-            "cpu_baseline": None, "clocks": clk}
-    print(json.dumps(line), flush=True)
+            "cpu_baseline": None, "clocks": clk, "parity": parity}
+    return line
 
 
 def run_adjoint(args, wl):
@@ -584,6 +612,25 @@ def run_adjoint(args, wl):
     d.eqwp_record(n, rec)
     fwd_ms.append((time.perf_counter() - t0) * 1e3)
     d.close()
+    # parity: the gradient's derivative along the anomaly (the model
+    # difference that made the observed data) against a central finite
+    # difference of the misfit, two more forwards at the full size
+    m0, m1 = model(0.0), model(0.05)
+    delta = [b - a for a, b in zip(m0, m1)]
+    inner = (slice(2, -2),) * 3
+    an = float(sum((gk * dk[inner]).sum() for gk, dk in zip(g[:2], delta[:2])))
+    eps = 0.05
+
+    def misfit_at(s):
+        dd, _ = domain([a + s * eps * dl for a, dl in zip(m0, delta)])
+        syn = dd.eqwp_record(n, rec)
+        dd.close()
+        return 0.5 * float(((syn.astype(np.float64) - d_obs) ** 2).sum())
+
+    fd = (misfit_at(1) - misfit_at(-1)) / (2 * eps)
+    parity = {"direction": "the 5 % Gaussian anomaly of vp (lambda, mu)", "adjoint": an,
+              "central_difference": fd, "rel_diff": abs(fd - an) / max(abs(fd), 1e-300),
+              "eps": eps, "note": "FP64 gradient oracle at 64^3 and 16-direction differences: the GPU tests"}
     cells = env[0] * env[1] * env[2]
     gms = float(np.median(grad_ms))
     fms = float(np.median(fwd_ms))
@@ -606,8 +653,72 @@ def run_adjoint(args, wl):
                          "frac": round(wl["bytes_per_cell"] * value / peak, 4), "traffic": None,
                          "peak_source": peak_src, "kernel": "adjoint (whole gradient)",
                          "note": "84 B per cell-step of the forward, over the whole gradient time"},
-            "cpu_baseline": None, "clocks": clk}
-    print(json.dumps(line), flush=True)
+            "cpu_baseline": None, "clocks": clk, "parity": parity}
+    return line
+
+
+def parity_sample(d, wl, host):
+    """A short run of the timed schedule (the knobs the handle holds) from the
+    workload's own seeded input, checked against the oracle after the timed
+    region: heat against the FP32 and FP64 restatements, Game of Life bit for
+    bit, the elastic waves against the FP32 and FP64 restatements."""
+    from oracle import orc
+    model = wl["model"]
+    if model == 1:
+        D = wl["D"]
+        n = 4
+        d.upload(host)
+        d.step(n)
+        got = d.download()
+        r32 = host.copy()
+        orc.heat_run(r32, D, D, n, *wl["coef"])
+        r64 = host.astype(np.float64)
+        orc.heat_run(r64, D, D, n, *wl["coef"])
+        return {"time_steps": n, "rel_l2_fp32": rel_l2(got, r32), "rel_l2_fp64": rel_l2(got, r64),
+                "tolerance": 1e-5, "oracle": "oracle/b2r_oracle.c heat restatement (FP32, FP64)"}
+    if model == 2:
+        n = 2 * wl["R"]
+        d.upload(host)
+        d.step(n)
+        got = d.download()
+        ref = host.copy()
+        orc.gol_run_periodic(ref, n)
+        bad = int(np.count_nonzero(got != ref))
+        return {"generations": n, "bit_exact": bad == 0, "mismatched_cells": bad,
+                "oracle": "oracle/b2r_oracle.c rule restatement"}
+    if model == 4:
+        n = 2 * wl["R"]
+        mat, amps = stag_model(d.domain_shape, d.cfg.dt, n)
+        rng = np.random.default_rng(12)
+        init = []
+        for k in range(9):
+            f = np.zeros(d.domain_shape, np.float32)
+            f[4:-4, 4:-4, 4:-4] = ((rng.random(tuple(v - 8 for v in f.shape), dtype=np.float32) - 0.5) *
+                                   (1e-3 if k < 3 else 1e5))
+            init.append(f)
+            d.upload(f, field=k)
+        d.set_source(amps)
+        d.step(n)
+        got = [d.download(field=k) for k in range(9)]
+        src = tuple(int(v) + 2 for v in d.cfg.src)
+        f32 = [a.copy() for a in init]
+        f64 = [a.astype(np.float64) for a in init]
+        m64 = [m.astype(np.float64) for m in mat]
+        for t in range(n):
+            orc.eqwp_stag_step(f32, mat, d.cfg.dt, d.cfg.h, 0, 2, 63, src, float(amps[t]))
+            orc.eqwp_stag_step(f64, m64, d.cfg.dt, d.cfg.h, 0, 2, 63, src, float(amps[t]))
+        return {"time_steps": n, "input": "random wavefield, the workload's material and source",
+                "bit_identical_fp32": all(np.array_equal(got[k], f32[k]) for k in range(9)),
+                "rel_l2_fp32": max(rel_l2(got[k], f32[k]) for k in range(9)),
+                "rel_l2_fp64": max(rel_l2(got[k], f64[k]) for k in range(9)), "tolerance": 1e-5,
+                "oracle": "oracle/b2r_oracle.c staggered restatement (FP32, FP64), worst of 9 fields"}
+    return None
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
 def run_ours(args, wl):
@@ -743,10 +854,13 @@ def run_ours(args, wl):
         algo = wl["bytes_per_cell"] * cells * steps_per_launch
         per_launch_ms = ms / per_launch
         achieved = algo / (per_launch_ms / 1000.0) / 1e9
+        tb = (tuned or tune or {}).get("tblock", 2)
+        kern = (wl["kernel"] if steps_per_launch < 1.5 else
+                "heat2_kernel (two time steps per launch)" if tb == 2 else
+                f"heat_tb_kernel<{tb}> ({tb} time steps per launch)")
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": profiled_traffic(args.workload),
-                "peak_source": peak_src, "kernel": wl["kernel"] if steps_per_launch < 1.5
-                else "heat2_kernel (two time steps per launch)",
+                "frac": round(achieved / peak, 4), "traffic": profiled_traffic(args.workload, tb),
+                "peak_source": peak_src, "kernel": kern,
                 "algorithmic_bytes_per_launch": int(algo), "time_steps_per_launch": steps_per_launch,
                 "avg_launch_ms": round(per_launch_ms, 4)}
     elif wl["model"] == 2:
@@ -766,11 +880,15 @@ def run_ours(args, wl):
                 "note": "whole-step average (stages and halo exchanges) over the algorithmic bytes "
                         "of one step"}
 
+    # ---- parity of the timed schedule against the oracle (after timing)
+    parity = parity_sample(d, wl, host) if rank == 0 else None
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         v, kind, cores, sample = cpu_sample(wl, budget_s=10.0)
         cpu = {"value": round(v, 4), "unit": "GLUPS", "cores": cores, "kind": kind, "sample": sample}
 
+    line = None
     if rank == 0:
         line = {"metric": "GLUPS", "value": round(value, 3), "unit": "GLUPS", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
@@ -781,21 +899,57 @@ def run_ours(args, wl):
                 "e2e": ({"value": round(e2e_val, 3), "unit": "GLUPS", "h2d_bytes_per_step": h2d,
                          "d2h_bytes_per_step": d2h} if e2e_val is not None else None),
                 "gpu_launches": int(launches),
-                "roofline": roof, "cpu_baseline": cpu, "clocks": clk}
-        print(json.dumps(line), flush=True)
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "parity": parity}
     d.close()
-    if world > 1:
-        dist.destroy_process_group()
+    return line
 
 
-def profiled_traffic(workload):
+def profiled_traffic(workload, tblock=None):
+    """DRAM bytes per launch of the dominant kernel from an ncu capture
+    (profiles/traffic.json), keyed by workload and, for the heat sweeps that
+    take several steps per launch, by "<workload>@tb<T>"."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(p):
         try:
-            return json.load(open(p)).get(workload)
+            t = json.load(open(p))
+            if tblock is not None and f"{workload}@tb{tblock}" in t:
+                return t[f"{workload}@tb{tblock}"]
+            return t.get(workload) if tblock in (None, 2) else None
         except Exception:
             return None
     return None
+
+
+def run_workload(args, name):
+    wl = WORKLOADS[name]
+    a = argparse.Namespace(**{**vars(args), "workload": name})
+    if wl["model"] == 5:
+        return run_batch(a, wl)
+    if wl["model"] == 6:
+        return run_adjoint(a, wl)
+    return run_ours(a, wl)
+
+
+# the BASELINE configurations other than the headline, carried under
+# "secondary" by the default one-GPU run so that one invocation measures them
+# all on the same box: each with its own value, roofline fraction, clocks and
+# parity figure
+SECONDARY = ("heat_128", "gol_256", "eqwp_stag", "heat4_512", "batch64", "adjoint256")
+
+
+def compact(line):
+    if line is None:
+        return None
+    roof = line.get("roofline") or {}
+    cfg = line.get("config") or {}
+    keep = ("autotuned", "batched_over_sequential", "sequential_plain_glups", "gradient_over_forward",
+            "forward_ms", "gradient_ms", "time_steps_per_step", "env", "blocks", "R", "D", "l2")
+    return {"value": line["value"], "unit": line["unit"], "ms_per_step": line["ms_per_step"],
+            "steps": line["steps"], "warmup": line["warmup"],
+            "e2e": (line.get("e2e") or {}).get("value"), "gpu_launches": line.get("gpu_launches"),
+            "roofline_frac": roof.get("frac"), "roofline_kernel": roof.get("kernel"),
+            "roofline_achieved_gbs": roof.get("achieved"), "clocks": line.get("clocks"),
+            "parity": line.get("parity"), "config": {k: cfg[k] for k in keep if k in cfg}}
 
 
 def main():
@@ -803,12 +957,25 @@ def main():
     wl = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, wl)
-    elif wl["model"] == 5:
-        run_batch(args, wl)
-    elif wl["model"] == 6:
-        run_adjoint(args, wl)
-    else:
-        run_ours(args, wl)
+        return
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    line = run_workload(args, args.workload)
+    if line is not None and world == 1 and args.secondary and args.workload == "heat1_512" and not args.tune:
+        sec = {}
+        short = argparse.Namespace(**{**vars(args), "steps": min(args.steps, 3), "warmup": 3,
+                                      "no_cpu_baseline": True})
+        for name in SECONDARY:
+            try:
+                sec[name] = compact(run_workload(short, name))
+            except Exception as e:      # a secondary never takes the headline down
+                sec[name] = {"error": str(e)[:300]}
+        line["secondary"] = sec
+    if line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        if dist.is_initialized():
+            dist.destroy_process_group()
 
 
 if __name__ == "__main__":
