@@ -91,6 +91,9 @@ def lib():
         "b2r_boundary_updating": ([vp, i, i], i),
         "b2r_heat_3D_gpu_main": ([vp, i, i, C.c_char_p, i, i, i, d, d, d, d, vp,
                                   C.POINTER(d)], i),
+        "b2r_heat_3D_cpu_main": ([vp, i, i, C.c_char_p, i, i, i, d, d, d, d, i, C.POINTER(d)], i),
+        "b2r_heat_3D_hybrid_main": ([vp, i, i, C.c_char_p, i, i, i, d, d, d, d, i, i, vp,
+                                     C.POINTER(d)], i),
         "b2r_gol_3D_gpu_main": ([vp, i, C.c_char_p, i, i, i, vp, C.POINTER(d)], i),
         "b2r_eqwp_gpu_main": ([vp, i, i, C.POINTER(d)], i),
         "b2r_write_block_data": ([vp, i, i, i, C.c_char_p, i, C.c_char_p, i], i),
@@ -530,6 +533,31 @@ def heat_3D_gpu_main(h_in, R, D=1, edge_flag=None, alpha_dt=0.1 * 0.1, dx=1.0, d
     _check(lib().b2r_heat_3D_gpu_main(h_in.ctypes.data_as(C.c_void_p), R, D, _ef(edge_flag), nx,
                                       ny, nz, alpha_dt, dx, dy, dz, C.c_void_p(int(s)),
                                       C.byref(secs)))
+    return secs.value
+
+
+def heat_3D_cpu_main(h_in, R, D=1, edge_flag=None, alpha_dt=0.1 * 0.1, dx=1.0, dy=1.0, dz=0.5,
+                     nthreads=0):
+    """heat-3D.cpp:136 on the host cores, in place on a host float32 block
+    (nz,ny,nx), bit-identical to heat_3D_gpu_main; returns wall seconds."""
+    nz, ny, nx = _block(h_in, np.float32)
+    secs = C.c_double()
+    _check(lib().b2r_heat_3D_cpu_main(h_in.ctypes.data_as(C.c_void_p), R, D, _ef(edge_flag), nx, ny, nz,
+                                      alpha_dt, dx, dy, dz, int(nthreads), C.byref(secs)))
+    return secs.value
+
+
+def heat_3D_hybrid_main(h_in, R, cpu_planes, D=1, edge_flag=None, alpha_dt=0.1 * 0.1, dx=1.0, dy=1.0,
+                        dz=0.5, nthreads=0, stream=None):
+    """One block split along z between the host cores (the last cpu_planes
+    result planes) and the GPU (the rest), in place, bit-identical to
+    heat_3D_gpu_main; returns wall seconds."""
+    nz, ny, nx = _block(h_in, np.float32)
+    secs = C.c_double()
+    s = getattr(stream, "cuda_stream", stream) or 0
+    _check(lib().b2r_heat_3D_hybrid_main(h_in.ctypes.data_as(C.c_void_p), R, D, _ef(edge_flag), nx, ny, nz,
+                                         alpha_dt, dx, dy, dz, int(cpu_planes), int(nthreads),
+                                         C.c_void_p(int(s)), C.byref(secs)))
     return secs.value
 
 

@@ -34,6 +34,7 @@ struct b2r_handle {
     int cur = 0;
     CUtensorMap tmap[2];
     CUtensorMap tmap2[2];       // boxes of the two-step kernel (D = 1)
+    CUtensorMap tmap3[2];       // boxes of the three- and four-step kernel (D = 1)
     HeatCoef hc{};
     HeatTune tune{};
     // elastic wave: fields and material
@@ -154,7 +155,7 @@ size_t domain_cells(const b2r_handle* h);
 b2r_status ensure_kappa(b2r_handle* h);
 b2r_status ensure_staging(b2r_handle* h, size_t bytes);
 b2r_status build_heat_maps(b2r_handle* h);
-bool heat_fuse_ok(const b2r_handle* h, int i);
+int heat_pass_steps(const b2r_handle* h, int i, int left);
 int gol_pass_gens(const b2r_handle* h, int i, int left);
 b2r_status check_status(b2r_handle* h);
 b2r_status exchange_all(b2r_handle* h, bool staged);
@@ -165,5 +166,30 @@ b2r_status substep2(b2r_handle* h, int i);
 void drop_graphs(b2r_handle* h);
 b2r_status advance(b2r_handle* h, int n);
 b2r_status capture_graph(b2r_handle* h, int c, int periods);
+
+// heat_3D_gpu_main on one host block, in two halves so that host work can
+// run between them: begin() allocates the two ping-pong device blocks and
+// the status word, copies the block in (both buffers) and enqueues the R
+// shrinking sub-steps on st; end() copies planes [R*D, Ngz-R*D) of the
+// result into h_out and waits for the stream.  edge: the fixed-shell face
+// bits of BlockLayout::fixed_edge.  The destructor frees what begin()
+// allocated.
+struct HeatBlockRun {
+    BlockLayout L{};
+    void* buf[2] = {nullptr, nullptr};
+    void* status = nullptr;
+    EventPair ev;
+    cudaStream_t st = nullptr;
+    int R = 0, H = 0, Ngz = 0, cur = 0;
+    HeatBlockRun() = default;
+    HeatBlockRun(const HeatBlockRun&) = delete;
+    HeatBlockRun& operator=(const HeatBlockRun&) = delete;
+    b2r_status begin(const float* h_in, int R, int D, int edge, int Ngx, int Ngy, int Ngz, double alpha_dt,
+                     double dx, double dy, double dz, cudaStream_t st);
+    b2r_status end(float* h_out, double* gpu_seconds);
+    ~HeatBlockRun();
+};
+// edge_flag[3] in {-1, 0, 1} (NULL: 0, 0, 0) as face bits
+int edge_bits_of_flags(const char* edge_flag);
 
 }  // namespace b2r_api

@@ -216,12 +216,18 @@ b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* bes
     HeatTune bestT = h->tune;
     float bestMs = 1e30f;
     b2r_status st = B2R_OK;
-    // candidates: the two-step sweep (radius 1) by z-chunk, then the one-step
-    // sweep by z-chunk x persistent CTAs per SM x PDL
+    // candidates: the several-step sweeps (radius 1: two, three and four steps
+    // per pass) by z-chunk, then the one-step sweep by z-chunk x persistent
+    // CTAs per SM x PDL.  Every trial advances a multiple of 12 time steps,
+    // so that each schedule runs whole passes.
     struct Cand { int tb, zc2, zc, cp, pdl; };
     std::vector<Cand> cands;
-    if (h->cfg.D == 1)
+    if (h->cfg.D == 1) {
         for (int z2 : {4, 8, 16, 32, 64}) cands.push_back({2, z2, 0, 0, 1});
+        for (int tb : {3, 4})
+            for (int z2 : {0, 32, 48, 96, 128}) cands.push_back({tb, z2, 0, 0, 1});
+        trial_steps = (trial_steps + 11) / 12 * 12;
+    }
     for (int pdl = 0; pdl < 2; ++pdl)
         for (int zc : zchunks)
             for (int cp : persist)

@@ -104,20 +104,23 @@ b2r_status build_heat_maps(b2r_handle* h)
         if (!make_block_tmap(&h->tmap[b], h->buf[b], h->L, 4, heat_box_w(), heat_box_h(h->cfg.D), 1))
             return fail(h, B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed for the heat field");
         if (h->cfg.D == 1 &&
-            !make_block_tmap(&h->tmap2[b], h->buf[b], h->L, 4, heat2_box_w(), heat2_box_h(), 1))
+            (!make_block_tmap(&h->tmap2[b], h->buf[b], h->L, 4, heat2_box_w(), heat2_box_h(), 1) ||
+             !make_block_tmap(&h->tmap3[b], h->buf[b], h->L, 4, heat_tb_box_w(), heat_tb_box_h(), 1)))
             return fail(h, B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed for the heat field");
     }
     return B2R_OK;
 }
 
-// Can sub-steps i and i+1 run in one two-step launch?  Radius 1 only, and no
-// halo exchange may fall between them: within one period, or always when the
-// exchange is empty (one block, not periodic).
-bool heat_fuse_ok(const b2r_handle* h, int i)
+// Time steps one heat launch may take from sub-step i with `left` to go:
+// radius 1 takes up to tblock (<= 4) per HBM pass, and no halo exchange may
+// fall between them -- within one period, or any number when the exchange is
+// empty (one block, not periodic); 1 = the one-step sweep.
+int heat_pass_steps(const b2r_handle* h, int i, int left)
 {
-    if (h->cfg.model != B2R_MODEL_HEAT || h->cfg.D != 1 || h->tune.tblock < 2) return false;
-    if (h->L.nblk == 1 && !h->L.periodic) return true;
-    return i + 1 < h->cfg.R;
+    if (h->cfg.model != B2R_MODEL_HEAT || h->cfg.D != 1 || h->tune.tblock < 2) return 1;
+    int k = std::min(std::min(h->tune.tblock, 4), left);
+    if (!(h->L.nblk == 1 && !h->L.periodic)) k = std::min(k, h->cfg.R - i);
+    return std::max(k, 1);
 }
 
 // Game of Life generations that one pass may advance from sub-step i with
@@ -271,8 +274,9 @@ void drop_graphs(b2r_handle* h)
 b2r_status substep2(b2r_handle* h, int i);
 
 // Advance n time steps from h->ts: a halo exchange at every period start
-// (skipped right after an upload, whose scatter filled the halos), two steps
-// per launch where heat_fuse_ok allows, one otherwise.
+// (skipped right after an upload, whose scatter filled the halos), several
+// steps per launch where heat_pass_steps or gol_pass_gens allow, one
+// otherwise.
 b2r_status advance(b2r_handle* h, int n)
 {
     b2r_status st;
@@ -298,10 +302,16 @@ b2r_status advance(b2r_handle* h, int n)
             h->ts += gg;
             s += gg;
             h->halos_fresh = push;
-        } else if (n - s >= 2 && heat_fuse_ok(h, i)) {
-            if ((st = substep2(h, i)) != B2R_OK) return st;
-            h->ts += 2;
-            s += 2;
+        } else if (const int k = heat_pass_steps(h, i, n - s); k >= 2) {
+            if (k == 2) {
+                if ((st = substep2(h, i)) != B2R_OK) return st;
+            } else {
+                CK(h, launch_heat_substep_tb(k, &h->tmap3[h->cur], static_cast<float*>(h->buf[1 - h->cur]), h->L,
+                                             i, h->hc, h->d_status, h->stream, h->tune.zchunk2));
+                h->cur = 1 - h->cur;
+            }
+            h->ts += k;
+            s += k;
         } else {
             if ((st = substep(h, i)) != B2R_OK) return st;
             h->ts++;
@@ -860,14 +870,17 @@ struct Scratch {
 
 }  // namespace
 
-b2r_status b2r_heat_3D_gpu_main(float* h_in, int R, int D, const char* edge_flag, int Ngx, int Ngy,
-                                int Ngz, double alpha_dt, double dx, double dy, double dz,
-                                void* cuda_stream, double* gpu_seconds)
+}  // extern "C"
+
+namespace b2r_api {
+
+b2r_status HeatBlockRun::begin(const float* h_in, int R_, int D, int edge, int Ngx, int Ngy, int Ngz_,
+                               double alpha_dt, double dx, double dy, double dz, cudaStream_t st_)
 {
-    if (!h_in) return fail(nullptr, B2R_ERR_ARG, "null h_in");
-    if (D < 1 || D > 4) return fail(nullptr, B2R_ERR_ARG, "unsupported delta %d", D);
-    if (R < 1) return fail(nullptr, B2R_ERR_ARG, "R must be >= 1");
-    const int H = R * D;
+    R = R_;
+    H = R_ * D;
+    Ngz = Ngz_;
+    st = st_;
     const int n[3] = {Ngx, Ngy, Ngz};
     int B[3];
     for (int a = 0; a < 3; ++a) {
@@ -875,48 +888,77 @@ b2r_status b2r_heat_3D_gpu_main(float* h_in, int R, int D, const char* edge_flag
         if (B[a] < 1) return fail(nullptr, B2R_ERR_ARG, "block too small for R*D = %d", H);
     }
     const int nb[3] = {1, 1, 1};
-    BlockLayout L{};
-    fill_layout(L, n, B, nb, H, 4, 0, edge_from_flags(edge_flag));
-    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    fill_layout(L, n, B, nb, H, 4, 0, edge);
     const size_t fb = (size_t)L.bstride * sizeof(float);
-    Scratch s;
-    DevBuf status_buf;
-    CK(nullptr, cudaMalloc(&s.p[0], fb));
-    CK(nullptr, cudaMalloc(&s.p[1], fb));
-    CK(nullptr, cudaMalloc(&status_buf.p, sizeof(int)));
-    int* d_status = static_cast<int*>(status_buf.p);
-    CK(nullptr, cudaMemsetAsync(d_status, 0, sizeof(int), st));
+    CK(nullptr, cudaMalloc(&buf[0], fb));
+    CK(nullptr, cudaMalloc(&buf[1], fb));
+    CK(nullptr, cudaMalloc(&status, sizeof(int)));
+    CK(nullptr, cudaMemsetAsync(status, 0, sizeof(int), st));
     // host block (dense rows of Ngx) -> pitched device rows (heat-3D.cu:590-592)
     for (int b = 0; b < 2; ++b)
-        CK(nullptr, cudaMemcpy2DAsync((float*)s.p[b] + L.xoff, L.P * sizeof(float), h_in,
+        CK(nullptr, cudaMemcpy2DAsync(static_cast<float*>(buf[b]) + L.xoff, L.P * sizeof(float), h_in,
                                       Ngx * sizeof(float), Ngx * sizeof(float), (size_t)Ngy * Ngz,
                                       cudaMemcpyHostToDevice, st));
     CUtensorMap tm[2];
     for (int b = 0; b < 2; ++b)
-        if (!make_block_tmap(&tm[b], s.p[b], L, 4, heat_box_w(), heat_box_h(D), 1))
+        if (!make_block_tmap(&tm[b], buf[b], L, 4, heat_box_w(), heat_box_h(D), 1))
             return fail(nullptr, B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed");
     const HeatCoef hc = heat_coef(D, alpha_dt, dx, dy, dz);
-    EventPair ev;
     CK(nullptr, ev.create());
     CK(nullptr, cudaEventRecord(ev.e0, st));
-    int cur = 0;
+    cur = 0;
     for (int i = 0; i < R; ++i) {   // heat-3D.cu:602-628
-        cudaError_t e = launch_heat_substep(&tm[cur], (float*)s.p[1 - cur], L, D, i, hc, d_status, st);
+        cudaError_t e = launch_heat_substep(&tm[cur], static_cast<float*>(buf[1 - cur]), L, D, i, hc,
+                                            static_cast<int*>(status), st);
         if (e != cudaSuccess) return fail(nullptr, B2R_ERR_CUDA, "heat launch: %s", cudaGetErrorString(e));
         cur = 1 - cur;
     }
     CK(nullptr, cudaEventRecord(ev.e1, st));
+    return B2R_OK;
+}
+
+b2r_status HeatBlockRun::end(float* h_out, double* gpu_seconds)
+{
     // planes [R*D, Ngz-R*D) back to the host (heat-3D.cu:633-635)
+    const int Ngx = L.n[0], Ngy = L.n[1];
     const int zc = Ngz - 2 * H;
-    CK(nullptr, cudaMemcpy2DAsync(h_in + (size_t)H * Ngx * Ngy, Ngx * sizeof(float),
-                                  (float*)s.p[cur] + L.xoff + (size_t)H * L.plane, L.P * sizeof(float),
-                                  Ngx * sizeof(float), (size_t)Ngy * zc, cudaMemcpyDeviceToHost, st));
+    CK(nullptr, cudaMemcpy2DAsync(h_out + (size_t)H * Ngx * Ngy, Ngx * sizeof(float),
+                                  static_cast<float*>(buf[cur]) + L.xoff + (size_t)H * L.plane,
+                                  L.P * sizeof(float), Ngx * sizeof(float), (size_t)Ngy * zc,
+                                  cudaMemcpyDeviceToHost, st));
     int dev_st = 0;
-    CK(nullptr, cudaMemcpyAsync(&dev_st, d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(nullptr, cudaMemcpyAsync(&dev_st, status, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(nullptr, cudaStreamSynchronize(st));
     if (gpu_seconds) *gpu_seconds = ev.seconds();
     if (dev_st != DEV_OK) return fail(nullptr, B2R_ERR_TIMEOUT, "device wait gave up (code %d)", dev_st);
     return B2R_OK;
+}
+
+HeatBlockRun::~HeatBlockRun()
+{
+    for (int i = 0; i < 2; ++i)
+        if (buf[i]) cudaFree(buf[i]);
+    if (status) cudaFree(status);
+}
+
+int edge_bits_of_flags(const char* edge_flag) { return edge_from_flags(edge_flag); }
+
+}  // namespace b2r_api
+
+extern "C" {
+
+b2r_status b2r_heat_3D_gpu_main(float* h_in, int R, int D, const char* edge_flag, int Ngx, int Ngy,
+                                int Ngz, double alpha_dt, double dx, double dy, double dz,
+                                void* cuda_stream, double* gpu_seconds)
+{
+    if (!h_in) return fail(nullptr, B2R_ERR_ARG, "null h_in");
+    if (D < 1 || D > 4) return fail(nullptr, B2R_ERR_ARG, "unsupported delta %d", D);
+    if (R < 1) return fail(nullptr, B2R_ERR_ARG, "R must be >= 1");
+    HeatBlockRun run;
+    b2r_status s = run.begin(h_in, R, D, edge_from_flags(edge_flag), Ngx, Ngy, Ngz, alpha_dt, dx, dy, dz,
+                             static_cast<cudaStream_t>(cuda_stream));
+    if (s != B2R_OK) return s;
+    return run.end(h_in, gpu_seconds);
 }
 
 b2r_status b2r_gol_3D_gpu_main(uint8_t* h_in, int R, const char* edge_flag, int Ngx, int Ngy,

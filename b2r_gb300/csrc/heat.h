@@ -37,8 +37,8 @@ struct HeatTune {
     int zchunk = 0;        // output planes per work unit; 0 = 16 (fewer for small grids)
     int ctas_per_sm = 0;   // 0 = one CTA per unit; k > 0 = persistent, k CTAs per SM
     int pdl = 1;           // programmatic dependent launch on the stream
-    int tblock = 2;        // time steps per HBM pass (2 = heat2.cu, radius 1 only)
-    int zchunk2 = 0;       // output planes per unit of the two-step kernel (0 = 16)
+    int tblock = 2;        // time steps per HBM pass, radius 1 only (2 = heat2.cu, 3-4 = heat_tb.cu)
+    int zchunk2 = 0;       // output planes per unit of the several-step kernels (0 = 16 / 64)
 };
 
 // One sub-step of every block: units (block, z-chunk, tile row, tile column)
@@ -53,5 +53,13 @@ int heat2_box_w();
 int heat2_box_h();
 cudaError_t launch_heat_substep2(const CUtensorMap* tin, float* out, const BlockLayout& L, int step_i,
                                  const HeatCoef& c, int* status, cudaStream_t st, int zchunk);
+
+// T = 3 or 4 sub-steps (step_i .. step_i+T-1) of radius 1 per launch
+// (heat_tb.cu).  The tensor map must have the box heat_tb_box_w() x
+// heat_tb_box_h().
+int heat_tb_box_w();
+int heat_tb_box_h();
+cudaError_t launch_heat_substep_tb(int T, const CUtensorMap* tin, float* out, const BlockLayout& L, int step_i,
+                                   const HeatCoef& c, int* status, cudaStream_t st, int zchunk);
 
 }  // namespace b2r

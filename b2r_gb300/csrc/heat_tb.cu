@@ -1,0 +1,422 @@
+// heat_tb.cu -- T = 3 or 4 heat time steps per HBM pass (temporal blocking),
+// radius 1.
+//
+// B2R's deep halo turned inward, deeper than heat2.cu: a CTA reads a tile of
+// the field once, advances it T sub-steps on chip and writes it once, so HBM
+// traffic per lattice-site update falls to 8/T bytes.  Bit-identical to T
+// launches of the plain sweep: every cell runs the same float operations on
+// the same inputs (heat-3D.cu:228-231 folded as in heat.cu).
+//
+// Shape.  CTA = 16 warps; thread = 4 consecutive x cells (float4) of 2 rows;
+// the CTA computes 128 x 32 cells per stage.  Per input plane p (one TMA 4-D
+// box of 136 x 34 cells into an S-deep mbarrier ring: the computed cells, 4
+// more on each side in x for the first stage's edge neighbours, 1 more row on
+// each side in y):
+//   stage s (sub-step i+s-1), s = 1..T, computes plane p-s: z neighbours from
+//   a 3-plane float4 register queue of stage s-1 (its newest plane computed
+//   in this same iteration), x neighbours by warp shuffles (stage 1's edge
+//   lanes read the box's extra columns), y neighbours from the thread's other
+//   row or, across warps, from stage s-1's plane in shared memory (stage 1:
+//   the input box; later stages: a 2-plane exchange buffer written one
+//   iteration earlier), so one barrier per plane orders everything;
+//   stage T stores lanes 1..30 of rows T-1 .. 32-T to HBM (float4 stores).
+// The valid region shrinks by one cell per stage on each side; cells outside
+// a stage's window keep their value (fixed shell, B2R window).  With T = 4
+// the input queue would not fit the register budget, so stage 1 reads its
+// three input planes from the ring (two more slots).
+#include "b2r_common.cuh"
+#include "heat.h"
+
+namespace b2r {
+namespace {
+
+constexpr int kWarps = 16;
+constexpr int kThreads = 32 * kWarps;   // 512
+constexpr int kRows = 2 * kWarps;       // computed rows per stage
+constexpr int kBW = 136;                // box width (cells)
+constexpr int kBH = kRows + 2;          // box height (rows)
+constexpr int kSlot = 4640;             // floats per ring slot: 136 x 34 = 4624, rounded to 128 B
+constexpr int kXPlane = 128 * kRows;    // floats per exchange plane
+constexpr int kOutW = 120;              // output cells per tile row (lanes 1..30)
+
+template <int T>
+struct TbCfg {
+    static constexpr bool INQ = T <= 3;                // input planes queued in registers
+    static constexpr int S = INQ ? 4 : 6;              // ring slots
+    static constexpr int OH = kRows + 2 - 2 * T;       // output rows: T-1 .. kRows-T
+    static constexpr int NQ = INQ ? T : T - 1;         // register queues (stage 0 = input)
+    static constexpr size_t SMEM =
+        size_t(S) * kSlot * 4 + size_t(T - 1) * 2 * kXPlane * 4 + S * 8 + 16 + 128;
+};
+
+struct TbSched {
+    int ntx, nty, nzc, Lz;
+    int out0;          // storage x of the first output cell of tile column 0
+    long long U;
+};
+
+__device__ __forceinline__ void pdl_wait_tb() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger_tb() { asm volatile("griddepcontrol.launch_dependents;"); }
+
+// one folded D = 1 update of 4 cells (the order of heat2.cu and heat.cu):
+// c centre, l / r = the cells left of x and right of x+3, ym / yp / zm / zp
+// neighbour float4s
+__device__ __forceinline__ float4 upd_tb(const HeatCoef& C, float4 c, float l, float r, float4 ym,
+                                         float4 yp, float4 zm, float4 zp)
+{
+    float4 o;
+    o.x = C.a0 * c.x;
+    o.y = C.a0 * c.y;
+    o.z = C.a0 * c.z;
+    o.w = C.a0 * c.w;
+    o.x = fmaf(C.ax[0], l + c.y, o.x);
+    o.y = fmaf(C.ax[0], c.x + c.z, o.y);
+    o.z = fmaf(C.ax[0], c.y + c.w, o.z);
+    o.w = fmaf(C.ax[0], c.z + r, o.w);
+    o.x = fmaf(C.ay[0], ym.x + yp.x, o.x);
+    o.y = fmaf(C.ay[0], ym.y + yp.y, o.y);
+    o.z = fmaf(C.ay[0], ym.z + yp.z, o.z);
+    o.w = fmaf(C.ay[0], ym.w + yp.w, o.w);
+    o.x = fmaf(C.az[0], zm.x + zp.x, o.x);
+    o.y = fmaf(C.az[0], zm.y + zp.y, o.y);
+    o.z = fmaf(C.az[0], zm.z + zp.z, o.z);
+    o.w = fmaf(C.az[0], zm.w + zp.w, o.w);
+    return o;
+}
+
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+
+// cells of a stage outside its window keep their value: bit rr*4+j of m is
+// cell j of row rr
+__device__ __forceinline__ float4 keep(unsigned m, int rr, float4 v, float4 c)
+{
+    const unsigned b = m >> (4 * rr);
+    return make_float4((b & 1u) ? v.x : c.x, (b & 2u) ? v.y : c.y, (b & 4u) ? v.z : c.z, (b & 8u) ? v.w : c.w);
+}
+
+template <int T>
+struct TbCtx {
+    using Cfg = TbCfg<T>;
+    float4 q[Cfg::NQ][3][2];   // [queue][slot][row]: queue k holds stage k (INQ) or stage k+1
+    const float* ring;
+    float* xch;                 // [stage 1..T-1][parity] exchange planes
+    uint64_t* bar;
+    int* abort_flag;
+    float* outb;                // out + block + this thread's storage x
+    const CUtensorMap* tmap;
+    HeatCoef C;
+    long long plane, P;
+    unsigned gp;
+    int np, first, zs, ze, X0, Y0, blk, ya, warp, lane, tid;
+    int loz[T + 1], hiz[T + 1];
+    unsigned mxy[T + 1];        // per stage: 8 bits of (row, cell) inside the xy window
+    unsigned mst;               // cells stored by stage T (its window, output lanes and rows)
+    unsigned issued_hi;
+    bool aborted;
+    unsigned stop;
+};
+
+// queue index of stage k's output (k >= 1) and of the input (k = 0)
+template <int T>
+__device__ __forceinline__ constexpr int qi(int k) { return TbCfg<T>::INQ ? k : k - 1; }
+
+template <int T, int PH>
+__device__ __forceinline__ void tb_iter(TbCtx<T>& c, int pr)
+{
+    using Cfg = TbCfg<T>;
+    constexpr int S = Cfg::S;
+    constexpr int NEW = PH, CUR = (PH + 2) % 3, OLD = (PH + 1) % 3;   // planes p, p-1, p-2 of a queue
+    const unsigned g = c.gp + pr;
+    if (!mbar_wait_bounded(&c.bar[g % S], (g / S) & 1)) *c.abort_flag = 1;
+    const int p = c.first + pr;
+    const int wrow = 2 * c.warp;
+    if constexpr (Cfg::INQ) {
+        const float* pl = c.ring + (g % S) * kSlot + 4 + 4 * c.lane;
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr) c.q[0][NEW][rr] = ld4(pl + (wrow + 1 + rr) * kBW);
+    }
+    // ---- stage 1 at plane p-1
+    if (pr >= 2) {
+        const int z = p - 1;
+        const float* pc = c.ring + ((g - 1) % S) * kSlot;
+        const float4 up = ld4(pc + wrow * kBW + 4 + 4 * c.lane);
+        const float4 dn = ld4(pc + (wrow + 3) * kBW + 4 + 4 * c.lane);
+        float4 in[3][2];     // input planes p-2, p-1, p of this thread's rows
+        if constexpr (Cfg::INQ) {
+#pragma unroll
+            for (int rr = 0; rr < 2; ++rr) {
+                in[0][rr] = c.q[0][OLD][rr];
+                in[1][rr] = c.q[0][CUR][rr];
+                in[2][rr] = c.q[0][NEW][rr];
+            }
+        } else {
+            const float* p0 = c.ring + ((g - 2) % S) * kSlot + 4 + 4 * c.lane;
+            const float* p2 = c.ring + (g % S) * kSlot + 4 + 4 * c.lane;
+#pragma unroll
+            for (int rr = 0; rr < 2; ++rr) {
+                in[0][rr] = ld4(p0 + (wrow + 1 + rr) * kBW);
+                in[1][rr] = ld4(pc + (wrow + 1 + rr) * kBW + 4 + 4 * c.lane);
+                in[2][rr] = ld4(p2 + (wrow + 1 + rr) * kBW);
+            }
+        }
+        const bool zin = z >= c.loz[1] && z <= c.hiz[1];
+        float* xo = c.xch + (size_t)(z & 1) * kXPlane;
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr) {
+            const float4 ce = in[1][rr];
+            float l = __shfl_up_sync(0xffffffffu, ce.w, 1);
+            float r = __shfl_down_sync(0xffffffffu, ce.x, 1);
+            if (c.lane == 0) l = pc[(wrow + 1 + rr) * kBW + 3];
+            if (c.lane == 31) r = pc[(wrow + 1 + rr) * kBW + 132];
+            const float4 ym = rr == 0 ? up : in[1][0];
+            const float4 yp = rr == 0 ? in[1][1] : dn;
+            float4 v = upd_tb(c.C, ce, l, r, ym, yp, in[0][rr], in[2][rr]);
+            if (!zin) v = ce;
+            else if (c.mxy[1] != 0xFFu) v = keep(c.mxy[1], rr, v, ce);
+            c.q[qi<T>(1)][NEW][rr] = v;
+            if constexpr (T > 1) st4(xo + (wrow + rr) * 128 + 4 * c.lane, v);
+        }
+    }
+    // ---- stages 2..T at planes p-2 .. p-T
+#pragma unroll
+    for (int s = 2; s <= T; ++s) {
+        if (pr >= 2 * s) {
+            const int z = p - s;
+            const int qa = qi<T>(s - 1);
+            const float* xi = c.xch + (size_t)((s - 2) * 2 + (z & 1)) * kXPlane + 4 * c.lane;
+            const int ru = wrow - 1 < 0 ? 0 : wrow - 1;
+            const int rd = wrow + 2 >= kRows ? kRows - 1 : wrow + 2;
+            const float4 up = ld4(xi + ru * 128);
+            const float4 dn = ld4(xi + rd * 128);
+            const bool zin = z >= c.loz[s] && z <= c.hiz[s];
+            float4 res[2];
+#pragma unroll
+            for (int rr = 0; rr < 2; ++rr) {
+                const float4 ce = c.q[qa][CUR][rr];
+                const float l = __shfl_up_sync(0xffffffffu, ce.w, 1);
+                const float r = __shfl_down_sync(0xffffffffu, ce.x, 1);
+                const float4 ym = rr == 0 ? up : c.q[qa][CUR][0];
+                const float4 yp = rr == 0 ? c.q[qa][CUR][1] : dn;
+                float4 v = upd_tb(c.C, ce, l, r, ym, yp, c.q[qa][OLD][rr], c.q[qa][NEW][rr]);
+                if (!zin) v = ce;
+                else if (c.mxy[s] != 0xFFu) v = keep(c.mxy[s], rr, v, ce);
+                res[rr] = v;
+            }
+            if (s < T) {
+                float* xo = c.xch + (size_t)((s - 1) * 2 + (z & 1)) * kXPlane + 4 * c.lane;
+#pragma unroll
+                for (int rr = 0; rr < 2; ++rr) {
+                    c.q[qi<T>(s)][NEW][rr] = res[rr];
+                    st4(xo + (wrow + rr) * 128, res[rr]);
+                }
+            } else if (z >= c.zs && z <= c.ze && c.mst) {
+                float* dst = c.outb + (long long)z * c.plane + (long long)c.ya * c.P;
+#pragma unroll
+                for (int rr = 0; rr < 2; ++rr) {
+                    const unsigned b = c.mst >> (4 * rr);
+                    float* d = dst + rr * c.P;
+                    if ((b & 15u) == 15u) {
+                        st4(d, res[rr]);
+                    } else if (b & 15u) {
+                        if (b & 1u) d[0] = res[rr].x;
+                        if (b & 2u) d[1] = res[rr].y;
+                        if (b & 4u) d[2] = res[rr].z;
+                        if (b & 8u) d[3] = res[rr].w;
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (*c.abort_flag) {
+        c.aborted = true;
+        c.stop = g;
+        return;
+    }
+    // the oldest plane still held is no longer needed: refill its slot
+    constexpr int lag = Cfg::INQ ? 1 : 2;
+    if (pr >= lag) {
+        const int nxt = pr - lag + S;
+        if (nxt < c.np) {
+            const unsigned g2 = c.gp + nxt;
+            if (c.tid == 0) {
+                mbar_expect_tx(&c.bar[g2 % S], kBW * kBH * 4);
+                tma_load_4d(const_cast<float*>(c.ring) + (g2 % S) * kSlot, c.tmap, c.X0 - 4, c.Y0 - 1,
+                            c.first + nxt, c.blk, &c.bar[g2 % S]);
+            }
+            c.issued_hi = g2 + 1;
+        }
+    }
+}
+
+template <int T>
+__global__ void __launch_bounds__(kThreads, 1)
+heat_tb_kernel(const __grid_constant__ CUtensorMap tin, float* __restrict__ out, const BlockLayout L,
+               const int step_i, const HeatCoef C, const TbSched sch, int* __restrict__ status)
+{
+    using Cfg = TbCfg<T>;
+    constexpr int S = Cfg::S;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    TbCtx<T> c;
+    float* ring = reinterpret_cast<float*>(smem_raw + ((128 - (smem_u32(smem_raw) & 127)) & 127));
+    c.ring = ring;
+    c.xch = ring + S * kSlot;
+    c.bar = reinterpret_cast<uint64_t*>(c.xch + (T - 1) * 2 * kXPlane);
+    c.abort_flag = reinterpret_cast<int*>(c.bar + S);
+    c.tid = threadIdx.x;
+    c.lane = c.tid & 31;
+    c.warp = c.tid >> 5;
+    c.tmap = &tin;
+    c.C = C;
+    c.plane = L.plane;
+    c.P = L.P;
+    if (c.tid == 0) {
+        *c.abort_flag = 0;
+        for (int s = 0; s < S; ++s) mbar_init(&c.bar[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    pdl_wait_tb();
+    pdl_trigger_tb();
+
+    c.gp = 0;
+    c.issued_hi = 0;
+    c.stop = 0;
+    c.aborted = false;
+    for (long long u = blockIdx.x; u < sch.U && !c.aborted; u += gridDim.x) {
+        const int tx = (int)(u % sch.ntx);
+        long long rem = u / sch.ntx;
+        const int ty = (int)(rem % sch.nty);
+        rem /= sch.nty;
+        const int zc = (int)(rem % sch.nzc);
+        c.blk = (int)(rem / sch.nzc);
+        const int edge = edge_bits(L, c.blk);
+        int lo[T + 1][3], hi[T + 1][3];
+#pragma unroll
+        for (int s = 1; s <= T; ++s)
+#pragma unroll
+            for (int a = 0; a < 3; ++a) stage_region(L, edge, a, step_i + s, lo[s][a], hi[s][a]);
+        c.X0 = sch.out0 - 4 + tx * kOutW;               // storage x of lane 0's first cell
+        c.Y0 = 1 + ty * Cfg::OH - (T - 1);              // block y of computed row 0
+        const int zi0 = zc * sch.Lz;
+        c.zs = max(1 + zi0, lo[T][2]);
+        c.ze = min(zi0 + sch.Lz, hi[T][2]);             // output planes [zs, ze]
+        if (c.zs > c.ze) continue;
+        const int ox0 = c.X0 + 4 - L.xoff, oy0 = c.Y0 + T - 1;   // first output cell (block x, y)
+        if (ox0 > hi[T][0] || ox0 + kOutW - 1 < lo[T][0]) continue;
+        if (oy0 > hi[T][1] || oy0 + Cfg::OH - 1 < lo[T][1]) continue;
+        c.first = c.zs - T;
+        c.np = c.ze + T - c.first + 1;
+#pragma unroll
+        for (int s = 1; s <= T; ++s) {
+            c.loz[s] = lo[s][2];
+            c.hiz[s] = hi[s][2];
+        }
+        if (c.tid == 0)
+            for (int s = 0; s < S && s < c.np; ++s) {
+                const unsigned g = c.gp + s;
+                mbar_expect_tx(&c.bar[g % S], kBW * kBH * 4);
+                tma_load_4d(ring + (g % S) * kSlot, &tin, c.X0 - 4, c.Y0 - 1, c.first + s, c.blk, &c.bar[g % S]);
+            }
+        c.issued_hi = c.gp + min(S, c.np);
+
+        const int xb = c.X0 + 4 * c.lane - L.xoff;      // block x of this thread's first cell
+        c.ya = c.Y0 + 2 * c.warp;                       // block y of this thread's first row
+#pragma unroll
+        for (int s = 1; s <= T; ++s) {
+            unsigned m = 0;
+#pragma unroll
+            for (int rr = 0; rr < 2; ++rr)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const bool in = xb + j >= lo[s][0] && xb + j <= hi[s][0] && c.ya + rr >= lo[s][1] &&
+                                    c.ya + rr <= hi[s][1];
+                    m |= (in ? 1u : 0u) << (4 * rr + j);
+                }
+            c.mxy[s] = m;
+        }
+        unsigned mst = c.mxy[T];
+        if (c.lane < 1 || c.lane > 30) mst = 0;
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr) {
+            const int row = 2 * c.warp + rr;
+            if (row < T - 1 || row > kRows - T) mst &= ~(15u << (4 * rr));
+        }
+        c.mst = mst;
+        c.outb = out + (long long)c.blk * L.bstride + c.X0 + 4 * c.lane;
+
+        for (int pr = 0; pr < c.np;) {
+            tb_iter<T, 0>(c, pr++);
+            if (c.aborted || pr >= c.np) break;
+            tb_iter<T, 1>(c, pr++);
+            if (c.aborted || pr >= c.np) break;
+            tb_iter<T, 2>(c, pr++);
+            if (c.aborted) break;
+        }
+        if (!c.aborted) c.gp += c.np;
+    }
+    if (c.aborted && c.tid == 0) {
+        report(status, DEV_TIMEOUT);
+        for (unsigned g = c.stop; g < c.issued_hi; ++g)
+            mbar_wait_bounded(&c.bar[g % S], (g / S) & 1, 100000000ull);
+    }
+}
+
+template <int T>
+cudaError_t launch_tb(const CUtensorMap* tin, float* out, const BlockLayout& L, int step_i, const HeatCoef& c,
+                      int* status, cudaStream_t st, int zchunk)
+{
+    using Cfg = TbCfg<T>;
+    static KernelSetup setup;
+    int resident = 0;
+    if (cudaError_t e = kernel_setup(setup, heat_tb_kernel<T>, kThreads, Cfg::SMEM, nullptr, &resident)) return e;
+    TbSched sch;
+    sch.out0 = (L.xoff + 1) & ~3;                   // aligned float4 holding x = 1
+    const int xend = L.xoff + L.n[0] - 1;           // storage x one past the last region cell
+    sch.ntx = (xend - sch.out0 + kOutW - 1) / kOutW;
+    sch.nty = (L.n[1] - 2 + Cfg::OH - 1) / Cfg::OH;
+    const int NZ = L.n[2] - 2;
+    const long long tiles = (long long)sch.ntx * sch.nty * L.nblk;
+    int Lz = zchunk > 0 ? zchunk : 64;
+    if (zchunk <= 0 && tiles * ((NZ + Lz - 1) / Lz) < 2LL * resident) {
+        long long nzc = (2LL * resident + tiles - 1) / tiles;
+        if (nzc > NZ / 8) nzc = NZ / 8 > 0 ? NZ / 8 : 1;
+        Lz = (int)((NZ + nzc - 1) / nzc);
+    }
+    if (Lz > NZ) Lz = NZ;
+    sch.Lz = Lz;
+    sch.nzc = (NZ + Lz - 1) / Lz;
+    sch.U = tiles * sch.nzc;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(sch.U < 1 ? 1 : sch.U));
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = Cfg::SMEM;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, heat_tb_kernel<T>, *tin, out, L, step_i, c, sch, status);
+    count_launches(1);
+    if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+int heat_tb_box_w() { return kBW; }
+int heat_tb_box_h() { return kBH; }
+
+cudaError_t launch_heat_substep_tb(int T, const CUtensorMap* tin, float* out, const BlockLayout& L, int step_i,
+                                   const HeatCoef& c, int* status, cudaStream_t st, int zchunk)
+{
+    switch (T) {
+    case 3: return launch_tb<3>(tin, out, L, step_i, c, status, st, zchunk);
+    case 4: return launch_tb<4>(tin, out, L, step_i, c, status, st, zchunk);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace b2r

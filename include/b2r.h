@@ -130,11 +130,13 @@ enum {
     B2R_TUNE_ZCHUNK = 1,       /* planes per work unit of the one-step sweep (0 = 16) */
     B2R_TUNE_CTAS_PER_SM = 2,  /* 0 = one CTA per unit, k = persistent k CTAs per SM */
     B2R_TUNE_PDL = 3,          /* programmatic dependent launch on / off */
-    B2R_TUNE_TBLOCK = 4,       /* time steps per pass: >= 2 (default 2) lets heat of radius 1
-                                  take two steps per HBM pass and Game of Life (bit-sliced cells)
-                                  up to four generations per L2 pass, never across a halo
-                                  exchange; byte cells need >= 4; 1 = one step per pass */
-    B2R_TUNE_ZCHUNK2 = 5,      /* planes per work unit of the two-step sweep (0 = 16) */
+    B2R_TUNE_TBLOCK = 4,       /* time steps per pass: heat of radius 1 takes up to tblock (2, 3
+                                  or 4; default 2) steps per HBM pass and Game of Life
+                                  (bit-sliced cells, tblock >= 2) up to four generations per L2
+                                  pass, never across a halo exchange; byte cells need >= 4;
+                                  1 = one step per pass */
+    B2R_TUNE_ZCHUNK2 = 5,      /* planes per work unit of the several-step heat sweeps (0 = 16
+                                  for two steps, 64 for three or four) */
     B2R_TUNE_EQWP_FUSED = 6,   /* staggered elastic wave: 1 = one-pass step, 0 = the velocity
                                   and stress stages as two passes (default); bit-identical */
     B2R_TUNE_GOL_BYTES = 7,    /* Game of Life one-generation kernel: 0 = bit-sliced cells
@@ -213,6 +215,29 @@ b2r_status b2r_heat_3D_gpu_main(float* h_in, int R, int D, const char* edge_flag
                                 int Ngx, int Ngy, int Ngz, double alpha_dt,
                                 double dx, double dy, double dz, void* cuda_stream,
                                 double* gpu_seconds);
+/* heat_3D_cpu_main (heat-3D.hpp:12, heat-3D.cpp:136-184) on the host cores:
+ * the contract of b2r_heat_3D_gpu_main (same arguments, edge flags and
+ * copy-back of planes [R*D, Ngz-R*D)), computed with the GPU sweep's float
+ * operations in its order, so the result is bit-identical to
+ * b2r_heat_3D_gpu_main's.  nthreads <= 0: every hardware thread.
+ * *cpu_seconds (may be NULL) gets the wall time (heat-3D.cpp:141,181).
+ * Touches no GPU; no GPU entry falls back to it. */
+b2r_status b2r_heat_3D_cpu_main(float* h_in, int R, int D, const char* edge_flag, int Ngx, int Ngy, int Ngz,
+                                double alpha_dt, double dx, double dy, double dz, int nthreads,
+                                double* cpu_seconds);
+/* The hybrid CPU+GPU form of one block (heat-3D.cpp:47,170): the block is
+ * cut along z, the host cores compute the last cpu_planes result planes and
+ * the GPU the others, at the same time; each side holds R*D planes of the
+ * other's beyond the cut, so the R sub-steps need no exchange between them.
+ * The result is bit-identical to b2r_heat_3D_gpu_main's.  cpu_planes = 0 is
+ * the GPU alone, cpu_planes >= Ngz - 2*R*D the host alone.  A part's deep
+ * halo never crosses a fixed z face: with edge_flag[2] = 1 a positive
+ * cpu_planes below R*D is raised to R*D, and with edge_flag[2] = -1 a split
+ * that would leave the GPU fewer than R*D result planes gives the host the
+ * whole block.  *seconds (may be NULL) gets the wall time of the call. */
+b2r_status b2r_heat_3D_hybrid_main(float* h_in, int R, int D, const char* edge_flag, int Ngx, int Ngy, int Ngz,
+                                   double alpha_dt, double dx, double dy, double dz, int cpu_planes,
+                                   int nthreads, void* cuda_stream, double* seconds);
 /* gol_3D_gpu_main (gol-3D.cu:119): R generations on one padded host block,
  * region [i+1, N-2-i]; the whole block is copied back (gol-3D.cu:149). */
 b2r_status b2r_gol_3D_gpu_main(uint8_t* h_in, int R, const char* edge_flag, int Ngx,
@@ -225,12 +250,15 @@ b2r_status b2r_gol_3D_gpu_main(uint8_t* h_in, int R, const char* edge_flag, int 
  * Ngx*Ngy*Ngz floats (may be the same block); on return d_out holds d_in
  * with planes [R*D, Ngz-R*D) replaced by the result of R sub-steps.  The
  * ping-pong blocks live in a fixed 32 MiB device array inside the library
- * (held by every GPU that loads it until exit): blocks whose padded size
- * exceeds 4,194,304 cells per buffer (about 160^3) are rejected with
- * B2R_ERR_ARG and a message on stderr.  All calls share that array, so calls
- * that overlap on the GPU race; the first call on each device looks up the
- * array's address and should come before any stream capture.  Synchronous
- * on cuda_stream; allocates nothing. */
+ * (held by every GPU that loads it until exit): a block is accepted when
+ * P * Ngy * Ngz <= 4,194,304 cells, P being its row pitch padded as
+ * b2r_heat_3D_gpu_main pads it (Ngx plus at least 12 cells, rounded up to a
+ * multiple of 32) -- cubes up to 147^3 at R*D = 1; larger blocks are
+ * rejected with B2R_ERR_ARG and a message on stderr.  All calls share that
+ * array, so calls that overlap on the GPU race.  Every call looks up the
+ * array's address on the current device; the first call on a device also
+ * loads the library's device code there and should come before any stream
+ * capture.  Synchronous on cuda_stream; allocates nothing. */
 b2r_status b2r_heat_3D_gpu_main_noalloc(const float* d_in, float* d_out, int R, int D,
                                         const char* edge_flag, int Ngx, int Ngy, int Ngz,
                                         double alpha_dt, double dx, double dy, double dz,
