@@ -303,7 +303,7 @@ b2r_status advance(b2r_handle* h, int n)
             s += gg;
             h->halos_fresh = push;
         } else if (const int k = heat_pass_steps(h, i, n - s); k >= 2) {
-            if (k == 2) {
+            if (k == 2 && !h->tune.tb16) {
                 if ((st = substep2(h, i)) != B2R_OK) return st;
             } else {
                 CK(h, launch_heat_substep_tb(k, &h->tmap3[h->cur], static_cast<float*>(h->buf[1 - h->cur]), h->L,

@@ -39,6 +39,7 @@ struct HeatTune {
     int pdl = 1;           // programmatic dependent launch on the stream
     int tblock = 2;        // time steps per HBM pass, radius 1 only (2 = heat2.cu, 3-4 = heat_tb.cu)
     int zchunk2 = 0;       // output planes per unit of the several-step kernels (0 = 16 / 64)
+    int tb16 = 0;          // two steps per pass: 0 = heat2.cu (8-warp CTAs), 1 = heat_tb.cu (16 warps)
 };
 
 // One sub-step of every block: units (block, z-chunk, tile row, tile column)
@@ -54,7 +55,7 @@ int heat2_box_h();
 cudaError_t launch_heat_substep2(const CUtensorMap* tin, float* out, const BlockLayout& L, int step_i,
                                  const HeatCoef& c, int* status, cudaStream_t st, int zchunk);
 
-// T = 3 or 4 sub-steps (step_i .. step_i+T-1) of radius 1 per launch
+// T = 2, 3 or 4 sub-steps (step_i .. step_i+T-1) of radius 1 per launch
 // (heat_tb.cu).  The tensor map must have the box heat_tb_box_w() x
 // heat_tb_box_h().
 int heat_tb_box_w();

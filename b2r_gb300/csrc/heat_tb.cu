@@ -1,5 +1,5 @@
-// heat_tb.cu -- T = 3 or 4 heat time steps per HBM pass (temporal blocking),
-// radius 1.
+// heat_tb.cu -- T = 2, 3 or 4 heat time steps per HBM pass (temporal
+// blocking), radius 1.
 //
 // B2R's deep halo turned inward, deeper than heat2.cu: a CTA reads a tile of
 // the field once, advances it T sub-steps on chip and writes it once, so HBM
@@ -20,10 +20,13 @@
 //   the input box; later stages: a 2-plane exchange buffer written one
 //   iteration earlier), so one barrier per plane orders everything;
 //   stage T stores lanes 1..30 of rows T-1 .. 32-T to HBM (float4 stores).
-// The valid region shrinks by one cell per stage on each side; cells outside
-// a stage's window keep their value (fixed shell, B2R window).  With T = 4
+// The valid region shrinks by one cell per stage on each side; on fixed faces
+// the shell layer next to the window keeps its value at every stage
+// (restore(); nothing else outside a window can reach a stored cell).  With T = 4
 // the input queue would not fit the register budget, so stage 1 reads its
 // three input planes from the ring (two more slots).
+#include <climits>
+
 #include "b2r_common.cuh"
 #include "heat.h"
 
@@ -87,12 +90,19 @@ __device__ __forceinline__ float4 upd_tb(const HeatCoef& C, float4 c, float l, f
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 
-// cells of a stage outside its window keep their value: bit rr*4+j of m is
-// cell j of row rr
-__device__ __forceinline__ float4 keep(unsigned m, int rr, float4 v, float4 c)
+// Which cells must keep their value.  A stage's window shrinks by one cell
+// per step on an interior face, so in-window cells of a stage use only
+// in-window cells of the stage before, and whatever the out-of-window cells
+// hold never reaches a stored cell.  On a fixed face the window stays put at
+// the shell depth H, and the window's first cells use the shell layer next
+// to it (cell H-1, or n-H on the high side): that layer must keep its value
+// at every stage.  Deeper shell cells and cells beyond the block are never
+// used.  So the only mask is that layer: a plane (the same for the whole
+// CTA), a row (the same for the whole warp) or, in x, cells of one lane;
+// bit j of m is cell j of the thread's 4.
+__device__ __forceinline__ float4 restore_x(unsigned m, float4 v, float4 c)
 {
-    const unsigned b = m >> (4 * rr);
-    return make_float4((b & 1u) ? v.x : c.x, (b & 2u) ? v.y : c.y, (b & 4u) ? v.z : c.z, (b & 8u) ? v.w : c.w);
+    return make_float4((m & 1u) ? c.x : v.x, (m & 2u) ? c.y : v.y, (m & 4u) ? c.z : v.z, (m & 8u) ? c.w : v.w);
 }
 
 template <int T>
@@ -109,8 +119,9 @@ struct TbCtx {
     long long plane, P;
     unsigned gp;
     int np, first, zs, ze, X0, Y0, blk, ya, warp, lane, tid;
-    int loz[T + 1], hiz[T + 1];
-    unsigned mxy[T + 1];        // per stage: 8 bits of (row, cell) inside the xy window
+    int zk0, zk1;               // the fixed-shell layer planes (restored at every stage), or INT_MIN
+    bool yk[2];                 // this thread's rows in the fixed-shell layer
+    unsigned xkm;               // this thread's cells in the fixed-shell layer in x (restore_x())
     unsigned mst;               // cells stored by stage T (its window, output lanes and rows)
     unsigned issued_hi;
     bool aborted;
@@ -121,7 +132,8 @@ struct TbCtx {
 template <int T>
 __device__ __forceinline__ constexpr int qi(int k) { return TbCfg<T>::INQ ? k : k - 1; }
 
-template <int T, int PH>
+// MX: the unit's tile touches a fixed x face (some lane holds a shell cell)
+template <int T, int PH, bool MX>
 __device__ __forceinline__ void tb_iter(TbCtx<T>& c, int pr)
 {
     using Cfg = TbCfg<T>;
@@ -160,7 +172,7 @@ __device__ __forceinline__ void tb_iter(TbCtx<T>& c, int pr)
                 in[2][rr] = ld4(p2 + (wrow + 1 + rr) * kBW);
             }
         }
-        const bool zin = z >= c.loz[1] && z <= c.hiz[1];
+        const bool zk = z == c.zk0 || z == c.zk1;
         float* xo = c.xch + (size_t)(z & 1) * kXPlane;
 #pragma unroll
         for (int rr = 0; rr < 2; ++rr) {
@@ -172,8 +184,8 @@ __device__ __forceinline__ void tb_iter(TbCtx<T>& c, int pr)
             const float4 ym = rr == 0 ? up : in[1][0];
             const float4 yp = rr == 0 ? in[1][1] : dn;
             float4 v = upd_tb(c.C, ce, l, r, ym, yp, in[0][rr], in[2][rr]);
-            if (!zin) v = ce;
-            else if (c.mxy[1] != 0xFFu) v = keep(c.mxy[1], rr, v, ce);
+            if (zk || c.yk[rr]) v = ce;
+            else if (MX && c.xkm) v = restore_x(c.xkm, v, ce);
             c.q[qi<T>(1)][NEW][rr] = v;
             if constexpr (T > 1) st4(xo + (wrow + rr) * 128 + 4 * c.lane, v);
         }
@@ -189,7 +201,7 @@ __device__ __forceinline__ void tb_iter(TbCtx<T>& c, int pr)
             const int rd = wrow + 2 >= kRows ? kRows - 1 : wrow + 2;
             const float4 up = ld4(xi + ru * 128);
             const float4 dn = ld4(xi + rd * 128);
-            const bool zin = z >= c.loz[s] && z <= c.hiz[s];
+            const bool zk = s < T && (z == c.zk0 || z == c.zk1);   // stage T stores no shell cell
             float4 res[2];
 #pragma unroll
             for (int rr = 0; rr < 2; ++rr) {
@@ -199,8 +211,10 @@ __device__ __forceinline__ void tb_iter(TbCtx<T>& c, int pr)
                 const float4 ym = rr == 0 ? up : c.q[qa][CUR][0];
                 const float4 yp = rr == 0 ? c.q[qa][CUR][1] : dn;
                 float4 v = upd_tb(c.C, ce, l, r, ym, yp, c.q[qa][OLD][rr], c.q[qa][NEW][rr]);
-                if (!zin) v = ce;
-                else if (c.mxy[s] != 0xFFu) v = keep(c.mxy[s], rr, v, ce);
+                if (s < T) {
+                    if (zk || c.yk[rr]) v = ce;
+                    else if (MX && c.xkm) v = restore_x(c.xkm, v, ce);
+                }
                 res[rr] = v;
             }
             if (s < T) {
@@ -250,6 +264,19 @@ __device__ __forceinline__ void tb_iter(TbCtx<T>& c, int pr)
     }
 }
 
+template <int T, bool MX>
+__device__ __forceinline__ void tb_unit(TbCtx<T>& c)
+{
+    for (int pr = 0; pr < c.np;) {
+        tb_iter<T, 0, MX>(c, pr++);
+        if (c.aborted || pr >= c.np) break;
+        tb_iter<T, 1, MX>(c, pr++);
+        if (c.aborted || pr >= c.np) break;
+        tb_iter<T, 2, MX>(c, pr++);
+        if (c.aborted) break;
+    }
+}
+
 template <int T>
 __global__ void __launch_bounds__(kThreads, 1)
 heat_tb_kernel(const __grid_constant__ CUtensorMap tin, float* __restrict__ out, const BlockLayout L,
@@ -292,27 +319,23 @@ heat_tb_kernel(const __grid_constant__ CUtensorMap tin, float* __restrict__ out,
         const int zc = (int)(rem % sch.nzc);
         c.blk = (int)(rem / sch.nzc);
         const int edge = edge_bits(L, c.blk);
-        int lo[T + 1][3], hi[T + 1][3];
+        int lo[3], hi[3];           // window of the last stage: the stored cells
 #pragma unroll
-        for (int s = 1; s <= T; ++s)
-#pragma unroll
-            for (int a = 0; a < 3; ++a) stage_region(L, edge, a, step_i + s, lo[s][a], hi[s][a]);
+        for (int a = 0; a < 3; ++a) stage_region(L, edge, a, step_i + T, lo[a], hi[a]);
         c.X0 = sch.out0 - 4 + tx * kOutW;               // storage x of lane 0's first cell
         c.Y0 = 1 + ty * Cfg::OH - (T - 1);              // block y of computed row 0
         const int zi0 = zc * sch.Lz;
-        c.zs = max(1 + zi0, lo[T][2]);
-        c.ze = min(zi0 + sch.Lz, hi[T][2]);             // output planes [zs, ze]
+        c.zs = max(1 + zi0, lo[2]);
+        c.ze = min(zi0 + sch.Lz, hi[2]);             // output planes [zs, ze]
         if (c.zs > c.ze) continue;
         const int ox0 = c.X0 + 4 - L.xoff, oy0 = c.Y0 + T - 1;   // first output cell (block x, y)
-        if (ox0 > hi[T][0] || ox0 + kOutW - 1 < lo[T][0]) continue;
-        if (oy0 > hi[T][1] || oy0 + Cfg::OH - 1 < lo[T][1]) continue;
+        if (ox0 > hi[0] || ox0 + kOutW - 1 < lo[0]) continue;
+        if (oy0 > hi[1] || oy0 + Cfg::OH - 1 < lo[1]) continue;
         c.first = c.zs - T;
         c.np = c.ze + T - c.first + 1;
-#pragma unroll
-        for (int s = 1; s <= T; ++s) {
-            c.loz[s] = lo[s][2];
-            c.hiz[s] = hi[s][2];
-        }
+        // the fixed-shell layer next to the window on fixed faces (restore())
+        c.zk0 = ((edge >> 4) & 1) ? L.H - 1 : INT_MIN;
+        c.zk1 = ((edge >> 5) & 1) ? L.n[2] - L.H : INT_MIN;
         if (c.tid == 0)
             for (int s = 0; s < S && s < c.np; ++s) {
                 const unsigned g = c.gp + s;
@@ -323,20 +346,23 @@ heat_tb_kernel(const __grid_constant__ CUtensorMap tin, float* __restrict__ out,
 
         const int xb = c.X0 + 4 * c.lane - L.xoff;      // block x of this thread's first cell
         c.ya = c.Y0 + 2 * c.warp;                       // block y of this thread's first row
+        unsigned xkm = 0, mst = 0;
 #pragma unroll
-        for (int s = 1; s <= T; ++s) {
-            unsigned m = 0;
-#pragma unroll
-            for (int rr = 0; rr < 2; ++rr)
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const bool in = xb + j >= lo[s][0] && xb + j <= hi[s][0] && c.ya + rr >= lo[s][1] &&
-                                    c.ya + rr <= hi[s][1];
-                    m |= (in ? 1u : 0u) << (4 * rr + j);
-                }
-            c.mxy[s] = m;
+        for (int j = 0; j < 4; ++j) {
+            const int x = xb + j;
+            const bool xk = ((edge & 1) && x == L.H - 1) || (((edge >> 1) & 1) && x == L.n[0] - L.H);
+            xkm |= (xk ? 1u : 0u) << j;
         }
-        unsigned mst = c.mxy[T];
+#pragma unroll
+        for (int rr = 0; rr < 2; ++rr) {
+            const int y = c.ya + rr;
+            c.yk[rr] = (((edge >> 2) & 1) && y == L.H - 1) || (((edge >> 3) & 1) && y == L.n[1] - L.H);
+            const bool yin = y >= lo[1] && y <= hi[1];
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                mst |= (yin && xb + j >= lo[0] && xb + j <= hi[0] ? 1u : 0u) << (4 * rr + j);
+        }
+        c.xkm = xkm;
         if (c.lane < 1 || c.lane > 30) mst = 0;
 #pragma unroll
         for (int rr = 0; rr < 2; ++rr) {
@@ -346,14 +372,7 @@ heat_tb_kernel(const __grid_constant__ CUtensorMap tin, float* __restrict__ out,
         c.mst = mst;
         c.outb = out + (long long)c.blk * L.bstride + c.X0 + 4 * c.lane;
 
-        for (int pr = 0; pr < c.np;) {
-            tb_iter<T, 0>(c, pr++);
-            if (c.aborted || pr >= c.np) break;
-            tb_iter<T, 1>(c, pr++);
-            if (c.aborted || pr >= c.np) break;
-            tb_iter<T, 2>(c, pr++);
-            if (c.aborted) break;
-        }
+        tb_unit<T, true>(c);
         if (!c.aborted) c.gp += c.np;
     }
     if (c.aborted && c.tid == 0) {
@@ -413,6 +432,7 @@ cudaError_t launch_heat_substep_tb(int T, const CUtensorMap* tin, float* out, co
                                    const HeatCoef& c, int* status, cudaStream_t st, int zchunk)
 {
     switch (T) {
+    case 2: return launch_tb<2>(tin, out, L, step_i, c, status, st, zchunk);
     case 3: return launch_tb<3>(tin, out, L, step_i, c, status, st, zchunk);
     case 4: return launch_tb<4>(tin, out, L, step_i, c, status, st, zchunk);
     default: return cudaErrorInvalidValue;

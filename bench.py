@@ -754,7 +754,7 @@ def run_ours(args, wl):
     # this shape (timed on the live fields, which it restores); not part of
     # the timing
     tuned = None
-    knobs = {1: ("zchunk", "ctas_per_sm", "pdl", "tblock", "zchunk2"),
+    knobs = {1: ("zchunk", "ctas_per_sm", "pdl", "tblock", "zchunk2", "tb16"),
              2: ("tblock", "gol_bytes", "gol_push"), 4: ("eqwp_fused",)}
     if wl["model"] in knobs and not tune:
         d.autotune(trial_steps=4)
@@ -855,8 +855,9 @@ def run_ours(args, wl):
         per_launch_ms = ms / per_launch
         achieved = algo / (per_launch_ms / 1000.0) / 1e9
         tb = (tuned or tune or {}).get("tblock", 2)
+        w16 = (tuned or tune or {}).get("tb16", 0)
         kern = (wl["kernel"] if steps_per_launch < 1.5 else
-                "heat2_kernel (two time steps per launch)" if tb == 2 else
+                "heat2_kernel (two time steps per launch)" if tb == 2 and not w16 else
                 f"heat_tb_kernel<{tb}> ({tb} time steps per launch)")
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": profiled_traffic(args.workload, tb),

@@ -144,11 +144,13 @@ enum {
     B2R_TUNE_ADJ_FUSED = 8,    /* elastic-wave adjoint: 1 = the stress adjoint and the lambda /
                                   mu gradients in one sweep (default), 0 = two kernels;
                                   bit-identical */
-    B2R_TUNE_GOL_PUSH = 9      /* Game of Life: 1 = a several-generation pass that ends a period
+    B2R_TUNE_GOL_PUSH = 9,     /* Game of Life: 1 = a several-generation pass that ends a period
                                   also fills the next period's halos, so no gather runs between
                                   periods (block rows of a multiple of 32 cells; otherwise the
                                   gather runs); 0 = the gather (default, faster on this GPU so
                                   far); identical results */
+    B2R_TUNE_TB16 = 10         /* heat, two steps per pass: 0 = two 8-warp CTAs per SM (default),
+                                  1 = the 16-warp kernel of three and four steps; bit-identical */
 };
 b2r_status b2r_set_tuning(b2r_handle* h, int key, int value);
 /* Current value of a knob (after b2r_autotune: the schedule it picked). */
