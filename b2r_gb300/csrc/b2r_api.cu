@@ -105,7 +105,8 @@ b2r_status build_heat_maps(b2r_handle* h)
             return fail(h, B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed for the heat field");
         if (h->cfg.D == 1 &&
             (!make_block_tmap(&h->tmap2[b], h->buf[b], h->L, 4, heat2_box_w(), heat2_box_h(), 1) ||
-             !make_block_tmap(&h->tmap3[b], h->buf[b], h->L, 4, heat_tb_box_w(), heat_tb_box_h(), 1)))
+             !make_block_tmap(&h->tmap3[b], h->buf[b], h->L, 4, heat_tb_box_w(0), heat_tb_box_h(0), 1) ||
+             !make_block_tmap(&h->tmap4[b], h->buf[b], h->L, 4, heat_tb_box_w(1), heat_tb_box_h(1), 1)))
             return fail(h, B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed for the heat field");
     }
     return B2R_OK;
@@ -306,7 +307,8 @@ b2r_status advance(b2r_handle* h, int n)
             if (k == 2 && !h->tune.tb16) {
                 if ((st = substep2(h, i)) != B2R_OK) return st;
             } else {
-                CK(h, launch_heat_substep_tb(k, &h->tmap3[h->cur], static_cast<float*>(h->buf[1 - h->cur]), h->L,
+                CK(h, launch_heat_substep_tb(k, h->tune.tbn, h->tune.tbn ? &h->tmap4[h->cur] : &h->tmap3[h->cur],
+                                             static_cast<float*>(h->buf[1 - h->cur]), h->L,
                                              i, h->hc, h->d_status, h->stream, h->tune.zchunk2));
                 h->cur = 1 - h->cur;
             }

@@ -40,6 +40,7 @@ struct HeatTune {
     int tblock = 2;        // time steps per HBM pass, radius 1 only (2 = heat2.cu, 3-4 = heat_tb.cu)
     int zchunk2 = 0;       // output planes per unit of the several-step kernels (0 = 16 / 64)
     int tb16 = 0;          // two steps per pass: 0 = heat2.cu (8-warp CTAs), 1 = heat_tb.cu (16 warps)
+    int tbn = 0;           // heat_tb.cu tiles: 0 = 128 x 32 cells, 1 = 64 x 64 cells
 };
 
 // One sub-step of every block: units (block, z-chunk, tile row, tile column)
@@ -56,11 +57,12 @@ cudaError_t launch_heat_substep2(const CUtensorMap* tin, float* out, const Block
                                  const HeatCoef& c, int* status, cudaStream_t st, int zchunk);
 
 // T = 2, 3 or 4 sub-steps (step_i .. step_i+T-1) of radius 1 per launch
-// (heat_tb.cu).  The tensor map must have the box heat_tb_box_w() x
-// heat_tb_box_h().
-int heat_tb_box_w();
-int heat_tb_box_h();
-cudaError_t launch_heat_substep_tb(int T, const CUtensorMap* tin, float* out, const BlockLayout& L, int step_i,
-                                   const HeatCoef& c, int* status, cudaStream_t st, int zchunk);
+// (heat_tb.cu), on tiles of 128 x 32 cells (narrow = 0) or 64 x 64 cells
+// (narrow = 1).  The tensor map must have the box heat_tb_box_w(narrow) x
+// heat_tb_box_h(narrow).
+int heat_tb_box_w(int narrow);
+int heat_tb_box_h(int narrow);
+cudaError_t launch_heat_substep_tb(int T, int narrow, const CUtensorMap* tin, float* out, const BlockLayout& L,
+                                   int step_i, const HeatCoef& c, int* status, cudaStream_t st, int zchunk);
 
 }  // namespace b2r

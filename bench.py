@@ -754,7 +754,7 @@ def run_ours(args, wl):
     # this shape (timed on the live fields, which it restores); not part of
     # the timing
     tuned = None
-    knobs = {1: ("zchunk", "ctas_per_sm", "pdl", "tblock", "zchunk2", "tb16"),
+    knobs = {1: ("zchunk", "ctas_per_sm", "pdl", "tblock", "zchunk2", "tb16", "tb_narrow"),
              2: ("tblock", "gol_bytes", "gol_push"), 4: ("eqwp_fused",)}
     if wl["model"] in knobs and not tune:
         d.autotune(trial_steps=4)
@@ -856,9 +856,10 @@ def run_ours(args, wl):
         achieved = algo / (per_launch_ms / 1000.0) / 1e9
         tb = (tuned or tune or {}).get("tblock", 2)
         w16 = (tuned or tune or {}).get("tb16", 0)
+        tile = "64 x 64" if (tuned or tune or {}).get("tb_narrow", 0) else "128 x 32"
         kern = (wl["kernel"] if steps_per_launch < 1.5 else
                 "heat2_kernel (two time steps per launch)" if tb == 2 and not w16 else
-                f"heat_tb_kernel<{tb}> ({tb} time steps per launch)")
+                f"heat_tb_kernel<{tb}> ({tb} time steps per launch, {tile}-cell tiles)")
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": profiled_traffic(args.workload, tb),
                 "peak_source": peak_src, "kernel": kern,

@@ -149,8 +149,10 @@ enum {
                                   periods (block rows of a multiple of 32 cells; otherwise the
                                   gather runs); 0 = the gather (default, faster on this GPU so
                                   far); identical results */
-    B2R_TUNE_TB16 = 10         /* heat, two steps per pass: 0 = two 8-warp CTAs per SM (default),
+    B2R_TUNE_TB16 = 10,        /* heat, two steps per pass: 0 = two 8-warp CTAs per SM (default),
                                   1 = the 16-warp kernel of three and four steps; bit-identical */
+    B2R_TUNE_TB_NARROW = 11    /* heat, the 16-warp several-step kernel: 0 = tiles of 128 x 32
+                                  cells (default), 1 = 64 x 64 cells; bit-identical */
 };
 b2r_status b2r_set_tuning(b2r_handle* h, int key, int value);
 /* Current value of a knob (after b2r_autotune: the schedule it picked). */

@@ -52,6 +52,7 @@ def test_heat_512_bench_schedule_matches_oracle(b2r, orc, workload, nsteps):
             schedules = {"two-step": dict(tblock=2, zchunk2=64, pdl=1), "one-step": dict(tblock=1),
                          "two-step-16w": dict(tblock=2, zchunk2=0, tb16=1),
                          "three-step": dict(tblock=3, zchunk2=0), "four-step": dict(tblock=4, zchunk2=96),
+                         "three-step-64x64": dict(tblock=3, zchunk2=0, tb_narrow=1),
                          **schedules}
         for name, knobs in schedules.items():
             d.upload(dom)

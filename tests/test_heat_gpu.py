@@ -143,10 +143,12 @@ def test_run_host_roundtrip(b2r, orc):
                                                    ((240, 52, 40), (2, 2, 1), 5, False),
                                                    ((96, 96, 96), (2, 2, 2), 8, True),
                                                    ((7, 130, 12), (1, 1, 1), 1, False)])
-@pytest.mark.parametrize("tb,zc2,tb16", [(2, 0, 0), (2, 0, 1), (3, 0, 0), (3, 33, 0), (4, 0, 0), (4, 8, 0)])
-def test_several_step_sweeps_bit_identical(b2r, orc, env, blocks, R, periodic, tb, zc2, tb16):
+@pytest.mark.parametrize("tb,zc2,tb16,nar", [(2, 0, 0, 0), (2, 0, 1, 0), (2, 0, 1, 1), (3, 0, 0, 0), (3, 33, 0, 0),
+                                            (3, 0, 0, 1), (3, 17, 0, 1), (4, 0, 0, 0), (4, 8, 0, 0), (4, 0, 0, 1)])
+def test_several_step_sweeps_bit_identical(b2r, orc, env, blocks, R, periodic, tb, zc2, tb16, nar):
     """Two (8-warp and 16-warp kernels), three and four sub-steps per HBM
-    pass (radius 1) against one step per launch: 11 steps, so every schedule also runs a shorter pass (four
+    pass (radius 1; tiles of 128 x 32 and 64 x 64 cells) against one step
+    per launch: 11 steps, so every schedule also runs a shorter pass (four
     steps: 4 + 4 + 3; three: 3 + 3 + 3 + 2), and passes stop at period ends
     where the blocks exchange halos."""
     bc = b2r.BC_PERIODIC if periodic else b2r.BC_SHELL
@@ -156,9 +158,9 @@ def test_several_step_sweeps_bit_identical(b2r, orc, env, blocks, R, periodic, t
     else:
         dom = shell_domain(env, 1, 8)
     outs = []
-    for t, z, w in ((1, 0, 0), (tb, zc2, tb16)):
+    for t, z, w, n in ((1, 0, 0, 0), (tb, zc2, tb16, nar)):
         with b2r.Domain(b2r.MODEL_HEAT, env, blocks=blocks, R=R, D=1, boundary=bc, alpha_dt=0.1) as d:
-            d.set_tuning(tblock=t, zchunk2=z, tb16=w)
+            d.set_tuning(tblock=t, zchunk2=z, tb16=w, tb_narrow=n)
             d.upload(dom)
             d.step(11)
             outs.append(d.download())
