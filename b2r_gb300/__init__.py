@@ -20,7 +20,7 @@ import os
 
 import numpy as np
 
-__all__ = ["Domain", "Batch", "B2RError", "heat_3D_gpu_main", "gol_3D_gpu_main", "lib", "LIB_PATH",
+__all__ = ["Domain", "Batch", "EqwpBatch", "B2RError", "heat_3D_gpu_main", "gol_3D_gpu_main", "lib", "LIB_PATH",
            "MODEL_HEAT", "MODEL_GOL", "MODEL_EQWP_REF", "MODEL_EQWP_STAG", "BC_SHELL",
            "BC_PERIODIC", "FIELDS"]
 
@@ -118,6 +118,16 @@ def lib():
         "b2r_batch_autotune": ([vp, vp, C.POINTER(C.c_int), C.POINTER(d)], i),
         "b2r_batch_set_tile": ([vp, i], i),
         "b2r_batch_tile": ([vp], i),
+        "b2r_batch_instance_tile": ([vp, i], i),
+        "b2r_batch_set_pass_steps": ([vp, i], i),
+        "b2r_eqwp_batch_create": ([C.POINTER(vp), C.POINTER(i), i, C.POINTER(vp)], i),
+        "b2r_eqwp_batch_destroy": ([vp], i),
+        "b2r_eqwp_batch_last_error": ([], C.c_char_p),
+        "b2r_eqwp_batch_run": ([vp, vp, i], i),
+        "b2r_eqwp_batch_synchronize": ([vp, vp], i),
+        "b2r_eqwp_batch_lups": ([vp], C.c_int64),
+        "b2r_eqwp_batch_set_zchunk": ([vp, i], i),
+        "b2r_batch_instance_pass_steps": ([vp, i], i),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -436,6 +446,60 @@ def _bcheck(st):
         raise B2RError(st, msg.decode() if msg else "")
 
 
+def _ebcheck(st):
+    if st != 0:
+        msg = lib().b2r_eqwp_batch_last_error()
+        raise B2RError(st, msg.decode() if msg else "")
+
+
+class EqwpBatch:
+    """Staggered elastic-wave Domains (one block each, fixed shell) advanced
+    in one persistent launch (b2r_eqwp_batch_*): each run advances domain i
+    by nsteps[i] steps, in place.  The domains must outlive the batch; their
+    own streams must be idle during a run."""
+
+    def __init__(self, domains, nsteps, stream=None):
+        self.domains = list(domains)
+        n = len(self.domains)
+        hs = (C.c_void_p * n)(*[d.h.value for d in self.domains])
+        ns = (C.c_int * n)(*[int(v) for v in nsteps])
+        self.nsteps = [int(v) for v in nsteps]
+        hnd = C.c_void_p()
+        _ebcheck(lib().b2r_eqwp_batch_create(hs, ns, n, C.byref(hnd)))
+        self.h = hnd
+        self.stream = C.c_void_p(int(getattr(stream, "cuda_stream", stream) or 0))
+
+    @property
+    def lups(self):
+        return int(lib().b2r_eqwp_batch_lups(self.h))
+
+    def set_zchunk(self, z):
+        _ebcheck(lib().b2r_eqwp_batch_set_zchunk(self.h, int(z)))
+
+    def run(self, graph=True):
+        _ebcheck(lib().b2r_eqwp_batch_run(self.h, self.stream, 1 if graph else 0))
+
+    def synchronize(self):
+        _ebcheck(lib().b2r_eqwp_batch_synchronize(self.h, self.stream))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().b2r_eqwp_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
 class Batch:
     """Independent heat instances advanced in one persistent launch (b2r_batch_*).
 
@@ -491,12 +555,26 @@ class Batch:
         _bcheck(lib().b2r_batch_set_zchunk(self.h, int(z)))
 
     def set_tile(self, width):
-        """Tile width of every instance: 128, 64, 32, or 0 for the mix's default."""
+        """Tile width of every instance: 128, 64, 32, or 0 for each
+        instance's fewest-cells shape (the default)."""
         _bcheck(lib().b2r_batch_set_tile(self.h, int(width)))
 
     @property
     def tile(self):
+        """Tile width shared by every instance, 0 if they differ."""
         return int(lib().b2r_batch_tile(self.h))
+
+    def instance_tiles(self):
+        """Tile width of each instance (caller order)."""
+        return [int(lib().b2r_batch_instance_tile(self.h, i)) for i in range(len(self.items))]
+
+    def set_pass_steps(self, steps):
+        """Time steps per HBM pass of the radius-1 instances: 1 or 2."""
+        _bcheck(lib().b2r_batch_set_pass_steps(self.h, int(steps)))
+
+    def instance_pass_steps(self):
+        """Time steps per HBM pass of each instance (caller order)."""
+        return [int(lib().b2r_batch_instance_pass_steps(self.h, i)) for i in range(len(self.items))]
 
     def autotune(self):
         z = C.c_int()

@@ -137,6 +137,21 @@ int gol_pass_gens(const b2r_handle* h, int i, int left)
     return std::max(g, 1);
 }
 
+// Periods per graph replay: at least 32 time steps; when heat passes may
+// run across period starts (radius 1, several steps per pass, nothing to
+// exchange), also a multiple of the steps per pass, so that no replay ends
+// with a shorter pass.
+int graph_periods(const b2r_handle* h)
+{
+    int m = (32 + h->cfg.R - 1) / h->cfg.R;
+    if (h->cfg.model == B2R_MODEL_HEAT && h->cfg.D == 1 && h->tune.tblock >= 2 && h->L.nblk == 1 &&
+        !h->L.periodic) {
+        const int k = std::min(h->tune.tblock, 4);
+        while ((m * h->cfg.R) % k) ++m;
+    }
+    return m;
+}
+
 b2r_status check_status(b2r_handle* h)
 {
     int s = 0;
@@ -683,7 +698,7 @@ b2r_status b2r_step(b2r_handle* h, int nsteps)
         const int i = (int)(h->ts % h->cfg.R);
         if (use_graphs && i == 0) {
             // whole periods replayed from a graph: >= 32 time steps per launch
-            const int periods = (32 + h->cfg.R - 1) / h->cfg.R;
+            const int periods = graph_periods(h);
             const int unit = periods * h->cfg.R;
             if (nsteps - s >= unit) {
                 if (h->gsteps != unit) {
@@ -704,10 +719,7 @@ b2r_status b2r_step(b2r_handle* h, int nsteps)
         // up to the next period start (or all of it when nothing is graphed)
         int chunk = nsteps - s;
         if (use_graphs && i != 0) chunk = std::min(chunk, h->cfg.R - i);
-        if (use_graphs && i == 0) {
-            const int periods = (32 + h->cfg.R - 1) / h->cfg.R;
-            chunk = std::min(chunk, periods * h->cfg.R);
-        }
+        if (use_graphs && i == 0) chunk = std::min(chunk, graph_periods(h) * h->cfg.R);
         if ((st = advance(h, chunk)) != B2R_OK) return st;
         s += chunk;
     }

@@ -6,15 +6,11 @@
 // scheme of heat-3D.cu:228-231/315-318/410-413/514-517 exactly as the plain
 // sweep does, so results are bit-identical to per-instance plain runs.
 //
-// Work items (step t, instance k, unit u) are numbered step-major; instances
-// are sorted by step count (descending), so the instances still active at
-// step t are a prefix of the list.  A CTA claims the next item with one
-// atomicAdd on a head counter.  Before reading step t of instance k it waits
-// until done[k] >= t * units[k] (every unit of step t-1 of that instance has
-// finished), then streams the unit exactly as the plain sweep does and bumps
-// done[k].  Items are claimed in increasing order and an item only waits on
-// smaller items, which are held by running CTAs, so the queue cannot
-// deadlock; every wait is bounded (2 s) and reports B2R_ERR_TIMEOUT.
+// Work items (round t, instance k, unit u) go through the device work queue
+// of work_queue.cuh.  A round is one time step of an instance on one-step
+// units (heat_unit.cuh, tile shape per instance) or two of an instance on
+// two-step units (heat2_unit.cuh, radius 1; the last round of an odd step
+// count takes one), chosen per (order, size class) by the autotuner.
 #include <algorithm>
 #include <mutex>
 #include <cstdio>
@@ -22,7 +18,9 @@
 #include <new>
 #include <vector>
 
+#include "heat2_unit.cuh"
 #include "heat_unit.cuh"
+#include "work_queue.cuh"
 
 namespace b2r {
 namespace {
@@ -46,8 +44,16 @@ constexpr int slot_max()
     return cmax(cmax(BCfg<1, LPR>::SLOT, BCfg<2, LPR>::SLOT), cmax(BCfg<3, LPR>::SLOT, BCfg<4, LPR>::SLOT));
 }
 constexpr int kSlot = cmax(cmax(slot_max<32>(), slot_max<16>()), slot_max<8>());
+static_assert(kSlot >= h2k::kPlane, "the two-step units stream through the same ring slots");
 constexpr size_t kSmem = size_t(kS) * kSlot * sizeof(float) + kS * sizeof(uint64_t) + 16 + 128;
-constexpr int kLpr[3] = {32, 16, 8};
+// the two-step units' two stage-1 planes, after the schedule tables
+constexpr size_t kSmemS1 = 2 * size_t(h2k::kP1) * sizeof(float) + 128;
+// tile shapes 0..2: one step per unit, LPR lanes per row = 32, 16, 8 -> 128,
+// 64, 32 cells wide; shape 3: two steps per unit on 128 x 16-cell tiles
+// (radius 1 only, heat2_unit.cuh)
+constexpr int kShapes = 4;
+constexpr int kTwoStep = 3;
+constexpr int kLpr[kShapes] = {32, 16, 8, 32};
 constexpr int kBoxH[5][3] = {{0, 0, 0},
                              {BCfg<1, 32>::BH, BCfg<1, 16>::BH, BCfg<1, 8>::BH},
                              {BCfg<2, 32>::BH, BCfg<2, 16>::BH, BCfg<2, 8>::BH},
@@ -64,27 +70,24 @@ struct InstDev {
     float* buf[2];
     HeatCoef C;
     int D, nsteps, ntx, nty, NZ, Lz, nzc, units;
+    int shape;                           // tile shape: index into kLpr
+    int lpr;                             // its lanes per tile row (kLpr[shape])
+    int tb;                              // time steps per unit: 1, or 2 (shape kTwoStep)
+    int rounds;                          // rounds of units: nsteps / tb, rounded up
 };
 
 struct BatchArgs {
-    const InstDev* inst;                 // sorted by nsteps, descending
+    const InstDev* inst;                 // sorted by rounds, descending
     const CUtensorMap* maps;             // 2 per instance: buffer 0, buffer 1
-    const long long* step_off;           // items before step t (size maxsteps+1)
+    const long long* step_off;           // items before round t (size maxsteps+1)
     const int* active;                   // instances still stepping at step t
     const long long* unit_prefix;        // units of instances [0, k) (size n+1)
     unsigned long long* head;            // next item (zeroed per run)
     unsigned* done;                      // finished units per instance (zeroed per run)
     int* status;
-    int maxsteps, ninst;
+    int maxsteps, ninst;                 // maxsteps: rounds of the longest instance
     long long total;
 };
-
-__device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
-{
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
 
 // the four unit bodies are inlined into the kernel (measured faster than
 // separate calls, whose calling convention spills the register queues)
@@ -93,7 +96,9 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
 #else
 #define B2R_UNIT_INLINE __forceinline__
 #endif
-template <int D, int LPR>
+// the tile shape is the instance's own (run time), so that instances of
+// different shapes share the launch
+template <int D>
 __device__ B2R_UNIT_INLINE bool run_unit(const BatchArgs& a, const InstDev& in, int k, int t, int u,
                                          heatk::Ring& rg)
 {
@@ -103,36 +108,42 @@ __device__ B2R_UNIT_INLINE bool run_unit(const BatchArgs& a, const InstDev& in, 
     const int zc = r / in.nty;
     const int zi0 = zc * in.Lz;
     const int zi1 = min(in.NZ, zi0 + in.Lz);
-    return heatk::sweep_unit<D, RowsPerWarp<D>::value, kS, kSlot, LPR>(
-        &a.maps[2 * k + (t & 1)], in.buf[(t + 1) & 1], in.L, 0, in.C, 0, tx, ty, zi0, zi1, rg);
+    return heatk::sweep_unit<D, RowsPerWarp<D>::value, kS, kSlot, 0>(
+        &a.maps[2 * k + (t & 1)], in.buf[(t + 1) & 1], in.L, 0, in.C, 0, tx, ty, zi0, zi1, rg, in.lpr);
 }
 
-// Item -> (step, instance, unit) by binary searches in the shared-memory
-// copies of the schedule tables.
-__device__ __forceinline__ void decode(long long item, const long long* step_off, const int* active,
-                                       const long long* prefix, int maxsteps, int& t, int& k, int& u)
+// A two-step unit: round t = sub-steps 2t, 2t+1 (the last round of an odd
+// step count: 2t only), through the same ring (positions gp, issued_hi,
+// stop in, updated positions and the success flag out).  Not inlined: its
+// register queues would otherwise share the budget of the one-step units'.
+__device__ __noinline__ uint4 run_two_step(const BatchArgs& a, int k, int t, int u, unsigned gp,
+                                           unsigned issued_hi, unsigned stop, float* s1, float* ring)
 {
-    int lo = 0, hi = maxsteps;                      // last t with step_off[t] <= item
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (step_off[mid] <= item) lo = mid; else hi = mid;
-    }
-    t = lo;
-    const long long r = item - step_off[t];
-    int kl = 0, kh = active[t];                     // last k with prefix[k] <= r
-    while (kh - kl > 1) {
-        const int mid = (kl + kh) >> 1;
-        if (prefix[mid] <= r) kl = mid; else kh = mid;
-    }
-    k = kl;
-    u = (int)(r - prefix[k]);
+    const InstDev& in = a.inst[k];
+    h2k::H2Ctx c;
+    c.ring = ring;
+    c.s1 = s1;
+    c.bar = reinterpret_cast<uint64_t*>(ring + kS * kSlot);
+    c.abort_flag = reinterpret_cast<int*>(c.bar + kS);
+    c.tid = threadIdx.x;
+    c.lane = threadIdx.x & 31;
+    c.warp = threadIdx.x >> 5;
+    c.C = in.C;
+    c.plane = in.L.plane;
+    c.P = in.L.P;
+    c.gp = gp;
+    c.issued_hi = issued_hi;
+    c.stop = stop;
+    c.aborted = false;
+    const int tx = u % in.ntx, r = u / in.ntx, ty = r % in.nty, zc = r / in.nty;
+    const bool ok = h2k::h2_unit<kS, kSlot>(c, &a.maps[2 * k + (t & 1)], in.buf[(t + 1) & 1], in.L, 0, 0, tx,
+                                            ty, zc * in.Lz, in.Lz, 2 * t + 1 == in.nsteps);
+    return make_uint4(c.gp, c.issued_hi, c.stop, ok ? 1u : 0u);
 }
 
 #ifndef B2R_BATCH_MINB
 #define B2R_BATCH_MINB 2   // resident CTAs per SM the register budget is fitted to (no spills)
 #endif
-// LPR: tile shape of every instance of the launch (lanes per tile row)
-template <int LPR>
 __global__ void __launch_bounds__(kThreads, B2R_BATCH_MINB) batch_kernel(const BatchArgs a)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -143,6 +154,9 @@ __global__ void __launch_bounds__(kThreads, B2R_BATCH_MINB) batch_kernel(const B
         reinterpret_cast<unsigned char*>(rg.abort_flag) + 16);
     long long* s_prefix = s_step_off + (a.maxsteps + 1);
     int* s_active = reinterpret_cast<int*>(s_prefix + (a.ninst + 1));
+    // the two-step units' stage-1 planes after the tables, 128-byte aligned
+    float* s1 = reinterpret_cast<float*>(
+        (reinterpret_cast<uintptr_t>(s_active + (a.maxsteps + 1)) + 127) & ~uintptr_t(127));
     for (int i = threadIdx.x; i <= a.maxsteps; i += blockDim.x) {
         s_step_off[i] = a.step_off[i];
         s_active[i] = a.active[i];
@@ -158,23 +172,10 @@ __global__ void __launch_bounds__(kThreads, B2R_BATCH_MINB) batch_kernel(const B
             s_cur = item;
             if (item < a.total) {
             int t, k, u;
-            decode(item, s_step_off, s_active, s_prefix, a.maxsteps, t, k, u);
+            wq::decode(item, s_step_off, s_active, s_prefix, a.maxsteps, t, k, u);
             int ok = 1;
-            if (t > 0) {        // wait for step t-1 of this instance (bounded)
-                const unsigned need = (unsigned)t * (unsigned)a.inst[k].units;
-                if (ld_acquire(&a.done[k]) < need) {
-                    const uint64_t t0 = global_ns();
-                    while (ld_acquire(&a.done[k]) < need) {
-                        if (global_ns() - t0 > 2000000000ull) {
-                            ok = 0;
-                            break;
-                        }
-                        __nanosleep(100);
-                    }
-                }
-                // data written by other CTAs' generic stores is read by TMA
-                asm volatile("fence.proxy.async.global;" ::: "memory");
-            }
+            // wait for round t-1 of this instance (bounded)
+            if (t > 0) ok = wq::wait_done(&a.done[k], (unsigned)t * (unsigned)a.inst[k].units) ? 1 : 0;
             s_t = t;
             s_k = k;
             s_u = u;
@@ -192,11 +193,17 @@ __global__ void __launch_bounds__(kThreads, B2R_BATCH_MINB) batch_kernel(const B
         const int t = s_t, k = s_k, u = s_u;
         const InstDev& in = a.inst[k];
         bool ok;
-        switch (in.D) {
-        case 1: ok = run_unit<1, LPR>(a, in, k, t, u, rg); break;
-        case 2: ok = run_unit<2, LPR>(a, in, k, t, u, rg); break;
-        case 3: ok = run_unit<3, LPR>(a, in, k, t, u, rg); break;
-        default: ok = run_unit<4, LPR>(a, in, k, t, u, rg); break;
+        if (in.tb == 2) {
+            const uint4 r = run_two_step(a, k, t, u, rg.gp, rg.issued_hi, rg.stop, s1, rg.smem);
+            rg.gp = r.x;
+            rg.issued_hi = r.y;
+            rg.stop = r.z;
+            ok = r.w != 0;
+        } else switch (in.D) {
+        case 1: ok = run_unit<1>(a, in, k, t, u, rg); break;
+        case 2: ok = run_unit<2>(a, in, k, t, u, rg); break;
+        case 3: ok = run_unit<3>(a, in, k, t, u, rg); break;
+        default: ok = run_unit<4>(a, in, k, t, u, rg); break;
         }
         if (!ok) {
             if (threadIdx.x == 0) report(a.status, DEV_TIMEOUT);
@@ -204,12 +211,7 @@ __global__ void __launch_bounds__(kThreads, B2R_BATCH_MINB) batch_kernel(const B
             return;
         }
         __syncthreads();                     // every store of this unit is issued
-        if (threadIdx.x == 0) {
-            // release at gpu scope; PTX fences are cumulative, so this orders
-            // the whole CTA's stores (ordered before it by the barrier) before
-            // the count that the next step's readers acquire
-            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(&a.done[k]) : "memory");
-        }
+        if (threadIdx.x == 0) wq::release_done(&a.done[k]);
     }
 }
 
@@ -223,8 +225,9 @@ struct b2r_batch {
     std::vector<b2r_batch_item> items;
     std::vector<int> order;          // sorted position -> caller index
     std::vector<int> pos;            // caller index -> sorted position
-    std::vector<InstDev> host;       // sorted
-    std::vector<CUtensorMap> maps;   // sorted, 2 per instance
+    std::vector<InstDev> host;       // sorted by step count
+    std::vector<CUtensorMap> maps;   // sorted by step count, 2 per instance
+    std::vector<int> sched;          // queue position -> host index (by rounds, descending)
     InstDev* d_inst = nullptr;
     CUtensorMap* d_maps = nullptr;
     long long* d_step_off = nullptr;
@@ -236,10 +239,10 @@ struct b2r_batch {
     float* staging = nullptr;
     size_t staging_bytes = 0;
     int maxsteps = 0;
+    int maxrounds = 0;               // rounds of the current schedule's longest instance
     long long total = 0;
     int lz_policy = 16;              // z chunk cap per unit (autotuned)
-    int shape = 0;                   // tile shape of every instance: index into kLpr (autotuned)
-    int grid[3] = {0, 0, 0};         // persistent grid per tile shape
+    int grid = 0;                    // persistent grid: every resident slot
     size_t smem = 0;                 // ring + schedule tables
     cudaGraphExec_t gexec = nullptr;
     cudaStream_t gstream = nullptr;
@@ -279,18 +282,16 @@ long long plane_cells(const b2r_batch* b, int k, int s)
     return (long long)((X + tw - 1) / tw) * tw * ((Y + th - 1) / th) * th;
 }
 
-// The tile shape for the whole mix: the fewest cells computed over every
-// instance's steps, narrow tiles paying a little for their wider skirt.
-int default_shape(const b2r_batch* b)
+// The tile shape of instance k: the fewest cells computed per plane, narrow
+// tiles paying a little for their wider skirt (their boxes re-read a larger
+// share of the neighbouring tiles).
+int default_shape(const b2r_batch* b, int k)
 {
     static const double penalty[3] = {1.0, 1.03, 1.08};
     int best = 0;
     double bc = 1e300;
     for (int s = 0; s < 3; ++s) {
-        double c = 0;
-        for (int k = 0; k < b->n; ++k)
-            c += (double)plane_cells(b, k, s) * b->host[k].NZ * b->host[k].nsteps;
-        c *= penalty[s];
+        const double c = (double)plane_cells(b, k, s) * penalty[s];
         if (c < bc - 1e-9) {
             bc = c;
             best = s;
@@ -299,52 +300,92 @@ int default_shape(const b2r_batch* b)
     return best;
 }
 
+std::vector<int> default_shapes(const b2r_batch* b)
+{
+    std::vector<int> sh(b->n);
+    for (int k = 0; k < b->n; ++k) sh[k] = default_shape(b, k);
+    return sh;
+}
+
 b2r_status build_schedule(b2r_batch* b);
 
-// tile counts and tensor-map boxes of every instance for shape s
-b2r_status apply_shape(b2r_batch* b, int s)
+// tile counts, steps per unit and tensor-map boxes of every instance for
+// its shape sh[k] (two-step units for radius 1 only)
+b2r_status apply_shapes(b2r_batch* b, const std::vector<int>& sh)
 {
-    b->shape = s;
     for (int k = 0; k < b->n; ++k) {
         InstDev& in = b->host[k];
         const BlockLayout& L = in.L;
         const int D = in.D;
-        const int X = L.xoff + L.n[0] - D - ((L.xoff + D) & ~3), Y = L.n[1] - 2 * D;
-        const int tw = 4 * kLpr[s], th = kTileY[D][s];
-        in.ntx = (X + tw - 1) / tw;
-        in.nty = (Y + th - 1) / th;
+        const int s = (sh[k] == kTwoStep && D != 1) ? default_shape(b, k) : sh[k];
+        in.shape = s;
+        in.lpr = kLpr[s];
+        int bw, bh;
+        if (s == kTwoStep) {
+            in.tb = 2;
+            in.ntx = h2k::h2_ntx(L);
+            in.nty = h2k::h2_nty(L);
+            bw = h2k::kBoxW;
+            bh = h2k::kBoxH;
+        } else {
+            in.tb = 1;
+            const int X = L.xoff + L.n[0] - D - ((L.xoff + D) & ~3), Y = L.n[1] - 2 * D;
+            const int tw = 4 * kLpr[s], th = kTileY[D][s];
+            in.ntx = (X + tw - 1) / tw;
+            in.nty = (Y + th - 1) / th;
+            bw = tw + 8;
+            bh = kBoxH[D][s];
+        }
+        in.rounds = (in.nsteps + in.tb - 1) / in.tb;
         for (int f = 0; f < 2; ++f)
-            if (!make_block_tmap(&b->maps[2 * k + f], in.buf[f], L, 4, tw + 8, kBoxH[D][s], 1))
+            if (!make_block_tmap(&b->maps[2 * k + f], in.buf[f], L, 4, bw, bh, 1))
                 return bfail(B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed");
     }
-    BCK(cudaMemcpy(b->d_maps, b->maps.data(), sizeof(CUtensorMap) * 2 * b->n, cudaMemcpyHostToDevice),
-        "copy tensor maps");
     return build_schedule(b);
 }
 
-// schedule tables for the current Lz policy
+b2r_status apply_shape(b2r_batch* b, int s) { return apply_shapes(b, std::vector<int>(b->n, s)); }
+
+// Schedule tables for the current shapes and Lz policy.  Items are (round,
+// instance, unit), round-major; a round is one step of a one-step instance
+// or two of a two-step one.  The queue holds the instances sorted by their
+// round count (descending), so those still active at round t are a prefix.
 b2r_status build_schedule(b2r_batch* b)
 {
+    b->sched.resize(b->n);
+    for (int k = 0; k < b->n; ++k) b->sched[k] = k;
+    std::stable_sort(b->sched.begin(), b->sched.end(),
+                     [&](int x, int y) { return b->host[x].rounds > b->host[y].rounds; });
     std::vector<long long> prefix(b->n + 1, 0);
-    for (int k = 0; k < b->n; ++k) {
-        InstDev& in = b->host[k];
+    std::vector<InstDev> dev(b->n);
+    std::vector<CUtensorMap> maps(2 * b->n);
+    b->maxrounds = 0;
+    for (int j = 0; j < b->n; ++j) {
+        InstDev& in = b->host[b->sched[j]];
         in.Lz = std::min(in.NZ, b->lz_policy > 0 ? b->lz_policy : in.NZ);
         in.nzc = (in.NZ + in.Lz - 1) / in.Lz;
         in.units = in.ntx * in.nty * in.nzc;
-        prefix[k + 1] = prefix[k] + in.units;
+        prefix[j + 1] = prefix[j] + in.units;
+        dev[j] = in;
+        maps[2 * j] = b->maps[2 * b->sched[j]];
+        maps[2 * j + 1] = b->maps[2 * b->sched[j] + 1];
+        b->maxrounds = std::max(b->maxrounds, in.rounds);
     }
-    std::vector<long long> step_off(b->maxsteps + 1, 0);
-    std::vector<int> active(b->maxsteps + 1, 0);
-    for (int t = 0; t < b->maxsteps; ++t) {
+    const int R = b->maxrounds;
+    std::vector<long long> step_off(R + 1, 0);
+    std::vector<int> active(R + 1, 0);
+    for (int t = 0; t < R; ++t) {
         int A = 0;
-        while (A < b->n && b->host[A].nsteps > t) ++A;
+        while (A < b->n && dev[A].rounds > t) ++A;
         active[t] = A;
         step_off[t + 1] = step_off[t] + prefix[A];
     }
-    b->total = step_off[b->maxsteps];
-    BCK(cudaMemcpy(b->d_inst, b->host.data(), sizeof(InstDev) * b->n, cudaMemcpyHostToDevice), "copy descriptors");
-    BCK(cudaMemcpy(b->d_step_off, step_off.data(), sizeof(long long) * (b->maxsteps + 1), cudaMemcpyHostToDevice), "copy step table");
-    BCK(cudaMemcpy(b->d_active, active.data(), sizeof(int) * (b->maxsteps + 1), cudaMemcpyHostToDevice), "copy active table");
+    b->total = step_off[R];
+    BCK(cudaMemcpy(b->d_inst, dev.data(), sizeof(InstDev) * b->n, cudaMemcpyHostToDevice), "copy descriptors");
+    BCK(cudaMemcpy(b->d_maps, maps.data(), sizeof(CUtensorMap) * 2 * b->n, cudaMemcpyHostToDevice),
+        "copy tensor maps");
+    BCK(cudaMemcpy(b->d_step_off, step_off.data(), sizeof(long long) * (R + 1), cudaMemcpyHostToDevice), "copy step table");
+    BCK(cudaMemcpy(b->d_active, active.data(), sizeof(int) * (R + 1), cudaMemcpyHostToDevice), "copy active table");
     BCK(cudaMemcpy(b->d_prefix, prefix.data(), sizeof(long long) * (b->n + 1), cudaMemcpyHostToDevice), "copy prefix table");
     if (b->gexec) {
         cudaGraphExecDestroy(b->gexec);
@@ -366,14 +407,10 @@ b2r_status enqueue_run(b2r_batch* b, cudaStream_t st)
     a.head = b->d_head;
     a.done = b->d_done;
     a.status = b->d_status;
-    a.maxsteps = b->maxsteps;
+    a.maxsteps = b->maxrounds;
     a.ninst = b->n;
     a.total = b->total;
-    switch (b->shape) {
-    case 0: batch_kernel<32><<<b->grid[0], kThreads, b->smem, st>>>(a); break;
-    case 1: batch_kernel<16><<<b->grid[1], kThreads, b->smem, st>>>(a); break;
-    default: batch_kernel<8><<<b->grid[2], kThreads, b->smem, st>>>(a); break;
-    }
+    batch_kernel<<<b->grid, kThreads, b->smem, st>>>(a);
     BCK(cudaGetLastError(), "batch launch");
     return B2R_OK;
 }
@@ -453,27 +490,24 @@ b2r_status b2r_batch_create(const b2r_batch_item* items, int n, b2r_batch** out)
         return bail(bfail(B2R_ERR_OOM, "batch table allocation failed"));
     cudaMemset(b->d_status, 0, sizeof(int));
     // persistent grid: every resident slot
-    b->smem = kSmem + sizeof(long long) * (b->maxsteps + 1 + n + 1) + sizeof(int) * (b->maxsteps + 1) + 16;
+    b->smem = kSmem + sizeof(long long) * (b->maxsteps + 1 + n + 1) + sizeof(int) * (b->maxsteps + 1) + 16 +
+              kSmemS1;
     if (b->smem > 200 * 1024) return bail(bfail(B2R_ERR_ARG, "too many time steps for the batch schedule"));
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     {
-        const void* fns[3] = {(const void*)batch_kernel<32>, (const void*)batch_kernel<16>,
-                              (const void*)batch_kernel<8>};
         // the limit is per function and device: only ever raised, so that a
         // batch with a smaller schedule does not lower it under one created
         // before it
-        static SmemLimit limit[3];
-        for (int s = 0; s < 3; ++s) {
-            int occ = 0;
-            if (raise_smem_limit(limit[s], fns[s], b->smem) != cudaSuccess)
-                return bail(bfail(B2R_ERR_CUDA, "smem attribute"));
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fns[s], kThreads, b->smem);
-            b->grid[s] = std::max(1, occ) * std::max(1, sms);
-        }
+        static SmemLimit limit;
+        int occ = 0;
+        if (raise_smem_limit(limit, (const void*)batch_kernel, b->smem) != cudaSuccess)
+            return bail(bfail(B2R_ERR_CUDA, "smem attribute"));
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel, kThreads, b->smem);
+        b->grid = std::max(1, occ) * std::max(1, sms);
     }
-    b2r_status st = apply_shape(b, default_shape(b));
+    b2r_status st = apply_shapes(b, default_shapes(b));
     if (st != B2R_OK) return bail(st);
     if (cudaDeviceSynchronize() != cudaSuccess) return bail(bfail(B2R_ERR_CUDA, "batch set-up failed"));
     *out = b;
@@ -520,7 +554,7 @@ b2r_status b2r_batch_download(b2r_batch* b, int i, float* dst, int dst_is_device
     const InstDev& in = b->host[b->pos[i]];
     const BlockLayout& L = in.L;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const float* src = in.buf[in.nsteps & 1];
+    const float* src = in.buf[in.rounds & 1];
     BCK(cudaMemcpy2DAsync(dst, L.n[0] * sizeof(float), src + L.xoff, L.P * sizeof(float),
                           L.n[0] * sizeof(float), (size_t)L.n[1] * L.n[2],
                           dst_is_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st),
@@ -610,32 +644,74 @@ b2r_status b2r_batch_autotune(b2r_batch* b, void* stream, int* best_zchunk, doub
         BCK(cudaMalloc(&save[k], fb), "autotune save");
         BCK(cudaMemcpyAsync(save[k], b->host[k].buf[0], fb, cudaMemcpyDeviceToDevice, st), "save");
     }
-    static const int cands[] = {8, 16, 32, 64, 0};
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    float best = 1e30f;
-    int bestz = b->lz_policy, bests = b->shape;
-    b2r_status s = B2R_OK;
-    for (int c = 0; c < 3 * 5 && s == B2R_OK; ++c) {
-        const int sh = c / 5, z = cands[c % 5];
-        if (sh != b->shape && (s = apply_shape(b, sh)) != B2R_OK) break;
-        if ((s = b2r_batch_set_zchunk(b, z)) != B2R_OK) break;
+    // one whole run from the saved inputs, timed
+    auto trial = [&](float& ms) -> b2r_status {
         for (int k = 0; k < b->n; ++k)
             cudaMemcpyAsync(b->host[k].buf[0], save[k], (size_t)b->host[k].L.bstride * sizeof(float),
                             cudaMemcpyDeviceToDevice, st);
         cudaEventRecord(e0, st);
-        if ((s = enqueue_run(b, st)) != B2R_OK) break;
+        b2r_status r = enqueue_run(b, st);
+        if (r != B2R_OK) return r;
         cudaEventRecord(e1, st);
-        if ((s = b2r_batch_synchronize(b, st)) != B2R_OK) break;
-        float ms = 0.f;
+        if ((r = b2r_batch_synchronize(b, st)) != B2R_OK) return r;
         cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best) {
-            best = ms;
-            bestz = z;
-            bests = sh;
+        return B2R_OK;
+    };
+    static const int cands[] = {8, 16, 32, 64, 0};
+    float best = 1e30f;
+    int bestz = b->lz_policy;
+    // the z-chunk cap for the current shapes (a change must gain 0.5 %)
+    auto tune_zchunk = [&]() -> b2r_status {
+        for (int c = 0; c < 5; ++c) {
+            float ms = 0.f;
+            b2r_status r = b2r_batch_set_zchunk(b, cands[c]);
+            if (r == B2R_OK) r = trial(ms);
+            if (r != B2R_OK) return r;
+            if (ms < best * (cands[c] == bestz ? 1.f : 0.995f)) {
+                best = ms;
+                bestz = cands[c];
+            }
         }
-    }
+        return b2r_batch_set_zchunk(b, bestz);
+    };
+    // 1. the z-chunk cap with every instance on its fewest-cells shape
+    std::vector<int> sh = default_shapes(b);
+    b2r_status s = apply_shapes(b, sh);
+    if (s == B2R_OK) s = tune_zchunk();
+    // 2. tile shapes per (stencil order, size class): the instances of one
+    // class try each other shape while the rest keep theirs (radius 1 also
+    // the two-step units); the size class is the interior width (the extent
+    // a tile width divides)
+    auto cls = [&](int k) {
+        const int w = b->items[b->order[k]].env[0];
+        return (b->host[k].D - 1) * 3 + (w <= 64 ? 0 : (w <= 128 ? 1 : 2));
+    };
+    bool changed = false;
+    for (int c = 0; c < 12 && s == B2R_OK; ++c)
+        for (int t = 0; t < kShapes && s == B2R_OK; ++t) {
+            if (t == kTwoStep && c >= 3) continue;      // two-step units: radius 1 only
+            std::vector<int> cand = sh;
+            bool differs = false;
+            for (int k = 0; k < b->n; ++k)
+                if (cls(k) == c && cand[k] != t) {
+                    cand[k] = t;
+                    differs = true;
+                }
+            if (!differs) continue;
+            float ms = 0.f;
+            if ((s = apply_shapes(b, cand)) != B2R_OK || (s = trial(ms)) != B2R_OK) break;
+            if (ms < best * 0.995f) {
+                best = ms;
+                sh = cand;
+                changed = true;
+            }
+        }
+    // 3. the z-chunk cap again for the shapes picked
+    if (s == B2R_OK) s = apply_shapes(b, sh);
+    if (s == B2R_OK && changed) s = tune_zchunk();
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     // restore every instance even after a failed trial; report the first failure
@@ -652,24 +728,47 @@ b2r_status b2r_batch_autotune(b2r_batch* b, void* stream, int* best_zchunk, doub
     BCK(rerr, "restoring the instances after the trials");
     if (best_zchunk) *best_zchunk = bestz;
     if (best_ms) *best_ms = best;
-    if ((s = apply_shape(b, bests)) != B2R_OK) return s;
-    return b2r_batch_set_zchunk(b, bestz);
+    return B2R_OK;
 }
 
 b2r_status b2r_batch_set_tile(b2r_batch* b, int width)
 {
     if (!b) return bfail(B2R_ERR_ARG, "null batch");
-    int s;
     switch (width) {
-    case 0: s = default_shape(b); break;
-    case 128: s = 0; break;
-    case 64: s = 1; break;
-    case 32: s = 2; break;
+    case 0: return apply_shapes(b, default_shapes(b));
+    case 128: return apply_shape(b, 0);
+    case 64: return apply_shape(b, 1);
+    case 32: return apply_shape(b, 2);
     default: return bfail(B2R_ERR_ARG, "tile width must be 128, 64, 32 or 0");
     }
-    return apply_shape(b, s);
 }
 
-int b2r_batch_tile(const b2r_batch* b) { return b ? 4 * kLpr[b->shape] : 0; }
+int b2r_batch_tile(const b2r_batch* b)
+{
+    if (!b) return 0;
+    for (int k = 1; k < b->n; ++k)
+        if (b->host[k].lpr != b->host[0].lpr) return 0;
+    return 4 * b->host[0].lpr;
+}
+
+int b2r_batch_instance_tile(const b2r_batch* b, int i)
+{
+    return b && i >= 0 && i < b->n ? 4 * b->host[b->pos[i]].lpr : 0;
+}
+
+b2r_status b2r_batch_set_pass_steps(b2r_batch* b, int steps)
+{
+    if (!b) return bfail(B2R_ERR_ARG, "null batch");
+    if (steps != 1 && steps != 2) return bfail(B2R_ERR_ARG, "steps per pass must be 1 or 2");
+    std::vector<int> sh(b->n);
+    for (int k = 0; k < b->n; ++k)
+        sh[k] = b->host[k].D == 1 ? (steps == 2 ? kTwoStep : default_shape(b, k)) : b->host[k].shape;
+    return apply_shapes(b, sh);
+}
+
+int b2r_batch_instance_pass_steps(const b2r_batch* b, int i)
+{
+    return b && i >= 0 && i < b->n ? b->host[b->pos[i]].tb : 0;
+}
 
 }  // extern "C"

@@ -22,6 +22,15 @@ constexpr int kBX = 32, kBY = 8;
 enum { VX, VY, VZ, SXX, SXY, SXZ, SYY, SYZ, SZZ, DISP };
 
 __device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+// NC: the read-only path (fields that no thread writes during the kernel);
+// otherwise a coherent load, for a persistent kernel whose other CTAs
+// update the fields between its work units
+template <bool NC>
+__device__ __forceinline__ float4 ldf4(const float* p)
+{
+    if constexpr (NC) return __ldg(reinterpret_cast<const float4*>(p));
+    else return *reinterpret_cast<const float4*>(p);
+}
 __device__ __forceinline__ float4 ldw4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ float cmp(const float4& v, int j)
 {
@@ -31,14 +40,22 @@ __device__ __forceinline__ float cmp(const float4& v, int j)
 // 12 cells x-4 .. x+7 of a row around the thread's 4 cells
 struct Row12 {
     float v[12];
+    template <bool NC = true>
     __device__ __forceinline__ void load(const float* p)
     {
-        const float4 a = ld4(p - 4), b = ld4(p), c = ld4(p + 4);
+        const float4 a = ldf4<NC>(p - 4), b = ldf4<NC>(p), c = ldf4<NC>(p + 4);
         v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
         v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
         v[8] = c.x; v[9] = c.y; v[10] = c.z; v[11] = c.w;
     }
 };
+template <bool NC>
+__device__ __forceinline__ Row12 row12(const float* p)
+{
+    Row12 r{};
+    r.template load<NC>(p);
+    return r;
+}
 
 // five planes z-2 .. z+2 of the thread's 4 cells
 struct Q5v {
@@ -76,12 +93,25 @@ struct Cell {
     long long base;             // element offset of (xb, y, 0) in the field buffers
 };
 
-__device__ __forceinline__ bool cell_setup(const BlockLayout& L, const Win& w, int blk, Cell& c, int x0, int y0)
+// The thread's place in a stage launch: tile (bx, by), thread (tx, ty) of a
+// CTA of dx x dy threads -- the launch's own indices, or those a persistent
+// kernel assigns to a work unit.
+struct TilePos {
+    int bx, by, tx, ty, dx, dy;
+};
+__device__ __forceinline__ TilePos launch_pos()
 {
-    const int xs0 = x0 + blockIdx.x * (4 * blockDim.x) + 4 * threadIdx.x;
+    return TilePos{(int)blockIdx.x, (int)blockIdx.y, (int)threadIdx.x, (int)threadIdx.y, (int)blockDim.x,
+                   (int)blockDim.y};
+}
+
+__device__ __forceinline__ bool cell_setup(const BlockLayout& L, const Win& w, int blk, Cell& c, int x0, int y0,
+                                           const TilePos& q)
+{
+    const int xs0 = x0 + q.bx * (4 * q.dx) + 4 * q.tx;
     c.blk = blk;
     c.xb = xs0 - L.xoff;
-    c.y = y0 + blockIdx.y * blockDim.y + threadIdx.y;
+    c.y = y0 + q.by * q.dy + q.ty;
     if (!w.ok || c.y < w.lo[1] || c.y > w.hi[1]) return false;
     c.any = false;
     c.all = true;
@@ -93,6 +123,10 @@ __device__ __forceinline__ bool cell_setup(const BlockLayout& L, const Win& w, i
     }
     c.base = (long long)blk * L.bstride + (long long)c.y * L.P + xs0;
     return c.any;
+}
+__device__ __forceinline__ bool cell_setup(const BlockLayout& L, const Win& w, int blk, Cell& c, int x0, int y0)
+{
+    return cell_setup(L, w, blk, c, x0, y0, launch_pos());
 }
 
 // Read-modify-write of the thread's 4 cells, split so that every load of an
@@ -203,31 +237,29 @@ __device__ __forceinline__ void stress_update(const StressIn& e, float dt, float
 //   ay = Dm_x xy + Dp_y yy + Dm_z yz
 //   az = Dm_x xz + Dm_y yz + Dp_z zz
 // z neighbours come from register queues advanced one plane per eval().
-struct VelOp {
+template <bool NC>
+struct VelOpT {
     const float *xx, *xy, *xz, *yy, *yz, *zz;
     Q5v qxz, qyz, qzz;
     __device__ __forceinline__ void begin(int zs, long long S)
     {
         const long long o = (long long)(zs - 2) * S;
-        qxz.m1 = ld4(xz + o); qyz.m1 = ld4(yz + o); qzz.m1 = ld4(zz + o);
-        qxz.c = ld4(xz + o + S); qyz.c = ld4(yz + o + S); qzz.c = ld4(zz + o + S);
-        qxz.p1 = ld4(xz + o + 2 * S); qyz.p1 = ld4(yz + o + 2 * S); qzz.p1 = ld4(zz + o + 2 * S);
-        qxz.p2 = ld4(xz + o + 3 * S); qyz.p2 = ld4(yz + o + 3 * S); qzz.p2 = ld4(zz + o + 3 * S);
+        qxz.m1 = ldf4<NC>(xz + o); qyz.m1 = ldf4<NC>(yz + o); qzz.m1 = ldf4<NC>(zz + o);
+        qxz.c = ldf4<NC>(xz + o + S); qyz.c = ldf4<NC>(yz + o + S); qzz.c = ldf4<NC>(zz + o + S);
+        qxz.p1 = ldf4<NC>(xz + o + 2 * S); qyz.p1 = ldf4<NC>(yz + o + 2 * S); qzz.p1 = ldf4<NC>(zz + o + 2 * S);
+        qxz.p2 = ldf4<NC>(xz + o + 3 * S); qyz.p2 = ldf4<NC>(yz + o + 3 * S); qzz.p2 = ldf4<NC>(zz + o + 3 * S);
     }
     // o: element offset of plane z; planes must be visited in increasing z
     __device__ __forceinline__ void eval(long long o, long long P, long long S, float (&ax)[4],
                                          float (&ay)[4], float (&az)[4])
     {
-        qxz.shift(ld4(xz + o + 2 * S));
-        qyz.shift(ld4(yz + o + 2 * S));
-        qzz.shift(ld4(zz + o + 2 * S));
-        Row12 rxx, rxy, rxz;
-        rxx.load(xx + o);
-        rxy.load(xy + o);
-        rxz.load(xz + o);
-        const float4 xym2 = ld4(xy + o - 2 * P), xym1 = ld4(xy + o - P), xyp1 = ld4(xy + o + P);
-        const float4 yym1 = ld4(yy + o - P), yyc = ld4(yy + o), yyp1 = ld4(yy + o + P), yyp2 = ld4(yy + o + 2 * P);
-        const float4 yzm2 = ld4(yz + o - 2 * P), yzm1 = ld4(yz + o - P), yzp1 = ld4(yz + o + P);
+        qxz.shift(ldf4<NC>(xz + o + 2 * S));
+        qyz.shift(ldf4<NC>(yz + o + 2 * S));
+        qzz.shift(ldf4<NC>(zz + o + 2 * S));
+        const Row12 rxx = row12<NC>(xx + o), rxy = row12<NC>(xy + o), rxz = row12<NC>(xz + o);
+        const float4 xym2 = ldf4<NC>(xy + o - 2 * P), xym1 = ldf4<NC>(xy + o - P), xyp1 = ldf4<NC>(xy + o + P);
+        const float4 yym1 = ldf4<NC>(yy + o - P), yyc = ldf4<NC>(yy + o), yyp1 = ldf4<NC>(yy + o + P), yyp2 = ldf4<NC>(yy + o + 2 * P);
+        const float4 yzm2 = ldf4<NC>(yz + o - 2 * P), yzm1 = ldf4<NC>(yz + o - P), yzp1 = ldf4<NC>(yz + o + P);
         const float4 xyc = make_float4(rxy.v[4], rxy.v[5], rxy.v[6], rxy.v[7]);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -242,32 +274,30 @@ struct VelOp {
 // velocity-like fields x, y, z:
 //   e[0] = Dm_x x, e[1] = Dm_y y, e[2] = Dm_z z,
 //   e[3] = Dp_y x + Dp_x y, e[4] = Dp_z x + Dp_x z, e[5] = Dp_z y + Dp_y z
-struct StrOp {
+template <bool NC>
+struct StrOpT {
     const float *x, *y, *z;
     Q5v qx, qy, qz;
     __device__ __forceinline__ void begin(int zs, long long S)
     {
         const long long o = (long long)(zs - 2) * S;
-        qx.m1 = ld4(x + o); qy.m1 = ld4(y + o); qz.m1 = ld4(z + o);
-        qx.c = ld4(x + o + S); qy.c = ld4(y + o + S); qz.c = ld4(z + o + S);
-        qx.p1 = ld4(x + o + 2 * S); qy.p1 = ld4(y + o + 2 * S); qz.p1 = ld4(z + o + 2 * S);
-        qx.p2 = ld4(x + o + 3 * S); qy.p2 = ld4(y + o + 3 * S); qz.p2 = ld4(z + o + 3 * S);
+        qx.m1 = ldf4<NC>(x + o); qy.m1 = ldf4<NC>(y + o); qz.m1 = ldf4<NC>(z + o);
+        qx.c = ldf4<NC>(x + o + S); qy.c = ldf4<NC>(y + o + S); qz.c = ldf4<NC>(z + o + S);
+        qx.p1 = ldf4<NC>(x + o + 2 * S); qy.p1 = ldf4<NC>(y + o + 2 * S); qz.p1 = ldf4<NC>(z + o + 2 * S);
+        qx.p2 = ldf4<NC>(x + o + 3 * S); qy.p2 = ldf4<NC>(y + o + 3 * S); qz.p2 = ldf4<NC>(z + o + 3 * S);
     }
     __device__ __forceinline__ void eval(long long o, long long P, long long S, float (&e)[6][4])
     {
-        qx.shift(ld4(x + o + 2 * S));
-        qy.shift(ld4(y + o + 2 * S));
-        qz.shift(ld4(z + o + 2 * S));
-        Row12 rx, ry, rz;
-        rx.load(x + o);
-        ry.load(y + o);
-        rz.load(z + o);
+        qx.shift(ldf4<NC>(x + o + 2 * S));
+        qy.shift(ldf4<NC>(y + o + 2 * S));
+        qz.shift(ldf4<NC>(z + o + 2 * S));
+        const Row12 rx = row12<NC>(x + o), ry = row12<NC>(y + o), rz = row12<NC>(z + o);
         const float4 xc = make_float4(rx.v[4], rx.v[5], rx.v[6], rx.v[7]);
         const float4 yc = make_float4(ry.v[4], ry.v[5], ry.v[6], ry.v[7]);
         const float4 zc = make_float4(rz.v[4], rz.v[5], rz.v[6], rz.v[7]);
-        const float4 xm1 = ld4(x + o - P), xp1 = ld4(x + o + P), xp2 = ld4(x + o + 2 * P);
-        const float4 ym2 = ld4(y + o - 2 * P), ym1 = ld4(y + o - P), yp1 = ld4(y + o + P);
-        const float4 zm1 = ld4(z + o - P), zp1 = ld4(z + o + P), zp2 = ld4(z + o + 2 * P);
+        const float4 xm1 = ldf4<NC>(x + o - P), xp1 = ldf4<NC>(x + o + P), xp2 = ldf4<NC>(x + o + 2 * P);
+        const float4 ym2 = ldf4<NC>(y + o - 2 * P), ym1 = ldf4<NC>(y + o - P), yp1 = ldf4<NC>(y + o + P);
+        const float4 zm1 = ldf4<NC>(z + o - P), zp1 = ldf4<NC>(z + o + P), zp2 = ldf4<NC>(z + o + 2 * P);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             e[0][j] = dmx(rx, j);
@@ -279,6 +309,8 @@ struct StrOp {
         }
     }
 };
+using VelOp = VelOpT<true>;
+using StrOp = StrOpT<true>;
 
 // L2 prefetch of the thread's 16 bytes of a plane a few iterations ahead:
 // the z-marching stages are latency bound (each iteration waits on its own

@@ -77,24 +77,30 @@ __device__ __forceinline__ void ring_drain(const Ring& rg)
 
 // Sweep one unit.  Returns false if a bounded wait gave up (all threads
 // agree: the decision is taken after a __syncthreads on a shared flag).
+// LPR = 0: the tile shape is the run-time lpr (32, 16 or 8 lanes per tile
+// row), so that one kernel serves instances of different tile shapes; the
+// tensor map's box must match it.
 template <int D, int RY, int S, int SLOT, int LPR = 32>
 __device__ __forceinline__ bool sweep_unit(const CUtensorMap* tmap, float* __restrict__ out,
                                            const BlockLayout& L, int step_i, const HeatCoef& C,
-                                           int blk, int tx, int ty, int zi0, int zi1, Ring& rg)
+                                           int blk, int tx, int ty, int zi0, int zi1, Ring& rg, int lpr = LPR)
 {
-    using G = Cfg<D, RY, S, SLOT, LPR>;
-    constexpr int kTXW = G::TXW, kRPW = G::RPW;
+    if (LPR > 0) lpr = LPR;
+    const int lg = lpr == 32 ? 5 : (lpr == 16 ? 4 : 3);   // log2(lpr)
+    const int kTXW = 4 * lpr, kRPW = 32 >> lg;
+    const int kTY = kWarps * RY * kRPW, kBW = kTXW + 8;
+    const int kPLANE = kBW * (kTY + 2 * D);
     const int tid = threadIdx.x, warp = tid >> 5;
-    const int lane = (tid & 31) % LPR;        // x group of this thread in its row
-    const int sr = (tid & 31) / LPR;          // row of this thread within a row slot
+    const int lane = (tid & 31) & (lpr - 1);  // x group of this thread in its row
+    const int sr = (tid & 31) >> lg;          // row of this thread within a row slot
     const int edge = edge_bits(L, blk);
     int lo[3], hi[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) stage_region(L, edge, a, D * (step_i + 1), lo[a], hi[a]);
     const int xs0 = ((L.xoff + D) & ~3) + tx * kTXW;     // storage x of tile column 0
-    const int y0 = D + ty * G::TY;                       // block y of tile row 0
+    const int y0 = D + ty * kTY;                       // block y of tile row 0
     if (xs0 - L.xoff > hi[0] || xs0 + kTXW - 1 - L.xoff < lo[0]) return true;
-    if (y0 > hi[1] || y0 + G::TY - 1 < lo[1]) return true;
+    if (y0 > hi[1] || y0 + kTY - 1 < lo[1]) return true;
     const int zs = max(D + zi0, lo[2]);
     const int ze = min(D + zi1 - 1, hi[2]);
     if (zs > ze) return true;
@@ -110,7 +116,7 @@ __device__ __forceinline__ bool sweep_unit(const CUtensorMap* tmap, float* __res
     if (tid == 0) {
         for (int s = 0; s < S && s < np; ++s) {
             const unsigned g = gp + s;
-            mbar_expect_tx(&rg.bar[g % S], G::PLANE * sizeof(float));
+            mbar_expect_tx(&rg.bar[g % S], kPLANE * sizeof(float));
             tma_load_4d(rg.smem + (g % S) * SLOT, tmap, xs0 - 4, y0 - D, first + s, blk, &rg.bar[g % S]);
         }
     }
@@ -146,7 +152,7 @@ __device__ __forceinline__ bool sweep_unit(const CUtensorMap* tmap, float* __res
 #pragma unroll
             for (int k = 0; k < 2 * D; ++k) q[r2][k] = q[r2][k + 1];
             const int row = D + (warp * RY + r2) * kRPW + sr;
-            q[r2][2 * D] = *reinterpret_cast<const float4*>(pl + row * G::BW + 4 + 4 * lane);
+            q[r2][2 * D] = *reinterpret_cast<const float4*>(pl + row * kBW + 4 + 4 * lane);
         }
         if (pr >= 2 * D && vx_any) {
             const int z = first + pr - D;
@@ -156,7 +162,7 @@ __device__ __forceinline__ bool sweep_unit(const CUtensorMap* tmap, float* __res
                 const int y = y0 + (warp * RY + r2) * kRPW + sr;
                 if (y < lo[1] || y > hi[1]) continue;
                 const int row = D + (warp * RY + r2) * kRPW + sr;
-                const float* prow = pc + row * G::BW + 4 * lane;
+                const float* prow = pc + row * kBW + 4 * lane;
                 const float4 xl = *reinterpret_cast<const float4*>(prow);
                 const float4 c4 = q[r2][D];
                 const float4 xr = *reinterpret_cast<const float4*>(prow + 8);
@@ -167,8 +173,8 @@ __device__ __forceinline__ bool sweep_unit(const CUtensorMap* tmap, float* __res
                 for (int j = 0; j < 4; ++j) res[j] = a0 * v[4 + j];
 #pragma unroll
                 for (int k = 1; k <= D; ++k) {
-                    const float4 ym = *reinterpret_cast<const float4*>(prow + 4 - k * G::BW);
-                    const float4 yp = *reinterpret_cast<const float4*>(prow + 4 + k * G::BW);
+                    const float4 ym = *reinterpret_cast<const float4*>(prow + 4 - k * kBW);
+                    const float4 yp = *reinterpret_cast<const float4*>(prow + 4 + k * kBW);
                     const float4 zm = q[r2][D - k];
                     const float4 zp = q[r2][D + k];
                     const float ys[4] = {ym.x + yp.x, ym.y + yp.y, ym.z + yp.z, ym.w + yp.w};
@@ -200,7 +206,7 @@ __device__ __forceinline__ bool sweep_unit(const CUtensorMap* tmap, float* __res
             if (nxt < np) {
                 const unsigned g2 = gp + nxt;
                 if (tid == 0) {
-                    mbar_expect_tx(&rg.bar[g2 % S], G::PLANE * sizeof(float));
+                    mbar_expect_tx(&rg.bar[g2 % S], kPLANE * sizeof(float));
                     tma_load_4d(rg.smem + (g2 % S) * SLOT, tmap, xs0 - 4, y0 - D, first + nxt, blk,
                                 &rg.bar[g2 % S]);
                 }

@@ -63,6 +63,11 @@ WORKLOADS = {
     # steps U[50,500], seed 4, in one persistent launch replayed from a CUDA graph
     "batch64": dict(model=5, n=64, seed=4, env=(0, 0, 0), blocks=(1, 1, 1), R=1, D=0, sub_steps=0,
                     bytes_per_cell=8, kernel="batch_kernel"),
+    # 16 independent staggered elastic-wave instances (one block each, fixed shell),
+    # edges U{32,48,..,128} per axis, steps U[50,150], seed 6, layered model and a
+    # Ricker source at each centre, in one persistent launch replayed from a CUDA graph
+    "eqwp_batch16": dict(model=7, n=16, seed=6, env=(0, 0, 0), blocks=(1, 1, 1), R=1, D=2, sub_steps=0,
+                         bytes_per_cell=84, kernel="eqwp_batch_kernel"),
     # adjoint gradient of a receiver misfit wrt lambda, mu, rho: 256^3, layered model
     # + 5% Gaussian anomaly (sigma 8 cells) for the observed data, 64 receivers on the
     # top plane, Ricker 12 Hz, 2000 steps, checkpoints every 50 steps
@@ -441,7 +446,9 @@ def run_batch(args, wl):
     for i, a in enumerate(ins):
         bt.upload(i, a)
     tuned = bt.autotune()
-    tuned_tile = bt.tile
+    widths = bt.instance_tiles()
+    # instances per tile width, as the autotuner left them (per order and size class)
+    tuned_tile = {str(w): widths.count(w) for w in (128, 64, 32) if w in widths}
     lups = bt.lups
     for _ in range(args.warmup):
         bt.run()
@@ -512,7 +519,7 @@ def run_batch(args, wl):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded U[0,1))",
             "config": {"workload": args.workload, "instances": len(items), "lups_per_step": lups,
-                       "autotuned_zchunk": tuned[0], "autotuned_tile_width": tuned_tile,
+                       "autotuned_zchunk": tuned[0], "autotuned_tile_widths": tuned_tile,
                        "sequential_plain_glups": round(seq, 3),
                        "batched_over_sequential": round(value / seq, 3),
                        "max_rel_l2_vs_sequential": max_rel,
@@ -523,6 +530,105 @@ def run_batch(args, wl):
                          "kernel": "batch_kernel", "note": "8 B per lattice-site update, whole run"},
             "cpu_baseline": None, "clocks": clk, "parity": parity}
     return line
+
+
+def eqwp_batch_items(wl):
+    rng = np.random.default_rng(wl["seed"])
+    edges = np.arange(32, 129, 16)
+    return [dict(env=tuple(int(v) for v in rng.choice(edges, 3)), nsteps=int(rng.integers(50, 151)))
+            for _ in range(wl["n"])]
+
+
+def run_eqwp_batch(args, wl):
+    """Batched staggered elastic-wave instances vs the same handles stepped
+    one after the other (two-pass step, graphs of their own)."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    import b2r_gb300 as b2r
+    items = eqwp_batch_items(wl)
+    stream = torch.cuda.Stream(device=torch.device("cuda", 0))
+    h = 10.0
+    dt = 0.5 * h / (4000 * 3 ** 0.5 * (9 / 8 + 1 / 24))
+
+    def domains(st):
+        out = []
+        for it in items:
+            d = b2r.Domain(4, it["env"], D=2, R=1, dt=dt, h=h, src=tuple(e // 2 for e in it["env"]), stream=st)
+            mat, amps = stag_model(d.domain_shape, dt, 64 * max(i["nsteps"] for i in items))
+            for name, arr in zip(("lambda", "mu", "buoy"), mat):
+                d.upload(arr, field=name)
+            zero = np.zeros(d.domain_shape, np.float32)
+            for k in range(9):
+                d.upload(zero, field=k)
+            d.set_source(amps)
+            d.synchronize()
+            out.append(d)
+        return out
+
+    doms = domains(stream)
+    bt = b2r.EqwpBatch(doms, [it["nsteps"] for it in items], stream=stream)
+    lups = bt.lups
+    for _ in range(args.warmup):
+        bt.run()
+    bt.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    l0 = b2r.kernel_launches()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        bt.run()
+    e1.record(stream)
+    e1.synchronize()
+    launches = b2r.kernel_launches() - l0
+    bt.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    value = lups / (ms / 1e3) / 1e9
+    # the same handles, state and time steps included, stepped one after the
+    # other: timed, then compared field by field with the batch's next run
+    refs = domains(stream)
+    runs = args.warmup + args.steps
+    for r, it in zip(refs, items):
+        r.step(runs * it["nsteps"])
+    for r in refs:
+        r.synchronize()
+    seq_ms = 0.0
+    for r, it in zip(refs, items):
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        r.step(it["nsteps"])
+        a1.record(stream)
+        a1.synchronize()
+        seq_ms += a0.elapsed_time(a1)
+    bt.run()
+    bt.synchronize()
+    identical = all(np.array_equal(d.download(field=k), r.download(field=k))
+                    for d, r in zip(doms, refs) for k in range(9))
+    seq = lups / (seq_ms / 1e3) / 1e9
+    peak, peak_src = measured_peak()
+    achieved = wl["bytes_per_cell"] * lups / (ms / 1e3) / 1e9
+    bt.close()
+    for d in doms + refs:
+        d.close()
+    return {"metric": "GLUPS", "value": round(value, 3), "unit": "GLUPS", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded layered model, Ricker source)",
+            "config": {"workload": args.workload, "instances": len(items), "lups_per_step": lups,
+                       "sequential_plain_glups": round(seq, 3), "batched_over_sequential": round(value / seq, 3),
+                       "l2": "inputs larger than L2"},
+            "e2e": None, "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_src,
+                         "kernel": "eqwp_batch_kernel", "note": "84 B per cell-step, whole run"},
+            "cpu_baseline": None, "clocks": clk,
+            "parity": {"bit_identical_to_handles": identical,
+                       "note": "every field of every instance against the same handle stepped alone "
+                               "(two-pass step), which the GPU tests hold bit-identical to the FP32 oracle"}}
 
 
 def run_adjoint(args, wl):
@@ -929,6 +1035,8 @@ def run_workload(args, name):
         return run_batch(a, wl)
     if wl["model"] == 6:
         return run_adjoint(a, wl)
+    if wl["model"] == 7:
+        return run_eqwp_batch(a, wl)
     return run_ours(a, wl)
 
 
@@ -936,7 +1044,7 @@ def run_workload(args, name):
 # "secondary" by the default one-GPU run so that one invocation measures them
 # all on the same box: each with its own value, roofline fraction, clocks and
 # parity figure
-SECONDARY = ("heat_128", "gol_256", "eqwp_stag", "heat4_512", "batch64", "adjoint256")
+SECONDARY = ("heat_128", "gol_256", "eqwp_stag", "heat4_512", "batch64", "eqwp_batch16", "adjoint256")
 
 
 def compact(line):

@@ -354,16 +354,59 @@ b2r_status b2r_batch_synchronize(b2r_batch* b, void* cuda_stream);
 int64_t b2r_batch_lups(const b2r_batch* b);
 /* Planes per work unit along z (0 = whole column). */
 b2r_status b2r_batch_set_zchunk(b2r_batch* b, int zchunk);
-/* Tile shape of every instance: 128 x 16, 64 x 32 or 32 x 64 cells (x by
- * y, for D <= 2; half the rows for D >= 3), by width 128, 64 or 32; 0 picks
- * the shape that computes the fewest cells over the whole mix (the default
- * at creation).  b2r_batch_tile returns the current width. */
+/* Tile shape of the instances: 128 x 16, 64 x 32 or 32 x 64 cells (x by
+ * y, for D <= 2; half the rows for D >= 3), by width 128, 64 or 32, for
+ * every instance; 0 gives each instance the shape that computes the fewest
+ * cells of its planes (the default at creation).  Instances of different
+ * shapes share the one launch.  b2r_batch_tile returns the width shared by
+ * every instance (0 if they differ), b2r_batch_instance_tile the width of
+ * instance i (caller order). */
 b2r_status b2r_batch_set_tile(b2r_batch* b, int width);
 int b2r_batch_tile(const b2r_batch* b);
-/* Time whole runs with each tile shape x z-chunk candidate (8, 16, 32, 64,
- * whole column) on the uploaded inputs, keep the fastest and restore the
- * inputs. */
+int b2r_batch_instance_tile(const b2r_batch* b, int i);
+/* Time steps per HBM pass of the radius-1 instances: 2 puts every one of
+ * them on two-step units (tiles of 128 x 16 cells read once per two steps,
+ * the last unit of an odd step count taking one step; bit-identical to one
+ * step per pass), 1 back on one-step units of their fewest-cells shape.
+ * Instances of other radii keep their shapes.  b2r_batch_instance_pass_steps
+ * returns 1 or 2 for instance i (caller order). */
+b2r_status b2r_batch_set_pass_steps(b2r_batch* b, int steps);
+int b2r_batch_instance_pass_steps(const b2r_batch* b, int i);
+/* Autotune on the uploaded inputs (restored afterwards), timing whole runs:
+ * the z-chunk cap (8, 16, 32, 64, whole column), then the tile shape and
+ * steps per pass per (stencil order, size class) -- the instances of one
+ * class (order D, interior width <= 64, <= 128 or wider) try each tile shape
+ * and, at radius 1, the two-step units, while the others keep theirs --
+ * then the z-chunk cap again. */
 b2r_status b2r_batch_autotune(b2r_batch* b, void* cuda_stream, int* best_zchunk, double* best_ms);
+
+/* ---- batched elastic-wave instances (no reference counterpart) ----------- */
+/* Many staggered elastic-wave handles (B2R_MODEL_EQWP_STAG, one block each,
+ * fixed shell) of uneven sizes advanced in one persistent launch driven by a
+ * device work queue of (stage round, instance, tile chunk) items: a time step
+ * of an instance is its velocity stage then its stress stage, each waiting
+ * for the instance's previous stage to finish everywhere.  Each run advances
+ * handle i by nsteps[i] steps from its current time step, in place, with its
+ * own material and source; results are identical to b2r_step on each handle
+ * with the two-pass step.  The batch keeps pointers to the handles: they must
+ * outlive it, and their own streams must be idle during a run (b2r_synchronize
+ * before, b2r_eqwp_batch_synchronize after, then the handles are used as
+ * usual: b2r_download, b2r_step, b2r_time_step). */
+typedef struct b2r_eqwp_batch b2r_eqwp_batch;
+b2r_status b2r_eqwp_batch_create(b2r_handle* const* handles, const int* nsteps, int n, b2r_eqwp_batch** out);
+b2r_status b2r_eqwp_batch_destroy(b2r_eqwp_batch* b);
+const char* b2r_eqwp_batch_last_error(void);
+/* One run on the stream (asynchronous): the per-step source increments are
+ * copied first, then the persistent launch (captured once into a CUDA graph
+ * and replayed when use_graph != 0 and the stream is not the legacy default
+ * stream); every handle's time step advances by its nsteps. */
+b2r_status b2r_eqwp_batch_run(b2r_eqwp_batch* b, void* cuda_stream, int use_graph);
+/* Wait for the stream and report a device-side timeout of the work queue. */
+b2r_status b2r_eqwp_batch_synchronize(b2r_eqwp_batch* b, void* cuda_stream);
+/* Lattice-site updates of one run (sum of interior cells x steps). */
+int64_t b2r_eqwp_batch_lups(const b2r_eqwp_batch* b);
+/* Planes per work unit along z (default 32; 0 = whole column). */
+b2r_status b2r_eqwp_batch_set_zchunk(b2r_eqwp_batch* b, int zchunk);
 
 /* ---- diagnostics (no reference counterpart) ------------------------------- *
  * Run the device-side failure path once: a one-CTA kernel waits with the

@@ -1,4 +1,5 @@
-"""Batched persistent launch: every instance matches its own plain run."""
+"""Batched persistent launch: every instance matches its own plain run,
+whatever tile shape each instance runs with."""
 import numpy as np
 import pytest
 
@@ -27,15 +28,32 @@ def inputs(items, seed):
     return out
 
 
-@pytest.mark.parametrize("graph,tile", [(False, 0), (True, 0), (False, 128), (True, 64), (False, 32)])
-def test_batch_matches_plain_runs(b2r, orc, graph, tile):
+@pytest.mark.parametrize("graph,tile,steps", [(False, 0, 1), (True, 0, 1), (False, 128, 1), (True, 64, 1),
+                                              (False, 32, 1), (False, 0, 2), (True, 32, 2)])
+def test_batch_matches_plain_runs(b2r, orc, graph, tile, steps):
+    """steps = 2: the radius-1 instances on two-step units (odd step counts
+    end with a one-step unit), beside one-step instances of the other
+    radii in the same launch."""
     import torch
     items = mix(12, 1)
     ins = inputs(items, 2)
     s = torch.cuda.Stream()
     with b2r.Batch(items, stream=s) as bt:
         bt.set_tile(tile)
-        assert bt.tile in (128, 64, 32)
+        widths = bt.instance_tiles()
+        assert set(widths) <= {128, 64, 32}
+        if tile:
+            assert bt.tile == tile and set(widths) == {tile}
+        else:
+            # each instance on its own fewest-cells shape: this mix holds
+            # 64- and 32-cell-wide tiles in the one launch
+            assert len(set(widths)) >= 2 and bt.tile == 0
+        bt.set_pass_steps(steps)
+        ps = bt.instance_pass_steps()
+        assert ps == [steps if it["D"] == 1 else 1 for it in items]
+        if steps == 2:
+            d1 = [it["nsteps"] for it in items if it["D"] == 1]
+            assert any(n % 2 for n in d1) and any(n % 2 == 0 for n in d1)
         for i, a in enumerate(ins):
             bt.upload(i, a)
         bt.run(graph=graph)
@@ -73,6 +91,8 @@ def test_batch_autotune_keeps_inputs(b2r):
             bt.upload(i, a)
         z, ms = bt.autotune()
         assert z in (8, 16, 32, 64, 0) and ms > 0
+        assert set(bt.instance_tiles()) <= {128, 64, 32}
+        assert set(bt.instance_pass_steps()) <= {1, 2}
         bt.run()
         bt.synchronize()
         got = [bt.download(i) for i in range(len(items))]
@@ -111,9 +131,11 @@ def test_batches_with_different_schedules_coexist(b2r):
             assert np.array_equal(got, want)
 
 
-def test_batch_tiny_and_thin_instances(b2r):
+@pytest.mark.parametrize("steps", [1, 2])
+def test_batch_tiny_and_thin_instances(b2r, steps):
     """Instances smaller than one tile, and a few cells thick, next to a
-    larger one: each matches its own plain run."""
+    larger one: each matches its own plain run (radius 1 on one-step or
+    two-step units)."""
     import torch
     items = [dict(env=(5, 6, 7), D=1, nsteps=9), dict(env=(8, 8, 8), D=2, nsteps=4),
              dict(env=(16, 3, 40), D=1, nsteps=12), dict(env=(96, 80, 64), D=3, nsteps=6),
@@ -123,6 +145,7 @@ def test_batch_tiny_and_thin_instances(b2r):
     ins = inputs(items, 16)
     s = torch.cuda.Stream()
     with b2r.Batch(items, stream=s) as bt:
+        bt.set_pass_steps(steps)
         for i, a in enumerate(ins):
             bt.upload(i, a)
         bt.run()
