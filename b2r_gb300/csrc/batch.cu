@@ -144,6 +144,9 @@ __device__ __noinline__ uint4 run_two_step(const BatchArgs& a, int k, int t, int
 #ifndef B2R_BATCH_MINB
 #define B2R_BATCH_MINB 2   // resident CTAs per SM the register budget is fitted to (no spills)
 #endif
+// TWO: some instance runs on two-step units (a separate instantiation, so
+// that runs without them keep the one-step units' register allocation)
+template <bool TWO>
 __global__ void __launch_bounds__(kThreads, B2R_BATCH_MINB) batch_kernel(const BatchArgs a)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -193,7 +196,7 @@ __global__ void __launch_bounds__(kThreads, B2R_BATCH_MINB) batch_kernel(const B
         const int t = s_t, k = s_k, u = s_u;
         const InstDev& in = a.inst[k];
         bool ok;
-        if (in.tb == 2) {
+        if (TWO && in.tb == 2) {
             const uint4 r = run_two_step(a, k, t, u, rg.gp, rg.issued_hi, rg.stop, s1, rg.smem);
             rg.gp = r.x;
             rg.issued_hi = r.y;
@@ -242,7 +245,8 @@ struct b2r_batch {
     int maxrounds = 0;               // rounds of the current schedule's longest instance
     long long total = 0;
     int lz_policy = 16;              // z chunk cap per unit (autotuned)
-    int grid = 0;                    // persistent grid: every resident slot
+    int grid[2] = {0, 0};            // persistent grid (every resident slot) per kernel variant
+    bool two = false;                // some instance runs on two-step units
     size_t smem = 0;                 // ring + schedule tables
     cudaGraphExec_t gexec = nullptr;
     cudaStream_t gstream = nullptr;
@@ -360,8 +364,10 @@ b2r_status build_schedule(b2r_batch* b)
     std::vector<InstDev> dev(b->n);
     std::vector<CUtensorMap> maps(2 * b->n);
     b->maxrounds = 0;
+    b->two = false;
     for (int j = 0; j < b->n; ++j) {
         InstDev& in = b->host[b->sched[j]];
+        b->two = b->two || in.tb == 2;
         in.Lz = std::min(in.NZ, b->lz_policy > 0 ? b->lz_policy : in.NZ);
         in.nzc = (in.NZ + in.Lz - 1) / in.Lz;
         in.units = in.ntx * in.nty * in.nzc;
@@ -410,7 +416,8 @@ b2r_status enqueue_run(b2r_batch* b, cudaStream_t st)
     a.maxsteps = b->maxrounds;
     a.ninst = b->n;
     a.total = b->total;
-    batch_kernel<<<b->grid, kThreads, b->smem, st>>>(a);
+    if (b->two) batch_kernel<true><<<b->grid[1], kThreads, b->smem, st>>>(a);
+    else batch_kernel<false><<<b->grid[0], kThreads, b->smem, st>>>(a);
     BCK(cudaGetLastError(), "batch launch");
     return B2R_OK;
 }
@@ -500,12 +507,15 @@ b2r_status b2r_batch_create(const b2r_batch_item* items, int n, b2r_batch** out)
         // the limit is per function and device: only ever raised, so that a
         // batch with a smaller schedule does not lower it under one created
         // before it
-        static SmemLimit limit;
-        int occ = 0;
-        if (raise_smem_limit(limit, (const void*)batch_kernel, b->smem) != cudaSuccess)
-            return bail(bfail(B2R_ERR_CUDA, "smem attribute"));
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel, kThreads, b->smem);
-        b->grid = std::max(1, occ) * std::max(1, sms);
+        static SmemLimit limit[2];
+        const void* fns[2] = {(const void*)batch_kernel<false>, (const void*)batch_kernel<true>};
+        for (int v = 0; v < 2; ++v) {
+            int occ = 0;
+            if (raise_smem_limit(limit[v], fns[v], b->smem) != cudaSuccess)
+                return bail(bfail(B2R_ERR_CUDA, "smem attribute"));
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fns[v], kThreads, b->smem);
+            b->grid[v] = std::max(1, occ) * std::max(1, sms);
+        }
     }
     b2r_status st = apply_shapes(b, default_shapes(b));
     if (st != B2R_OK) return bail(st);

@@ -26,6 +26,7 @@
 #pragma once
 #include "b2r_common.cuh"
 #include "heat.h"
+#include "heat_upd.cuh"
 
 namespace b2r {
 namespace h2k {
@@ -39,31 +40,6 @@ constexpr int kOutW = 120;            // output cells per tile row
 constexpr int kOutH = kRows1 - 2;     // output rows (14)
 constexpr int kPlane = kBoxW * kBoxH; // floats per input plane
 constexpr int kP1 = kBoxW * kRows1;   // floats per stage-1 plane
-
-// one folded D = 1 update of 4 cells: c centre, l/r = x-1 / x+4 cells,
-// ym/yp/zm/zp neighbour float4s
-__device__ __forceinline__ float4 upd(const HeatCoef& C, float4 c, float l, float r, float4 ym,
-                                      float4 yp, float4 zm, float4 zp)
-{
-    float4 o;
-    o.x = C.a0 * c.x;
-    o.y = C.a0 * c.y;
-    o.z = C.a0 * c.z;
-    o.w = C.a0 * c.w;
-    o.x = fmaf(C.ax[0], l + c.y, o.x);
-    o.y = fmaf(C.ax[0], c.x + c.z, o.y);
-    o.z = fmaf(C.ax[0], c.y + c.w, o.z);
-    o.w = fmaf(C.ax[0], c.z + r, o.w);
-    o.x = fmaf(C.ay[0], ym.x + yp.x, o.x);
-    o.y = fmaf(C.ay[0], ym.y + yp.y, o.y);
-    o.z = fmaf(C.ay[0], ym.z + yp.z, o.z);
-    o.w = fmaf(C.ay[0], ym.w + yp.w, o.w);
-    o.x = fmaf(C.az[0], zm.x + zp.x, o.x);
-    o.y = fmaf(C.az[0], zm.y + zp.y, o.y);
-    o.z = fmaf(C.az[0], zm.z + zp.z, o.z);
-    o.w = fmaf(C.az[0], zm.w + zp.w, o.w);
-    return o;
-}
 
 // Per-CTA state of the plane loop.  The 3-plane queues rotate by index:
 // at loop phase PH (= pr mod 3) the newest plane goes to slot PH, so the
@@ -134,7 +110,7 @@ __device__ __forceinline__ void h2_iter(H2Ctx& c, int pr)
             const float rt = __shfl_down_sync(0xffffffffu, ce.x, 1);
             const float4 ym = rr == 0 ? up : c.q0[0][CZ];
             const float4 yp = rr == 0 ? c.q0[1][CZ] : dn;
-            const float4 v = upd(c.C, ce, l, rt, ym, yp, c.q0[rr][MZ], c.q0[rr][NZ]);
+            const float4 v = heat_upd4(c.C, ce, l, rt, ym, yp, c.q0[rr][MZ], c.q0[rr][NZ]);
             float4 res;
             if (zin) {
                 res.x = c.m1[rr][0] ? v.x : ce.x;
@@ -165,7 +141,7 @@ __device__ __forceinline__ void h2_iter(H2Ctx& c, int pr)
             const float rt = __shfl_down_sync(0xffffffffu, ce.x, 1);
             const float4 ym = rr == 0 ? up : c.q1[0][CZ];
             const float4 yp = rr == 0 ? c.q1[1][CZ] : dn;
-            const float4 v = upd(c.C, ce, l, rt, ym, yp, c.q1[rr][MZ], c.q1[rr][NZ]);
+            const float4 v = heat_upd4(c.C, ce, l, rt, ym, yp, c.q1[rr][MZ], c.q1[rr][NZ]);
             if (zin && c.in2y[rr] && c.st_any)
                 h2_store(c.outb + (long long)z2 * c.plane + (long long)(c.ya + rr) * c.P, v, c.st_all, c.in2x);
         }

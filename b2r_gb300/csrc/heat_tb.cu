@@ -30,6 +30,7 @@
 
 #include "b2r_common.cuh"
 #include "heat.h"
+#include "heat_upd.cuh"
 
 namespace b2r {
 namespace {
@@ -61,32 +62,6 @@ struct TbSched {
 
 __device__ __forceinline__ void pdl_wait_tb() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger_tb() { asm volatile("griddepcontrol.launch_dependents;"); }
-
-// one folded D = 1 update of 4 cells (the order of heat2.cu and heat.cu):
-// c centre, l / r = the cells left of x and right of x+3, ym / yp / zm / zp
-// neighbour float4s
-__device__ __forceinline__ float4 upd_tb(const HeatCoef& C, float4 c, float l, float r, float4 ym,
-                                         float4 yp, float4 zm, float4 zp)
-{
-    float4 o;
-    o.x = C.a0 * c.x;
-    o.y = C.a0 * c.y;
-    o.z = C.a0 * c.z;
-    o.w = C.a0 * c.w;
-    o.x = fmaf(C.ax[0], l + c.y, o.x);
-    o.y = fmaf(C.ax[0], c.x + c.z, o.y);
-    o.z = fmaf(C.ax[0], c.y + c.w, o.z);
-    o.w = fmaf(C.ax[0], c.z + r, o.w);
-    o.x = fmaf(C.ay[0], ym.x + yp.x, o.x);
-    o.y = fmaf(C.ay[0], ym.y + yp.y, o.y);
-    o.z = fmaf(C.ay[0], ym.z + yp.z, o.z);
-    o.w = fmaf(C.ay[0], ym.w + yp.w, o.w);
-    o.x = fmaf(C.az[0], zm.x + zp.x, o.x);
-    o.y = fmaf(C.az[0], zm.y + zp.y, o.y);
-    o.z = fmaf(C.az[0], zm.z + zp.z, o.z);
-    o.w = fmaf(C.az[0], zm.w + zp.w, o.w);
-    return o;
-}
 
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
@@ -193,7 +168,7 @@ __device__ __forceinline__ void tb_iter(TbCtx<T, LX>& c, int pr)
             if (c.lx == LX - 1) r = pc[(wrow + 1 + rr) * BW + 4 + CW];
             const float4 ym = rr == 0 ? up : in[1][0];
             const float4 yp = rr == 0 ? in[1][1] : dn;
-            const float4 v = fix(c, zk, rr, upd_tb(c.C, ce, l, r, ym, yp, in[0][rr], in[2][rr]), ce);
+            const float4 v = fix(c, zk, rr, heat_upd4(c.C, ce, l, r, ym, yp, in[0][rr], in[2][rr]), ce);
             c.q[qi<T, LX>(1)][NEW][rr] = v;
             st4(xo + (wrow + rr) * CW, v);
         }
@@ -218,7 +193,7 @@ __device__ __forceinline__ void tb_iter(TbCtx<T, LX>& c, int pr)
                 const float r = __shfl_down_sync(0xffffffffu, ce.x, 1, LX);
                 const float4 ym = rr == 0 ? up : c.q[qa][CUR][0];
                 const float4 yp = rr == 0 ? c.q[qa][CUR][1] : dn;
-                const float4 v = upd_tb(c.C, ce, l, r, ym, yp, c.q[qa][OLD][rr], c.q[qa][NEW][rr]);
+                const float4 v = heat_upd4(c.C, ce, l, r, ym, yp, c.q[qa][OLD][rr], c.q[qa][NEW][rr]);
                 res[rr] = s < T ? fix(c, zk, rr, v, ce) : v;
             }
             if (s < T) {

@@ -168,24 +168,26 @@ __device__ __forceinline__ bool sweep_unit(const CUtensorMap* tmap, float* __res
                 const float4 xr = *reinterpret_cast<const float4*>(prow + 8);
                 const float v[12] = {xl.x, xl.y, xl.z, xl.w, c4.x, c4.y, c4.z, c4.w,
                                      xr.x, xr.y, xr.z, xr.w};
-                float res[4];
-#pragma unroll
-                for (int j = 0; j < 4; ++j) res[j] = a0 * v[4 + j];
+                // cells (0, 1) and (2, 3) in packed two-lane FP32 operations,
+                // each lane the scalar round-to-nearest one (heat_upd.cuh)
+                float2 lo = __fmul2_rn(make_float2(a0, a0), make_float2(v[4], v[5]));
+                float2 hi = __fmul2_rn(make_float2(a0, a0), make_float2(v[6], v[7]));
 #pragma unroll
                 for (int k = 1; k <= D; ++k) {
                     const float4 ym = *reinterpret_cast<const float4*>(prow + 4 - k * kBW);
                     const float4 yp = *reinterpret_cast<const float4*>(prow + 4 + k * kBW);
                     const float4 zm = q[r2][D - k];
                     const float4 zp = q[r2][D + k];
-                    const float ys[4] = {ym.x + yp.x, ym.y + yp.y, ym.z + yp.z, ym.w + yp.w};
-                    const float zsum[4] = {zm.x + zp.x, zm.y + zp.y, zm.z + zp.z, zm.w + zp.w};
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        res[j] = fmaf(ax[k - 1], v[4 + j - k] + v[4 + j + k], res[j]);
-                        res[j] = fmaf(ay[k - 1], ys[j], res[j]);
-                        res[j] = fmaf(az[k - 1], zsum[j], res[j]);
-                    }
+                    const float2 cx = make_float2(ax[k - 1], ax[k - 1]), cy = make_float2(ay[k - 1], ay[k - 1]),
+                                 cz = make_float2(az[k - 1], az[k - 1]);
+                    lo = __ffma2_rn(cx, make_float2(v[4 - k] + v[4 + k], v[5 - k] + v[5 + k]), lo);
+                    hi = __ffma2_rn(cx, make_float2(v[6 - k] + v[6 + k], v[7 - k] + v[7 + k]), hi);
+                    lo = __ffma2_rn(cy, __fadd2_rn(make_float2(ym.x, ym.y), make_float2(yp.x, yp.y)), lo);
+                    hi = __ffma2_rn(cy, __fadd2_rn(make_float2(ym.z, ym.w), make_float2(yp.z, yp.w)), hi);
+                    lo = __ffma2_rn(cz, __fadd2_rn(make_float2(zm.x, zm.y), make_float2(zp.x, zp.y)), lo);
+                    hi = __ffma2_rn(cz, __fadd2_rn(make_float2(zm.z, zm.w), make_float2(zp.z, zp.w)), hi);
                 }
+                const float res[4] = {lo.x, lo.y, hi.x, hi.y};
                 float* dst = outb + (long long)z * L.plane + (long long)y * L.P;
                 if (vx_all) {
                     *reinterpret_cast<float4*>(dst) = make_float4(res[0], res[1], res[2], res[3]);
