@@ -447,8 +447,10 @@ def run_batch(args, wl):
         bt.upload(i, a)
     tuned = bt.autotune()
     widths = bt.instance_tiles()
-    # instances per tile width, as the autotuner left them (per order and size class)
+    # instances per tile width and on two-step units, as the autotuner left
+    # them (per order and size class)
     tuned_tile = {str(w): widths.count(w) for w in (128, 64, 32) if w in widths}
+    tuned_tile["two_step"] = bt.instance_pass_steps().count(2)
     lups = bt.lups
     for _ in range(args.warmup):
         bt.run()
