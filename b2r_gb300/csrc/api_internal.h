@@ -34,7 +34,7 @@ struct b2r_handle {
     int cur = 0;
     CUtensorMap tmap[2];
     CUtensorMap tmap2[2];       // boxes of the two-step kernel (D = 1)
-    CUtensorMap tmap3[2];       // boxes of the several-step kernel's 128 x 32 tiles (D = 1)
+    CUtensorMap tmap3[2];       // boxes of the several-step kernel's 128 x 32 tiles (D = 1) or of the radius-2 two-step kernel
     CUtensorMap tmap4[2];       // boxes of its 64 x 64 tiles
     HeatCoef hc{};
     HeatTune tune{};

@@ -234,6 +234,9 @@ b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* bes
                 for (int z2 : {0, 32, 48, 96, 128}) cands.push_back({tb, z2, 0, 0, 1, 0, tbn});
         }
         trial_steps = (trial_steps + 11) / 12 * 12;
+    } else if (h->cfg.D == 2) {
+        for (int z2 : {0, 32, 64, 96, 128}) cands.push_back({2, z2, 0, 0, 1, 0, 0});
+        trial_steps = (trial_steps + 1) / 2 * 2;
     }
     for (int pdl = 0; pdl < 2; ++pdl)
         for (int zc : zchunks)

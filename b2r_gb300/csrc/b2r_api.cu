@@ -108,18 +108,30 @@ b2r_status build_heat_maps(b2r_handle* h)
              !make_block_tmap(&h->tmap3[b], h->buf[b], h->L, 4, heat_tb_box_w(0), heat_tb_box_h(0), 1) ||
              !make_block_tmap(&h->tmap4[b], h->buf[b], h->L, 4, heat_tb_box_w(1), heat_tb_box_h(1), 1)))
             return fail(h, B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed for the heat field");
+        if (h->cfg.D == 2 &&
+            !make_block_tmap(&h->tmap3[b], h->buf[b], h->L, 4, heat_tb2_box_w(), heat_tb2_box_h(), 1))
+            return fail(h, B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed for the heat field");
     }
     return B2R_OK;
 }
 
-// Time steps one heat launch may take from sub-step i with `left` to go:
-// radius 1 takes up to tblock (<= 4) per HBM pass, and no halo exchange may
-// fall between them -- within one period, or any number when the exchange is
-// empty (one block, not periodic); 1 = the one-step sweep.
+// Steps per HBM pass the heat schedule allows: radius 1 up to tblock (<= 4),
+// radius 2 two (tblock >= 2); 1 = the one-step sweep.
+int heat_max_pass_steps(const b2r_handle* h)
+{
+    if (h->cfg.model != B2R_MODEL_HEAT || h->tune.tblock < 2) return 1;
+    if (h->cfg.D == 1) return std::min(h->tune.tblock, 4);
+    return h->cfg.D == 2 ? 2 : 1;
+}
+
+// Time steps one heat launch may take from sub-step i with `left` to go: up
+// to heat_max_pass_steps, and no halo exchange may fall between them --
+// within one period, or any number when the exchange is empty (one block,
+// not periodic); 1 = the one-step sweep.
 int heat_pass_steps(const b2r_handle* h, int i, int left)
 {
-    if (h->cfg.model != B2R_MODEL_HEAT || h->cfg.D != 1 || h->tune.tblock < 2) return 1;
-    int k = std::min(std::min(h->tune.tblock, 4), left);
+    if (heat_max_pass_steps(h) < 2) return 1;
+    int k = std::min(heat_max_pass_steps(h), left);
     if (!(h->L.nblk == 1 && !h->L.periodic)) k = std::min(k, h->cfg.R - i);
     return std::max(k, 1);
 }
@@ -144,11 +156,9 @@ int gol_pass_gens(const b2r_handle* h, int i, int left)
 int graph_periods(const b2r_handle* h)
 {
     int m = (32 + h->cfg.R - 1) / h->cfg.R;
-    if (h->cfg.model == B2R_MODEL_HEAT && h->cfg.D == 1 && h->tune.tblock >= 2 && h->L.nblk == 1 &&
-        !h->L.periodic) {
-        const int k = std::min(h->tune.tblock, 4);
+    const int k = heat_max_pass_steps(h);
+    if (k >= 2 && h->L.nblk == 1 && !h->L.periodic)
         while ((m * h->cfg.R) % k) ++m;
-    }
     return m;
 }
 
@@ -319,7 +329,11 @@ b2r_status advance(b2r_handle* h, int n)
             s += gg;
             h->halos_fresh = push;
         } else if (const int k = heat_pass_steps(h, i, n - s); k >= 2) {
-            if (k == 2 && !h->tune.tb16) {
+            if (h->cfg.D == 2) {
+                CK(h, launch_heat_substep_tb2(&h->tmap3[h->cur], static_cast<float*>(h->buf[1 - h->cur]), h->L, i,
+                                              h->hc, h->d_status, h->stream, h->tune.zchunk2));
+                h->cur = 1 - h->cur;
+            } else if (k == 2 && !h->tune.tb16) {
                 if ((st = substep2(h, i)) != B2R_OK) return st;
             } else {
                 CK(h, launch_heat_substep_tb(k, h->tune.tbn, h->tune.tbn ? &h->tmap4[h->cur] : &h->tmap3[h->cur],

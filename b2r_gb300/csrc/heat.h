@@ -37,7 +37,7 @@ struct HeatTune {
     int zchunk = 0;        // output planes per work unit; 0 = 16 (fewer for small grids)
     int ctas_per_sm = 0;   // 0 = one CTA per unit; k > 0 = persistent, k CTAs per SM
     int pdl = 1;           // programmatic dependent launch on the stream
-    int tblock = 2;        // time steps per HBM pass, radius 1 only (2 = heat2.cu, 3-4 = heat_tb.cu)
+    int tblock = 2;        // time steps per HBM pass: radius 1 (2 = heat2.cu, 3-4 = heat_tb.cu), radius 2 (2 = heat_tb2.cu)
     int zchunk2 = 0;       // output planes per unit of the several-step kernels (0 = 16 / 64)
     int tb16 = 0;          // two steps per pass: 0 = heat2.cu (8-warp CTAs), 1 = heat_tb.cu (16 warps)
     int tbn = 0;           // heat_tb.cu tiles: 0 = 128 x 32 cells, 1 = 64 x 64 cells
@@ -55,6 +55,14 @@ int heat2_box_w();
 int heat2_box_h();
 cudaError_t launch_heat_substep2(const CUtensorMap* tin, float* out, const BlockLayout& L, int step_i,
                                  const HeatCoef& c, int* status, cudaStream_t st, int zchunk);
+
+// Two sub-steps (step_i, step_i+1) of radius 2 per launch (heat_tb2.cu),
+// on tiles of 64 x 64 cells.  The tensor map must have the box
+// heat_tb2_box_w() x heat_tb2_box_h().
+int heat_tb2_box_w();
+int heat_tb2_box_h();
+cudaError_t launch_heat_substep_tb2(const CUtensorMap* tin, float* out, const BlockLayout& L, int step_i,
+                                    const HeatCoef& c, int* status, cudaStream_t st, int zchunk);
 
 // T = 2, 3 or 4 sub-steps (step_i .. step_i+T-1) of radius 1 per launch
 // (heat_tb.cu), on tiles of 128 x 32 cells (narrow = 0) or 64 x 64 cells

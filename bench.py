@@ -53,6 +53,9 @@ WORKLOADS = {
     # FP32 heat delta4 (fdm_heat_diffuse_delta4), 512^3
     "heat4_512": dict(model=1, env=(512, 512, 512), blocks=(1, 1, 1), R=1, D=4, sub_steps=100,
                       coef=(0.02, 1.0, 1.0, 1.0), bytes_per_cell=8, kernel="heat_sweep_kernel<4>"),
+    # FP32 heat delta2 (fdm_heat_diffuse_delta2), 512^3: the radius-2 temporal-blocking case
+    "heat2_512": dict(model=1, env=(512, 512, 512), blocks=(1, 1, 1), R=1, D=2, sub_steps=100,
+                      coef=(0.02, 1.0, 1.0, 1.0), bytes_per_cell=8, kernel="heat_sweep_kernel<2>"),
     # heat delta1 on the 128^3 case with the reference's constants (fits in L2)
     "heat_128": dict(model=1, env=(128, 128, 128), blocks=(1, 1, 1), R=1, D=1, sub_steps=100,
                      coef=(0.01, 1.0, 1.0, 0.5), bytes_per_cell=8, kernel="heat_sweep_kernel<1>"),
@@ -966,6 +969,7 @@ def run_ours(args, wl):
         w16 = (tuned or tune or {}).get("tb16", 0)
         tile = "64 x 64" if (tuned or tune or {}).get("tb_narrow", 0) else "128 x 32"
         kern = (wl["kernel"] if steps_per_launch < 1.5 else
+                "heat_tb2_kernel (radius 2, two time steps per launch, 64 x 64-cell tiles)" if wl["D"] == 2 else
                 "heat2_kernel (two time steps per launch)" if tb == 2 and not w16 else
                 f"heat_tb_kernel<{tb}> ({tb} time steps per launch, {tile}-cell tiles)")
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",

@@ -171,6 +171,38 @@ def test_several_step_sweeps_bit_identical(b2r, orc, env, blocks, R, periodic, t
         assert rel_l2(outs[1], ref) <= TOL
 
 
+@pytest.mark.parametrize("env,blocks,R,periodic", [((131, 37, 29), (1, 1, 1), 1, False),
+                                                   ((250, 61, 47), (1, 1, 1), 3, False),
+                                                   ((96, 48, 64), (2, 2, 2), 3, False),
+                                                   ((64, 64, 48), (2, 1, 2), 4, True),
+                                                   ((33, 17, 9), (1, 1, 1), 1, False),
+                                                   ((200, 130, 70), (1, 1, 1), 2, False),
+                                                   ((240, 52, 40), (2, 2, 1), 5, False),
+                                                   ((96, 96, 96), (2, 2, 2), 6, True),
+                                                   ((7, 130, 12), (1, 1, 1), 1, False)])
+@pytest.mark.parametrize("zc2", [0, 9, 64])
+def test_radius2_two_step_sweep_bit_identical(b2r, orc, env, blocks, R, periodic, zc2):
+    """Two sub-steps of radius 2 per HBM pass (heat_tb2.cu) against one step
+    per launch: 11 steps, so runs end with a one-step pass, and passes stop
+    at period ends where the blocks exchange halos (R = 1 and odd R leave
+    one-step passes inside the run)."""
+    bc = b2r.BC_PERIODIC if periodic else b2r.BC_SHELL
+    rng = np.random.default_rng(9)
+    dom = rng.random(env[::-1], dtype=np.float32) if periodic else shell_domain(env, 2, 9)
+    outs = []
+    for t in (1, 2):
+        with b2r.Domain(b2r.MODEL_HEAT, env, blocks=blocks, R=R, D=2, boundary=bc, alpha_dt=0.03) as d:
+            d.set_tuning(tblock=t, zchunk2=zc2)
+            d.upload(dom)
+            d.step(11)
+            outs.append(d.download())
+    assert np.array_equal(outs[0], outs[1])
+    if not periodic:
+        ref = dom.copy()
+        orc.heat_run(ref, 2, 2, 11, 0.03, 1.0, 1.0, 1.0)
+        assert rel_l2(outs[1], ref) <= TOL
+
+
 @pytest.mark.parametrize("env", [(64, 2, 48), (2, 40, 33), (37, 29, 2), (3, 3, 3)])
 @pytest.mark.parametrize("D", [1, 2])
 def test_heat_thin_domains(b2r, orc, env, D):
