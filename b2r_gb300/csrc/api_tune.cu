@@ -22,6 +22,7 @@ b2r_status b2r_set_tuning(b2r_handle* h, int key, int value)
     case B2R_TUNE_GOL_PUSH: h->gol_push = value != 0; break;
     case B2R_TUNE_TB16: h->tune.tb16 = value != 0; break;
     case B2R_TUNE_TB_NARROW: h->tune.tbn = value != 0; break;
+    case B2R_TUNE_TB_R2: h->tune.r2 = value != 0; break;
     default: return fail(h, B2R_ERR_ARG, "unknown tuning key %d", key);
     }
     drop_graphs(h);
@@ -43,6 +44,7 @@ b2r_status b2r_get_tuning(const b2r_handle* h, int key, int* value)
     case B2R_TUNE_GOL_PUSH: *value = h->gol_push ? 1 : 0; break;
     case B2R_TUNE_TB16: *value = h->tune.tb16; break;
     case B2R_TUNE_TB_NARROW: *value = h->tune.tbn; break;
+    case B2R_TUNE_TB_R2: *value = h->tune.r2; break;
     default: return fail(nullptr, B2R_ERR_ARG, "unknown tuning key %d", key);
     }
     return B2R_OK;
@@ -224,7 +226,7 @@ b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* bes
     // per pass) by z-chunk, then the one-step sweep by z-chunk x persistent
     // CTAs per SM x PDL.  Every trial advances a multiple of 12 time steps,
     // so that each schedule runs whole passes.
-    struct Cand { int tb, zc2, zc, cp, pdl, tb16, tbn; };
+    struct Cand { int tb, zc2, zc, cp, pdl, tb16, tbn, r2 = 0; };
     std::vector<Cand> cands;
     if (h->cfg.D == 1) {
         for (int z2 : {4, 8, 16, 32, 64}) cands.push_back({2, z2, 0, 0, 1, 0, 0});
@@ -235,7 +237,7 @@ b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* bes
         }
         trial_steps = (trial_steps + 11) / 12 * 12;
     } else if (h->cfg.D == 2) {
-        for (int z2 : {0, 32, 64, 96, 128}) cands.push_back({2, z2, 0, 0, 1, 0, 0});
+        for (int z2 : {0, 32, 64, 96, 128}) cands.push_back({2, z2, 0, 0, 1, 0, 0, 1});
         trial_steps = (trial_steps + 1) / 2 * 2;
     }
     for (int pdl = 0; pdl < 2; ++pdl)
@@ -246,6 +248,7 @@ b2r_status b2r_autotune(b2r_handle* h, int trial_steps, int best[3], double* bes
         if (st != B2R_OK) break;
         h->tune.tb16 = cd.tb16;
         h->tune.tbn = cd.tbn;
+        h->tune.r2 = cd.r2;
         h->tune.tblock = cd.tb;
         h->tune.zchunk2 = cd.zc2;
         h->tune.zchunk = cd.zc;

@@ -121,7 +121,7 @@ int heat_max_pass_steps(const b2r_handle* h)
 {
     if (h->cfg.model != B2R_MODEL_HEAT || h->tune.tblock < 2) return 1;
     if (h->cfg.D == 1) return std::min(h->tune.tblock, 4);
-    return h->cfg.D == 2 ? 2 : 1;
+    return h->cfg.D == 2 && h->tune.r2 ? 2 : 1;
 }
 
 // Time steps one heat launch may take from sub-step i with `left` to go: up

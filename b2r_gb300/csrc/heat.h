@@ -37,10 +37,11 @@ struct HeatTune {
     int zchunk = 0;        // output planes per work unit; 0 = 16 (fewer for small grids)
     int ctas_per_sm = 0;   // 0 = one CTA per unit; k > 0 = persistent, k CTAs per SM
     int pdl = 1;           // programmatic dependent launch on the stream
-    int tblock = 2;        // time steps per HBM pass: radius 1 (2 = heat2.cu, 3-4 = heat_tb.cu), radius 2 (2 = heat_tb2.cu)
+    int tblock = 2;        // time steps per HBM pass: radius 1 (2 = heat2.cu, 3-4 = heat_tb.cu), radius 2 (2 = heat_tb2.cu, with r2)
     int zchunk2 = 0;       // output planes per unit of the several-step kernels (0 = 16 / 64)
     int tb16 = 0;          // two steps per pass: 0 = heat2.cu (8-warp CTAs), 1 = heat_tb.cu (16 warps)
     int tbn = 0;           // heat_tb.cu tiles: 0 = 128 x 32 cells, 1 = 64 x 64 cells
+    int r2 = 0;            // radius 2: 1 = two steps per pass (heat_tb2.cu) when tblock >= 2
 };
 
 // One sub-step of every block: units (block, z-chunk, tile row, tile column)

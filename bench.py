@@ -865,7 +865,7 @@ def run_ours(args, wl):
     # this shape (timed on the live fields, which it restores); not part of
     # the timing
     tuned = None
-    knobs = {1: ("zchunk", "ctas_per_sm", "pdl", "tblock", "zchunk2", "tb16", "tb_narrow"),
+    knobs = {1: ("zchunk", "ctas_per_sm", "pdl", "tblock", "zchunk2", "tb16", "tb_narrow", "tb_r2"),
              2: ("tblock", "gol_bytes", "gol_push"), 4: ("eqwp_fused",)}
     if wl["model"] in knobs and not tune:
         d.autotune(trial_steps=4)

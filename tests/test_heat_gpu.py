@@ -192,7 +192,7 @@ def test_radius2_two_step_sweep_bit_identical(b2r, orc, env, blocks, R, periodic
     outs = []
     for t in (1, 2):
         with b2r.Domain(b2r.MODEL_HEAT, env, blocks=blocks, R=R, D=2, boundary=bc, alpha_dt=0.03) as d:
-            d.set_tuning(tblock=t, zchunk2=zc2)
+            d.set_tuning(tblock=t, zchunk2=zc2, tb_r2=1)
             d.upload(dom)
             d.step(11)
             outs.append(d.download())
