@@ -279,6 +279,28 @@ b2r_status substep(b2r_handle* h, int i)
             std::swap(h->smaps[0], h->smaps[1]);
             return B2R_OK;
         }
+        if (h->eqwp_tma) {
+            // tensor maps of the current field set (built on first use and
+            // whenever a one-pass step has swapped the sets)
+            const void* want[11] = {h->fld[B2R_F_VX], h->fld[B2R_F_VY], h->fld[B2R_F_VZ],
+                                    h->fld[B2R_F_SXX], h->fld[B2R_F_SYY], h->fld[B2R_F_SZZ],
+                                    h->fld[B2R_F_SXY], h->fld[B2R_F_SXZ], h->fld[B2R_F_SYZ], h->mat[0], h->mat[1]};
+            if (!std::equal(want, want + 11, h->emaps_of)) {
+                for (int k = 0; k < 11; ++k) {
+                    const bool v = k < 3;
+                    CUtensorMap* m = v ? &h->emaps.v[k] : &h->emaps.o[k - 3];
+                    if (!make_block_tmap(m, want[k], h->L, 4, v ? eqwp_stress_tma_box_vw() : eqwp_stress_tma_box_ow(),
+                                         v ? eqwp_stress_tma_box_vh() : eqwp_stress_tma_box_oh(), 1))
+                        return fail(h, B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed for the elastic-wave fields");
+                }
+                std::copy(want, want + 11, h->emaps_of);
+            }
+            const int ts = (int)h->ts;
+            const float amp = (p.src_host && ts >= 0 && ts < p.src_len) ? p.src_host[ts] : 0.f;
+            CK(h, launch_eqwp_stag_velocity(h->fld, h->mat, h->L, i, p, h->stream));
+            CK(h, launch_eqwp_stress_tma(h->emaps, h->fld, h->L, i, amp, p, h->d_status, h->stream));
+            return B2R_OK;
+        }
         CK(h, launch_eqwp_stag_substep(h->fld, h->mat, h->L, i, (int)h->ts, p, h->stream));
         return B2R_OK;
     }

@@ -261,6 +261,19 @@ cudaError_t launch_eqwp_stag_substep(float* const* fld, float* const* mat, const
     return cudaGetLastError();
 }
 
+cudaError_t launch_eqwp_stag_velocity(float* const* fld, float* const* mat, const BlockLayout& L, int step_i,
+                                      const EqwpStagParams& p, cudaStream_t st)
+{
+    FieldPtrs F{};
+    for (int f = 0; f < 9; ++f) F.p[f] = fld[f];
+    MatPtrs M{};
+    for (int m = 0; m < 3; ++m) M.p[m] = mat[m];
+    const Grid ga = stage_grid(L, 4 * step_i + 2);
+    eqwp_stag_velocity<false><<<ga.g, ga.b, 0, st>>>(F, F, M, L, step_i, ga.t, p, AccPtrs{});
+    count_launches(1);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_eqwp_stag_step_replay(const float* const* v_in, float* const* s, float* const* v_out,
                                          float* const* acc, float* const* mat, const BlockLayout& L,
                                          int ts, const EqwpStagParams& p, cudaStream_t st)

@@ -42,6 +42,27 @@ cudaError_t launch_eqwp_stag_step_replay(const float* const* v_in, float* const*
                                          float* const* acc, float* const* mat, const BlockLayout& L,
                                          int ts, const EqwpStagParams& p, cudaStream_t st);
 
+// eqwp_tma.cu: the staggered stress stage with its inputs streamed through
+// TMA rings.  maps.v: vx, vy, vz with boxes of eqwp_stress_tma_box_vw() x
+// _vh() cells; maps.o: sxx, syy, szz, sxy, sxz, syz, lambda, mu with boxes of
+// _ow() x _oh() cells.  In place on fld (the stresses); bit-identical to
+// the plain-load stress stage.
+struct EqwpStressMaps {
+    CUtensorMap v[3];
+    CUtensorMap o[8];
+};
+int eqwp_stress_tma_box_vw();
+int eqwp_stress_tma_box_vh();
+int eqwp_stress_tma_box_ow();
+int eqwp_stress_tma_box_oh();
+cudaError_t launch_eqwp_stress_tma(const EqwpStressMaps& maps, float* const* fld, const BlockLayout& L,
+                                   int step_i, float src_amp, const EqwpStagParams& p, int* status,
+                                   cudaStream_t st);
+// The velocity stage alone (plain loads), for a step whose stress stage is
+// launched separately.
+cudaError_t launch_eqwp_stag_velocity(float* const* fld, float* const* mat, const BlockLayout& L, int step_i,
+                                      const EqwpStagParams& p, cudaStream_t st);
+
 // eqwp_fused.cu: one staggered time step in one pass, v^n, s^n -> v^{n+1},
 // s^{n+1} (out of place).  maps: tensor maps of the six s^n fields (xx, xy,
 // xz, yy, yz, zz) with boxes of eqwp_fused_box()^2 cells; sout in the same

@@ -153,9 +153,12 @@ enum {
                                   1 = the 16-warp kernel of three and four steps; bit-identical */
     B2R_TUNE_TB_NARROW = 11,   /* heat, the 16-warp several-step kernel: 0 = tiles of 128 x 32
                                   cells (default), 1 = 64 x 64 cells; bit-identical */
-    B2R_TUNE_TB_R2 = 12        /* heat radius 2: 1 = two steps per HBM pass (with TBLOCK >= 2) on
+    B2R_TUNE_TB_R2 = 12,       /* heat radius 2: 1 = two steps per HBM pass (with TBLOCK >= 2) on
                                   64 x 64-cell tiles, 0 = one step per pass (default: the one-step
                                   sweep is faster on this GPU so far); bit-identical */
+    B2R_TUNE_EQWP_TMA = 13     /* staggered elastic wave, two-pass step: 1 = the stress stage with
+                                  its inputs streamed through TMA rings, 0 = plain loads (default);
+                                  bit-identical */
 };
 b2r_status b2r_set_tuning(b2r_handle* h, int key, int value);
 /* Current value of a knob (after b2r_autotune: the schedule it picked). */

@@ -106,6 +106,36 @@ def test_eqwp_stag_matches_oracle(b2r, orc, blocks, R, fused):
 
 
 @pytest.mark.parametrize("env,blocks,R", [((150, 90, 70), (3, 2, 1), 2), ((97, 61, 131), (1, 1, 1), 1),
+                                          ((64, 64, 64), (2, 2, 2), 3), ((260, 33, 17), (2, 1, 1), 1),
+                                          ((40, 120, 90), (1, 2, 3), 2)])
+def test_eqwp_stag_tma_stress_equals_plain(b2r, env, blocks, R):
+    """The stress stage with TMA-streamed inputs against the plain-load
+    stage (two-pass step both), on sizes that leave ragged tiles, short z
+    chunks and several blocks, with the source switched on."""
+    nsteps = 2 * R + 1
+    h = 10.0
+    mat = layered(env)
+    dt = 0.5 * h / (4000 * np.sqrt(3) * (9 / 8 + 1 / 24))
+    src = (env[0] // 3, env[1] // 2, env[2] // 2)
+    amps = ricker(nsteps, dt, 10.0, 1e6 * dt).astype(np.float32)
+    outs = []
+    for tma in (0, 1):
+        with b2r.Domain(b2r.MODEL_EQWP_STAG, env, blocks=blocks, R=R, D=2, dt=dt, h=h, src=src) as d:
+            d.set_tuning(eqwp_fused=0, eqwp_tma=tma)
+            for m, name in enumerate(["lambda", "mu", "buoy"]):
+                d.upload(mat[m].astype(np.float32), field=name)
+            rng = np.random.default_rng(12)
+            for k in range(9):
+                d.upload(rng.standard_normal(d.domain_shape).astype(np.float32), field=k)
+            d.set_source(amps)
+            d.step(nsteps)
+            outs.append([d.download(field=k) for k in range(9)])
+            d.synchronize()
+    for k in range(9):
+        assert np.array_equal(outs[0][k], outs[1][k]), NAMES[k]
+
+
+@pytest.mark.parametrize("env,blocks,R", [((150, 90, 70), (3, 2, 1), 2), ((97, 61, 131), (1, 1, 1), 1),
                                           ((64, 64, 64), (2, 2, 2), 3)])
 def test_eqwp_stag_one_pass_equals_two_pass(b2r, env, blocks, R):
     """The one-pass step against the two stage kernels, on sizes that leave
