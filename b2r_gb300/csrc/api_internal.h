@@ -48,8 +48,8 @@ struct b2r_handle {
     StressMaps smaps[2];
     bool eqwp_fused = false;   // two-pass by default: faster on this GPU so far
     bool eqwp_tma = false;     // two-pass: the stress stage with TMA-streamed inputs (eqwp_tma.cu)
-    EqwpStressMaps emaps{};    // its tensor maps, built for the pointers in emaps_of
-    const void* emaps_of[11] = {};
+    std::map<int, EqwpStressMaps> emaps;   // its tensor maps per tile width (threads per row), built
+    const void* emaps_of[11] = {};         // for the field pointers in emaps_of
     bool gol_bytes = false;    // Game of Life: byte-SWAR kernel instead of bit-sliced cells
     bool adj_fused = true;     // adjoint: stress adjoint + lambda/mu gradients in one sweep
     bool gol_push = false;     // Game of Life: period-end passes fill the next period's halos (opt-in: slower so far)

@@ -286,19 +286,26 @@ b2r_status substep(b2r_handle* h, int i)
                                     h->fld[B2R_F_SXX], h->fld[B2R_F_SYY], h->fld[B2R_F_SZZ],
                                     h->fld[B2R_F_SXY], h->fld[B2R_F_SXZ], h->fld[B2R_F_SYZ], h->mat[0], h->mat[1]};
             if (!std::equal(want, want + 11, h->emaps_of)) {
+                h->emaps.clear();
+                std::copy(want, want + 11, h->emaps_of);
+            }
+            int tx = 0, ty = 0;
+            eqwp_stress_tma_shape(h->L, i, &tx, &ty);
+            auto it = h->emaps.find(tx);
+            if (it == h->emaps.end()) {
+                EqwpStressMaps m{};
                 for (int k = 0; k < 11; ++k) {
                     const bool v = k < 3;
-                    CUtensorMap* m = v ? &h->emaps.v[k] : &h->emaps.o[k - 3];
-                    if (!make_block_tmap(m, want[k], h->L, 4, v ? eqwp_stress_tma_box_vw() : eqwp_stress_tma_box_ow(),
-                                         v ? eqwp_stress_tma_box_vh() : eqwp_stress_tma_box_oh(), 1))
+                    if (!make_block_tmap(v ? &m.v[k] : &m.o[k - 3], want[k], h->L, 4, v ? 4 * tx + 8 : 4 * tx,
+                                         v ? ty + 4 : ty, 1))
                         return fail(h, B2R_ERR_CUDA, "cuTensorMapEncodeTiled failed for the elastic-wave fields");
                 }
-                std::copy(want, want + 11, h->emaps_of);
+                it = h->emaps.emplace(tx, m).first;
             }
             const int ts = (int)h->ts;
             const float amp = (p.src_host && ts >= 0 && ts < p.src_len) ? p.src_host[ts] : 0.f;
             CK(h, launch_eqwp_stag_velocity(h->fld, h->mat, h->L, i, p, h->stream));
-            CK(h, launch_eqwp_stress_tma(h->emaps, h->fld, h->L, i, amp, p, h->d_status, h->stream));
+            CK(h, launch_eqwp_stress_tma(it->second, tx, h->fld, h->L, i, amp, p, h->d_status, h->stream));
             return B2R_OK;
         }
         CK(h, launch_eqwp_stag_substep(h->fld, h->mat, h->L, i, (int)h->ts, p, h->stream));

@@ -43,19 +43,17 @@ cudaError_t launch_eqwp_stag_step_replay(const float* const* v_in, float* const*
                                          int ts, const EqwpStagParams& p, cudaStream_t st);
 
 // eqwp_tma.cu: the staggered stress stage with its inputs streamed through
-// TMA rings.  maps.v: vx, vy, vz with boxes of eqwp_stress_tma_box_vw() x
-// _vh() cells; maps.o: sxx, syy, szz, sxy, sxz, syz, lambda, mu with boxes of
-// _ow() x _oh() cells.  In place on fld (the stresses); bit-identical to
-// the plain-load stress stage.
+// TMA rings, on the plain stage launch's tiles: eqwp_stress_tma_shape gives
+// the CTA shape tx x ty of sub-step step_i; maps.v: vx, vy, vz with boxes of
+// (4 tx + 8) x (ty + 4) cells; maps.o: sxx, syy, szz, sxy, sxz, syz, lambda,
+// mu with boxes of 4 tx x ty cells.  In place on fld (the stresses);
+// bit-identical to the plain-load stress stage.
 struct EqwpStressMaps {
     CUtensorMap v[3];
     CUtensorMap o[8];
 };
-int eqwp_stress_tma_box_vw();
-int eqwp_stress_tma_box_vh();
-int eqwp_stress_tma_box_ow();
-int eqwp_stress_tma_box_oh();
-cudaError_t launch_eqwp_stress_tma(const EqwpStressMaps& maps, float* const* fld, const BlockLayout& L,
+void eqwp_stress_tma_shape(const BlockLayout& L, int step_i, int* tx, int* ty);
+cudaError_t launch_eqwp_stress_tma(const EqwpStressMaps& maps, int tx, float* const* fld, const BlockLayout& L,
                                    int step_i, float src_amp, const EqwpStagParams& p, int* status,
                                    cudaStream_t st);
 // The velocity stage alone (plain loads), for a step whose stress stage is

@@ -5,14 +5,17 @@
 // each plane.  Here one thread of the CTA issues the tile's boxes a few
 // planes ahead into shared memory, so the loads are in flight while the
 // threads compute:
-//   ring V: the three velocities of a plane, 136 x 12 cells (the tile, 4 more
-//     cells on each side in x, 2 more rows on each side in y), 5 planes: the
+//   ring V: the three velocities of a plane (the tile, 4 more cells on each
+//     side in x, 2 more rows on each side in y), 5 planes: the
 //     plane being updated (x and y neighbours), the plane two ahead (its
 //     columns feed the 5-plane z queues) and the planes between and ahead;
-//   ring O: the six stresses and lambda, mu of the plane, 128 x 8 cells (the
-//     tile itself), 3 planes.
-// CTA = 32 x 8 threads, thread = 4 consecutive x cells (float4) of one row,
-// tile = 128 x 8 cells over a z chunk of one block.  The arithmetic is
+//   ring O: the six stresses and lambda, mu of the plane (the tile itself),
+//     3 planes.
+// CTA = 256 threads: tx x ty of them (tx = 8 .. 32, ty = 256 / tx, the tile
+// shape the plain stage launch picks for the window, so that no tile column
+// is mostly outside it), thread = 4 consecutive x cells (float4) of one row,
+// tile = 4 tx x ty cells over a z chunk of one block; the velocity boxes are
+// (4 tx + 8) x (ty + 4) cells, the own boxes 4 tx x ty.  The arithmetic is
 // stag_stress_unit's, operation for operation (the same stencil helpers on
 // the same values), so the result is bit-identical to it.
 #include "b2r_common.cuh"
@@ -25,15 +28,18 @@ namespace {
 
 using namespace eqk;
 
-constexpr int kTX = 32, kTY = 8;                 // threads per row, rows
-constexpr int kThr = kTX * kTY;                  // 256
-constexpr int kVW = 4 * kTX + 8, kVH = kTY + 4;  // velocity box (136 x 12)
-constexpr int kVF = kVW * kVH;                   // floats per velocity box (1632: a multiple of 32)
-constexpr int kOW = 4 * kTX, kOH = kTY;          // own-cell box (128 x 8)
-constexpr int kOF = kOW * kOH;                   // 1024
+constexpr int kThr = 256;
+constexpr int kVF = 1632;                        // floats per velocity box slot: the largest box (136 x 12)
+constexpr int kOF = 1024;                        // floats per own box slot: 4 * 256 cells
 constexpr int kSV = 5, kSO = 3;                  // ring slots
-constexpr uint32_t kVBytes = 3u * kVF * 4u, kOBytes = 8u * kOF * 4u;
 constexpr size_t kSmemT = size_t(kSV) * 3 * kVF * 4 + size_t(kSO) * 8 * kOF * 4 + (kSV + kSO) * 8 + 16 + 128;
+
+// tile geometry of a launch
+struct TGeo {
+    int tx, ty;             // threads per row, rows
+    int vw, vh;             // velocity box (4 tx + 8) x (ty + 4)
+    int ow, oh;             // own box 4 tx x ty
+};
 
 struct TmaArgs {
     float* out[6];          // stresses of the updated plane: xx, yy, zz, xy, xz, yz (stress_update order)
@@ -46,8 +52,10 @@ __device__ __forceinline__ float4 lds4(const float* p) { return *reinterpret_cas
 
 __global__ void __launch_bounds__(kThr, 1)
 eqwp_stress_tma_kernel(const __grid_constant__ EqwpStressMaps maps, const TmaArgs A, const BlockLayout L,
-                       const int step_i, const Tiles T)
+                       const int step_i, const Tiles T, const TGeo G)
 {
+    const int kVW = G.vw, kOW = G.ow, kOH = G.oh;
+    const uint32_t kVBytes = 3u * G.vw * G.vh * 4u, kOBytes = 8u * G.ow * G.oh * 4u;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* rv = reinterpret_cast<float*>(smem_raw + ((128 - (smem_u32(smem_raw) & 127)) & 127));
     float* ro = rv + kSV * 3 * kVF;
@@ -62,9 +70,11 @@ eqwp_stress_tma_kernel(const __grid_constant__ EqwpStressMaps maps, const TmaArg
     const int X0 = T.x0 + blockIdx.x * kOW, Y0 = T.y0 + blockIdx.y * kOH;
     if (!w.ok || X0 - L.xoff > w.hi[0] || X0 - L.xoff + kOW - 1 < w.lo[0] || Y0 > w.hi[1] || Y0 + kOH - 1 < w.lo[1])
         return;
-    const int tid = threadIdx.x, tx = tid % kTX, ty = tid / kTX;
+    const int tid = threadIdx.x, tx = tid % G.tx, ty0 = tid / G.tx;
+    const bool inrow = ty0 < G.ty;         // the threads beyond tx * ty rows only join the barriers
+    const int ty = inrow ? ty0 : G.ty - 1;
     Cell c;
-    const bool act = cell_setup(L, w, blk, c, T.x0, T.y0, TilePos{(int)blockIdx.x, (int)blockIdx.y, tx, ty, kTX, kTY});
+    const bool act = inrow && cell_setup(L, w, blk, c, T.x0, T.y0, TilePos{(int)blockIdx.x, (int)blockIdx.y, tx, ty, G.tx, G.ty});
     const int zs = w.zs, ze = w.ze;
     const int nv = ze - zs + 5;            // velocity planes zs-2 .. ze+2
     const int no = ze - zs + 1;            // own planes zs .. ze
@@ -223,40 +233,59 @@ eqwp_stress_tma_kernel(const __grid_constant__ EqwpStressMaps maps, const TmaArg
 
 }  // namespace
 
-int eqwp_stress_tma_box_vw() { return kVW; }
-int eqwp_stress_tma_box_vh() { return kVH; }
-int eqwp_stress_tma_box_ow() { return kOW; }
-int eqwp_stress_tma_box_oh() { return kOH; }
+void eqwp_stress_tma_shape(const BlockLayout& L, int step_i, int* tx, int* ty)
+{
+    const Grid g = stage_grid(L, 4 * step_i + 4);
+    *tx = (int)g.b.x;
+    *ty = (int)g.b.y;
+}
 
-cudaError_t launch_eqwp_stress_tma(const EqwpStressMaps& maps, float* const* fld, const BlockLayout& L,
+cudaError_t launch_eqwp_stress_tma(const EqwpStressMaps& maps, int tpr, float* const* fld, const BlockLayout& L,
                                    int step_i, float src_amp, const EqwpStagParams& p, int* status,
                                    cudaStream_t st)
 {
     static KernelSetup setup;
     if (cudaError_t e = kernel_setup(setup, eqwp_stress_tma_kernel, kThr, kSmemT, nullptr, nullptr)) return e;
-    // tiles of 128 x 8 cells over the union of the blocks' windows; the
-    // first tile starts on a 16-byte boundary
+    // the plain stage launch's tiles over the union of the blocks' windows
     const int shrink = 4 * step_i + 4;
-    int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-1, -1, -1};
-    for (int b = 0; b < L.nblk; ++b) {
-        const int e = edge_bits(L, b);
-        for (int a = 0; a < 3; ++a) {
-            int l, h;
-            stage_region(L, e, a, shrink, l, h);
-            lo[a] = std::min(lo[a], l);
-            hi[a] = std::max(hi[a], h);
+    const Grid g = stage_grid(L, shrink);
+    if ((int)g.b.x != tpr) return cudaErrorInvalidValue;   // maps built for another tile shape
+    TGeo G;
+    G.tx = (int)g.b.x;
+    G.ty = (int)g.b.y;
+    G.vw = 4 * G.tx + 8;
+    G.vh = G.ty + 4;
+    G.ow = 4 * G.tx;
+    G.oh = G.ty;
+    if (G.vw * G.vh > kVF || G.ow * G.oh > kOF || G.tx * G.ty > kThr) return cudaErrorInvalidValue;
+    Tiles T = g.t;
+    const long long tiles = (long long)g.g.x * g.g.y * L.nblk;
+    int lo2, hi2;
+    stage_region(L, edge_bits(L, 0), 2, shrink, lo2, hi2);
+    int nzmax = hi2 - lo2 + 1;
+    for (int b = 1; b < L.nblk; ++b) {
+        stage_region(L, edge_bits(L, b), 2, shrink, lo2, hi2);
+        nzmax = std::max(nzmax, hi2 - lo2 + 1);
+    }
+    const int nz = std::max(1, nzmax);
+    // z chunks: the fewest waves of one CTA per SM, each weighted by its
+    // chunk length plus the four planes of queue warm-up
+    int sms = 152;
+    {
+        int dev = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        sms = std::max(1, sms);
+    }
+    int nzc = 1;
+    double best_cost = 1e300;
+    for (int k = 1; k <= std::max(1, nz / 8); ++k) {
+        const double waves = (double)((tiles * k + sms - 1) / sms);
+        const double cost = waves * ((nz + k - 1) / k + 4);
+        if (cost < best_cost - 1e-9) {
+            best_cost = cost;
+            nzc = k;
         }
     }
-    Tiles T{};
-    T.x0 = (L.xoff + lo[0]) & ~3;
-    T.y0 = lo[1];
-    const int tx = std::max(1, (L.xoff + hi[0] + 1 - T.x0 + kOW - 1) / kOW);
-    const int ty = std::max(1, (hi[1] + 1 - lo[1] + kOH - 1) / kOH);
-    const long long tiles = (long long)tx * ty * L.nblk;
-    const int nz = std::max(1, hi[2] - lo[2] + 1);
-    // z chunks: at least two waves of one CTA per SM, chunks of >= 16 planes
-    int nzc = (int)((2 * 152 + tiles - 1) / tiles);
-    nzc = std::max(1, std::min(nzc, nz / 16));
     T.nzc = nzc;
     TmaArgs A{};
     // stress_update order: xx, yy, zz, xy, xz, yz
@@ -271,8 +300,8 @@ cudaError_t launch_eqwp_stress_tma(const EqwpStressMaps& maps, float* const* fld
     A.src_amp = src_amp;
     for (int a = 0; a < 3; ++a) A.src[a] = p.src[a];
     A.status = status;
-    const dim3 grid(tx, ty, L.nblk * nzc);
-    eqwp_stress_tma_kernel<<<grid, kThr, kSmemT, st>>>(maps, A, L, step_i, T);
+    const dim3 grid(g.g.x, g.g.y, L.nblk * nzc);
+    eqwp_stress_tma_kernel<<<grid, kThr, kSmemT, st>>>(maps, A, L, step_i, T, G);
     count_launches(1);
     return cudaGetLastError();
 }
