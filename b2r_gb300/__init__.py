@@ -455,8 +455,8 @@ def _ebcheck(st):
 class EqwpBatch:
     """Staggered elastic-wave Domains (one block each, fixed shell) advanced
     in one persistent launch (b2r_eqwp_batch_*): each run advances domain i
-    by nsteps[i] steps, in place.  The domains must outlive the batch; their
-    own streams must be idle during a run."""
+    by nsteps[i] steps, in place, in stream order with the domains' own
+    work.  The domains must outlive the batch."""
 
     def __init__(self, domains, nsteps, stream=None):
         self.domains = list(domains)

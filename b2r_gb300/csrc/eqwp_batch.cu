@@ -136,6 +136,10 @@ struct b2r_eqwp_batch {
     size_t smem = 0;
     cudaGraphExec_t gexec = nullptr;
     cudaStream_t gstream = nullptr;
+    // stream order with the handles' own streams: the run waits for the work
+    // already queued on them, and their next work waits for the run
+    std::vector<cudaEvent_t> ev_in;  // per handle
+    cudaEvent_t ev_out = nullptr;
 };
 
 namespace {
@@ -292,6 +296,12 @@ b2r_status b2r_eqwp_batch_create(b2r_handle* const* hs, const int* nsteps, int n
         return bail(efail(B2R_ERR_OOM, "batch table allocation failed"));
     cudaMemset(b->d_status, 0, sizeof(int));
     cudaMemset(b->d_amp, 0, sizeof(float) * namp);
+    b->ev_in.assign(n, nullptr);
+    for (int k = 0; k < n; ++k)
+        if (cudaEventCreateWithFlags(&b->ev_in[k], cudaEventDisableTiming) != cudaSuccess)
+            return bail(efail(B2R_ERR_CUDA, "event creation failed"));
+    if (cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming) != cudaSuccess)
+        return bail(efail(B2R_ERR_CUDA, "event creation failed"));
     for (int k = 0; k < n; ++k) b->host[k].amp = b->d_amp + b->amp_off[k];
     b->smem = sizeof(long long) * (2 * maxsteps + 1 + n + 1) + sizeof(int) * (2 * maxsteps + 1) + 16;
     if (b->smem > 200 * 1024) return bail(efail(B2R_ERR_ARG, "too many time steps for the batch schedule"));
@@ -316,6 +326,9 @@ b2r_status b2r_eqwp_batch_destroy(b2r_eqwp_batch* b)
 {
     if (!b) return B2R_OK;
     if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    for (cudaEvent_t e : b->ev_in)
+        if (e) cudaEventDestroy(e);
+    if (b->ev_out) cudaEventDestroy(b->ev_out);
     cudaFree(b->d_inst);
     cudaFree(b->d_amp);
     cudaFree(b->d_step_off);
@@ -332,8 +345,12 @@ b2r_status b2r_eqwp_batch_run(b2r_eqwp_batch* b, void* stream, int use_graph)
 {
     if (!b) return efail(B2R_ERR_ARG, "null batch");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // the source increments of each instance's steps of this run (from its
-    // handle's time step on), copied in stream order before the launch
+    // the work already queued on the handles' streams comes first
+    for (int k = 0; k < b->n; ++k) {
+        if (b->hs[k]->stream == st) continue;
+        ECK(cudaEventRecord(b->ev_in[k], b->hs[k]->stream), "order after the handles' work");
+        ECK(cudaStreamWaitEvent(st, b->ev_in[k], 0), "order after the handles' work");
+    }
     // the handles' current field sets (a one-pass step swaps a handle's two sets)
     bool moved = false;
     for (int k = 0; k < b->n; ++k)
@@ -380,6 +397,10 @@ b2r_status b2r_eqwp_batch_run(b2r_eqwp_batch* b, void* stream, int use_graph)
         if (s != B2R_OK) return s;
     }
     count_launches(1);
+    // and the handles' next work comes after the run
+    ECK(cudaEventRecord(b->ev_out, st), "order the handles' next work");
+    for (int k = 0; k < b->n; ++k)
+        if (b->hs[k]->stream != st) ECK(cudaStreamWaitEvent(b->hs[k]->stream, b->ev_out, 0), "order the handles' next work");
     for (int k = 0; k < b->n; ++k) {
         b->hs[k]->ts += b->nsteps[k];
         b->hs[k]->halos_fresh = false;

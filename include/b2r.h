@@ -395,9 +395,10 @@ b2r_status b2r_batch_autotune(b2r_batch* b, void* cuda_stream, int* best_zchunk,
  * handle i by nsteps[i] steps from its current time step, in place, with its
  * own material and source; results are identical to b2r_step on each handle
  * with the two-pass step.  The batch keeps pointers to the handles: they must
- * outlive it, and their own streams must be idle during a run (b2r_synchronize
- * before, b2r_eqwp_batch_synchronize after, then the handles are used as
- * usual: b2r_download, b2r_step, b2r_time_step). */
+ * outlive it.  A run is ordered after the work already queued on the
+ * handles' streams, and the work queued on them afterwards after the run
+ * (events, no host wait), so the handles are used as usual around runs
+ * (b2r_upload, b2r_download, b2r_step, b2r_time_step). */
 typedef struct b2r_eqwp_batch b2r_eqwp_batch;
 b2r_status b2r_eqwp_batch_create(b2r_handle* const* handles, const int* nsteps, int n, b2r_eqwp_batch** out);
 b2r_status b2r_eqwp_batch_destroy(b2r_eqwp_batch* b);

@@ -24,7 +24,7 @@ def instances(n, seed):
     return out
 
 
-def make(b2r, it, stream=None):
+def make(b2r, it, stream=None, sync=True):
     d = b2r.Domain(b2r.MODEL_EQWP_STAG, it["env"], D=2, R=1, dt=DT, h=H, src=it["src"], stream=stream)
     mat = layered(it["env"], seed=it["seed"])
     for m, name in enumerate(["lambda", "mu", "buoy"]):
@@ -36,16 +36,21 @@ def make(b2r, it, stream=None):
         a[2:-2, 2:-2, 2:-2] = ((rng.random(tuple(s - 4 for s in shape)) - 0.5) * 1e-3).astype(np.float32)
         d.upload(a, field=k)
     d.set_source(ricker(64, DT, 10.0, 1e6 * DT).astype(np.float32))
-    d.synchronize()
+    if sync:
+        d.synchronize()
     return d
 
 
-@pytest.mark.parametrize("graph,zchunk", [(True, 32), (False, 8), (True, 0)])
-def test_eqwp_batch_matches_handles(b2r, graph, zchunk):
+@pytest.mark.parametrize("graph,zchunk,own", [(True, 32, False), (False, 8, False), (True, 0, False),
+                                              (True, 32, True)])
+def test_eqwp_batch_matches_handles(b2r, graph, zchunk, own):
+    """own: the domains on streams of their own, uploads not waited for --
+    the run is ordered after them, and the downloads after the run, by
+    events."""
     import torch
     items = instances(7, 5)
     s = torch.cuda.Stream()
-    doms = [make(b2r, it, stream=s) for it in items]
+    doms = [make(b2r, it, stream=None if own else s, sync=not own) for it in items]
     refs = [make(b2r, it) for it in items]
     try:
         with b2r.EqwpBatch(doms, [it["nsteps"] for it in items], stream=s) as bt:
