@@ -248,6 +248,9 @@ gather_kernel(T* __restrict__ dom, const T* __restrict__ blocks, const BlockLayo
 // cells without an owner (domain boundary, not periodic) keep their values.
 // Each region's rows move in the widest vectors (16 down to the cell size)
 // that its row length and row starts allow.
+#ifndef B2R_HALO_VPT
+#define B2R_HALO_VPT 4   // vectors per thread of the one-launch exchange
+#endif
 struct HaloDirs {
     int n;                  // regions with a possible owner
     int cta0[27];           // first CTA of region k (cta0[n] = total CTAs)
@@ -257,21 +260,37 @@ struct HaloDirs {
     int vb[26];                   // vector bytes of region k's rows
 };
 
-// copy ex x ey x ez vectors of VB bytes (rows of ex vectors), grid-stride
+// copy ex x ey x ez vectors of VB bytes (rows of ex vectors), grid-stride,
+// four vectors per thread and round: their loads are issued before their
+// stores (a region's cells are never another region's sources, so the
+// source and destination do not alias)
 template <int VB>
-__device__ __forceinline__ void copy_box(uint8_t* dst, const uint8_t* src, unsigned ex, unsigned ey,
-                                         unsigned total, long long rowb, long long planeb, unsigned e0,
-                                         unsigned stride)
+__device__ __forceinline__ void copy_box(uint8_t* __restrict__ dst, const uint8_t* __restrict__ src, unsigned ex,
+                                         unsigned ey, unsigned total, long long rowb, long long planeb,
+                                         unsigned e0, unsigned stride)
 {
     typedef typename std::conditional<VB == 16, uint4,
             typename std::conditional<VB == 8, uint2,
             typename std::conditional<VB == 4, uint32_t,
             typename std::conditional<VB == 2, uint16_t, uint8_t>::type>::type>::type>::type V;
-    for (unsigned e = e0; e < total; e += stride) {
-        const unsigned vx = e % ex, r = e / ex;
-        const unsigned y = r % ey, z = r / ey;
-        const long long off = (long long)vx * VB + y * rowb + z * planeb;
-        *reinterpret_cast<V*>(dst + off) = *reinterpret_cast<const V*>(src + off);
+    constexpr int U = 4;
+    for (unsigned e = e0; e < total; e += U * stride) {
+        V v[U];
+        long long off[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const unsigned ee = e + u * stride;
+            off[u] = -1;
+            if (ee < total) {
+                const unsigned vx = ee % ex, r = ee / ex;
+                const unsigned y = r % ey, z = r / ey;
+                off[u] = (long long)vx * VB + y * rowb + z * planeb;
+                v[u] = *reinterpret_cast<const V*>(src + off[u]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (off[u] >= 0) *reinterpret_cast<V*>(dst + off[u]) = v[u];
     }
 }
 
@@ -354,7 +373,7 @@ cudaError_t launch_halo_gather(const FieldSet<T>& fs, int nfields, const BlockLa
     if (L.nblk == 1 && !L.periodic) return cudaSuccess;   // all halos are shell
     const int cb = (int)sizeof(T);
     HaloDirs hd{};
-    const long long per_cta = 256LL * 4;    // vectors per CTA
+    const long long per_cta = 256LL * B2R_HALO_VPT;    // vectors per CTA
     int ctas = 0;
     for (int dz = -1; dz <= 1; ++dz)
         for (int dy = -1; dy <= 1; ++dy)
