@@ -178,11 +178,7 @@ __global__ void __launch_bounds__(kThreads, B2R_BATCH_MINB) batch_kernel(const B
             wq::decode(item, s_step_off, s_active, s_prefix, a.maxsteps, t, k, u);
             int ok = 1;
             // wait for round t-1 of this instance (bounded)
-            if (t > 0) {
-                const InstDev& in = a.inst[k];
-                ok = wq::wait_neighbours(a.done + s_prefix[k], u, in.ntx, in.nty, in.nzc, (unsigned)t, in.tb == 2)
-                         ? 1 : 0;
-            }
+            if (t > 0) ok = wq::wait_done(&a.done[k], (unsigned)t * (unsigned)a.inst[k].units) ? 1 : 0;
             s_t = t;
             s_k = k;
             s_u = u;
@@ -218,7 +214,7 @@ __global__ void __launch_bounds__(kThreads, B2R_BATCH_MINB) batch_kernel(const B
             return;
         }
         __syncthreads();                     // every store of this unit is issued
-        if (threadIdx.x == 0) wq::release_done(&a.done[s_prefix[k] + u]);
+        if (threadIdx.x == 0) wq::release_done(&a.done[k]);
     }
 }
 
@@ -241,8 +237,7 @@ struct b2r_batch {
     int* d_active = nullptr;
     long long* d_prefix = nullptr;
     unsigned long long* d_head = nullptr;
-    unsigned* d_done = nullptr;      // rounds finished per unit (units of every instance, queue order)
-    long long done_cap = 0, total_units = 0;
+    unsigned* d_done = nullptr;
     int* d_status = nullptr;
     float* staging = nullptr;
     size_t staging_bytes = 0;
@@ -373,8 +368,7 @@ b2r_status build_schedule(b2r_batch* b)
     for (int j = 0; j < b->n; ++j) {
         InstDev& in = b->host[b->sched[j]];
         b->two = b->two || in.tb == 2;
-        // z chunks of >= 8 planes: a unit's neighbours in z are the adjacent chunks
-        in.Lz = std::min(in.NZ, b->lz_policy > 0 ? std::max(8, b->lz_policy) : in.NZ);
+        in.Lz = std::min(in.NZ, b->lz_policy > 0 ? b->lz_policy : in.NZ);
         in.nzc = (in.NZ + in.Lz - 1) / in.Lz;
         in.units = in.ntx * in.nty * in.nzc;
         prefix[j + 1] = prefix[j] + in.units;
@@ -393,14 +387,6 @@ b2r_status build_schedule(b2r_batch* b)
         step_off[t + 1] = step_off[t] + prefix[A];
     }
     b->total = step_off[R];
-    b->total_units = prefix[b->n];
-    if (b->total_units > b->done_cap) {
-        if (b->d_done) cudaFree(b->d_done);
-        b->d_done = nullptr;
-        b->done_cap = 0;
-        BCK(cudaMalloc(&b->d_done, sizeof(unsigned) * std::max(1LL, b->total_units)), "unit counters");
-        b->done_cap = b->total_units;
-    }
     BCK(cudaMemcpy(b->d_inst, dev.data(), sizeof(InstDev) * b->n, cudaMemcpyHostToDevice), "copy descriptors");
     BCK(cudaMemcpy(b->d_maps, maps.data(), sizeof(CUtensorMap) * 2 * b->n, cudaMemcpyHostToDevice),
         "copy tensor maps");
@@ -417,7 +403,7 @@ b2r_status build_schedule(b2r_batch* b)
 b2r_status enqueue_run(b2r_batch* b, cudaStream_t st)
 {
     BCK(cudaMemsetAsync(b->d_head, 0, sizeof(unsigned long long), st), "reset queue");
-    BCK(cudaMemsetAsync(b->d_done, 0, sizeof(unsigned) * b->total_units, st), "reset counters");
+    BCK(cudaMemsetAsync(b->d_done, 0, sizeof(unsigned) * b->n, st), "reset counters");
     BatchArgs a;
     a.inst = b->d_inst;
     a.maps = b->d_maps;
@@ -506,7 +492,7 @@ b2r_status b2r_batch_create(const b2r_batch_item* items, int n, b2r_batch** out)
         cudaMalloc(&b->d_active, sizeof(int) * (b->maxsteps + 1)) != cudaSuccess ||
         cudaMalloc(&b->d_prefix, sizeof(long long) * (n + 1)) != cudaSuccess ||
         cudaMalloc(&b->d_head, sizeof(unsigned long long)) != cudaSuccess ||
-
+        cudaMalloc(&b->d_done, sizeof(unsigned) * n) != cudaSuccess ||
         cudaMalloc(&b->d_status, sizeof(int)) != cudaSuccess)
         return bail(bfail(B2R_ERR_OOM, "batch table allocation failed"));
     cudaMemset(b->d_status, 0, sizeof(int));

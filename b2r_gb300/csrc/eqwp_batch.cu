@@ -8,11 +8,10 @@
 // of the queue: the velocity stage, then the stress stage, each over the
 // tiles x z chunks of the stage kernels' grid (eqwp_stag.cuh, the same
 // bodies as the stage launches, so results are bit-identical to stepping
-// each handle on its own).  The stages update their fields in place; a unit
-// of a round starts only after itself and the six units sharing a face with
-// it have finished the previous round (the stencils reach along the axes
-// only, at most 2 cells), which orders both the reads of the neighbours' new
-// values and the in-place writes after the previous stage's reads.  The fields are
+// each handle on its own).  The stages update their fields in place; a round
+// starts only after every unit of the instance's previous round has
+// finished, which orders both the reads of the neighbours' new values and
+// the in-place writes after the previous stage's reads.  The fields are
 // read through coherent loads (other CTAs update them between rounds); the
 // material through the read-only path.
 #include <algorithm>
@@ -77,8 +76,7 @@ __global__ void __launch_bounds__(kEThreads, B2R_EQWP_MINB) eqwp_batch_kernel(co
                 int t, k, u;
                 wq::decode(item, s_step_off, s_active, s_prefix, a.maxrounds, t, k, u);
                 // wait for round t-1 of this instance (bounded)
-                const EInst& in = a.inst[k];
-                s_ok = t == 0 || wq::wait_neighbours(a.done + s_prefix[k], u, in.gx, in.gy, in.T.nzc, (unsigned)t, false);
+                s_ok = t == 0 || wq::wait_done(&a.done[k], (unsigned)t * (unsigned)a.inst[k].units);
                 s_t = t;
                 s_k = k;
                 s_u = u;
@@ -109,7 +107,7 @@ __global__ void __launch_bounds__(kEThreads, B2R_EQWP_MINB) eqwp_batch_kernel(co
                 stag_velocity_unit<false, false>(in.F, in.F, in.M, in.L, 0, in.T, in.p, AccPtrs{}, 0, zc, q);
         }
         __syncthreads();                     // every store of this unit is issued
-        if (threadIdx.x == 0) wq::release_done(&a.done[s_prefix[k] + u]);
+        if (threadIdx.x == 0) wq::release_done(&a.done[k]);
     }
 }
 
@@ -129,8 +127,7 @@ struct b2r_eqwp_batch {
     int* d_active = nullptr;
     long long* d_prefix = nullptr;
     unsigned long long* d_head = nullptr;
-    unsigned* d_done = nullptr;      // rounds finished per unit (units of every instance, queue order)
-    long long done_cap = 0, total_units = 0;
+    unsigned* d_done = nullptr;
     int* d_status = nullptr;
     int maxrounds = 0;
     long long total = 0;
@@ -179,8 +176,7 @@ b2r_status build(b2r_eqwp_batch* b)
         int lo, hi;
         stage_region(in.L, edge_bits(in.L, 0), 2, 2, lo, hi);
         const int nz = std::max(1, hi - lo + 1);
-        // z chunks of >= 8 planes: a unit's neighbours in z are the adjacent chunks
-        const int lz = b->lz_policy > 0 ? std::min(std::max(8, b->lz_policy), nz) : nz;
+        const int lz = b->lz_policy > 0 ? std::min(b->lz_policy, nz) : nz;
         in.T.nzc = (nz + lz - 1) / lz;
         in.units = in.gx * in.gy * in.T.nzc;
         in.rounds = 2 * in.nsteps;
@@ -207,14 +203,6 @@ b2r_status build(b2r_eqwp_batch* b)
         step_off[t + 1] = step_off[t] + prefix[A];
     }
     b->total = step_off[R];
-    b->total_units = prefix[b->n];
-    if (b->total_units > b->done_cap) {
-        if (b->d_done) cudaFree(b->d_done);
-        b->d_done = nullptr;
-        b->done_cap = 0;
-        ECK(cudaMalloc(&b->d_done, sizeof(unsigned) * std::max(1LL, b->total_units)), "unit counters");
-        b->done_cap = b->total_units;
-    }
     ECK(cudaMemcpy(b->d_inst, dev.data(), sizeof(EInst) * b->n, cudaMemcpyHostToDevice), "copy descriptors");
     ECK(cudaMemcpy(b->d_step_off, step_off.data(), sizeof(long long) * (R + 1), cudaMemcpyHostToDevice),
         "copy round table");
@@ -231,7 +219,7 @@ b2r_status build(b2r_eqwp_batch* b)
 b2r_status enqueue(b2r_eqwp_batch* b, cudaStream_t st)
 {
     ECK(cudaMemsetAsync(b->d_head, 0, sizeof(unsigned long long), st), "reset queue");
-    ECK(cudaMemsetAsync(b->d_done, 0, sizeof(unsigned) * b->total_units, st), "reset counters");
+    ECK(cudaMemsetAsync(b->d_done, 0, sizeof(unsigned) * b->n, st), "reset counters");
     EArgs a;
     a.inst = b->d_inst;
     a.step_off = b->d_step_off;
@@ -303,7 +291,7 @@ b2r_status b2r_eqwp_batch_create(b2r_handle* const* hs, const int* nsteps, int n
         cudaMalloc(&b->d_active, sizeof(int) * (2 * maxsteps + 1)) != cudaSuccess ||
         cudaMalloc(&b->d_prefix, sizeof(long long) * (n + 1)) != cudaSuccess ||
         cudaMalloc(&b->d_head, sizeof(unsigned long long)) != cudaSuccess ||
-
+        cudaMalloc(&b->d_done, sizeof(unsigned) * n) != cudaSuccess ||
         cudaMalloc(&b->d_status, sizeof(int)) != cudaSuccess)
         return bail(efail(B2R_ERR_OOM, "batch table allocation failed"));
     cudaMemset(b->d_status, 0, sizeof(int));

@@ -4,14 +4,12 @@
 // Work items (round t, instance k, unit u) are numbered round-major;
 // instances are sorted by round count (descending), so the instances still
 // active at round t are a prefix of the list.  A CTA claims the next item
-// with one atomicAdd on a head counter.  Before round t of unit u it waits
-// until u and the units next to it have finished round t-1 (a counter per
-// unit), runs the unit and bumps u's counter with a release reduction.
-// Items are claimed in increasing order and an item only waits on smaller
-// items, which are held by running CTAs, so the queue cannot deadlock; every
-// wait is bounded (2 s) and reports B2R_ERR_TIMEOUT.  Units must be at least
-// as large as the stencil's reach in every direction (tiles of >= 32 x 8
-// cells, z chunks of >= 8 planes), so that only adjacent units share cells.
+// with one atomicAdd on a head counter.  Before reading round t of instance
+// k it waits until done[k] >= t * units[k] (every unit of round t-1 of that
+// instance has finished), runs the unit and bumps done[k] with a release
+// reduction.  Items are claimed in increasing order and an item only waits
+// on smaller items, which are held by running CTAs, so the queue cannot
+// deadlock; every wait is bounded (2 s) and reports B2R_ERR_TIMEOUT.
 #pragma once
 #include "b2r_common.cuh"
 
@@ -47,33 +45,22 @@ __device__ __forceinline__ void decode(long long item, const long long* step_off
     u = (int)(r - prefix[k]);
 }
 
-// Bounded wait (2 s for all of them together) until unit u of an instance's
-// nx x ny x nz grid of units and its neighbours -- the six that share a face,
-// or all 26 around it when diag -- have each finished `need` rounds
-// (done[v]: rounds finished by unit v); false if it gave up.  A unit reads
-// and overwrites only cells of its own tile and of the tiles next to it, so
-// these are the only units whose previous round it depends on.
-__device__ __forceinline__ bool wait_neighbours(const unsigned* done, int u, int nx, int ny, int nz, unsigned need,
-                                                bool diag)
+// Bounded wait (2 s) until *done >= need; false if it gave up.  Afterwards
+// the data that other CTAs stored with generic stores may be read through
+// TMA as well.
+__device__ __forceinline__ bool wait_done(const unsigned* done, unsigned need)
 {
-    const int x = u % nx, r = u / nx, y = r % ny, z = r / ny;
-    const uint64_t t0 = global_ns();
     bool ok = true;
-    for (int dz = -1; dz <= 1 && ok; ++dz)
-        for (int dy = -1; dy <= 1 && ok; ++dy)
-            for (int dx = -1; dx <= 1 && ok; ++dx) {
-                if (!diag && (dx != 0) + (dy != 0) + (dz != 0) > 1) continue;
-                const int xx = x + dx, yy = y + dy, zz = z + dz;
-                if (xx < 0 || xx >= nx || yy < 0 || yy >= ny || zz < 0 || zz >= nz) continue;
-                const unsigned* d = done + (xx + nx * (yy + ny * zz));
-                while (ld_acquire(d) < need) {
-                    if (global_ns() - t0 > 2000000000ull) {
-                        ok = false;
-                        break;
-                    }
-                    __nanosleep(64);
-                }
+    if (ld_acquire(done) < need) {
+        const uint64_t t0 = global_ns();
+        while (ld_acquire(done) < need) {
+            if (global_ns() - t0 > 2000000000ull) {
+                ok = false;
+                break;
             }
+            __nanosleep(100);
+        }
+    }
     asm volatile("fence.proxy.async.global;" ::: "memory");
     return ok;
 }

@@ -358,7 +358,7 @@ b2r_status b2r_batch_run(b2r_batch* b, void* cuda_stream, int use_graph);
 b2r_status b2r_batch_synchronize(b2r_batch* b, void* cuda_stream);
 /* Total lattice-site updates of one run (sum of cells x steps). */
 int64_t b2r_batch_lups(const b2r_batch* b);
-/* Planes per work unit along z (at least 8; 0 = whole column). */
+/* Planes per work unit along z (0 = whole column). */
 b2r_status b2r_batch_set_zchunk(b2r_batch* b, int zchunk);
 /* Tile shape of the instances: 128 x 16, 64 x 32 or 32 x 64 cells (x by
  * y, for D <= 2; half the rows for D >= 3), by width 128, 64 or 32, for
@@ -390,9 +390,8 @@ b2r_status b2r_batch_autotune(b2r_batch* b, void* cuda_stream, int* best_zchunk,
 /* Many staggered elastic-wave handles (B2R_MODEL_EQWP_STAG, one block each,
  * fixed shell) of uneven sizes advanced in one persistent launch driven by a
  * device work queue of (stage round, instance, tile chunk) items: a time step
- * of an instance is its velocity stage then its stress stage, a tile chunk
- * of a stage waiting for itself and the chunks next to it to finish the
- * previous stage.  Each run advances
+ * of an instance is its velocity stage then its stress stage, each waiting
+ * for the instance's previous stage to finish everywhere.  Each run advances
  * handle i by nsteps[i] steps from its current time step, in place, with its
  * own material and source; results are identical to b2r_step on each handle
  * with the two-pass step.  The batch keeps pointers to the handles: they must
@@ -413,7 +412,7 @@ b2r_status b2r_eqwp_batch_run(b2r_eqwp_batch* b, void* cuda_stream, int use_grap
 b2r_status b2r_eqwp_batch_synchronize(b2r_eqwp_batch* b, void* cuda_stream);
 /* Lattice-site updates of one run (sum of interior cells x steps). */
 int64_t b2r_eqwp_batch_lups(const b2r_eqwp_batch* b);
-/* Planes per work unit along z (default 32, at least 8; 0 = whole column). */
+/* Planes per work unit along z (default 32; 0 = whole column). */
 b2r_status b2r_eqwp_batch_set_zchunk(b2r_eqwp_batch* b, int zchunk);
 
 /* ---- diagnostics (no reference counterpart) ------------------------------- *
