@@ -14,9 +14,14 @@
 //   3. velocity stage: w = b*vb on W (0 elsewhere);  sb += dt*D^T w;
 //      g_b += dt*(D s)*vb on W
 // with Dp^T = -Dm and Dm^T = -Dp for the 4th-order staggered differences.
-// The per-step gradient increments are formed in FP32 and accumulated in
-// FP64 (this GPU's FP64 rate is a small fraction of its FP32 rate, so the
-// products stay in FP32).  g_rho = -g_b / rho^2 at the end.
+// The per-step gradient increments are formed in FP32 and summed in FP32
+// partial sums, which adjoint_fold adds into the FP64 gradients every
+// kFoldSteps reverse steps on a fixed schedule of step numbers (so the bits
+// do not depend on the checkpoint interval); a partial sum holds at most
+// kFoldSteps increments.  This GPU's FP64 rate is a small fraction of its
+// FP32 rate, so the products stay in FP32, and the per-step read-modify-write
+// of the sums moves 4 B per gradient instead of 8.  g_rho = -g_b / rho^2 at
+// the end.
 #include <cstdio>
 #include <vector>
 
@@ -34,27 +39,25 @@ using namespace eqk;
 #define B2R_ADJ_PREFETCH 1
 #endif
 
-// FP64 gradient cells of a thread, loaded before and stored after the
-// field stores of an iteration (32-byte aligned: the first cell of a thread
-// is a multiple of 4 elements from the buffer base)
+// FP32 partial gradient sums of a thread's 4 cells, loaded before and stored
+// after the field stores of an iteration (16-byte aligned: the first cell of
+// a thread is a multiple of 4 elements from the buffer base)
 struct G4 {
-    double v[4];
-    __device__ __forceinline__ void load(const double* g, const Cell& c)
+    float v[4];
+    __device__ __forceinline__ void load(const float* g, const Cell& c)
     {
         if (c.all) {
-            const double2 a = reinterpret_cast<const double2*>(g)[0];
-            const double2 b = reinterpret_cast<const double2*>(g)[1];
-            v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+            const float4 a = ldw4(g);
+            v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
         } else {
 #pragma unroll
-            for (int j = 0; j < 4; ++j) v[j] = c.vx[j] ? g[j] : 0.0;
+            for (int j = 0; j < 4; ++j) v[j] = c.vx[j] ? g[j] : 0.f;
         }
     }
-    __device__ __forceinline__ void store(double* g, const Cell& c) const
+    __device__ __forceinline__ void store(float* g, const Cell& c) const
     {
         if (c.all) {
-            reinterpret_cast<double2*>(g)[0] = make_double2(v[0], v[1]);
-            reinterpret_cast<double2*>(g)[1] = make_double2(v[2], v[3]);
+            *reinterpret_cast<float4*>(g) = make_float4(v[0], v[1], v[2], v[3]);
         } else {
 #pragma unroll
             for (int j = 0; j < 4; ++j)
@@ -71,16 +74,16 @@ __device__ constexpr int kStrainS[6] = {0, 3, 5, 1, 2, 4};
 //   g_lambda += k tr(e) tr(sb),  g_mu += k (2 e_ii sb_ii + gamma_ij sb_ij)
 // (sb in strain-row order xx, yy, zz, xy, xz, yz; e = E v^n, raw sums)
 __device__ __forceinline__ void lm_increment(float k, const float4 (&sb)[6], const float (&ev)[6][4], int j,
-                                             double& gl, double& gm)
+                                             float& gl, float& gm)
 {
     const float sxx = cmp(sb[0], j), syy = cmp(sb[1], j), szz = cmp(sb[2], j);
     const float sxy = cmp(sb[3], j), sxz = cmp(sb[4], j), syz = cmp(sb[5], j);
     const float exx = ev[0][j], eyy = ev[1][j], ezz = ev[2][j];
     const float tr = add3(sxx, syy, szz);
-    gl += (double)__fmul_rn(k, __fmul_rn(add3(exx, eyy, ezz), tr));
+    gl = __fadd_rn(gl, __fmul_rn(k, __fmul_rn(add3(exx, eyy, ezz), tr)));
     const float nrm = add3(__fmul_rn(exx, sxx), __fmul_rn(eyy, syy), __fmul_rn(ezz, szz));
     const float shr = add3(__fmul_rn(ev[3][j], sxy), __fmul_rn(ev[4][j], sxz), __fmul_rn(ev[5][j], syz));
-    gm += (double)__fmul_rn(k, __fadd_rn(__fmul_rn(2.f, nrm), shr));
+    gm = __fadd_rn(gm, __fmul_rn(k, __fadd_rn(__fmul_rn(2.f, nrm), shr)));
 }
 
 struct AdjV {
@@ -89,7 +92,7 @@ struct AdjV {
     float* w[3];           // b*vb on the window (out)
     const float* acc[3];   // forward stencil sums (D s^n) of this step
     const float* buoy;
-    double* g_b;
+    float* g_b;            // FP32 partial sums
     float k;               // dt / h
 };
 
@@ -100,8 +103,8 @@ struct AdjS {
     const float* v[3];     // forward velocity v^n
     const float* lam;
     const float* mu;
-    double* g_lam;
-    double* g_mu;
+    float* g_lam;          // FP32 partial sums
+    float* g_mu;
     float k;
 };
 
@@ -143,8 +146,7 @@ adj_velocity_kernel(AdjV A, const BlockLayout L, Tiles T)
                 pf_l2(A.vb[f] + oa);
                 pf_l2(A.acc[f] + oa);
             }
-            pf_l2(reinterpret_cast<const float*>(A.g_b + oa));
-            pf_l2(reinterpret_cast<const float*>(A.g_b + oa) + 4);
+            pf_l2(A.g_b + oa);
         }
         float a[3][4];
         op.eval(o - c.base, P, S, a[0], a[1], a[2]);
@@ -172,7 +174,7 @@ adj_velocity_kernel(AdjV A, const BlockLayout L, Tiles T)
             wv[0][j] = b * x;
             wv[1][j] = b * y;
             wv[2][j] = b * zz;
-            gb.v[j] += (double)(A.k * (cmp(ac[0], j) * x + cmp(ac[1], j) * y + cmp(ac[2], j) * zz));
+            gb.v[j] = __fadd_rn(gb.v[j], A.k * (cmp(ac[0], j) * x + cmp(ac[1], j) * y + cmp(ac[2], j) * zz));
         }
 #pragma unroll
         for (int f = 0; f < 3; ++f) st4(A.w[f] + o, c, wv[f]);
@@ -267,10 +269,8 @@ adj_grad_lm_kernel(AdjS A, const BlockLayout L, Tiles T)
             pf_l2(ov.z + oq);
 #pragma unroll
             for (int f = 0; f < 6; ++f) pf_l2(A.sb[f] + oa);
-            pf_l2(reinterpret_cast<const float*>(A.g_lam + oa));
-            pf_l2(reinterpret_cast<const float*>(A.g_lam + oa) + 4);
-            pf_l2(reinterpret_cast<const float*>(A.g_mu + oa));
-            pf_l2(reinterpret_cast<const float*>(A.g_mu + oa) + 4);
+            pf_l2(A.g_lam + oa);
+            pf_l2(A.g_mu + oa);
         }
         float ev[6][4];
         ov.eval(o - c.base, P, S, ev);
@@ -327,10 +327,8 @@ adj_stress_lm_kernel(AdjS A, const BlockLayout L, Tiles T)
             pf_l2(A.mu + oa);
 #pragma unroll
             for (int f = 0; f < 6; ++f) pf_l2(A.sb[f] + oa);
-            pf_l2(reinterpret_cast<const float*>(A.g_lam + oa));
-            pf_l2(reinterpret_cast<const float*>(A.g_lam + oa) + 4);
-            pf_l2(reinterpret_cast<const float*>(A.g_mu + oa));
-            pf_l2(reinterpret_cast<const float*>(A.g_mu + oa) + 4);
+            pf_l2(A.g_lam + oa);
+            pf_l2(A.g_mu + oa);
         }
         float ew[6][4];
         ow.eval(o - c.base, P, S, ew);
@@ -437,7 +435,7 @@ cudaError_t adjoint_inject(float* vby, const long long* d_idx, int nrec, const f
 // fused, else the stress kernel and the gradient kernel).  tmp = vb[3],
 // sb[6], q[6], w[3]; v_n = forward v^n, acc_n = forward D s^n.
 cudaError_t adjoint_step(float* const* tmp, const float* const* v_n, const float* const* acc_n,
-                         const float* const* mat, double* const* g, const BlockLayout& L, float dt_h,
+                         const float* const* mat, float* const* g, const BlockLayout& L, float dt_h,
                          bool last, bool fused, cudaStream_t st)
 {
     AdjV V;
@@ -475,6 +473,40 @@ cudaError_t adjoint_step(float* const* tmp, const float* const* v_n, const float
             count_launches(2);
         }
     }
+    return cudaGetLastError();
+}
+
+namespace {
+constexpr int kFoldSteps = 32;    // reverse steps per FP32 partial sum
+
+__global__ void adjoint_fold_kernel(float* g0, float* g1, float* g2, double* h0, double* h1, double* h2,
+                                    long long n4)
+{
+    float* g[3] = {g0, g1, g2};
+    double* h[3] = {h0, h1, h2};
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n4; i += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            float4* gp = reinterpret_cast<float4*>(g[m]) + i;
+            double2* hp = reinterpret_cast<double2*>(h[m]) + 2 * i;
+            const float4 a = *gp;
+            const double2 b0 = hp[0], b1 = hp[1];
+            hp[0] = make_double2(b0.x + (double)a.x, b0.y + (double)a.y);
+            hp[1] = make_double2(b1.x + (double)a.z, b1.y + (double)a.w);
+            *gp = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
+}
+}  // namespace
+
+int adjoint_fold_steps() { return kFoldSteps; }
+
+cudaError_t adjoint_fold(float* const* g, double* const* g64, const BlockLayout& L, cudaStream_t st)
+{
+    const long long n4 = L.bstride * L.nblk / 4;   // bstride is a multiple of 4 cells (rows of 32)
+    const long long blocks = std::min<long long>((n4 + 255) / 256, 152LL * 16);
+    adjoint_fold_kernel<<<(unsigned)std::max(1LL, blocks), 256, 0, st>>>(g[0], g[1], g[2], g64[0], g64[1], g64[2], n4);
+    count_launches(1);
     return cudaGetLastError();
 }
 

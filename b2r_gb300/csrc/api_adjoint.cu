@@ -85,7 +85,7 @@ b2r_status b2r_eqwp_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const i
     const size_t fba = (fb + 255) & ~(size_t)255, gba = (gbytes + 255) & ~(size_t)255;
     int nbuf = nseg > 1 ? 2 : 1;
     for (;; --nbuf) {
-        const size_t nfields = nf_ckpt + nbuf * (nf_v + nf_a + 6) + 18;
+        const size_t nfields = nf_ckpt + nbuf * (nf_v + nf_a + 6) + 18 + 3;
         const size_t need = nfields * fba + 3 * gba;
         if (h->adj_ws_bytes >= need) break;
         if (h->adj_ws) cudaFree(h->adj_ws);
@@ -110,11 +110,14 @@ b2r_status b2r_eqwp_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const i
     carve(nf_a * nbuf, arep);
     carve(6 * (size_t)nbuf, srep);
     carve(18, tmp);
+    std::vector<float*> g32;            // FP32 partial gradient sums, folded into gp
+    carve(3, g32);
     double* gp[3];
     for (int m = 0; m < 3; ++m, ws += gba) {
         gp[m] = reinterpret_cast<double*>(ws);
         CK(h, cudaMemsetAsync(gp[m], 0, gbytes, h->stream));
     }
+    for (float* b : g32) CK(h, cudaMemsetAsync(b, 0, fb, h->stream));
     DevBuf d_idx, d_rec, d_res;
     // cells outside the update window never change: every replay slot starts
     // as a copy of the initial state there
@@ -222,7 +225,10 @@ b2r_status b2r_eqwp_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const i
             const float* vn[3] = {vslot(sgi, k, 0), vslot(sgi, k, 1), vslot(sgi, k, 2)};
             float* const* a = aslot(sgi, k);
             const float* an[3] = {a[0], a[1], a[2]};
-            CK(h, adjoint_step(tp, vn, an, mat, gp, h->L, dt_h, n == 0, h->adj_fused, h->stream));
+            CK(h, adjoint_step(tp, vn, an, mat, g32.data(), h->L, dt_h, n == 0, h->adj_fused, h->stream));
+            // the partial sums into FP64 on a fixed schedule of step numbers
+            // (step 0 is the last reverse step, so nothing is left behind)
+            if (n % adjoint_fold_steps() == 0) CK(h, adjoint_fold(g32.data(), gp, h->L, h->stream));
         }
         if (nbuf == 2) CK(h, cudaEventRecord(ax.rev[sgi % 2], h->stream));
         else if (sgi >= 1 && (st = replay(sgi - 1, h->stream)) != B2R_OK) return st;

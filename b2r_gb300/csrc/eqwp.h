@@ -77,13 +77,18 @@ cudaError_t launch_eqwp_stag_fused(const StressMaps& maps, const float* const* v
 // adjoint.cu: receiver sampling / injection and one reverse step of the
 // staggered scheme (tmp = vb[3], sb[6], q[6], w[3]; stress order xx, xy, xz,
 // yy, yz, zz; v_n = forward v^n, acc_n = forward stencil sums of step n;
-// last = step 0, whose stress-side half has no earlier step to feed),
-// gradients in FP64.
+// last = step 0, whose stress-side half has no earlier step to feed).
 cudaError_t adjoint_sample(const float* vy, const long long* d_idx, int nrec, float* out, cudaStream_t st);
 cudaError_t adjoint_inject(float* vby, const long long* d_idx, int nrec, const float* res, cudaStream_t st);
 cudaError_t adjoint_step(float* const* tmp, const float* const* v_n, const float* const* acc_n,
-                         const float* const* mat, double* const* g, const BlockLayout& L, float dt_h,
+                         const float* const* mat, float* const* g, const BlockLayout& L, float dt_h,
                          bool last, bool fused, cudaStream_t st);
+// g holds FP32 partial sums of the lambda, mu and b gradients; every
+// adjoint_fold_steps() reverse steps (at step numbers that are multiples of
+// it, and at step 0) adjoint_fold adds them into the FP64 gradients g64 and
+// clears them.
+int adjoint_fold_steps();
+cudaError_t adjoint_fold(float* const* g, double* const* g64, const BlockLayout& L, cudaStream_t st);
 cudaError_t adjoint_grad_out(const double* g, const float* buoy, int rho, const BlockLayout& L,
                              double* out, cudaStream_t st);
 
