@@ -246,6 +246,7 @@ b2r_status b2r_eqwp_misfit_gradient(b2r_handle* h, int nsteps, int nrec, const i
     CK(h, cudaStreamSynchronize(h->stream));
     h->ts = nsteps;
     h->halos_fresh = false;
+    h->upmask = 0;
     return check_status(h);
 }
 

@@ -48,6 +48,15 @@ struct b2r_handle {
     StressMaps smaps[2];
     bool eqwp_fused = false;   // two-pass by default: faster on this GPU so far
     bool eqwp_tma = false;     // two-pass: the stress stage with TMA-streamed inputs (eqwp_tma.cu)
+    // two-pass, several blocks: the halo exchange of the next period runs on
+    // the stream xs while the last stress stage of a period finishes the
+    // tiles that the exchange does not read (opt-in: on one GPU the exchange
+    // is a copy that competes for the same HBM, and the split stage costs
+    // more than the overlap returns)
+    bool eqwp_overlap = false;
+    bool xdone = false;        // the last sub-step issued the next period's exchange
+    cudaStream_t xs = nullptr;
+    cudaEvent_t xev[2] = {};   // [band tiles done, exchange done]
     std::map<int, EqwpStressMaps> emaps;   // its tensor maps per tile width (threads per row), built
     const void* emaps_of[11] = {};         // for the field pointers in emaps_of
     bool gol_bytes = false;    // Game of Life: byte-SWAR kernel instead of bit-sliced cells
@@ -68,6 +77,7 @@ struct b2r_handle {
     int* d_status = nullptr;
     long long ts = 0;
     bool halos_fresh = false;
+    unsigned upmask = 0;         // fields uploaded since the last step while the halos were not fresh
     unsigned xmask = 0;          // fields exchanged by the caller at time step xts
     long long xts = -1;
     // CUDA graphs of whole periods (heat, GoL on a non-default stream)
@@ -162,10 +172,13 @@ b2r_status build_heat_maps(b2r_handle* h);
 int heat_pass_steps(const b2r_handle* h, int i, int left);
 int gol_pass_gens(const b2r_handle* h, int i, int left);
 b2r_status check_status(b2r_handle* h);
-b2r_status exchange_all(b2r_handle* h, bool staged);
+b2r_status exchange_all(b2r_handle* h, bool staged, cudaStream_t xst = nullptr);   // xst: another stream than the handle's
 b2r_status exchange_one(b2r_handle* h, int field, bool staged);
 EqwpStagParams stag_params(const b2r_handle* h);
-b2r_status substep(b2r_handle* h, int i);
+// One sub-step i of a period.  xnext: the caller starts the next period
+// without an exchange if h->xdone is set afterwards (the sub-step may then
+// issue that exchange itself, overlapped with its last stage).
+b2r_status substep(b2r_handle* h, int i, bool xnext = false);
 b2r_status substep2(b2r_handle* h, int i);
 void drop_graphs(b2r_handle* h);
 b2r_status advance(b2r_handle* h, int n);

@@ -24,6 +24,7 @@ b2r_status b2r_set_tuning(b2r_handle* h, int key, int value)
     case B2R_TUNE_TB_NARROW: h->tune.tbn = value != 0; break;
     case B2R_TUNE_TB_R2: h->tune.r2 = value != 0; break;
     case B2R_TUNE_EQWP_TMA: h->eqwp_tma = value != 0; break;
+    case B2R_TUNE_EQWP_OVERLAP: h->eqwp_overlap = value != 0; break;
     default: return fail(h, B2R_ERR_ARG, "unknown tuning key %d", key);
     }
     drop_graphs(h);
@@ -47,6 +48,7 @@ b2r_status b2r_get_tuning(const b2r_handle* h, int key, int* value)
     case B2R_TUNE_TB_NARROW: *value = h->tune.tbn; break;
     case B2R_TUNE_TB_R2: *value = h->tune.r2; break;
     case B2R_TUNE_EQWP_TMA: *value = h->eqwp_tma ? 1 : 0; break;
+    case B2R_TUNE_EQWP_OVERLAP: *value = h->eqwp_overlap ? 1 : 0; break;
     default: return fail(nullptr, B2R_ERR_ARG, "unknown tuning key %d", key);
     }
     return B2R_OK;
@@ -57,7 +59,7 @@ b2r_status b2r_get_tuning(const b2r_handle* h, int key, int* value)
 // the period-end halo fill (GoL); the one-pass or two-pass step (elastic
 // wave).  Trials run on the live fields, which are restored afterwards.
 struct KnobSet {
-    int tblock, gol_bytes, gol_push, eqwp_fused, eqwp_tma = 0;
+    int tblock, gol_bytes, gol_push, eqwp_fused, eqwp_tma = 0, eqwp_overlap = 0;
 };
 static std::map<TuneKey, KnobSet> g_knob_cache;
 
@@ -68,6 +70,7 @@ static void apply_knobs(b2r_handle* h, const KnobSet& k)
     h->gol_push = k.gol_push != 0;
     h->eqwp_fused = k.eqwp_fused != 0;
     h->eqwp_tma = k.eqwp_tma != 0;
+    h->eqwp_overlap = k.eqwp_overlap != 0;
 }
 
 static b2r_status autotune_knobs(b2r_handle* h, int trial_steps, int best[3], double* best_ms)
@@ -91,17 +94,22 @@ static b2r_status autotune_knobs(b2r_handle* h, int trial_steps, int best[3], do
         }
     }
     std::vector<KnobSet> cands;
-    const KnobSet cur{h->tune.tblock, h->gol_bytes, h->gol_push, h->eqwp_fused, h->eqwp_tma};
+    const KnobSet cur{h->tune.tblock, h->gol_bytes, h->gol_push, h->eqwp_fused, h->eqwp_tma, h->eqwp_overlap};
     if (h->cfg.model == B2R_MODEL_GOL) {
         for (int tb : {1, 2, 4})
             for (int bytes = 0; bytes < 2; ++bytes)
                 for (int push = 0; push < 2; ++push)
-                    if (!push || (tb >= 2 && !bytes)) cands.push_back({tb, bytes, push, cur.eqwp_fused, cur.eqwp_tma});
+                    if (!push || (tb >= 2 && !bytes))
+                        cands.push_back({tb, bytes, push, cur.eqwp_fused, cur.eqwp_tma, cur.eqwp_overlap});
     } else {
-        // the two-pass step with plain-load or TMA-streamed stress stage, the one-pass step
-        cands.push_back({cur.tblock, cur.gol_bytes, cur.gol_push, 0, 0});
-        if (h->cfg.model == B2R_MODEL_EQWP_STAG) cands.push_back({cur.tblock, cur.gol_bytes, cur.gol_push, 0, 1});
-        cands.push_back({cur.tblock, cur.gol_bytes, cur.gol_push, 1, 0});
+        // the two-pass step with plain-load or TMA-streamed stress stage (and,
+        // on several blocks, with the exchange overlapped), the one-pass step
+        const bool stag = h->cfg.model == B2R_MODEL_EQWP_STAG;
+        cands.push_back({cur.tblock, cur.gol_bytes, cur.gol_push, 0, 0, 0});
+        if (stag) cands.push_back({cur.tblock, cur.gol_bytes, cur.gol_push, 0, 1, 0});
+        if (stag && (h->L.nblk > 1 || h->L.periodic))
+            cands.push_back({cur.tblock, cur.gol_bytes, cur.gol_push, 0, 0, 1});
+        cands.push_back({cur.tblock, cur.gol_bytes, cur.gol_push, 1, 0, 0});
     }
     // the state the trials overwrite: the current buffer (GoL) or every
     // field of the current set with the set's pointers (elastic wave)

@@ -175,9 +175,10 @@ b2r_status check_status(b2r_handle* h)
     return B2R_OK;
 }
 
-b2r_status exchange_all(b2r_handle* h, bool staged)
+b2r_status exchange_all(b2r_handle* h, bool staged, cudaStream_t xst)
 {
     const BlockLayout& L = h->L;
+    const cudaStream_t st = xst ? xst : h->stream;
     void* bounce = nullptr;
     int nf = 1;
     if (h->cfg.model == B2R_MODEL_EQWP_REF || h->cfg.model == B2R_MODEL_EQWP_STAG) nf = h->nfld;
@@ -197,15 +198,15 @@ b2r_status exchange_all(b2r_handle* h, bool staged)
     if (h->cell_bytes == 1) {
         FieldSet<uint8_t> fs{};
         fs.p[0] = static_cast<uint8_t*>(h->buf[h->cur]);
-        if (gather) CK(h, launch_halo_gather<uint8_t>(fs, 1, L, h->stream));
-        else CK(h, launch_halo_exchange<uint8_t>(fs, 1, L, static_cast<uint8_t*>(bounce), h->stream));
+        if (gather) CK(h, launch_halo_gather<uint8_t>(fs, 1, L, st));
+        else CK(h, launch_halo_exchange<uint8_t>(fs, 1, L, static_cast<uint8_t*>(bounce), st));
     } else {
         FieldSet<float> fs{};
         if (nf == 1) fs.p[0] = static_cast<float*>(h->buf[h->cur]);
         else
             for (int f = 0; f < nf; ++f) fs.p[f] = h->fld[f];
-        if (gather) CK(h, launch_halo_gather<float>(fs, nf, L, h->stream));
-        else CK(h, launch_halo_exchange<float>(fs, nf, L, static_cast<float*>(bounce), h->stream));
+        if (gather) CK(h, launch_halo_gather<float>(fs, nf, L, st));
+        else CK(h, launch_halo_exchange<float>(fs, nf, L, static_cast<float*>(bounce), st));
     }
     return B2R_OK;
 }
@@ -248,8 +249,9 @@ EqwpStagParams stag_params(const b2r_handle* h)
     return p;
 }
 
-b2r_status substep(b2r_handle* h, int i)
+b2r_status substep(b2r_handle* h, int i, bool xnext)
 {
+    h->upmask = 0;
     switch (h->cfg.model) {
     case B2R_MODEL_HEAT:
         CK(h, launch_heat_substep(&h->tmap[h->cur], static_cast<float*>(h->buf[1 - h->cur]), h->L,
@@ -308,6 +310,27 @@ b2r_status substep(b2r_handle* h, int i)
             CK(h, launch_eqwp_stress_tma(it->second, tx, h->fld, h->L, i, amp, p, h->d_status, h->stream));
             return B2R_OK;
         }
+        if (xnext && h->eqwp_overlap && i == h->cfg.R - 1 && (h->L.nblk > 1 || h->L.periodic)) {
+            // the last sub-step of a period: the stress tiles that hold the
+            // cells the next exchange reads, then that exchange on the stream
+            // xs while the other tiles finish (they read no halo cell)
+            if (!h->xs) {
+                int lo = 0, hi = 0;
+                CK(h, cudaDeviceGetStreamPriorityRange(&lo, &hi));
+                CK(h, cudaStreamCreateWithPriority(&h->xs, cudaStreamNonBlocking, hi));
+                for (int k = 0; k < 2; ++k) CK(h, cudaEventCreateWithFlags(&h->xev[k], cudaEventDisableTiming));
+            }
+            CK(h, launch_eqwp_stag_velocity(h->fld, h->mat, h->L, i, p, h->stream));
+            CK(h, launch_eqwp_stag_stress(h->fld, h->mat, h->L, i, (int)h->ts, p, 1, h->stream));
+            CK(h, cudaEventRecord(h->xev[0], h->stream));
+            CK(h, cudaStreamWaitEvent(h->xs, h->xev[0], 0));
+            if (b2r_status st = exchange_all(h, false, h->xs); st != B2R_OK) return st;
+            CK(h, cudaEventRecord(h->xev[1], h->xs));
+            CK(h, launch_eqwp_stag_stress(h->fld, h->mat, h->L, i, (int)h->ts, p, 2, h->stream));
+            CK(h, cudaStreamWaitEvent(h->stream, h->xev[1], 0));
+            h->xdone = true;
+            return B2R_OK;
+        }
         CK(h, launch_eqwp_stag_substep(h->fld, h->mat, h->L, i, (int)h->ts, p, h->stream));
         return B2R_OK;
     }
@@ -335,6 +358,7 @@ b2r_status substep2(b2r_handle* h, int i);
 b2r_status advance(b2r_handle* h, int n)
 {
     b2r_status st;
+    if (n > 0) h->upmask = 0;
     for (int s = 0; s < n;) {
         const int i = (int)(h->ts % h->cfg.R);
         if (i == 0 && !h->halos_fresh)
@@ -373,9 +397,12 @@ b2r_status advance(b2r_handle* h, int n)
             h->ts += k;
             s += k;
         } else {
-            if ((st = substep(h, i)) != B2R_OK) return st;
+            if ((st = substep(h, i, true)) != B2R_OK) return st;
             h->ts++;
             ++s;
+            // the next period's halos were exchanged inside the sub-step
+            h->halos_fresh = h->xdone;
+            h->xdone = false;
         }
     }
     return B2R_OK;
@@ -585,6 +612,9 @@ b2r_status b2r_destroy(b2r_handle* h)
             if (e) cudaEventDestroy(e);
     if (h->cin) cudaStreamDestroy(h->cin);
     if (h->cout) cudaStreamDestroy(h->cout);
+    if (h->xs) cudaStreamDestroy(h->xs);
+    for (cudaEvent_t e : h->xev)
+        if (e) cudaEventDestroy(e);
     if (h->bounce) cudaFree(h->bounce);
     if (h->d_status) cudaFree(h->d_status);
     delete h;
@@ -678,7 +708,13 @@ b2r_status b2r_upload(b2r_handle* h, int field, const void* src, int src_is_devi
         CK(h, launch_scatter<float>(static_cast<const float*>(dsrc), static_cast<float*>(dst),
                                     static_cast<float*>(dst2), h->L, h->shell, h->stream));
     h->ts = 0;
-    h->halos_fresh = true;
+    // the scatter filled this field's halos; the others are fresh only if
+    // they were, or once every field has been uploaded since the last step
+    if (!h->halos_fresh && !is_mat) {   // material never changes: its halos stay consistent
+        const int nf = eq ? h->nfld : 1;
+        h->upmask |= 1u << (eq ? field : 0);
+        h->halos_fresh = h->upmask == (nf >= 32 ? ~0u : (1u << nf) - 1u);
+    }
     return B2R_OK;
 }
 
@@ -755,6 +791,7 @@ b2r_status b2r_step(b2r_handle* h, int nsteps)
                 if (h->gflip[h->cur]) h->cur = 1 - h->cur;
                 h->ts += unit;
                 h->halos_fresh = false;
+                h->upmask = 0;
                 s += unit;
                 continue;
             }

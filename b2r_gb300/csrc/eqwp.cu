@@ -195,12 +195,35 @@ eqwp_stag_velocity(FieldPtrs F, FieldPtrs O, MatPtrs M, const BlockLayout L, int
     stag_velocity_unit<ACC>(F, O, M, L, step_i, T, p, A, blk, zc, launch_pos());
 }
 
+// Tiles of a stress-stage launch that hold a cell the halo exchange reads:
+// an owned cell within H of a face that has a neighbour block (H = the halo
+// width; the owned cells of an axis are [H, H + B)).
+__device__ __forceinline__ bool band_tile(const BlockLayout& L, int blk, const Tiles& T, const TilePos& q, int zs,
+                                          int ze)
+{
+    const int e = edge_bits(L, blk), H = L.H;
+    const int x0 = T.x0 - L.xoff + q.bx * 4 * q.dx, x1 = x0 + 4 * q.dx - 1;
+    const int y0 = T.y0 + q.by * q.dy, y1 = y0 + q.dy - 1;
+    const int lo[3] = {x0, y0, zs}, hi[3] = {x1, y1, ze};
+    bool band = false;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        band |= (!(e & (1 << (2 * a))) && lo[a] < 2 * H) || (!(e & (2 << (2 * a))) && hi[a] >= L.B[a]);
+    return band;
+}
+
+// split: 0 every tile; 1 the tiles of band_tile only; 2 the others only
 __global__ void __launch_bounds__(kBX * kBY, B2R_EQWP_MINB)
 eqwp_stag_stress(FieldPtrs F, FieldPtrs O, MatPtrs M, const BlockLayout L, int step_i, Tiles T,
-                 EqwpStagParams p, float src_amp)
+                 EqwpStagParams p, float src_amp, int split)
 {
     const int blk = blockIdx.z / T.nzc, zc = blockIdx.z % T.nzc;
-    stag_stress_unit(F, O, M, L, step_i, T, p, src_amp, blk, zc, launch_pos());
+    const TilePos q = launch_pos();
+    if (split) {
+        const Win w = window(L, blk, zc, T.nzc, 4 * step_i + 4);
+        if (band_tile(L, blk, T, q, w.zs, w.ze) != (split == 1)) return;
+    }
+    stag_stress_unit(F, O, M, L, step_i, T, p, src_amp, blk, zc, q);
 }
 
 }  // namespace
@@ -256,8 +279,23 @@ cudaError_t launch_eqwp_stag_substep(float* const* fld, float* const* mat, const
     float amp = 0.f;
     if (p.src_host && ts >= 0 && ts < p.src_len) amp = p.src_host[ts];
     eqwp_stag_velocity<false><<<ga.g, ga.b, 0, st>>>(F, F, M, L, step_i, ga.t, p, AccPtrs{});
-    eqwp_stag_stress<<<gb.g, gb.b, 0, st>>>(F, F, M, L, step_i, gb.t, p, amp);
+    eqwp_stag_stress<<<gb.g, gb.b, 0, st>>>(F, F, M, L, step_i, gb.t, p, amp, 0);
     count_launches(2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_eqwp_stag_stress(float* const* fld, float* const* mat, const BlockLayout& L, int step_i, int ts,
+                                    const EqwpStagParams& p, int split, cudaStream_t st)
+{
+    FieldPtrs F{};
+    for (int f = 0; f < 9; ++f) F.p[f] = fld[f];
+    MatPtrs M{};
+    for (int m = 0; m < 3; ++m) M.p[m] = mat[m];
+    const Grid gb = stage_grid(L, 4 * step_i + 4);
+    float amp = 0.f;
+    if (p.src_host && ts >= 0 && ts < p.src_len) amp = p.src_host[ts];
+    eqwp_stag_stress<<<gb.g, gb.b, 0, st>>>(F, F, M, L, step_i, gb.t, p, amp, split);
+    count_launches(1);
     return cudaGetLastError();
 }
 
@@ -293,7 +331,7 @@ cudaError_t launch_eqwp_stag_step_replay(const float* const* v_in, float* const*
     if (p.src_host && ts >= 0 && ts < p.src_len) amp = p.src_host[ts];
     eqwp_stag_velocity<true><<<ga.g, ga.b, 0, st>>>(F, O, M, L, 0, ga.t, p, A);
     // the stress stage reads the new velocities and updates the stresses in place
-    eqwp_stag_stress<<<gb.g, gb.b, 0, st>>>(O, O, M, L, 0, gb.t, p, amp);
+    eqwp_stag_stress<<<gb.g, gb.b, 0, st>>>(O, O, M, L, 0, gb.t, p, amp, 0);
     count_launches(2);
     return cudaGetLastError();
 }

@@ -56,6 +56,12 @@ void eqwp_stress_tma_shape(const BlockLayout& L, int step_i, int* tx, int* ty);
 cudaError_t launch_eqwp_stress_tma(const EqwpStressMaps& maps, int tx, float* const* fld, const BlockLayout& L,
                                    int step_i, float src_amp, const EqwpStagParams& p, int* status,
                                    cudaStream_t st);
+// The stress stage alone (plain loads; in place): split 0 = every tile,
+// 1 = only the tiles holding an owned cell within H of a face with a
+// neighbour block (every cell the halo exchange reads), 2 = only the other
+// tiles, which read no halo cell.
+cudaError_t launch_eqwp_stag_stress(float* const* fld, float* const* mat, const BlockLayout& L, int step_i, int ts,
+                                    const EqwpStagParams& p, int split, cudaStream_t st);
 // The velocity stage alone (plain loads), for a step whose stress stage is
 // launched separately.
 cudaError_t launch_eqwp_stag_velocity(float* const* fld, float* const* mat, const BlockLayout& L, int step_i,

@@ -404,6 +404,7 @@ b2r_status b2r_eqwp_batch_run(b2r_eqwp_batch* b, void* stream, int use_graph)
     for (int k = 0; k < b->n; ++k) {
         b->hs[k]->ts += b->nsteps[k];
         b->hs[k]->halos_fresh = false;
+        b->hs[k]->upmask = 0;
     }
     return B2R_OK;
 }

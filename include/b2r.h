@@ -156,9 +156,14 @@ enum {
     B2R_TUNE_TB_R2 = 12,       /* heat radius 2: 1 = two steps per HBM pass (with TBLOCK >= 2) on
                                   64 x 64-cell tiles, 0 = one step per pass (default: the one-step
                                   sweep is faster on this GPU so far); bit-identical */
-    B2R_TUNE_EQWP_TMA = 13     /* staggered elastic wave, two-pass step: 1 = the stress stage with
+    B2R_TUNE_EQWP_TMA = 13,    /* staggered elastic wave, two-pass step: 1 = the stress stage with
                                   its inputs streamed through TMA rings, 0 = plain loads (default);
                                   bit-identical */
+    B2R_TUNE_EQWP_OVERLAP = 14 /* staggered elastic wave, two-pass step on several blocks: 1 = the
+                                  last stress stage of a period computes the tiles that the next
+                                  halo exchange reads first, then that exchange runs on a second
+                                  stream while the other tiles finish; 0 = the exchange at the
+                                  period start (default: faster on one GPU so far); bit-identical */
 };
 b2r_status b2r_set_tuning(b2r_handle* h, int key, int value);
 /* Current value of a knob (after b2r_autotune: the schedule it picked). */
@@ -169,7 +174,10 @@ b2r_status b2r_get_tuning(const b2r_handle* h, int key, int* value);
  * programmatic dependent launch, best[3] = {zchunk, ctas_per_sm, pdl}.
  * Game of Life: generations per pass x bit-sliced / byte cells x period-end
  * halo fill, best = {tblock, gol_bytes, gol_push}.  Staggered elastic wave:
- * one-pass or two-pass step, best = {tblock, eqwp_fused, 0}.  Results are
+ * one-pass or two-pass step, the latter with the plain or TMA-streamed
+ * stress stage and, on several blocks, with the halo exchange at the period
+ * start or overlapped with the last stress stage, best = {tblock,
+ * eqwp_fused, 0} (the other choices: b2r_get_tuning).  Results are
  * cached per (model, D, block size, block count) for the process and
  * applied to later handles of the same shape.  best may be NULL; *best_ms
  * gets the time per step (-1 if cached). */

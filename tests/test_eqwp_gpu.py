@@ -162,3 +162,39 @@ def test_eqwp_stag_one_pass_equals_two_pass(b2r, env, blocks, R):
             d.synchronize()
     for k in range(9):
         assert np.array_equal(outs[0][k], outs[1][k]), NAMES[k]
+
+
+@pytest.mark.parametrize("env,blocks,R", [((150, 90, 70), (3, 2, 1), 2), ((64, 64, 64), (2, 2, 2), 3),
+                                          ((96, 40, 120), (2, 1, 3), 1), ((40, 120, 90), (1, 2, 3), 2)])
+def test_eqwp_stag_overlapped_exchange_bit_identical(b2r, orc, env, blocks, R):
+    """The next period's halo exchange issued inside the period's last
+    stress stage (band tiles first, the exchange on a second stream, the
+    other tiles meanwhile) against the exchange at the period start: the
+    same bits, stepping whole runs and in pieces that split periods, with an
+    upload in between (whose scatter fills the halos itself)."""
+    h = 10.0
+    mat = layered(env)
+    dt = 0.5 * h / (4000 * np.sqrt(3) * (9 / 8 + 1 / 24))
+    src = (env[0] // 3, env[1] // 2, env[2] // 2)
+    nsteps = 4 * R + 1
+    amps = ricker(2 * nsteps, dt, 10.0, 1e6 * dt).astype(np.float32)
+    outs = []
+    for overlap in (0, 1):
+        with b2r.Domain(b2r.MODEL_EQWP_STAG, env, blocks=blocks, R=R, D=2, dt=dt, h=h, src=src) as d:
+            d.set_tuning(eqwp_fused=0, eqwp_tma=0, eqwp_overlap=overlap)
+            assert d.get_tuning()["eqwp_overlap"] == overlap
+            for m, name in enumerate(["lambda", "mu", "buoy"]):
+                d.upload(mat[m].astype(np.float32), field=name)
+            rng = np.random.default_rng(21)
+            for k in range(9):
+                d.upload(rng.standard_normal(d.domain_shape).astype(np.float32), field=k)
+            d.set_source(amps)
+            d.step(nsteps)
+            mid = d.download(field=4)
+            d.upload(mid, field=4)
+            for n in (1, R, 2, 1):
+                d.step(n)
+            outs.append([d.download(field=k) for k in range(9)])
+            d.synchronize()
+    for k in range(9):
+        assert np.array_equal(outs[0][k], outs[1][k]), NAMES[k]
