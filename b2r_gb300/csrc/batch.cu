@@ -76,16 +76,22 @@ struct InstDev {
     int rounds;                          // rounds of units: nsteps / tb, rounded up
 };
 
+// A work item packed into 64 bits: round t (bits 40..63), instance k in
+// the sorted order (bits 24..39), unit u (bits 0..23).
+constexpr int kItemKBits = 16, kItemUBits = 24;
+__host__ __device__ inline unsigned long long pack_item(int t, int k, int u)
+{
+    return ((unsigned long long)t << (kItemKBits + kItemUBits)) | ((unsigned long long)k << kItemUBits) |
+           (unsigned long long)u;
+}
+
 struct BatchArgs {
     const InstDev* inst;                 // sorted by rounds, descending
     const CUtensorMap* maps;             // 2 per instance: buffer 0, buffer 1
-    const long long* step_off;           // items before round t (size maxsteps+1)
-    const int* active;                   // instances still stepping at step t
-    const long long* unit_prefix;        // units of instances [0, k) (size n+1)
+    const unsigned long long* items;     // the queue: work items in claim order
     unsigned long long* head;            // next item (zeroed per run)
     unsigned* done;                      // finished units per instance (zeroed per run)
     int* status;
-    int maxsteps, ninst;                 // maxsteps: rounds of the longest instance
     long long total;
 };
 
@@ -152,19 +158,10 @@ __global__ void __launch_bounds__(kThreads, B2R_BATCH_MINB) batch_kernel(const B
     extern __shared__ __align__(128) unsigned char smem_raw[];
     heatk::Ring rg;
     heatk::ring_init<kS, kSlot>(rg, smem_raw);
-    // schedule tables after the ring (the ring ends 16 bytes after its barriers)
-    long long* s_step_off = reinterpret_cast<long long*>(
-        reinterpret_cast<unsigned char*>(rg.abort_flag) + 16);
-    long long* s_prefix = s_step_off + (a.maxsteps + 1);
-    int* s_active = reinterpret_cast<int*>(s_prefix + (a.ninst + 1));
-    // the two-step units' stage-1 planes after the tables, 128-byte aligned
+    // the two-step units' stage-1 planes after the ring (which ends 16 bytes
+    // after its barriers), 128-byte aligned
     float* s1 = reinterpret_cast<float*>(
-        (reinterpret_cast<uintptr_t>(s_active + (a.maxsteps + 1)) + 127) & ~uintptr_t(127));
-    for (int i = threadIdx.x; i <= a.maxsteps; i += blockDim.x) {
-        s_step_off[i] = a.step_off[i];
-        s_active[i] = a.active[i];
-    }
-    for (int i = threadIdx.x; i <= a.ninst; i += blockDim.x) s_prefix[i] = a.unit_prefix[i];
+        (reinterpret_cast<uintptr_t>(rg.abort_flag) + 16 + 127) & ~uintptr_t(127));
     __shared__ long long s_next, s_cur;
     __shared__ int s_t, s_k, s_u, s_ok;
     if (threadIdx.x == 0) s_next = (long long)atomicAdd(a.head, 1ull);
@@ -174,8 +171,10 @@ __global__ void __launch_bounds__(kThreads, B2R_BATCH_MINB) batch_kernel(const B
             const long long item = s_next;
             s_cur = item;
             if (item < a.total) {
-            int t, k, u;
-            wq::decode(item, s_step_off, s_active, s_prefix, a.maxsteps, t, k, u);
+            const unsigned long long x = a.items[item];
+            const int t = (int)(x >> (kItemKBits + kItemUBits));
+            const int k = (int)((x >> kItemUBits) & ((1u << kItemKBits) - 1));
+            const int u = (int)(x & ((1u << kItemUBits) - 1));
             int ok = 1;
             // wait for round t-1 of this instance (bounded)
             if (t > 0) ok = wq::wait_done(&a.done[k], (unsigned)t * (unsigned)a.inst[k].units) ? 1 : 0;
@@ -233,21 +232,19 @@ struct b2r_batch {
     std::vector<int> sched;          // queue position -> host index (by rounds, descending)
     InstDev* d_inst = nullptr;
     CUtensorMap* d_maps = nullptr;
-    long long* d_step_off = nullptr;
-    int* d_active = nullptr;
-    long long* d_prefix = nullptr;
+    unsigned long long* d_items = nullptr;   // the queue (capacity items_cap)
+    long long items_cap = 0;
     unsigned long long* d_head = nullptr;
     unsigned* d_done = nullptr;
     int* d_status = nullptr;
     float* staging = nullptr;
     size_t staging_bytes = 0;
-    int maxsteps = 0;
     int maxrounds = 0;               // rounds of the current schedule's longest instance
     long long total = 0;
     int lz_policy = 16;              // z chunk cap per unit (autotuned)
     int grid[2] = {0, 0};            // persistent grid (every resident slot) per kernel variant
     bool two = false;                // some instance runs on two-step units
-    size_t smem = 0;                 // ring + schedule tables
+    size_t smem = 0;                 // ring + the two-step units' planes
     cudaGraphExec_t gexec = nullptr;
     cudaStream_t gstream = nullptr;
     long long launches = 0;
@@ -350,17 +347,18 @@ b2r_status apply_shapes(b2r_batch* b, const std::vector<int>& sh)
 
 b2r_status apply_shape(b2r_batch* b, int s) { return apply_shapes(b, std::vector<int>(b->n, s)); }
 
-// Schedule tables for the current shapes and Lz policy.  Items are (round,
-// instance, unit), round-major; a round is one step of a one-step instance
-// or two of a two-step one.  The queue holds the instances sorted by their
-// round count (descending), so those still active at round t are a prefix.
+// The queue for the current shapes and Lz policy: work items (round,
+// instance, unit) written out in claim order, round-major.  A round is one
+// step of a one-step instance or two of a two-step one; the instances are
+// sorted by their round count (descending), so those still stepping at round
+// t are a prefix.  A unit waits only for the previous round of its own
+// instance, which the queue holds earlier, so the queue cannot deadlock.
 b2r_status build_schedule(b2r_batch* b)
 {
     b->sched.resize(b->n);
     for (int k = 0; k < b->n; ++k) b->sched[k] = k;
     std::stable_sort(b->sched.begin(), b->sched.end(),
                      [&](int x, int y) { return b->host[x].rounds > b->host[y].rounds; });
-    std::vector<long long> prefix(b->n + 1, 0);
     std::vector<InstDev> dev(b->n);
     std::vector<CUtensorMap> maps(2 * b->n);
     b->maxrounds = 0;
@@ -371,28 +369,38 @@ b2r_status build_schedule(b2r_batch* b)
         in.Lz = std::min(in.NZ, b->lz_policy > 0 ? b->lz_policy : in.NZ);
         in.nzc = (in.NZ + in.Lz - 1) / in.Lz;
         in.units = in.ntx * in.nty * in.nzc;
-        prefix[j + 1] = prefix[j] + in.units;
+        if (in.units >= (1 << kItemUBits) || in.rounds >= (1 << (64 - kItemKBits - kItemUBits)))
+            return bfail(B2R_ERR_ARG, "an instance has too many work units or rounds for the batch queue");
         dev[j] = in;
         maps[2 * j] = b->maps[2 * b->sched[j]];
         maps[2 * j + 1] = b->maps[2 * b->sched[j] + 1];
         b->maxrounds = std::max(b->maxrounds, in.rounds);
     }
-    const int R = b->maxrounds;
-    std::vector<long long> step_off(R + 1, 0);
-    std::vector<int> active(R + 1, 0);
-    for (int t = 0; t < R; ++t) {
-        int A = 0;
-        while (A < b->n && dev[A].rounds > t) ++A;
-        active[t] = A;
-        step_off[t + 1] = step_off[t] + prefix[A];
+    long long total = 0;
+    for (const InstDev& in : dev) total += (long long)in.units * in.rounds;
+    if (total > (1ll << 28))
+        return bfail(B2R_ERR_ARG, "the batch queue would hold more than 2^28 work items: split the batch");
+    // no run of this batch may still read the queue or the descriptors
+    BCK(cudaDeviceSynchronize(), "waiting for the batch's runs");
+    std::vector<unsigned long long> items;
+    items.reserve((size_t)total);
+    for (int t = 0; t < b->maxrounds; ++t)
+        for (int j = 0; j < b->n && dev[j].rounds > t; ++j)
+            for (int u = 0; u < dev[j].units; ++u) items.push_back(pack_item(t, j, u));
+    b->total = (long long)items.size();
+    if (b->total > b->items_cap) {
+        cudaFree(b->d_items);
+        b->d_items = nullptr;
+        b->items_cap = 0;
+        BCK(cudaMalloc(&b->d_items, sizeof(unsigned long long) * std::max<long long>(1, b->total)), "queue allocation");
+        b->items_cap = b->total;
     }
-    b->total = step_off[R];
     BCK(cudaMemcpy(b->d_inst, dev.data(), sizeof(InstDev) * b->n, cudaMemcpyHostToDevice), "copy descriptors");
     BCK(cudaMemcpy(b->d_maps, maps.data(), sizeof(CUtensorMap) * 2 * b->n, cudaMemcpyHostToDevice),
         "copy tensor maps");
-    BCK(cudaMemcpy(b->d_step_off, step_off.data(), sizeof(long long) * (R + 1), cudaMemcpyHostToDevice), "copy step table");
-    BCK(cudaMemcpy(b->d_active, active.data(), sizeof(int) * (R + 1), cudaMemcpyHostToDevice), "copy active table");
-    BCK(cudaMemcpy(b->d_prefix, prefix.data(), sizeof(long long) * (b->n + 1), cudaMemcpyHostToDevice), "copy prefix table");
+    if (b->total > 0)
+        BCK(cudaMemcpy(b->d_items, items.data(), sizeof(unsigned long long) * b->total, cudaMemcpyHostToDevice),
+            "copy the queue");
     if (b->gexec) {
         cudaGraphExecDestroy(b->gexec);
         b->gexec = nullptr;
@@ -407,14 +415,10 @@ b2r_status enqueue_run(b2r_batch* b, cudaStream_t st)
     BatchArgs a;
     a.inst = b->d_inst;
     a.maps = b->d_maps;
-    a.step_off = b->d_step_off;
-    a.active = b->d_active;
-    a.unit_prefix = b->d_prefix;
+    a.items = b->d_items;
     a.head = b->d_head;
     a.done = b->d_done;
     a.status = b->d_status;
-    a.maxsteps = b->maxrounds;
-    a.ninst = b->n;
     a.total = b->total;
     if (b->two) batch_kernel<true><<<b->grid[1], kThreads, b->smem, st>>>(a);
     else batch_kernel<false><<<b->grid[0], kThreads, b->smem, st>>>(a);
@@ -484,22 +488,16 @@ b2r_status b2r_batch_create(const b2r_batch_item* items, int n, b2r_batch** out)
                 return bail(bfail(B2R_ERR_OOM, "instance allocation failed"));
             cudaMemset(in.buf[s], 0, fb);
         }
-        b->maxsteps = std::max(b->maxsteps, it.nsteps);
     }
     if (cudaMalloc(&b->d_inst, sizeof(InstDev) * n) != cudaSuccess ||
         cudaMalloc(&b->d_maps, sizeof(CUtensorMap) * 2 * n) != cudaSuccess ||
-        cudaMalloc(&b->d_step_off, sizeof(long long) * (b->maxsteps + 1)) != cudaSuccess ||
-        cudaMalloc(&b->d_active, sizeof(int) * (b->maxsteps + 1)) != cudaSuccess ||
-        cudaMalloc(&b->d_prefix, sizeof(long long) * (n + 1)) != cudaSuccess ||
         cudaMalloc(&b->d_head, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&b->d_done, sizeof(unsigned) * n) != cudaSuccess ||
         cudaMalloc(&b->d_status, sizeof(int)) != cudaSuccess)
         return bail(bfail(B2R_ERR_OOM, "batch table allocation failed"));
     cudaMemset(b->d_status, 0, sizeof(int));
     // persistent grid: every resident slot
-    b->smem = kSmem + sizeof(long long) * (b->maxsteps + 1 + n + 1) + sizeof(int) * (b->maxsteps + 1) + 16 +
-              kSmemS1;
-    if (b->smem > 200 * 1024) return bail(bfail(B2R_ERR_ARG, "too many time steps for the batch schedule"));
+    b->smem = kSmem + 16 + kSmemS1;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -533,9 +531,7 @@ b2r_status b2r_batch_destroy(b2r_batch* b)
             if (in.buf[s]) cudaFree(in.buf[s]);
     cudaFree(b->d_inst);
     cudaFree(b->d_maps);
-    cudaFree(b->d_step_off);
-    cudaFree(b->d_active);
-    cudaFree(b->d_prefix);
+    cudaFree(b->d_items);
     cudaFree(b->d_head);
     cudaFree(b->d_done);
     cudaFree(b->d_status);
@@ -632,6 +628,8 @@ b2r_status b2r_batch_set_zchunk(b2r_batch* b, int zchunk)
     b->lz_policy = zchunk;
     return build_schedule(b);
 }
+
+
 
 b2r_status b2r_batch_autotune(b2r_batch* b, void* stream, int* best_zchunk, double* best_ms)
 {

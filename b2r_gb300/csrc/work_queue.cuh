@@ -25,7 +25,8 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
 
 // Item -> (round, instance, unit) by binary searches in the schedule tables
 // (step_off: items before round t; active: instances still active at round
-// t; prefix: units of instances [0, k)).
+// t; prefix: units of instances [0, k)) -- the elastic-wave batch; the heat
+// batch reads its items from an array the host writes in claim order.
 __device__ __forceinline__ void decode(long long item, const long long* step_off, const int* active,
                                        const long long* prefix, int maxrounds, int& t, int& k, int& u)
 {
