@@ -157,3 +157,27 @@ def test_batch_tiny_and_thin_instances(b2r, steps):
             d.step(it["nsteps"])
             want = d.download()
         assert np.array_equal(got, want), it
+
+
+def test_batch_long_instance_beside_short_ones(b2r):
+    """An instance of 30000 steps (a queue of 30000 rounds, once refused for
+    the size of its schedule tables) beside short instances of every
+    radius: each equals its own plain run."""
+    import torch
+    items = [dict(env=(16, 16, 16), D=1, nsteps=30000, alpha_dt=0.02, dx=1.0, dy=1.0, dz=1.0)]
+    items += [dict(env=(24 + 8 * D, 20, 18), D=D, nsteps=3 + D, alpha_dt=0.02, dx=1.0, dy=1.0, dz=1.0)
+              for D in (1, 2, 3, 4)]
+    ins = inputs(items, 9)
+    s = torch.cuda.Stream()
+    with b2r.Batch(items, stream=s) as bt:
+        assert bt.lups == sum(int(np.prod(it["env"])) * it["nsteps"] for it in items)
+        for i, a in enumerate(ins):
+            bt.upload(i, a)
+        bt.run()
+        bt.synchronize()
+        got = [bt.download(i) for i in range(len(items))]
+    for i, it in enumerate(items):
+        with b2r.Domain(b2r.MODEL_HEAT, it["env"], D=it["D"], alpha_dt=0.02) as d:
+            d.upload(ins[i])
+            d.step(it["nsteps"])
+            assert np.array_equal(got[i], d.download()), i
