@@ -76,15 +76,6 @@ struct InstDev {
     int rounds;                          // rounds of units: nsteps / tb, rounded up
 };
 
-// A work item packed into 64 bits: round t (bits 40..63), instance k in
-// the sorted order (bits 24..39), unit u (bits 0..23).
-constexpr int kItemKBits = 16, kItemUBits = 24;
-__host__ __device__ inline unsigned long long pack_item(int t, int k, int u)
-{
-    return ((unsigned long long)t << (kItemKBits + kItemUBits)) | ((unsigned long long)k << kItemUBits) |
-           (unsigned long long)u;
-}
-
 struct BatchArgs {
     const InstDev* inst;                 // sorted by rounds, descending
     const CUtensorMap* maps;             // 2 per instance: buffer 0, buffer 1
@@ -171,10 +162,8 @@ __global__ void __launch_bounds__(kThreads, B2R_BATCH_MINB) batch_kernel(const B
             const long long item = s_next;
             s_cur = item;
             if (item < a.total) {
-            const unsigned long long x = a.items[item];
-            const int t = (int)(x >> (kItemKBits + kItemUBits));
-            const int k = (int)((x >> kItemUBits) & ((1u << kItemKBits) - 1));
-            const int u = (int)(x & ((1u << kItemUBits) - 1));
+            int t, k, u;
+            wq::unpack_item(a.items[item], t, k, u);
             int ok = 1;
             // wait for round t-1 of this instance (bounded)
             if (t > 0) ok = wq::wait_done(&a.done[k], (unsigned)t * (unsigned)a.inst[k].units) ? 1 : 0;
@@ -369,24 +358,22 @@ b2r_status build_schedule(b2r_batch* b)
         in.Lz = std::min(in.NZ, b->lz_policy > 0 ? b->lz_policy : in.NZ);
         in.nzc = (in.NZ + in.Lz - 1) / in.Lz;
         in.units = in.ntx * in.nty * in.nzc;
-        if (in.units >= (1 << kItemUBits) || in.rounds >= (1 << (64 - kItemKBits - kItemUBits)))
-            return bfail(B2R_ERR_ARG, "an instance has too many work units or rounds for the batch queue");
         dev[j] = in;
         maps[2 * j] = b->maps[2 * b->sched[j]];
         maps[2 * j + 1] = b->maps[2 * b->sched[j] + 1];
         b->maxrounds = std::max(b->maxrounds, in.rounds);
     }
-    long long total = 0;
-    for (const InstDev& in : dev) total += (long long)in.units * in.rounds;
-    if (total > (1ll << 28))
-        return bfail(B2R_ERR_ARG, "the batch queue would hold more than 2^28 work items: split the batch");
     // no run of this batch may still read the queue or the descriptors
     BCK(cudaDeviceSynchronize(), "waiting for the batch's runs");
+    std::vector<int> rounds(b->n), units(b->n);
+    for (int j = 0; j < b->n; ++j) {
+        rounds[j] = dev[j].rounds;
+        units[j] = dev[j].units;
+    }
     std::vector<unsigned long long> items;
-    items.reserve((size_t)total);
-    for (int t = 0; t < b->maxrounds; ++t)
-        for (int j = 0; j < b->n && dev[j].rounds > t; ++j)
-            for (int u = 0; u < dev[j].units; ++u) items.push_back(pack_item(t, j, u));
+    if (!wq::round_major_items(rounds.data(), units.data(), b->n, items))
+        return bfail(B2R_ERR_ARG, "the batch queue is too long (an instance with more than 2^24 units or "
+                                  "rounds, or more than 2^28 work items): split the batch");
     b->total = (long long)items.size();
     if (b->total > b->items_cap) {
         cudaFree(b->d_items);

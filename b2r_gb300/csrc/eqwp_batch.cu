@@ -41,13 +41,10 @@ struct EInst {
 
 struct EArgs {
     const EInst* inst;                   // sorted by rounds, descending
-    const long long* step_off;           // items before round t (maxrounds + 1)
-    const int* active;                   // instances still active at round t
-    const long long* unit_prefix;        // units of instances [0, k) (ninst + 1)
+    const unsigned long long* items;     // the queue: work items in claim order
     unsigned long long* head;
     unsigned* done;
     int* status;
-    int maxrounds, ninst;
     long long total;
 };
 
@@ -55,15 +52,6 @@ constexpr int kEThreads = kBX * kBY;   // 256
 
 __global__ void __launch_bounds__(kEThreads, B2R_EQWP_MINB) eqwp_batch_kernel(const EArgs a)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    long long* s_step_off = reinterpret_cast<long long*>(smem_raw);
-    long long* s_prefix = s_step_off + (a.maxrounds + 1);
-    int* s_active = reinterpret_cast<int*>(s_prefix + (a.ninst + 1));
-    for (int i = threadIdx.x; i <= a.maxrounds; i += blockDim.x) {
-        s_step_off[i] = a.step_off[i];
-        s_active[i] = a.active[i];
-    }
-    for (int i = threadIdx.x; i <= a.ninst; i += blockDim.x) s_prefix[i] = a.unit_prefix[i];
     __shared__ long long s_next, s_cur;
     __shared__ int s_t, s_k, s_u, s_ok;
     if (threadIdx.x == 0) s_next = (long long)atomicAdd(a.head, 1ull);
@@ -74,7 +62,7 @@ __global__ void __launch_bounds__(kEThreads, B2R_EQWP_MINB) eqwp_batch_kernel(co
             s_cur = item;
             if (item < a.total) {
                 int t, k, u;
-                wq::decode(item, s_step_off, s_active, s_prefix, a.maxrounds, t, k, u);
+                wq::unpack_item(a.items[item], t, k, u);
                 // wait for round t-1 of this instance (bounded)
                 s_ok = t == 0 || wq::wait_done(&a.done[k], (unsigned)t * (unsigned)a.inst[k].units);
                 s_t = t;
@@ -123,17 +111,14 @@ struct b2r_eqwp_batch {
     EInst* d_inst = nullptr;
     float* d_amp = nullptr;          // every instance's source increments, back to back
     std::vector<long long> amp_off;  // caller index -> offset in d_amp
-    long long* d_step_off = nullptr;
-    int* d_active = nullptr;
-    long long* d_prefix = nullptr;
+    unsigned long long* d_items = nullptr;   // the queue (capacity items_cap)
+    long long items_cap = 0;
     unsigned long long* d_head = nullptr;
     unsigned* d_done = nullptr;
     int* d_status = nullptr;
-    int maxrounds = 0;
     long long total = 0;
     int lz_policy = 32;              // z chunk cap per unit
     int grid = 0;
-    size_t smem = 0;
     cudaGraphExec_t gexec = nullptr;
     cudaStream_t gstream = nullptr;
     // stream order with the handles' own streams: the run waits for the work
@@ -186,29 +171,30 @@ b2r_status build(b2r_eqwp_batch* b)
     std::stable_sort(b->sched.begin(), b->sched.end(),
                      [&](int x, int y) { return b->host[x].rounds > b->host[y].rounds; });
     std::vector<EInst> dev(b->n);
-    std::vector<long long> prefix(b->n + 1, 0);
-    b->maxrounds = 0;
+    std::vector<int> rounds(b->n), units(b->n);
     for (int j = 0; j < b->n; ++j) {
         dev[j] = b->host[b->sched[j]];
-        prefix[j + 1] = prefix[j] + dev[j].units;
-        b->maxrounds = std::max(b->maxrounds, dev[j].rounds);
+        rounds[j] = dev[j].rounds;
+        units[j] = dev[j].units;
     }
-    const int R = b->maxrounds;
-    std::vector<long long> step_off(R + 1, 0);
-    std::vector<int> active(R + 1, 0);
-    for (int t = 0; t < R; ++t) {
-        int A = 0;
-        while (A < b->n && dev[A].rounds > t) ++A;
-        active[t] = A;
-        step_off[t + 1] = step_off[t] + prefix[A];
+    // no run of this batch may still read the queue or the descriptors
+    ECK(cudaDeviceSynchronize(), "waiting for the batch's runs");
+    std::vector<unsigned long long> items;
+    if (!wq::round_major_items(rounds.data(), units.data(), b->n, items))
+        return efail(B2R_ERR_ARG, "the batch queue is too long (an instance with more than 2^24 units or "
+                                  "rounds, or more than 2^28 work items): split the batch");
+    b->total = (long long)items.size();
+    if (b->total > b->items_cap) {
+        cudaFree(b->d_items);
+        b->d_items = nullptr;
+        b->items_cap = 0;
+        ECK(cudaMalloc(&b->d_items, sizeof(unsigned long long) * std::max<long long>(1, b->total)), "queue allocation");
+        b->items_cap = b->total;
     }
-    b->total = step_off[R];
     ECK(cudaMemcpy(b->d_inst, dev.data(), sizeof(EInst) * b->n, cudaMemcpyHostToDevice), "copy descriptors");
-    ECK(cudaMemcpy(b->d_step_off, step_off.data(), sizeof(long long) * (R + 1), cudaMemcpyHostToDevice),
-        "copy round table");
-    ECK(cudaMemcpy(b->d_active, active.data(), sizeof(int) * (R + 1), cudaMemcpyHostToDevice), "copy active table");
-    ECK(cudaMemcpy(b->d_prefix, prefix.data(), sizeof(long long) * (b->n + 1), cudaMemcpyHostToDevice),
-        "copy prefix table");
+    if (b->total > 0)
+        ECK(cudaMemcpy(b->d_items, items.data(), sizeof(unsigned long long) * b->total, cudaMemcpyHostToDevice),
+            "copy the queue");
     if (b->gexec) {
         cudaGraphExecDestroy(b->gexec);
         b->gexec = nullptr;
@@ -222,16 +208,12 @@ b2r_status enqueue(b2r_eqwp_batch* b, cudaStream_t st)
     ECK(cudaMemsetAsync(b->d_done, 0, sizeof(unsigned) * b->n, st), "reset counters");
     EArgs a;
     a.inst = b->d_inst;
-    a.step_off = b->d_step_off;
-    a.active = b->d_active;
-    a.unit_prefix = b->d_prefix;
+    a.items = b->d_items;
     a.head = b->d_head;
     a.done = b->d_done;
     a.status = b->d_status;
-    a.maxrounds = b->maxrounds;
-    a.ninst = b->n;
     a.total = b->total;
-    eqwp_batch_kernel<<<b->grid, kEThreads, b->smem, st>>>(a);
+    eqwp_batch_kernel<<<b->grid, kEThreads, 0, st>>>(a);
     ECK(cudaGetLastError(), "batch launch");
     return B2R_OK;
 }
@@ -268,7 +250,6 @@ b2r_status b2r_eqwp_batch_create(b2r_handle* const* hs, const int* nsteps, int n
     b->nsteps.assign(nsteps, nsteps + n);
     b->host.resize(n);
     b->amp_off.resize(n + 1, 0);
-    int maxsteps = 0;
     for (int k = 0; k < n; ++k) {
         const b2r_handle* h = hs[k];
         EInst& in = b->host[k];
@@ -282,14 +263,10 @@ b2r_status b2r_eqwp_batch_create(b2r_handle* const* hs, const int* nsteps, int n
         in.p.src_len = 0;
         in.nsteps = nsteps[k];
         b->amp_off[k + 1] = b->amp_off[k] + std::max(1, nsteps[k]);
-        maxsteps = std::max(maxsteps, nsteps[k]);
     }
     const long long namp = b->amp_off[n];
     if (cudaMalloc(&b->d_inst, sizeof(EInst) * n) != cudaSuccess ||
         cudaMalloc(&b->d_amp, sizeof(float) * namp) != cudaSuccess ||
-        cudaMalloc(&b->d_step_off, sizeof(long long) * (2 * maxsteps + 1)) != cudaSuccess ||
-        cudaMalloc(&b->d_active, sizeof(int) * (2 * maxsteps + 1)) != cudaSuccess ||
-        cudaMalloc(&b->d_prefix, sizeof(long long) * (n + 1)) != cudaSuccess ||
         cudaMalloc(&b->d_head, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&b->d_done, sizeof(unsigned) * n) != cudaSuccess ||
         cudaMalloc(&b->d_status, sizeof(int)) != cudaSuccess)
@@ -303,18 +280,10 @@ b2r_status b2r_eqwp_batch_create(b2r_handle* const* hs, const int* nsteps, int n
     if (cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming) != cudaSuccess)
         return bail(efail(B2R_ERR_CUDA, "event creation failed"));
     for (int k = 0; k < n; ++k) b->host[k].amp = b->d_amp + b->amp_off[k];
-    b->smem = sizeof(long long) * (2 * maxsteps + 1 + n + 1) + sizeof(int) * (2 * maxsteps + 1) + 16;
-    if (b->smem > 200 * 1024) return bail(efail(B2R_ERR_ARG, "too many time steps for the batch schedule"));
     int dev = 0, sms = 0, occ = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    {
-        // per function and device; only ever raised (see batch.cu)
-        static SmemLimit limit;
-        if (raise_smem_limit(limit, (const void*)eqwp_batch_kernel, b->smem) != cudaSuccess)
-            return bail(efail(B2R_ERR_CUDA, "smem attribute"));
-    }
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, eqwp_batch_kernel, kEThreads, b->smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, eqwp_batch_kernel, kEThreads, 0);
     b->grid = std::max(1, occ) * std::max(1, sms);
     b2r_status st = build(b);
     if (st != B2R_OK) return bail(st);
@@ -331,9 +300,7 @@ b2r_status b2r_eqwp_batch_destroy(b2r_eqwp_batch* b)
     if (b->ev_out) cudaEventDestroy(b->ev_out);
     cudaFree(b->d_inst);
     cudaFree(b->d_amp);
-    cudaFree(b->d_step_off);
-    cudaFree(b->d_active);
-    cudaFree(b->d_prefix);
+    cudaFree(b->d_items);
     cudaFree(b->d_head);
     cudaFree(b->d_done);
     cudaFree(b->d_status);

@@ -1,16 +1,18 @@
 // work_queue.cuh -- the device work queue of the batched persistent kernels
 // (batch.cu: heat instances; eqwp_batch.cu: elastic-wave instances).
 //
-// Work items (round t, instance k, unit u) are numbered round-major;
-// instances are sorted by round count (descending), so the instances still
-// active at round t are a prefix of the list.  A CTA claims the next item
-// with one atomicAdd on a head counter.  Before reading round t of instance
+// Work items (round t, instance k, unit u) are listed round-major by the
+// host; instances are sorted by round count (descending), so the instances
+// still active at round t are a prefix of the list.  A CTA claims the next
+// item with one atomicAdd on a head counter.  Before reading round t of instance
 // k it waits until done[k] >= t * units[k] (every unit of round t-1 of that
 // instance has finished), runs the unit and bumps done[k] with a release
 // reduction.  Items are claimed in increasing order and an item only waits
 // on smaller items, which are held by running CTAs, so the queue cannot
 // deadlock; every wait is bounded (2 s) and reports B2R_ERR_TIMEOUT.
 #pragma once
+#include <vector>
+
 #include "b2r_common.cuh"
 
 namespace b2r {
@@ -23,27 +25,44 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p)
     return v;
 }
 
-// Item -> (round, instance, unit) by binary searches in the schedule tables
-// (step_off: items before round t; active: instances still active at round
-// t; prefix: units of instances [0, k)) -- the elastic-wave batch; the heat
-// batch reads its items from an array the host writes in claim order.
-__device__ __forceinline__ void decode(long long item, const long long* step_off, const int* active,
-                                       const long long* prefix, int maxrounds, int& t, int& k, int& u)
+// A work item packed into 64 bits: round t (bits 40..63), instance k in the
+// queue's instance order (bits 24..39), unit u (bits 0..23).
+constexpr int kItemKBits = 16, kItemUBits = 24;
+__host__ __device__ inline unsigned long long pack_item(int t, int k, int u)
 {
-    int lo = 0, hi = maxrounds;                     // last t with step_off[t] <= item
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (step_off[mid] <= item) lo = mid; else hi = mid;
+    return ((unsigned long long)t << (kItemKBits + kItemUBits)) | ((unsigned long long)k << kItemUBits) |
+           (unsigned long long)u;
+}
+__device__ __forceinline__ void unpack_item(unsigned long long x, int& t, int& k, int& u)
+{
+    t = (int)(x >> (kItemKBits + kItemUBits));
+    k = (int)((x >> kItemUBits) & ((1u << kItemKBits) - 1));
+    u = (int)(x & ((1u << kItemUBits) - 1));
+}
+
+// The queue, written out by the host in claim order: round-major over
+// instances sorted by their round count (descending), so that those still
+// stepping at round t are a prefix; each instance's units in order.  Returns
+// false if an instance has more units or rounds than an item can name, or
+// the queue would hold more than 2^28 items.
+inline bool round_major_items(const int* rounds, const int* units, int n, std::vector<unsigned long long>& items)
+{
+    long long total = 0;
+    int maxr = 0;
+    for (int j = 0; j < n; ++j) {
+        if (n >= (1 << kItemKBits) || units[j] >= (1 << kItemUBits) ||
+            rounds[j] >= (1 << (64 - kItemKBits - kItemUBits)))
+            return false;
+        total += (long long)units[j] * rounds[j];
+        maxr = rounds[j] > maxr ? rounds[j] : maxr;
     }
-    t = lo;
-    const long long r = item - step_off[t];
-    int kl = 0, kh = active[t];                     // last k with prefix[k] <= r
-    while (kh - kl > 1) {
-        const int mid = (kl + kh) >> 1;
-        if (prefix[mid] <= r) kl = mid; else kh = mid;
-    }
-    k = kl;
-    u = (int)(r - prefix[k]);
+    if (total > (1ll << 28)) return false;
+    items.clear();
+    items.reserve((size_t)total);
+    for (int t = 0; t < maxr; ++t)
+        for (int j = 0; j < n && rounds[j] > t; ++j)
+            for (int u = 0; u < units[j]; ++u) items.push_back(pack_item(t, j, u));
+    return true;
 }
 
 // Bounded wait (2 s) until *done >= need; false if it gave up.  Afterwards

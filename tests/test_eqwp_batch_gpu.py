@@ -83,3 +83,26 @@ def test_eqwp_batch_rejects_bad_instances(b2r):
             with pytest.raises(b2r.B2RError):
                 b2r.EqwpBatch(bad, ns)
     d.close()
+
+
+def test_eqwp_batch_long_instance(b2r):
+    """An instance of 9000 steps (18000 rounds of the queue, once refused
+    for the size of its schedule tables) beside a short one: both equal the
+    same handles stepped alone."""
+    import torch
+    items = [dict(env=(16, 16, 16), nsteps=9000, seed=31, src=(8, 8, 8)),
+             dict(env=(24, 16, 20), nsteps=5, seed=32, src=(12, 8, 10))]
+    s = torch.cuda.Stream()
+    doms = [make(b2r, it, stream=s) for it in items]
+    refs = [make(b2r, it) for it in items]
+    try:
+        with b2r.EqwpBatch(doms, [it["nsteps"] for it in items], stream=s) as bt:
+            bt.run(graph=False)
+            bt.synchronize()
+        for d, r, it in zip(doms, refs, items):
+            r.step(it["nsteps"])
+            for k in range(9):
+                assert np.array_equal(d.download(field=k), r.download(field=k)), (it["env"], k)
+    finally:
+        for d in doms + refs:
+            d.close()
