@@ -314,11 +314,23 @@ b2r_status substep(b2r_handle* h, int i, bool xnext)
             // the last sub-step of a period: the stress tiles that hold the
             // cells the next exchange reads, then that exchange on the stream
             // xs while the other tiles finish (they read no halo cell)
-            if (!h->xs) {
+            if (!h->xs) {   // the stream and its two events, kept only all together
                 int lo = 0, hi = 0;
-                CK(h, cudaDeviceGetStreamPriorityRange(&lo, &hi));
-                CK(h, cudaStreamCreateWithPriority(&h->xs, cudaStreamNonBlocking, hi));
-                for (int k = 0; k < 2; ++k) CK(h, cudaEventCreateWithFlags(&h->xev[k], cudaEventDisableTiming));
+                cudaStream_t xs = nullptr;
+                cudaEvent_t ev[2] = {};
+                cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo, &hi);
+                if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&xs, cudaStreamNonBlocking, hi);
+                for (int k = 0; k < 2 && e == cudaSuccess; ++k)
+                    e = cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming);
+                if (e != cudaSuccess) {
+                    for (cudaEvent_t x : ev)
+                        if (x) cudaEventDestroy(x);
+                    if (xs) cudaStreamDestroy(xs);
+                    return fail(h, B2R_ERR_CUDA, "exchange stream: %s", cudaGetErrorString(e));
+                }
+                h->xs = xs;
+                h->xev[0] = ev[0];
+                h->xev[1] = ev[1];
             }
             CK(h, launch_eqwp_stag_velocity(h->fld, h->mat, h->L, i, p, h->stream));
             CK(h, launch_eqwp_stag_stress(h->fld, h->mat, h->L, i, (int)h->ts, p, 1, h->stream));
