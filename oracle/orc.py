@@ -119,6 +119,21 @@ def heat_run(field, D, H, nsteps, alpha_dt, dx, dy, dz, nthreads=0):
     return field
 
 
+def heat_run_periodic(field, nsteps, alpha_dt, dx=1.0, dy=1.0, dz=1.0):
+    """nsteps radius-1 steps on a torus (every axis wraps), in float64: the
+    update of heat-3D.cpp:57-60, u' = u + alpha_dt * (Lx/dx^2 + Ly/dy^2 +
+    Lz/dz^2) with L = u[-1] - 2u + u[+1], its neighbour index wrapped (the
+    reference defines no periodic heat; the wrap is this build's boundary
+    option).  Returns a new float64 array."""
+    u = field.astype(np.float64)
+    for _ in range(nsteps):
+        lap = np.zeros_like(u)
+        for ax, h in ((2, dx), (1, dy), (0, dz)):
+            lap += (np.roll(u, 1, axis=ax) - 2.0 * u + np.roll(u, -1, axis=ax)) / (h * h)
+        u = u + alpha_dt * lap
+    return u
+
+
 def heat_cpu_main(block, R, D, alpha_dt, dx, dy, dz, nthreads=0):
     nz, ny, nx = block.shape
     return lib().orc_heat_cpu_main(_ptr(block, _fp), R, D, nx, ny, nz, alpha_dt, dx, dy,
