@@ -188,6 +188,50 @@ def eqwp_stag_step(fields, mat, dt, dx, i, H, edge, src_xyz, src):
     fn(fa, ma, nx, ny, nz, dt, dx, i, H, edge, src_xyz[0], src_xyz[1], src_xyz[2], src)
 
 
+def eqwp_stag_run_periodic(fields, mat, dt, dx, amps, src_xyz):
+    """len(amps) steps of the staggered FD4 scheme on a torus, in float64:
+    the step of orc_eqwp_stag_step (b2r_oracle.c, no reference counterpart)
+    with every neighbour index wrapped -- velocities from the stress
+    divergence, then stresses from the new velocities, the source amplitude
+    of the step added to sxx, syy and szz at src_xyz (x, y, z).  fields: vx,
+    vy, vz, sxx, sxy, sxz, syy, syz, szz; mat: lambda, mu, buoyancy; arrays
+    (nz, ny, nx).  Returns new float64 arrays."""
+    c1, c2 = 9.0 / 8.0, -1.0 / 24.0
+    f = [np.asarray(a, np.float64).copy() for a in fields]
+    lam, mu, b = (np.asarray(a, np.float64) for a in mat)
+    ax_of = {"x": 2, "y": 1, "z": 0}
+
+    def sh(a, d, ax):          # a[i + d] along the axis
+        return np.roll(a, -d, axis=ax_of[ax])
+
+    def dp(a, ax):             # forward difference at i + 1/2
+        return c1 * (sh(a, 1, ax) - a) + c2 * (sh(a, 2, ax) - sh(a, -1, ax))
+
+    def dm(a, ax):             # backward difference at i - 1/2
+        return c1 * (a - sh(a, -1, ax)) + c2 * (sh(a, 1, ax) - sh(a, -2, ax))
+
+    vx, vy, vz, sxx, sxy, sxz, syy, syz, szz = range(9)
+    x, y, z = src_xyz
+    for amp in amps:
+        a_x = dp(f[sxx], "x") + dm(f[sxy], "y") + dm(f[sxz], "z")
+        a_y = dm(f[sxy], "x") + dp(f[syy], "y") + dm(f[syz], "z")
+        a_z = dm(f[sxz], "x") + dm(f[syz], "y") + dp(f[szz], "z")
+        f[vx] = f[vx] + dt * b * (a_x / dx)
+        f[vy] = f[vy] + dt * b * (a_y / dx)
+        f[vz] = f[vz] + dt * b * (a_z / dx)
+        exx, eyy, ezz = dm(f[vx], "x") / dx, dm(f[vy], "y") / dx, dm(f[vz], "z") / dx
+        l2m = lam + 2 * mu
+        f[sxx] = f[sxx] + dt * (l2m * exx + lam * (eyy + ezz))
+        f[syy] = f[syy] + dt * (l2m * eyy + lam * (exx + ezz))
+        f[szz] = f[szz] + dt * (l2m * ezz + lam * (exx + eyy))
+        f[sxy] = f[sxy] + dt * mu * ((dp(f[vx], "y") + dp(f[vy], "x")) / dx)
+        f[sxz] = f[sxz] + dt * mu * ((dp(f[vx], "z") + dp(f[vz], "x")) / dx)
+        f[syz] = f[syz] + dt * mu * ((dp(f[vy], "z") + dp(f[vz], "y")) / dx)
+        for k in (sxx, syy, szz):
+            f[k][z, y, x] += amp
+    return f
+
+
 # ---------------------------------------------------------------- B2R blocks
 def edge_mask(b, nb, periodic=False):
     """Edge bit mask of block index b=(bx,by,bz) in a grid nb=(Bx,By,Bz)."""

@@ -225,3 +225,27 @@ def test_periodic_heat_oracle_against_explicit_loop(orc):
         u = n
     assert np.abs(got - u).max() < 1e-13
     assert abs(got.sum() - a.astype(np.float64).sum()) < 1e-9
+
+
+def test_periodic_staggered_oracle_against_c_oracle_inside(orc):
+    """The torus restatement of the staggered step (numpy, float64) against
+    the C oracle (fixed shell) on the cells the wrap cannot reach yet: a
+    disturbance confined to the middle, 3 steps (4 cells of reach per step)."""
+    env = (40, 36, 44)
+    rng = np.random.default_rng(3)
+    shape = env[::-1]
+    f = [np.zeros(shape) for _ in range(9)]
+    for k in range(9):
+        f[k][16:28, 14:22, 16:24] = rng.standard_normal((12, 8, 8)) * 1e-3
+    mat = [np.full(shape, 4.0e9), np.full(shape, 3.0e9), np.full(shape, 1.0 / 2300.0)]
+    mat[0][: shape[0] // 2] *= 1.2
+    dt, h = 1e-4, 10.0
+    amps = [0.5, -0.25, 0.125]
+    got = orc.eqwp_stag_run_periodic(f, mat, dt, h, amps, (20, 18, 22))
+    ref = [a.copy() for a in f]
+    for t, amp in enumerate(amps):
+        orc.eqwp_stag_step(ref, mat, dt, h, 0, 2, 63, (20, 18, 22), amp)
+    for k in range(9):
+        inner = (slice(4, -4), slice(4, -4), slice(4, -4))
+        assert np.allclose(got[k][inner], ref[k][inner], rtol=1e-12, atol=1e-18), k
+        assert np.abs(got[k]).max() > 0
