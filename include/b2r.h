@@ -106,7 +106,10 @@ int64_t b2r_cells(const b2r_handle* h);
  * it cannot be detected here. */
 /* Load a domain array into every block (interiors, halos and shell).
  * src_is_device: 0 = host memory (pinned recommended), 1 = device memory.
- * Resets the time-step counter to 0. */
+ * Resets the time-step counter to 0.  The next b2r_step starts without a
+ * halo exchange when every field's halos are current: they were before the
+ * upload, or every field (not the material) has been uploaded since the
+ * last step. */
 b2r_status b2r_upload(b2r_handle* h, int field, const void* src, int src_is_device);
 /* Gather the block interiors (and the shell) into a domain array. */
 b2r_status b2r_download(b2r_handle* h, int field, void* dst, int dst_is_device);
