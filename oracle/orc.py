@@ -119,17 +119,30 @@ def heat_run(field, D, H, nsteps, alpha_dt, dx, dy, dz, nthreads=0):
     return field
 
 
-def heat_run_periodic(field, nsteps, alpha_dt, dx=1.0, dy=1.0, dz=1.0):
-    """nsteps radius-1 steps on a torus (every axis wraps), in float64: the
-    update of heat-3D.cpp:57-60, u' = u + alpha_dt * (Lx/dx^2 + Ly/dy^2 +
-    Lz/dz^2) with L = u[-1] - 2u + u[+1], its neighbour index wrapped (the
+# central second-difference weights of order 2D (heat-3D.cu:15-28): centre,
+# then distance 1, 2, ...
+_LAP_W = {1: (-2.0, 1.0),
+          2: (-5.0 / 2.0, 4.0 / 3.0, -1.0 / 12.0),
+          3: (-49.0 / 18.0, 3.0 / 2.0, -3.0 / 20.0, 1.0 / 90.0),
+          4: (-205.0 / 72.0, 8.0 / 5.0, -1.0 / 5.0, 8.0 / 315.0, -1.0 / 560.0)}
+
+
+def heat_run_periodic(field, nsteps, alpha_dt, dx=1.0, dy=1.0, dz=1.0, D=1):
+    """nsteps steps of radius D on a torus (every axis wraps), in float64:
+    the update of heat-3D.cpp:57-60 / heat-3D.cu:228-231, u' = u + alpha_dt *
+    (Lx/dx^2 + Ly/dy^2 + Lz/dz^2), L the order-2D central second difference
+    (the weights of heat-3D.cu:15-28), its neighbour index wrapped (the
     reference defines no periodic heat; the wrap is this build's boundary
     option).  Returns a new float64 array."""
+    w = _LAP_W[D]
     u = field.astype(np.float64)
     for _ in range(nsteps):
         lap = np.zeros_like(u)
         for ax, h in ((2, dx), (1, dy), (0, dz)):
-            lap += (np.roll(u, 1, axis=ax) - 2.0 * u + np.roll(u, -1, axis=ax)) / (h * h)
+            a = w[0] * u
+            for k in range(1, D + 1):
+                a = a + w[k] * (np.roll(u, k, axis=ax) + np.roll(u, -k, axis=ax))
+            lap += a / (h * h)
         u = u + alpha_dt * lap
     return u
 

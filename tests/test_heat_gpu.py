@@ -225,3 +225,20 @@ def test_heat_thin_domains(b2r, orc, env, D):
     orc.heat_run(ref, D, D, 7, 0.05, 1.0, 1.0, 1.0)
     r = float(np.linalg.norm(got.astype(np.float64) - ref) / np.linalg.norm(ref))
     assert r <= 1e-5
+
+
+@pytest.mark.parametrize("D", [1, 2, 3, 4])
+def test_heat_periodic_matches_torus_oracle(b2r, orc, D):
+    """Radius 1-4 on a torus split into 2 x 1 x 2 blocks (deep halo R = 2,
+    exchanged across the wrap) against the float64 torus restatement."""
+    env = (48, 40, 56)
+    rng = np.random.default_rng(30 + D)
+    dom = rng.random(env[::-1], dtype=np.float32)
+    with b2r.Domain(b2r.MODEL_HEAT, env, blocks=(2, 1, 2), R=2, D=D, boundary=b2r.BC_PERIODIC,
+                    alpha_dt=0.02, dx=1.0, dy=1.5, dz=0.75) as d:
+        assert d.domain_shape == env[::-1]
+        d.upload(dom)
+        d.step(9)
+        got = d.download()
+    ref = orc.heat_run_periodic(dom, 9, 0.02, 1.0, 1.5, 0.75, D=D)
+    assert rel_l2(got, ref) <= TOL

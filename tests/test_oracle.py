@@ -249,3 +249,19 @@ def test_periodic_staggered_oracle_against_c_oracle_inside(orc):
         inner = (slice(4, -4), slice(4, -4), slice(4, -4))
         assert np.allclose(got[k][inner], ref[k][inner], rtol=1e-12, atol=1e-18), k
         assert np.abs(got[k]).max() > 0
+
+
+@pytest.mark.parametrize("D", [2, 3, 4])
+def test_periodic_heat_oracle_inside_matches_c_oracle(orc, D):
+    """Radius 2-4 on the torus (numpy, float64) against the C oracle's
+    fixed-shell float64 steps on the cells the wrap cannot reach: a
+    disturbance confined to the middle, 2 steps."""
+    n = 40
+    rng = np.random.default_rng(D)
+    a = np.zeros((n, n, n))
+    a[14:26, 14:26, 14:26] = rng.random((12, 12, 12))
+    got = orc.heat_run_periodic(a, 2, 0.02, 1.0, 1.5, 0.75, D=D)
+    ref = a.copy()
+    orc.heat_run(ref, D, D, 2, 0.02, 1.0, 1.5, 0.75)
+    inner = (slice(3 * D, -3 * D),) * 3
+    assert np.allclose(got[inner], ref[inner], rtol=1e-12, atol=1e-15)
