@@ -72,8 +72,10 @@ def test_batch_matches_plain_runs(b2r, orc, graph, tile, steps):
             plain = d.download()
         assert np.array_equal(got[i], plain), i
         assert np.array_equal(again[i], plain), i
-    # and the oracle agrees within the FP32 tolerance on a couple of them
-    for i in (0, 5):
+    # and the oracle agrees within the FP32 tolerance: on every instance (each
+    # radius and size) with each instance's own tile shape, one step or two
+    # per unit; on two of them otherwise
+    for i in (range(len(items)) if not graph and not tile else (0, 5)):
         ref = ins[i].copy()
         it = items[i]
         orc.heat_run(ref, it["D"], it["D"], it["nsteps"], 0.02, 1.0, 1.0, 1.0)
