@@ -183,3 +183,12 @@ def test_batch_long_instance_beside_short_ones(b2r):
             d.upload(ins[i])
             d.step(it["nsteps"])
             assert np.array_equal(got[i], d.download()), i
+
+
+def test_batch_refuses_a_queue_it_cannot_name(b2r):
+    """An instance of more than 2^24 rounds cannot be named by a queue item:
+    creation is refused (before any queue is allocated) with B2R_ERR_ARG."""
+    items = [dict(env=(16, 16, 16), D=1, nsteps=20_000_000, alpha_dt=0.02, dx=1.0, dy=1.0, dz=1.0)]
+    with pytest.raises(b2r.B2RError) as ei:
+        b2r.Batch(items)
+    assert "split the batch" in str(ei.value)

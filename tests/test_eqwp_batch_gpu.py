@@ -79,7 +79,8 @@ def test_eqwp_batch_rejects_bad_instances(b2r):
     d = make(b2r, it)
     with b2r.Domain(b2r.MODEL_HEAT, (16, 16, 16)) as heat, \
          b2r.Domain(b2r.MODEL_EQWP_STAG, (32, 16, 16), blocks=(2, 1, 1), D=2, R=1, dt=DT, h=H) as two:
-        for bad, ns in (([heat], [2]), ([two], [2]), ([d, d], [1, 1]), ([d], [-1])):
+        for bad, ns in (([heat], [2]), ([two], [2]), ([d, d], [1, 1]), ([d], [-1]),
+                        ([d], [9_000_000])):          # 18 M rounds: more than a queue item names
             with pytest.raises(b2r.B2RError):
                 b2r.EqwpBatch(bad, ns)
     d.close()
