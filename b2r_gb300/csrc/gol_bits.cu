@@ -206,11 +206,8 @@ constexpr int kBMaxGen = 4;
 #ifndef B2R_GOLP_ROWS
 #define B2R_GOLP_ROWS 32     // output rows per band at most
 #endif
-#ifndef B2R_GOLP_CTAS
-#define B2R_GOLP_CTAS 8      // CTAs per SM the grid aims at
-#endif
-#ifndef B2R_GOLP_ZMIN
-#define B2R_GOLP_ZMIN 2      // z chunk of at least this many planes per generation
+#ifndef B2R_GOLP_MINPER
+#define B2R_GOLP_MINPER 3    // CTAs per SM on average the period kernel's grid keeps at least
 #endif
 
 struct GolBitsPeriod {
@@ -520,12 +517,8 @@ cudaError_t launch_gol_bits_period(const uint8_t* in, uint8_t* out, const BlockL
     G.y0 = lo[1];
     const long long tiles = (long long)ntx * nty2 * L.nblk;
     const int nz = hi[2] - lo[2] + 1;
-    int nzc = (int)std::max(1LL, (152LL * B2R_GOLP_CTAS + tiles - 1) / tiles);
-    nzc = std::min(nzc, std::max(1, nz / (B2R_GOLP_ZMIN * ng)));
-    G.nzc = nzc;
     const size_t smem = (size_t)ng * 4 * GW * (G.PR + 2) * sizeof(uint32_t);
     const int threads = (GW * (G.PR / 4) + 31) / 32 * 32;   // whole warps: every lane takes part in the shuffles
-    const dim3 grid(ntx, nty2, L.nblk * nzc);
     // raised only, per device, under a lock: handles on other host threads share the limit
     static SmemLimit attr[3];
     const int gi = GW == 8 ? 0 : (GW == 16 ? 1 : 2);
@@ -533,6 +526,37 @@ cudaError_t launch_gol_bits_period(const uint8_t* in, uint8_t* out, const BlockL
                      : GW == 16 ? (const void*)gol_bits_period_kernel<16>
                                 : (const void*)gol_bits_period_kernel<32>;
     if (cudaError_t e = raise_smem_limit(attr[gi], kern, std::max<size_t>(smem, 48 * 1024))) return e;
+    // z chunks per block: the CTAs are dealt over the SMs, the busiest SM
+    // holding ceil(CTAs / SMs) of them, each computing its chunk plus about
+    // ng - 1 planes of z skirt per generation; the count that makes the
+    // busiest SM's planes fewest, with every CTA resident at once and, where
+    // the block allows, at least B2R_GOLP_MINPER CTAs per SM on average (the
+    // kernel needs several to hide its latencies).  Measured on the 256^3
+    // torus in 2 x 2 x 2 blocks: 987 GLUPS at the count this picks (19),
+    // against 928 for 16 and 764-911 for the counts around them.
+    int dev = 0, sms = 0, cap = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cap, kern, threads, smem);
+    sms = std::max(1, sms);
+    cap = std::max(1, cap);
+    int nzc = 1;
+    long long best = -1;
+    bool best_full = false;
+    for (int c = 1; c <= nz; ++c) {
+        const long long ctas = tiles * c;
+        if (c > 1 && ctas > (long long)sms * cap) break;
+        const bool full = ctas >= (long long)B2R_GOLP_MINPER * sms;
+        const long long busiest = (ctas + sms - 1) / sms;
+        const long long cost = busiest * ((nz + c - 1) / c + ng - 1);
+        if (best < 0 || (full && !best_full) || (full == best_full && cost < best)) {
+            best = cost;
+            best_full = full;
+            nzc = c;
+        }
+    }
+    G.nzc = nzc;
+    const dim3 grid(ntx, nty2, L.nblk * nzc);
     switch (GW) {
     case 8: gol_bits_period_kernel<8><<<grid, threads, smem, st>>>(in, out, L, G); break;
     case 16: gol_bits_period_kernel<16><<<grid, threads, smem, st>>>(in, out, L, G); break;
