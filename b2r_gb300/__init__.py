@@ -270,10 +270,10 @@ class Domain:
 
     def set_tuning(self, zchunk=None, ctas_per_sm=None, pdl=None, tblock=None, zchunk2=None,
                    eqwp_fused=None, gol_bytes=None, adj_fused=None, gol_push=None, tb16=None,
-                   tb_narrow=None, tb_r2=None, eqwp_tma=None, eqwp_overlap=None):
+                   tb_narrow=None, tb_r2=None, eqwp_tma=None, eqwp_overlap=None, gol_rows=None):
         for key, v in ((1, zchunk), (2, ctas_per_sm), (3, pdl), (4, tblock), (5, zchunk2),
                        (6, eqwp_fused), (7, gol_bytes), (8, adj_fused), (9, gol_push), (10, tb16),
-                       (11, tb_narrow), (12, tb_r2), (13, eqwp_tma), (14, eqwp_overlap)):
+                       (11, tb_narrow), (12, tb_r2), (13, eqwp_tma), (14, eqwp_overlap), (15, gol_rows)):
             if v is not None:
                 _check(lib().b2r_set_tuning(self.h, key, int(v)), self.h)
 
@@ -283,7 +283,7 @@ class Domain:
         for key, name in ((1, "zchunk"), (2, "ctas_per_sm"), (3, "pdl"), (4, "tblock"), (5, "zchunk2"),
                           (6, "eqwp_fused"), (7, "gol_bytes"), (8, "adj_fused"), (9, "gol_push"),
                           (10, "tb16"), (11, "tb_narrow"), (12, "tb_r2"), (13, "eqwp_tma"),
-                          (14, "eqwp_overlap")):
+                          (14, "eqwp_overlap"), (15, "gol_rows")):
             v = C.c_int()
             _check(lib().b2r_get_tuning(self.h, key, C.byref(v)), self.h)
             out[name] = v.value

@@ -62,6 +62,7 @@ struct b2r_handle {
     bool gol_bytes = false;    // Game of Life: byte-SWAR kernel instead of bit-sliced cells
     bool adj_fused = true;     // adjoint: stress adjoint + lambda/mu gradients in one sweep
     bool gol_push = false;     // Game of Life: period-end passes fill the next period's halos (opt-in: slower so far)
+    int gol_rows = 0;          // Game of Life several-generation pass: output rows per band at most (0 = 32)
     float* mat[3] = {};
     std::vector<float> src;     // per-step source increment of sxx/syy/szz (STAG)
     void* staging = nullptr;

@@ -25,6 +25,7 @@ b2r_status b2r_set_tuning(b2r_handle* h, int key, int value)
     case B2R_TUNE_TB_R2: h->tune.r2 = value != 0; break;
     case B2R_TUNE_EQWP_TMA: h->eqwp_tma = value != 0; break;
     case B2R_TUNE_EQWP_OVERLAP: h->eqwp_overlap = value != 0; break;
+    case B2R_TUNE_GOL_ROWS: h->gol_rows = value < 0 ? 0 : value; break;
     default: return fail(h, B2R_ERR_ARG, "unknown tuning key %d", key);
     }
     drop_graphs(h);
@@ -49,6 +50,7 @@ b2r_status b2r_get_tuning(const b2r_handle* h, int key, int* value)
     case B2R_TUNE_TB_R2: *value = h->tune.r2; break;
     case B2R_TUNE_EQWP_TMA: *value = h->eqwp_tma ? 1 : 0; break;
     case B2R_TUNE_EQWP_OVERLAP: *value = h->eqwp_overlap ? 1 : 0; break;
+    case B2R_TUNE_GOL_ROWS: *value = h->gol_rows; break;
     default: return fail(nullptr, B2R_ERR_ARG, "unknown tuning key %d", key);
     }
     return B2R_OK;
@@ -59,7 +61,7 @@ b2r_status b2r_get_tuning(const b2r_handle* h, int key, int* value)
 // the period-end halo fill (GoL); the one-pass or two-pass step (elastic
 // wave).  Trials run on the live fields, which are restored afterwards.
 struct KnobSet {
-    int tblock, gol_bytes, gol_push, eqwp_fused, eqwp_tma = 0, eqwp_overlap = 0;
+    int tblock, gol_bytes, gol_push, eqwp_fused, eqwp_tma = 0, eqwp_overlap = 0, gol_rows = 0;
 };
 static std::map<TuneKey, KnobSet> g_knob_cache;
 
@@ -71,6 +73,7 @@ static void apply_knobs(b2r_handle* h, const KnobSet& k)
     h->eqwp_fused = k.eqwp_fused != 0;
     h->eqwp_tma = k.eqwp_tma != 0;
     h->eqwp_overlap = k.eqwp_overlap != 0;
+    h->gol_rows = k.gol_rows;
 }
 
 static b2r_status autotune_knobs(b2r_handle* h, int trial_steps, int best[3], double* best_ms)
@@ -94,22 +97,28 @@ static b2r_status autotune_knobs(b2r_handle* h, int trial_steps, int best[3], do
         }
     }
     std::vector<KnobSet> cands;
-    const KnobSet cur{h->tune.tblock, h->gol_bytes, h->gol_push, h->eqwp_fused, h->eqwp_tma, h->eqwp_overlap};
+    const KnobSet cur{h->tune.tblock, h->gol_bytes, h->gol_push, h->eqwp_fused, h->eqwp_tma, h->eqwp_overlap,
+                      h->gol_rows};
     if (h->cfg.model == B2R_MODEL_GOL) {
+        // the several-generation bit-sliced pass also by its band height:
+        // 32 rows, 48, or the whole block (one band)
         for (int tb : {1, 2, 4})
             for (int bytes = 0; bytes < 2; ++bytes)
                 for (int push = 0; push < 2; ++push)
                     if (!push || (tb >= 2 && !bytes))
-                        cands.push_back({tb, bytes, push, cur.eqwp_fused, cur.eqwp_tma, cur.eqwp_overlap});
+                        for (int rows : {0, 48, 1 << 20})
+                            if (rows == 0 || (tb >= 2 && !bytes))
+                                cands.push_back({tb, bytes, push, cur.eqwp_fused, cur.eqwp_tma, cur.eqwp_overlap,
+                                                 rows});
     } else {
         // the two-pass step with plain-load or TMA-streamed stress stage (and,
         // on several blocks, with the exchange overlapped), the one-pass step
         const bool stag = h->cfg.model == B2R_MODEL_EQWP_STAG;
-        cands.push_back({cur.tblock, cur.gol_bytes, cur.gol_push, 0, 0, 0});
-        if (stag) cands.push_back({cur.tblock, cur.gol_bytes, cur.gol_push, 0, 1, 0});
+        cands.push_back({cur.tblock, cur.gol_bytes, cur.gol_push, 0, 0, 0, cur.gol_rows});
+        if (stag) cands.push_back({cur.tblock, cur.gol_bytes, cur.gol_push, 0, 1, 0, cur.gol_rows});
         if (stag && (h->L.nblk > 1 || h->L.periodic))
-            cands.push_back({cur.tblock, cur.gol_bytes, cur.gol_push, 0, 0, 1});
-        cands.push_back({cur.tblock, cur.gol_bytes, cur.gol_push, 1, 0, 0});
+            cands.push_back({cur.tblock, cur.gol_bytes, cur.gol_push, 0, 0, 1, cur.gol_rows});
+        cands.push_back({cur.tblock, cur.gol_bytes, cur.gol_push, 1, 0, 0, cur.gol_rows});
     }
     // the state the trials overwrite: the current buffer (GoL) or every
     // field of the current set with the set's pointers (elastic wave)

@@ -388,7 +388,7 @@ b2r_status advance(b2r_handle* h, int n)
             else
                 CK(h, launch_gol_bits_period(static_cast<const uint8_t*>(h->buf[h->cur]),
                                              static_cast<uint8_t*>(h->buf[1 - h->cur]), h->L, i, gg, push,
-                                             h->stream));
+                                             h->stream, h->gol_rows));
             h->cur = 1 - h->cur;
             h->ts += gg;
             s += gg;

@@ -24,9 +24,10 @@ cudaError_t launch_gol_bits_substep(const uint8_t* in, uint8_t* out, const Block
 // only the window of the last one is written to `out`.  push_halos (a pass
 // that ends a period; block rows of a multiple of 32 cells) also copies the
 // new band cells into the neighbour blocks' halos of `out`, as the next
-// period's halo gather would.
+// period's halo gather would.  rows: output rows per band of a CTA at most
+// (0 = 32; any value at least the block height: one band per block).
 cudaError_t launch_gol_bits_period(const uint8_t* in, uint8_t* out, const BlockLayout& L, int i0, int ng,
-                                   bool push_halos, cudaStream_t st);
+                                   bool push_halos, cudaStream_t st, int rows = 0);
 int gol_bits_max_generations_per_pass();
 
 }  // namespace b2r

@@ -478,7 +478,7 @@ cudaError_t launch_gol_bits_substep(const uint8_t* in, uint8_t* out, const Block
 int gol_bits_max_generations_per_pass() { return kBMaxGen; }
 
 cudaError_t launch_gol_bits_period(const uint8_t* in, uint8_t* out, const BlockLayout& L, int i0, int ng,
-                                   bool push_halos, cudaStream_t st)
+                                   bool push_halos, cudaStream_t st, int rows)
 {
     if (ng < 1 || ng > kBMaxGen) return cudaErrorInvalidValue;
     // a block row that is not a multiple of 32 cells ends in a word that the
@@ -507,9 +507,10 @@ cudaError_t launch_gol_bits_period(const uint8_t* in, uint8_t* out, const BlockL
         if (((nwt + g - 3) / (g - 2)) * g < ((nwt + GW - 3) / (GW - 2)) * GW) GW = g;
     const int ntx = (nwt + GW - 3) / (GW - 2);
     G.OW = GW - 2;
-    // bands of rows: at most B2R_GOLP_ROWS output rows, split evenly
+    // bands of rows: at most `rows` output rows, split evenly
     const int H = hi[1] - lo[1] + 1;
-    const int nty = (H + B2R_GOLP_ROWS - 1) / B2R_GOLP_ROWS;
+    const int band = rows > 0 ? std::min(rows, H) : B2R_GOLP_ROWS;
+    const int nty = (H + band - 1) / band;
     G.OR = (H + nty - 1) / nty;
     G.PR = (G.OR + 2 * ng + 3) / 4 * 4;
     if (GW * (G.PR / 4) > 512) G.PR = 512 / GW * 4, G.OR = G.PR - 2 * ng;

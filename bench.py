@@ -866,7 +866,7 @@ def run_ours(args, wl):
     # the timing
     tuned = None
     knobs = {1: ("zchunk", "ctas_per_sm", "pdl", "tblock", "zchunk2", "tb16", "tb_narrow", "tb_r2"),
-             2: ("tblock", "gol_bytes", "gol_push"), 4: ("eqwp_fused", "eqwp_tma", "eqwp_overlap")}
+             2: ("tblock", "gol_bytes", "gol_push", "gol_rows"), 4: ("eqwp_fused", "eqwp_tma", "eqwp_overlap")}
     if wl["model"] in knobs and not tune:
         d.autotune(trial_steps=4)
         tuned = {k: v for k, v in d.get_tuning().items() if k in knobs[wl["model"]]}

@@ -162,11 +162,14 @@ enum {
     B2R_TUNE_EQWP_TMA = 13,    /* staggered elastic wave, two-pass step: 1 = the stress stage with
                                   its inputs streamed through TMA rings, 0 = plain loads (default);
                                   bit-identical */
-    B2R_TUNE_EQWP_OVERLAP = 14 /* staggered elastic wave, two-pass step on several blocks: 1 = the
+    B2R_TUNE_EQWP_OVERLAP = 14,/* staggered elastic wave, two-pass step on several blocks: 1 = the
                                   last stress stage of a period computes the tiles that the next
                                   halo exchange reads first, then that exchange runs on a second
                                   stream while the other tiles finish; 0 = the exchange at the
                                   period start (default: faster on one GPU so far); bit-identical */
+    B2R_TUNE_GOL_ROWS = 15     /* Game of Life, the several-generation bit-sliced pass: output rows
+                                  per band of a CTA at most (0 = 32, the default; a value at least
+                                  the block height gives one band per block); identical results */
 };
 b2r_status b2r_set_tuning(b2r_handle* h, int key, int value);
 /* Current value of a knob (after b2r_autotune: the schedule it picked). */

@@ -90,18 +90,19 @@ def test_knob_autotune_keeps_state_and_bits(b2r, model):
 
 
 def test_every_knob_round_trips_and_unknown_keys_are_refused(b2r):
-    """Each of the 14 knobs reads back what was set (boolean knobs as 0/1),
-    on a handle of each model; keys outside 1..14 are refused through both
+    """Each of the 15 knobs reads back what was set (boolean knobs as 0/1),
+    on a handle of each model; keys outside 1..15 are refused through both
     entry points."""
     import ctypes as C
     values = dict(zchunk=24, ctas_per_sm=3, pdl=0, tblock=3, zchunk2=40, eqwp_fused=1, gol_bytes=1,
-                  adj_fused=0, gol_push=1, tb16=1, tb_narrow=1, tb_r2=1, eqwp_tma=1, eqwp_overlap=1)
+                  adj_fused=0, gol_push=1, tb16=1, tb_narrow=1, tb_r2=1, eqwp_tma=1, eqwp_overlap=1,
+                  gol_rows=48)
     for model, kw in ((b2r.MODEL_HEAT, dict(D=1)), (b2r.MODEL_GOL, dict(D=1)),
                       (b2r.MODEL_EQWP_STAG, dict(D=2, dt=1e-4, h=10.0))):
         with b2r.Domain(model, (32, 32, 32), **kw) as d:
             d.set_tuning(**values)
             assert d.get_tuning() == values, model
-            for key in (0, 15, -1):
+            for key in (0, 16, -1):
                 with pytest.raises(b2r.B2RError):
                     b2r._check(b2r.lib().b2r_set_tuning(d.h, key, 1), d.h)
                 v = C.c_int()

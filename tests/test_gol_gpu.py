@@ -226,3 +226,30 @@ def test_gol_single_fixed_shell_block(b2r, orc, env, R, tblock):
         orc.gol_substep(a, b, 0, 1, 63)
         a, b = b, a
     assert np.array_equal(got, a)
+
+
+@pytest.mark.parametrize("env,blocks,R,periodic", [((64, 64, 64), (2, 2, 2), 4, True), ((70, 36, 50), (2, 3, 1), 2, True),
+                                                   ((300, 40, 30), (1, 1, 1), 4, False), ((96, 130, 40), (1, 2, 1), 3, False)])
+def test_gol_band_heights_bit_identical(b2r, orc, env, blocks, R, periodic):
+    """The several-generation pass with bands of 7, 48 and a whole block of
+    rows against the default 32 (and the oracle on the torus)."""
+    bc = b2r.BC_PERIODIC if periodic else b2r.BC_SHELL
+    if periodic:
+        dom = bernoulli(env, 0.3, 23)
+    else:
+        dom = np.zeros(tuple(e + 2 for e in env[::-1]), np.uint8)
+        dom[1:-1, 1:-1, 1:-1] = bernoulli(env, 0.3, 23)
+    outs = []
+    for rows in (0, 7, 48, 1 << 20):
+        with b2r.Domain(b2r.MODEL_GOL, env, blocks=blocks, R=R, D=1, boundary=bc) as d:
+            d.set_tuning(tblock=4, gol_bytes=0, gol_push=0, gol_rows=rows)
+            assert d.get_tuning()["gol_rows"] == rows
+            d.upload(dom)
+            d.step(2 * R + 1)
+            outs.append(d.download())
+    for o in outs[1:]:
+        assert np.array_equal(outs[0], o)
+    if periodic:
+        ref = dom.copy()
+        orc.gol_run_periodic(ref, 2 * R + 1)
+        assert np.array_equal(outs[0], ref)
