@@ -179,7 +179,8 @@ b2r_status b2r_get_tuning(const b2r_handle* h, int key, int* value);
  * time steps per pass x z-chunk length x persistent CTAs per SM x
  * programmatic dependent launch, best[3] = {zchunk, ctas_per_sm, pdl}.
  * Game of Life: generations per pass x bit-sliced / byte cells x period-end
- * halo fill, best = {tblock, gol_bytes, gol_push}.  Staggered elastic wave:
+ * halo fill x band height of the several-generation pass, best = {tblock,
+ * gol_bytes, gol_push} (the band height: b2r_get_tuning).  Staggered elastic wave:
  * one-pass or two-pass step, the latter with the plain or TMA-streamed
  * stress stage and, on several blocks, with the halo exchange at the period
  * start or overlapped with the last stress stage, best = {tblock,
