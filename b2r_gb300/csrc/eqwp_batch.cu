@@ -117,7 +117,8 @@ struct b2r_eqwp_batch {
     unsigned* d_done = nullptr;
     int* d_status = nullptr;
     long long total = 0;
-    int lz_policy = 32;              // z chunk cap per unit
+    int lz_policy = 8;               // z chunk cap per unit: short units keep more of a round in
+                                     // flight (16 instances of 32-128 cells: 36.8 GLUPS at 8, 26.1 at 32)
     int grid = 0;
     cudaGraphExec_t gexec = nullptr;
     cudaStream_t gstream = nullptr;
