@@ -117,8 +117,7 @@ struct b2r_eqwp_batch {
     unsigned* d_done = nullptr;
     int* d_status = nullptr;
     long long total = 0;
-    int lz_policy = 8;               // z chunk cap per unit: short units keep more of a round in
-                                     // flight (16 instances of 32-128 cells: 36.8 GLUPS at 8, 26.1 at 32)
+    int lz_policy = -1;              // z chunk cap per unit; -1: by the batch's size (auto_lz)
     int grid = 0;
     cudaGraphExec_t gexec = nullptr;
     cudaStream_t gstream = nullptr;
@@ -148,7 +147,26 @@ b2r_status efail(b2r_status s, const char* msg, cudaError_t e = cudaSuccess)
         }                                                                                    \
     } while (0)
 
-// tiles, z chunks and the queue tables for the current z-chunk policy
+// z chunk of the units when the caller set none: short units keep more of a
+// round in flight, which small instances need (16 instances of 32-128 cells
+// per edge: 36.9 GLUPS at 8 planes, 26.1 at 32), while large ones have work
+// enough in 32-plane units and re-read fewer z-skirt planes with them -- 8
+// planes when units of 32 would give fewer than 8 per resident CTA in a
+// round, else 32.
+static int auto_lz(const b2r_eqwp_batch* b)
+{
+    long long units = 0;
+    for (int k = 0; k < b->n; ++k) {
+        const EInst& in = b->host[k];
+        int lo, hi;
+        stage_region(in.L, edge_bits(in.L, 0), 2, 2, lo, hi);
+        const int nz = std::max(1, hi - lo + 1);
+        units += (long long)in.gx * in.gy * ((nz + 31) / 32);
+    }
+    return units < 8LL * b->grid ? 8 : 32;
+}
+
+// tiles, z chunks and the queue for the current z-chunk policy
 b2r_status build(b2r_eqwp_batch* b)
 {
     for (int k = 0; k < b->n; ++k) {
@@ -159,10 +177,14 @@ b2r_status build(b2r_eqwp_batch* b)
         in.by = (int)g.b.y;
         in.gx = (int)g.g.x;
         in.gy = (int)g.g.y;
+    }
+    const int policy = b->lz_policy >= 0 ? b->lz_policy : auto_lz(b);
+    for (int k = 0; k < b->n; ++k) {
+        EInst& in = b->host[k];
         int lo, hi;
         stage_region(in.L, edge_bits(in.L, 0), 2, 2, lo, hi);
         const int nz = std::max(1, hi - lo + 1);
-        const int lz = b->lz_policy > 0 ? std::min(b->lz_policy, nz) : nz;
+        const int lz = policy > 0 ? std::min(policy, nz) : nz;
         in.T.nzc = (nz + lz - 1) / lz;
         in.units = in.gx * in.gy * in.T.nzc;
         in.rounds = 2 * in.nsteps;

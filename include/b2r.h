@@ -427,7 +427,9 @@ b2r_status b2r_eqwp_batch_run(b2r_eqwp_batch* b, void* cuda_stream, int use_grap
 b2r_status b2r_eqwp_batch_synchronize(b2r_eqwp_batch* b, void* cuda_stream);
 /* Lattice-site updates of one run (sum of interior cells x steps). */
 int64_t b2r_eqwp_batch_lups(const b2r_eqwp_batch* b);
-/* Planes per work unit along z (default 8; 0 = whole column). */
+/* Planes per work unit along z (0 = whole column).  Default: 8 when units
+ * of 32 planes would give fewer than 8 per resident CTA in a round (small
+ * instances), else 32. */
 b2r_status b2r_eqwp_batch_set_zchunk(b2r_eqwp_batch* b, int zchunk);
 
 /* ---- diagnostics (no reference counterpart) ------------------------------- *
