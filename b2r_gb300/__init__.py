@@ -271,6 +271,8 @@ class Domain:
     def set_tuning(self, zchunk=None, ctas_per_sm=None, pdl=None, tblock=None, zchunk2=None,
                    eqwp_fused=None, gol_bytes=None, adj_fused=None, gol_push=None, tb16=None,
                    tb_narrow=None, tb_r2=None, eqwp_tma=None, eqwp_overlap=None, gol_rows=None):
+        """Launch-schedule knobs (B2R_TUNE_* of b2r.h, keys 1..15); None
+        leaves a knob as it is.  Every choice gives the same results."""
         for key, v in ((1, zchunk), (2, ctas_per_sm), (3, pdl), (4, tblock), (5, zchunk2),
                        (6, eqwp_fused), (7, gol_bytes), (8, adj_fused), (9, gol_push), (10, tb16),
                        (11, tb_narrow), (12, tb_r2), (13, eqwp_tma), (14, eqwp_overlap), (15, gol_rows)):
