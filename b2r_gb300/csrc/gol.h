@@ -30,4 +30,32 @@ cudaError_t launch_gol_bits_period(const uint8_t* in, uint8_t* out, const BlockL
                                    bool push_halos, cudaStream_t st, int rows = 0);
 int gol_bits_max_generations_per_pass();
 
+// z chunks per block of the several-generation pass (host side): the CTAs
+// (tiles x chunks) are dealt over `sms` SMs, the busiest SM holding
+// ceil(CTAs / sms) of them, each computing its chunk of nz planes plus about
+// ng - 1 planes of z skirt per generation; the count that makes the busiest
+// SM's planes fewest, with every CTA resident at once (cap per SM) and, where
+// the block allows, at least minper CTAs per SM on average.
+inline int gol_period_chunks(long long tiles, int nz, int ng, int sms, int cap, int minper)
+{
+    sms = sms > 0 ? sms : 1;
+    cap = cap > 0 ? cap : 1;
+    int nzc = 1;
+    long long best = -1;
+    bool best_full = false;
+    for (int c = 1; c <= nz; ++c) {
+        const long long ctas = tiles * c;
+        if (c > 1 && ctas > (long long)sms * cap) break;
+        const bool full = ctas >= (long long)minper * sms;
+        const long long busiest = (ctas + sms - 1) / sms;
+        const long long cost = busiest * ((nz + c - 1) / c + ng - 1);
+        if (best < 0 || (full && !best_full) || (full == best_full && cost < best)) {
+            best = cost;
+            best_full = full;
+            nzc = c;
+        }
+    }
+    return nzc;
+}
+
 }  // namespace b2r

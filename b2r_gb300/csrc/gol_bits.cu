@@ -527,35 +527,15 @@ cudaError_t launch_gol_bits_period(const uint8_t* in, uint8_t* out, const BlockL
                      : GW == 16 ? (const void*)gol_bits_period_kernel<16>
                                 : (const void*)gol_bits_period_kernel<32>;
     if (cudaError_t e = raise_smem_limit(attr[gi], kern, std::max<size_t>(smem, 48 * 1024))) return e;
-    // z chunks per block: the CTAs are dealt over the SMs, the busiest SM
-    // holding ceil(CTAs / SMs) of them, each computing its chunk plus about
-    // ng - 1 planes of z skirt per generation; the count that makes the
-    // busiest SM's planes fewest, with every CTA resident at once and, where
-    // the block allows, at least B2R_GOLP_MINPER CTAs per SM on average (the
-    // kernel needs several to hide its latencies).  Measured on the 256^3
-    // torus in 2 x 2 x 2 blocks: 987 GLUPS at the count this picks (19),
-    // against 928 for 16 and 764-911 for the counts around them.
+    // z chunks per block by the cost model of gol_period_chunks (the kernel
+    // needs several CTAs per SM to hide its latencies).  Measured on the
+    // 256^3 torus in 2 x 2 x 2 blocks: 987 GLUPS at the count this picks
+    // (19), against 928 for 16 and 764-911 for the counts around them.
     int dev = 0, sms = 0, cap = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cap, kern, threads, smem);
-    sms = std::max(1, sms);
-    cap = std::max(1, cap);
-    int nzc = 1;
-    long long best = -1;
-    bool best_full = false;
-    for (int c = 1; c <= nz; ++c) {
-        const long long ctas = tiles * c;
-        if (c > 1 && ctas > (long long)sms * cap) break;
-        const bool full = ctas >= (long long)B2R_GOLP_MINPER * sms;
-        const long long busiest = (ctas + sms - 1) / sms;
-        const long long cost = busiest * ((nz + c - 1) / c + ng - 1);
-        if (best < 0 || (full && !best_full) || (full == best_full && cost < best)) {
-            best = cost;
-            best_full = full;
-            nzc = c;
-        }
-    }
+    const int nzc = gol_period_chunks(tiles, nz, ng, sms, cap, B2R_GOLP_MINPER);
     G.nzc = nzc;
     const dim3 grid(ntx, nty2, L.nblk * nzc);
     switch (GW) {
